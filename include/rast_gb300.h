@@ -1,0 +1,181 @@
+/*
+ * rast_gb300.h -- C ABI of the GB300 (sm_103a) rasteriser.
+ *
+ * Replaces the hot path of jaxrenderer (JoeyTeng/jaxrenderer v0.3.2):
+ *   renderer/pipeline.py:470-537  pipeline.render (vertex stage, per-face
+ *                                 gather, PerPrimitive.create :80-113,
+ *                                 _postprocessing :127-459)
+ *   renderer/shader.py:159-396    default primitive_chooser / interpolate /
+ *                                 fragment / mix
+ *   renderer/shaders/*.py         the seven built-in shaders
+ *   renderer/shadow.py:49-125     the light-space depth pass (+ offset)
+ *
+ * A call renders a batch of independent "jobs".  A job is one
+ * pipeline.render call: one shader, one camera, one vertex range, one face
+ * range and one (W, H) target.  Renderer.render with shadows is two jobs
+ * (the DEPTH job writing the shadow map, then the PHONG_REFLECTION_SHADOW
+ * job reading it) issued as two calls on the same stream.
+ *
+ * Conventions:
+ *  - every pointer inside RastPools and RastBatch.jobs is DEVICE memory the
+ *    caller owns; the library allocates nothing except where a function says
+ *    so, and keeps no global mutable state;
+ *  - buffers are x-major as in the reference (types.py:63-64): pixel (i, j)
+ *    of a job lives at pixel_begin + i * height + j; canvas has 3 channels;
+ *  - matrices are 4x4 row-major float32;
+ *  - calls are ordered on `stream` (a cudaStream_t, NULL = legacy default);
+ *  - every function returns RAST_OK (0) or a RastStatus code; nothing throws
+ *    across the ABI.  rast_error_string() names a code.
+ */
+#ifndef RAST_GB300_H
+#define RAST_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RAST_ABI_VERSION 1
+
+/* Built-in shader classes (renderer/shaders/*.py), one kernel path each. */
+typedef enum RastShader {
+  RAST_SHADER_DEPTH = 0,                   /* shaders/depth.py:38 DepthShader */
+  RAST_SHADER_GOURAUD = 1,                 /* shaders/gouraud.py:49 */
+  RAST_SHADER_GOURAUD_TEXTURE = 2,         /* shaders/gouraud_texture.py:55 */
+  RAST_SHADER_PHONG = 3,                   /* shaders/phong.py:65 PhongTextureShader */
+  RAST_SHADER_PHONG_DARBOUX = 4,           /* shaders/phong_darboux.py:106 */
+  RAST_SHADER_PHONG_REFLECTION = 5,        /* shaders/phong_reflection.py:91 */
+  RAST_SHADER_PHONG_REFLECTION_SHADOW = 6  /* shaders/phong_reflection_shadow.py:99 */
+} RastShader;
+
+typedef enum RastStatus {
+  RAST_OK = 0,
+  RAST_ERR_INVALID_ARGUMENT = 1,   /* bad sizes, NULL pointers, unknown shader */
+  RAST_ERR_WORKSPACE_TOO_SMALL = 2,
+  RAST_ERR_CUDA = 3,               /* a CUDA runtime call failed */
+  RAST_ERR_UNSUPPORTED = 4,
+  RAST_ERR_TIMEOUT = 5,            /* a bounded device-side wait ran out */
+  RAST_ERR_BIN_OVERFLOW = 6,       /* tiled form: a bin exceeded its capacity */
+  RAST_ERR_INDEX_OUT_OF_RANGE = 7  /* validation found a face index outside its vertex range */
+} RastStatus;
+
+/* One pipeline.render call.  Offsets are element rows into RastPools
+ * arrays; `*_begin` fields marked (ws) index library workspace and are
+ * filled by the caller as running sums of n_verts / n_faces over the jobs. */
+typedef struct RastJob {
+  int32_t shader;            /* RastShader */
+  int32_t width, height;     /* target buffers (W, H) */
+  int32_t n_verts;           /* vertices run through the vertex shader (len(extra[0])) */
+  int32_t n_faces;           /* faces (F, 3); indices relative to vert_begin */
+  int32_t n_darboux_faces;   /* rows of faces_indices (phong_darboux) */
+  int32_t n_objects;         /* rows of texture_shape (phong_reflection*) */
+  int32_t texture_offset;    /* MergedModel.offset (phong_reflection*) */
+  int64_t vert_begin;        /* row of position/normal/uv/colour/texture_index/id_to_face */
+  int64_t face_begin;        /* row of faces */
+  int64_t darboux_face_begin;/* row of darboux_faces */
+  int64_t pixel_begin;       /* pixel of zbuffer / canvas / prim_id */
+  int64_t vout_begin;        /* (ws) first vertex-output row: sum of n_verts before */
+  int64_t setup_begin;       /* (ws) first primitive-setup row: sum of n_faces before */
+  int64_t texture_begin;     /* element of texture pool; (tex_w, tex_h, tex_c) */
+  int64_t specular_begin;    /* element of specular pool; (spec_w, spec_h) */
+  int64_t normal_map_begin;  /* element of normal-map pool; (nm_w, nm_h, 3) */
+  int64_t texture_shape_begin; /* row of texture_shape (int32 pairs) */
+  int64_t shadow_begin;      /* element of shadow-map pool; (shadow_w, shadow_h) */
+  int32_t tex_w, tex_h, tex_c;
+  int32_t spec_w, spec_h;
+  int32_t nm_w, nm_h;
+  int32_t shadow_w, shadow_h;
+  float depth_offset;        /* with RAST_JOB_APPLY_DEPTH_OFFSET: added to every zbuffer
+                                pixel after the pass (Shadow offset, shadow.py:116) */
+  float viewport[16];        /* Camera.viewport */
+  float world_to_clip[16];   /* Camera.world_to_clip */
+  float world_to_eye_norm[16]; /* Camera.world_to_eye_norm */
+  float shadow_viewport[16];   /* Shadow.camera.viewport */
+  float shadow_world_to_clip[16]; /* Shadow.camera.world_to_clip */
+  float light_direction[3];  /* LightSource.direction */
+  float light_colour[3];     /* LightSource.colour */
+  float light_dir_eye[3];    /* PhongReflection*ExtraInput.light_dir_eye */
+  float ambient[3], diffuse[3], specular[3];
+  float shadow_strength[3];  /* Shadow.strength */
+  int32_t flags;             /* RAST_JOB_* bits */
+  int32_t reserved[2];
+} RastJob;
+
+/* RastJob.flags */
+#define RAST_JOB_APPLY_DEPTH_OFFSET 1  /* zbuffer += depth_offset on every pixel after the pass */
+
+/* Flat input/output arrays shared by all jobs of a batch (device). */
+typedef struct RastPools {
+  const float* position;       /* (rows, 3) */
+  const float* normal;         /* (rows, 3) */
+  const float* uv;             /* (rows, 2) */
+  const float* colour;         /* (rows, 3)  gouraud */
+  const int32_t* texture_index;/* (rows)     phong_reflection* */
+  const int32_t* id_to_face;   /* (rows)     phong_darboux */
+  const int32_t* faces;        /* (faces, 3) */
+  const int32_t* darboux_faces;/* (rows, 3)  phong_darboux faces_indices */
+  const float* texture;        /* diffuse maps, (w, h, c) each */
+  const float* specular_map;   /* (w, h) each */
+  const float* normal_map;     /* (w, h, 3) each */
+  const int32_t* texture_shape;/* (objects, 2) */
+  const float* shadow_map;     /* (w, h) each, read by PHONG_REFLECTION_SHADOW */
+  float* zbuffer;              /* (pixels)     in/out */
+  float* canvas;               /* (pixels, 3)  in/out; unused by DEPTH */
+  int32_t* prim_id;            /* (pixels)     out, optional (NULL): primitive written or -1 */
+} RastPools;
+
+typedef struct RastBatch {
+  const RastJob* jobs;   /* DEVICE array of n_jobs */
+  int32_t n_jobs;        /* 1 .. 65535 */
+  int32_t max_width;     /* max over jobs of width  */
+  int32_t max_height;    /* max over jobs of height */
+  int32_t max_verts;     /* max over jobs of n_verts */
+  int32_t max_faces;     /* max over jobs of n_faces */
+  int32_t shader_mask;   /* OR of (1 << shader) over jobs */
+  int64_t total_vout;    /* sum of n_verts   (vertex-output rows) */
+  int64_t total_setup;   /* sum of n_faces   (primitive-setup rows) */
+  int64_t total_pixels;  /* sum of width*height */
+  RastPools pools;
+  unsigned long long* near_ties; /* optional device counter (NULL): pixels whose two best
+                                    candidate depths are <= 1 ulp apart, accumulated */
+} RastBatch;
+
+/* Workspace the caller must pass to rast_render_plain, in bytes, 256-byte
+ * aligned base required. */
+size_t rast_plain_workspace_bytes(const RastBatch* batch);
+
+/* Plain form: the reference's own method.  Vertex-shader kernel, primitive
+ * setup kernel (det, keep, 3x3 LU inverse), per-pixel scan over every
+ * primitive of the job (FP32 barycentrics + depth, winner by the packed
+ * 64-bit (ordered depth | primitive id) minimum: lowest depth, then lowest
+ * primitive id), then interpolation + fragment shader + mixer + merge. */
+int rast_render_plain(const RastBatch* batch, void* workspace, size_t workspace_bytes,
+                      void* stream);
+
+/* Per-kernel timing of one call, for benchmarks: when passed to a
+ * *_profiled entry point, the library records CUDA events around each of its
+ * kernels on `stream`, synchronises the stream before returning and fills
+ * `ms` / `names` (at most 16 kernels, in launch order). */
+typedef struct RastProfile {
+  int32_t n;
+  float ms[16];
+  const char* names[16];
+} RastProfile;
+
+/* rast_render_plain with per-kernel timing (synchronises `stream`). */
+int rast_render_plain_profiled(const RastBatch* batch, void* workspace, size_t workspace_bytes,
+                               void* stream, RastProfile* profile);
+
+/* Host-side validation of one job against pool sizes (no device access):
+ * returns RAST_ERR_INVALID_ARGUMENT for inconsistent sizes. */
+int rast_validate_job(const RastJob* job);
+
+const char* rast_error_string(int status);
+int rast_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* RAST_GB300_H */

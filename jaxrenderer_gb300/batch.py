@@ -1,0 +1,329 @@
+"""Many scenes per call: the batched entry point of the rasteriser.
+
+A `SceneBatch` holds N scenes in flat device pools (per-corner vertex
+attributes, merged textures, one camera per scene) and renders them with one
+launch sequence per pass: the light-space depth pass of every scene, then the
+main pass of every scene.  This is the GPU counterpart of the reference's
+`jax.jit(jax.vmap(Renderer.get_camera_image))` over scenes
+(notebooks/84x84/A100.ipynb, examples/batch_rendering.py:87-95), with uneven
+triangle counts per scene instead of padded batches.
+
+`render_batch(batch, form="plain")` runs the plain per-pixel-scan kernels;
+`form="tiled"` runs the binned tiled kernels (rast_tiled.cu).
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass, field
+from typing import Dict, Optional, Sequence
+
+import numpy as np
+import torch
+
+from . import _lib
+from .geometry import Camera, normalise
+from .renderer import CameraParameters, LightParameters, Renderer, ShadowParameters
+from .shadow import Shadow
+
+F32 = np.float32
+JOB_DTYPE = np.dtype(_lib.RastJob)
+
+
+def job_table(n: int) -> np.ndarray:
+    """Zeroed structured array with the RastJob layout."""
+    return np.zeros(n, dtype=JOB_DTYPE)
+
+
+@dataclass
+class SceneBatch:
+    """N scenes, flattened per face corner, resident on one device."""
+
+    n_scenes: int
+    width: int
+    height: int
+    shadow_width: int
+    shadow_height: int
+    pools: Dict[str, torch.Tensor]
+    main_jobs: np.ndarray  # RastJob table of the main pass
+    shadow_jobs: Optional[np.ndarray]  # RastJob table of the depth pass, or None
+    device: torch.device
+    n_faces: np.ndarray = field(default=None)
+
+    @property
+    def total_faces(self) -> int:
+        return int(self.n_faces.sum())
+
+
+def _cameras(positions: np.ndarray, params: CameraParameters):
+    w2c, w2e, view = [], [], []
+    for p in positions:
+        cam = Renderer.create_camera_from_parameters(params._replace(position=p))
+        w2c.append(cam.world_to_clip)
+        w2e.append(cam.world_to_eye_norm)
+        view.append(cam.view)
+    return np.stack(w2c), np.stack(w2e), np.stack(view), cam.viewport
+
+
+@dataclass
+class SceneTables:
+    """Job tables of a flat scene batch (host only)."""
+
+    main_jobs: np.ndarray
+    shadow_jobs: Optional[np.ndarray]
+    width: int
+    height: int
+    shadow_width: int
+    shadow_height: int
+
+
+def scene_batch_tables(flat, width: int = 84, height: int = 84,
+                       light: LightParameters = LightParameters(),
+                       shadow_param: Optional[ShadowParameters] = ShadowParameters(),
+                       shadow_size=(128, 128), camera_params: Optional[CameraParameters] = None) -> SceneTables:
+    """RastJob tables of a synthetic.FlatScenes batch.
+
+    Each scene: PhongReflection(Shadow)TextureShader over its corners
+    (Renderer.render, renderer.py:254-385); with `shadow_param`, a DepthShader
+    pass into a shadow_size map seen through an orthographic light camera
+    with viewport shadow_size (the low-level Shadow.render_shadow_map API).
+    """
+    n = flat.n_scenes
+    params = camera_params or CameraParameters(viewWidth=width, viewHeight=height, near=0.01, far=1000.0,
+                                               hfov=58.0, vfov=58.0, target=np.zeros(3, F32))
+    w2c, w2e, views, viewport = _cameras(flat.camera_position, params)
+    light_dir = normalise(np.asarray(light.direction, F32))
+    light_dir_eye = np.stack([Camera.apply_vec(light_dir, v) for v in views])
+
+    shadow = shadow_param is not None
+    main = job_table(n)
+    main["shader"] = _lib.SHADER_PHONG_REFLECTION_SHADOW if shadow else _lib.SHADER_PHONG_REFLECTION
+    main["width"], main["height"] = width, height
+    main["n_verts"] = 3 * flat.n_faces
+    main["n_faces"] = flat.n_faces
+    main["n_objects"] = flat.n_objects
+    main["texture_offset"] = 4
+    main["vert_begin"] = flat.corner_begin
+    main["face_begin"] = 0
+    main["pixel_begin"] = np.arange(n, dtype=np.int64) * width * height
+    main["vout_begin"] = flat.corner_begin
+    main["setup_begin"] = np.concatenate([[0], np.cumsum(flat.n_faces.astype(np.int64))[:-1]])
+    main["texture_begin"] = flat.tex_begin * 4 * 3
+    main["specular_begin"] = flat.tex_begin * 4
+    obj_begin = np.concatenate([[0], np.cumsum(flat.n_objects.astype(np.int64))[:-1]])
+    main["texture_shape_begin"] = obj_begin
+    main["tex_w"] = 4 * flat.n_objects
+    main["tex_h"], main["tex_c"] = 4, 3
+    main["spec_w"] = 4 * flat.n_objects
+    main["spec_h"] = 4
+    main["viewport"] = np.broadcast_to(viewport.reshape(16), (n, 16))
+    main["world_to_clip"] = w2c.reshape(n, 16)
+    main["world_to_eye_norm"] = w2e.reshape(n, 16)
+    main["light_direction"] = light_dir
+    main["light_colour"] = np.asarray(light.colour, F32)
+    main["light_dir_eye"] = light_dir_eye
+    main["ambient"] = np.asarray(light.ambient, F32)
+    main["diffuse"] = np.asarray(light.diffuse, F32)
+    main["specular"] = np.asarray(light.specular, F32)
+    shadow_jobs = None
+    sw, sh = shadow_size
+    if shadow:
+        svp = Camera.viewport_matrix(np.zeros(2, np.int32), np.array((sw, sh)), 1.0)
+        scam = Shadow.light_camera(np.asarray(light.direction, F32), svp, shadow_param.centre, shadow_param.up)
+        shadow_jobs = job_table(n)
+        shadow_jobs["shader"] = _lib.SHADER_DEPTH
+        shadow_jobs["width"], shadow_jobs["height"] = sw, sh
+        for k in ("n_verts", "n_faces", "vert_begin", "face_begin", "vout_begin", "setup_begin"):
+            shadow_jobs[k] = main[k]
+        shadow_jobs["pixel_begin"] = np.arange(n, dtype=np.int64) * sw * sh
+        shadow_jobs["viewport"] = svp.reshape(16)
+        shadow_jobs["world_to_clip"] = scam.world_to_clip.reshape(16)
+        shadow_jobs["world_to_eye_norm"] = scam.world_to_eye_norm.reshape(16)
+        shadow_jobs["depth_offset"] = np.float32(shadow_param.offset)
+        shadow_jobs["flags"] = _lib.JOB_APPLY_DEPTH_OFFSET
+        main["shadow_begin"] = shadow_jobs["pixel_begin"]
+        main["shadow_w"], main["shadow_h"] = sw, sh
+        main["shadow_viewport"] = scam.viewport.reshape(16)
+        main["shadow_world_to_clip"] = scam.world_to_clip.reshape(16)
+        main["shadow_strength"] = np.asarray(shadow_param.strength, F32)
+    return SceneTables(main, shadow_jobs, width, height, sw, sh)
+
+
+def flat_pools(flat, device) -> Dict[str, torch.Tensor]:
+    """Device pools of a synthetic.FlatScenes batch."""
+
+    def T(x, dt=torch.float32):
+        return torch.from_numpy(np.ascontiguousarray(x)).to(device=device, dtype=dt)
+
+    max_f = int(flat.n_faces.max())
+    faces = np.arange(3 * max_f, dtype=np.int32).reshape(-1, 3)  # face f of every scene is corners 3f..3f+2
+    return {
+        "position": T(flat.position),
+        "normal": T(flat.normal),
+        "uv": T(flat.uv),
+        "texture_index": T(flat.texture_index, torch.int32),
+        "faces": T(faces, torch.int32),
+        "texture": T(flat.texture),
+        "specular_map": T(flat.specular_map),
+        "texture_shape": T(np.tile(np.array([[4, 4]], np.int32), (int(flat.n_objects.sum()), 1)), torch.int32),
+    }
+
+
+def scene_batch_from_flat(flat, width: int = 84, height: int = 84,
+                          light: LightParameters = LightParameters(),
+                          shadow_param: Optional[ShadowParameters] = ShadowParameters(),
+                          shadow_size=(128, 128), device=None,
+                          camera_params: Optional[CameraParameters] = None) -> SceneBatch:
+    """Upload a synthetic.FlatScenes batch and build its job tables."""
+    device = device if device is not None else torch.device("cuda", torch.cuda.current_device())
+    t = scene_batch_tables(flat, width, height, light, shadow_param, shadow_size, camera_params)
+    lib = _lib.load()
+    for tbl in (t.main_jobs, t.shadow_jobs):
+        if tbl is None:
+            continue
+        for k in range(min(len(tbl), 4)):
+            job = _lib.RastJob.from_buffer_copy(tbl[k].tobytes())
+            _lib.check(lib.rast_validate_job(ctypes.byref(job)), f"job {k}")
+    return SceneBatch(flat.n_scenes, width, height, t.shadow_width, t.shadow_height, flat_pools(flat, device),
+                      t.main_jobs, t.shadow_jobs, device, flat.n_faces)
+
+
+def scene_job_specs(flat, tables, s: int):
+    """The pipeline.render calls scene `s` of a flat batch makes, as JobSpecs
+    with host arrays: (depth pass or None, main pass)."""
+    from .jobs import JobSpec
+
+    m = tables.main_jobs[s]
+    cb, F = int(flat.corner_begin[s]), int(flat.n_faces[s])
+    tb, no = int(flat.tex_begin[s]), int(flat.n_objects[s])
+    faces = np.arange(3 * F, dtype=np.int32).reshape(F, 3)
+    rows = slice(cb, cb + 3 * F)
+    main = JobSpec(shader=int(m["shader"]), width=int(m["width"]), height=int(m["height"]),
+                   viewport=m["viewport"].reshape(4, 4), world_to_clip=m["world_to_clip"].reshape(4, 4),
+                   world_to_eye_norm=m["world_to_eye_norm"].reshape(4, 4), position=flat.position[rows],
+                   faces=faces)
+    main.normal = flat.normal[rows]
+    main.uv = flat.uv[rows]
+    main.texture_index = flat.texture_index[rows]
+    main.texture = flat.texture[tb : tb + 4 * no]
+    main.specular_map = flat.specular_map[tb : tb + 4 * no]
+    main.texture_shape = np.tile(np.array([[4, 4]], np.int32), (no, 1))
+    main.texture_offset = 4
+    for k in ("light_direction", "light_colour", "light_dir_eye", "ambient", "diffuse", "specular"):
+        setattr(main, k, np.asarray(m[k], F32))
+    depth = None
+    if tables.shadow_jobs is not None:
+        d = tables.shadow_jobs[s]
+        depth = JobSpec(shader=_lib.SHADER_DEPTH, width=int(d["width"]), height=int(d["height"]),
+                        viewport=d["viewport"].reshape(4, 4), world_to_clip=d["world_to_clip"].reshape(4, 4),
+                        world_to_eye_norm=d["world_to_eye_norm"].reshape(4, 4), position=flat.position[rows],
+                        faces=faces, depth_offset=float(d["depth_offset"]), apply_depth_offset=True)
+        main.shadow_viewport = m["shadow_viewport"].reshape(4, 4)
+        main.shadow_world_to_clip = m["shadow_world_to_clip"].reshape(4, 4)
+        main.shadow_strength = np.asarray(m["shadow_strength"], F32)
+    return depth, main
+
+
+def _rast_batch(jobs: np.ndarray, pools: Dict[str, torch.Tensor], zbuffer: torch.Tensor,
+                canvas: Optional[torch.Tensor], prim_id: Optional[torch.Tensor], ties, keep: list):
+    jt = torch.from_numpy(jobs.view(np.uint8).copy()).to(zbuffer.device)
+    keep.append(jt)
+    b = _lib.RastBatch()
+    b.jobs = jt.data_ptr()
+    b.n_jobs = len(jobs)
+    b.max_width = int(jobs["width"].max())
+    b.max_height = int(jobs["height"].max())
+    b.max_verts = int(jobs["n_verts"].max())
+    b.max_faces = int(jobs["n_faces"].max())
+    b.shader_mask = int(np.bitwise_or.reduce(1 << jobs["shader"].astype(np.int64)))
+    b.total_vout = int(jobs["n_verts"].astype(np.int64).sum())
+    b.total_setup = int(jobs["n_faces"].astype(np.int64).sum())
+    b.total_pixels = int((jobs["width"].astype(np.int64) * jobs["height"]).sum())
+    P = b.pools
+    for name, t in pools.items():
+        setattr(P, name, t.data_ptr())
+    P.zbuffer = zbuffer.data_ptr()
+    P.canvas = canvas.data_ptr() if canvas is not None else None
+    P.prim_id = prim_id.data_ptr() if prim_id is not None else None
+    b.near_ties = ties.data_ptr() if ties is not None else None
+    return b
+
+
+@dataclass
+class BatchOutputs:
+    canvas: torch.Tensor  # (N, W, H, 3)
+    zbuffer: torch.Tensor  # (N, W, H)
+    prim_id: Optional[torch.Tensor]  # (N, W, H)
+    shadow_map: Optional[torch.Tensor]  # (N, Ws, Hs)
+    shadow_prim_id: Optional[torch.Tensor]
+    near_ties: Optional[torch.Tensor]
+
+
+class BatchRunner:
+    """Reusable outputs + workspaces for repeated renders of one SceneBatch."""
+
+    def __init__(self, sb: SceneBatch, form: str = "plain", want_prim_id: bool = True, count_ties: bool = False):
+        self.sb = sb
+        self.form = form
+        dev = sb.device
+        n, W, H = sb.n_scenes, sb.width, sb.height
+        self.canvas = torch.empty((n, W, H, 3), dtype=torch.float32, device=dev)
+        self.zbuffer = torch.empty((n, W, H), dtype=torch.float32, device=dev)
+        self.prim_id = torch.empty((n, W, H), dtype=torch.int32, device=dev) if want_prim_id else None
+        self.ties = torch.zeros(1, dtype=torch.int64, device=dev) if count_ties else None
+        self.shadow_map = None
+        self.shadow_prim = None
+        self.keep = []
+        lib = _lib.load()
+        self.lib = lib
+        if sb.shadow_jobs is not None:
+            self.shadow_map = torch.empty((n, sb.shadow_width, sb.shadow_height), dtype=torch.float32, device=dev)
+            self.shadow_prim = torch.empty_like(self.shadow_map, dtype=torch.int32) if want_prim_id else None
+            self.shadow_batch = _rast_batch(sb.shadow_jobs, sb.pools, self.shadow_map, None, self.shadow_prim, None, self.keep)
+            pools = dict(sb.pools)
+            pools["shadow_map"] = self.shadow_map
+        else:
+            self.shadow_batch = None
+            pools = sb.pools
+        self.main_batch = _rast_batch(sb.main_jobs, pools, self.zbuffer, self.canvas, self.prim_id, self.ties, self.keep)
+        self.ws = {}
+        for name, b in (("shadow", self.shadow_batch), ("main", self.main_batch)):
+            if b is None:
+                continue
+            nbytes = int(self._ws_bytes(b))
+            self.ws[name] = (torch.empty(max(nbytes, 256), dtype=torch.uint8, device=dev), nbytes)
+
+    def _ws_bytes(self, b) -> int:
+        if self.form == "plain":
+            return self.lib.rast_plain_workspace_bytes(ctypes.byref(b))
+        return self.lib.rast_tiled_workspace_bytes(ctypes.byref(b))
+
+    def _launch(self, b, ws, stream) -> None:
+        buf, nbytes = ws
+        if self.form == "plain":
+            st = self.lib.rast_render_plain(ctypes.byref(b), buf.data_ptr(), nbytes, stream)
+        else:
+            st = self.lib.rast_render_tiled(ctypes.byref(b), buf.data_ptr(), nbytes, stream)
+        _lib.check(st, f"rast_render_{self.form}")
+
+    def run(self, stream: Optional[torch.cuda.Stream] = None, zbuffer_default: float = 1.0,
+            colour_default=(1.0, 1.0, 1.0)) -> BatchOutputs:
+        """Reset the buffers to their defaults and render every scene
+        (depth pass, then main pass) on `stream`."""
+        s = stream if stream is not None else torch.cuda.current_stream(self.sb.device)
+        with torch.cuda.stream(s):
+            self.zbuffer.fill_(zbuffer_default)
+            self.canvas.copy_(torch.tensor(colour_default, dtype=torch.float32, device=self.sb.device).expand_as(self.canvas))
+            if self.shadow_batch is not None:
+                self.shadow_map.fill_(float(np.finfo(np.float32).max))
+                self._launch(self.shadow_batch, self.ws["shadow"], s.cuda_stream)
+            self._launch(self.main_batch, self.ws["main"], s.cuda_stream)
+        return BatchOutputs(self.canvas, self.zbuffer, self.prim_id, self.shadow_map, self.shadow_prim, self.ties)
+
+
+def render_batch(sb: SceneBatch, form: str = "plain", want_prim_id: bool = True) -> BatchOutputs:
+    """Render every scene of `sb` (see BatchRunner)."""
+    return BatchRunner(sb, form=form, want_prim_id=want_prim_id).run()
+
+
+__all__ = ["SceneBatch", "SceneTables", "scene_batch_tables", "scene_batch_from_flat", "scene_job_specs",
+           "flat_pools", "render_batch", "BatchRunner", "BatchOutputs", "job_table"]

@@ -1,0 +1,217 @@
+// rast_internal.cuh -- pieces shared by the plain and tiled forms: the
+// primitive-setup record, the per-pixel resolve (chooser fallback,
+// barycentrics, fragment, mixer) and buffer merge.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+
+#include "rast_shaders.cuh"
+
+namespace rast {
+
+constexpr int kTile = 16;         // plain form: 16x16 pixels per CTA
+constexpr int kScanThreads = kTile * kTile;
+constexpr int kScanChunk = 512;   // primitive setups staged per shared-memory chunk
+
+// Setup record flags (float bits of record[3].y).
+constexpr int kKeep = 1;          // |det| > 1e-6 (pipeline.py:98-100)
+constexpr int kFront = 2;         // det >= 0 (pipeline.py:232)
+constexpr int kCandidate = kKeep | kFront;
+
+inline size_t align256(size_t x) { return (x + 255) & ~static_cast<size_t>(255); }
+
+// Last job whose *_begin <= row (jobs are laid out in increasing order).
+template <typename Get>
+__device__ __forceinline__ int find_job(const RastJob* jobs, int n, int64_t row, Get get) {
+  int lo = 0, hi = n;  // answer in [lo, hi)
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (get(jobs[mid]) <= row) lo = mid; else hi = mid;
+  }
+  return lo;
+}
+__device__ __forceinline__ int find_job_by_vout(const RastJob* jobs, int n, int64_t row) {
+  return find_job(jobs, n, row, [](const RastJob& j) { return j.vout_begin; });
+}
+__device__ __forceinline__ int find_job_by_setup(const RastJob* jobs, int n, int64_t row) {
+  return find_job(jobs, n, row, [](const RastJob& j) { return j.setup_begin; });
+}
+
+// PerPrimitive.create (pipeline.py:80-113) from the three clip positions.
+// Record: [inv0..3] [inv4..7] [inv8 z0 z1 z2] [det flags 0 0].
+__device__ __forceinline__ void setup_from_clip(const float4* c, float* inv, float* det_out,
+                                                int* flags_out) {
+  const float m[9] = {c[0].x, c[0].y, c[0].w, c[1].x, c[1].y, c[1].w, c[2].x, c[2].y, c[2].w};
+  const float det = det3(m);
+  inv3(m, inv);
+  int flags = 0;
+  if (fabsf(det) > 1e-6f) flags |= kKeep;
+  if (det >= 0.0f) flags |= kFront;
+  *det_out = det;
+  *flags_out = flags;
+}
+
+__device__ __forceinline__ void write_setup(const float4* c, float4* out) {
+  float inv[9], det;
+  int flags;
+  setup_from_clip(c, inv, &det, &flags);
+  out[0] = make_float4(inv[0], inv[1], inv[2], inv[3]);
+  out[1] = make_float4(inv[4], inv[5], inv[6], inv[7]);
+  out[2] = make_float4(inv[8], c[0].z, c[1].z, c[2].z);
+  out[3] = make_float4(det, __int_as_float(flags), 0.0f, 0.0f);
+}
+
+__device__ __forceinline__ bool is_near_tie(unsigned long long best, uint32_t second) {
+  const uint32_t o1 = static_cast<uint32_t>(best >> 32);
+  return best != kEmptyKey && o1 != kInfOrder && second != 0xffffffffu && second - o1 <= 1u;
+}
+
+// Warp-aggregated count of near ties; every lane of the warp must call it.
+__device__ __forceinline__ void count_near_tie(unsigned long long* counter, bool tie) {
+  const unsigned m = __ballot_sync(0xffffffffu, tie);
+  if ((threadIdx.x + threadIdx.y * blockDim.x) % 32 == 0 && m)
+    atomicAdd(counter, static_cast<unsigned long long>(__popc(m)));
+}
+
+__device__ __forceinline__ void load_job_to_shared(const RastJob* job, RastJob* dst) {
+  const int nthreads = blockDim.x * blockDim.y;
+  const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+  const int* src = reinterpret_cast<const int*>(job);
+  int* d = reinterpret_cast<int*>(dst);
+  for (int k = tid; k < static_cast<int>(sizeof(RastJob) / 4); k += nthreads) d[k] = __ldg(src + k);
+}
+
+// Where the vertex varyings of a face come from: the vertex kernel's output
+// (plain form) or a recomputation of the vertex shader (tiled form).
+struct VaryingSource {
+  const float* var;   // nullptr: recompute
+  int vstride;
+  int64_t vout_begin;
+};
+
+struct PixelResult {
+  bool keep;
+  float z;
+  float colour[3];
+  int prim;
+};
+
+// One pixel after the scan: `w` is the winning candidate (-1: none, or its
+// depth was +inf).  Reproduces the default chooser's fallback to primitive 0
+// (shader.py:215-217), then Shader.interpolate / fragment / mix
+// (pipeline.py:283-359) for the chosen primitive.
+__device__ __forceinline__ void resolve_pixel(const RastJob& J, const RastPools& P,
+                                              const float4* rec_base, int i, int j, int w,
+                                              const VaryingSource& src, PixelResult* r) {
+  r->keep = false;
+  r->prim = -1;
+  r->z = 0.0f;
+  r->colour[0] = r->colour[1] = r->colour[2] = 0.0f;
+  if (J.n_faces <= 0) return;
+  const int p = w < 0 ? 0 : w;
+  const float4* rec = rec_base + static_cast<int64_t>(p) * 4;
+  const float4 a = rec[0], b = rec[1], cz = rec[2], d = rec[3];
+  const float x = (static_cast<float>(i) - J.viewport[3]) / J.viewport[0];
+  const float y = (static_cast<float>(j) - J.viewport[7]) / J.viewport[5];
+  const float c[3] = {(x * a.x + y * a.w) + b.z, (x * a.y + y * b.x) + b.w,
+                      (x * a.z + y * b.y) + cz.x};
+  const bool in_tri = c[0] >= 0.0f && c[1] >= 0.0f && c[2] >= 0.0f;
+  const int flags = __float_as_int(d.y);
+  const bool chooser_keep = (flags & kKeep) && in_tri;
+  const bool front = (flags & kFront) != 0;
+  const float w_rcp = (c[0] + c[1]) + c[2];
+  const float z = ((c[0] * cz.y + c[1] * cz.z) + c[2] * cz.w) * J.viewport[10] + J.viewport[11];
+  const float bary[3] = {c[0] / w_rcp, c[1] / w_rcp, c[2] / w_rcp};
+  const int32_t* face = P.faces + (J.face_begin + p) * 3;
+  const int nv = varying_count(J.shader);
+  float v0[kMaxVarying], v1[kMaxVarying], v2[kMaxVarying];
+  if (nv > 0) {
+    const int i0 = gather_clamp(face[0], J.n_verts);
+    const int i1 = gather_clamp(face[1], J.n_verts);
+    const int i2 = gather_clamp(face[2], J.n_verts);
+    if (src.var) {
+      const float* r0 = src.var + (src.vout_begin + i0) * src.vstride;
+      const float* r1 = src.var + (src.vout_begin + i1) * src.vstride;
+      const float* r2 = src.var + (src.vout_begin + i2) * src.vstride;
+      for (int k = 0; k < nv; ++k) {
+        v0[k] = r0[k];
+        v1[k] = r1[k];
+        v2[k] = r2[k];
+      }
+    } else {
+      float clip[4];
+      vertex_shader(J, P, i0, clip, v0);
+      vertex_shader(J, P, i1, clip, v1);
+      vertex_shader(J, P, i2, clip, v2);
+    }
+  }
+  const bool frag_keep = fragment_shader(J, P, v0, v1, v2, bary, front, r->colour);
+  r->keep = chooser_keep && frag_keep;
+  r->z = z;
+  r->prim = r->keep ? p : -1;
+}
+
+// merge_buffers (pipeline.py:401-440): overwrite where kept, no depth test;
+// then the shadow pass's offset (shadow.py:116) when the job asks for it.
+__device__ __forceinline__ void store_pixel(const RastJob& J, const RastPools& P, int64_t pix,
+                                            const PixelResult& r) {
+  const bool offset = (J.flags & RAST_JOB_APPLY_DEPTH_OFFSET) != 0;
+  if (r.keep || offset) {
+    float zb = r.keep ? r.z : P.zbuffer[pix];
+    if (offset) zb = zb + J.depth_offset;
+    P.zbuffer[pix] = zb;
+  }
+  if (r.keep && J.shader != RAST_SHADER_DEPTH && P.canvas) {
+    P.canvas[pix * 3 + 0] = r.colour[0];
+    P.canvas[pix * 3 + 1] = r.colour[1];
+    P.canvas[pix * 3 + 2] = r.colour[2];
+  }
+  if (P.prim_id) P.prim_id[pix] = r.prim;
+}
+
+// Optional per-kernel event timing of an entry point (RastProfile).
+struct Profiler {
+  RastProfile* prof;
+  cudaStream_t stream;
+  cudaEvent_t ev[17];
+  int n = 0;
+  Profiler(RastProfile* p, cudaStream_t s) : prof(p), stream(s) {
+    if (prof) {
+      prof->n = 0;
+      cudaEventCreate(&ev[0]);
+      cudaEventRecord(ev[0], stream);
+    }
+  }
+  void mark(const char* name) {
+    if (!prof || n >= 16) return;
+    cudaEventCreate(&ev[n + 1]);
+    cudaEventRecord(ev[n + 1], stream);
+    prof->names[n] = name;
+    ++n;
+  }
+  int finish() {
+    if (!prof) return RAST_OK;
+    if (cudaStreamSynchronize(stream) != cudaSuccess) return RAST_ERR_CUDA;
+    for (int k = 0; k < n; ++k) cudaEventElapsedTime(&prof->ms[k], ev[k], ev[k + 1]);
+    for (int k = 0; k <= n; ++k) cudaEventDestroy(ev[k]);
+    prof->n = n;
+    return RAST_OK;
+  }
+};
+
+// Host-side argument checks shared by the entry points.
+inline int check_batch(const RastBatch* b) {
+  if (!b || !b->jobs) return RAST_ERR_INVALID_ARGUMENT;
+  if (b->n_jobs < 1 || b->n_jobs > 65535) return RAST_ERR_INVALID_ARGUMENT;
+  if (b->total_vout < 0 || b->total_setup < 0 || b->total_pixels < 0) return RAST_ERR_INVALID_ARGUMENT;
+  if (b->max_width < 0 || b->max_height < 0 || b->max_faces < 0 || b->max_verts < 0)
+    return RAST_ERR_INVALID_ARGUMENT;
+  if ((b->shader_mask & ~0x7f) != 0) return RAST_ERR_INVALID_ARGUMENT;
+  if (b->total_pixels > 0 && !b->pools.zbuffer) return RAST_ERR_INVALID_ARGUMENT;
+  if (b->total_setup > 0 && (!b->pools.faces || !b->pools.position)) return RAST_ERR_INVALID_ARGUMENT;
+  if (b->total_vout > 0 && !b->pools.position) return RAST_ERR_INVALID_ARGUMENT;
+  return RAST_OK;
+}
+
+}  // namespace rast

@@ -1,0 +1,68 @@
+"""pipeline.render (renderer/pipeline.py:470-537) on the GPU.
+
+One call renders one job: the vertex shader over every vertex of
+`extra[0]`, primitive set-up of every face of `face_indices`, the per-pixel
+scan over every primitive, and the chosen primitive's interpolation,
+fragment shader and mixer, merged into `buffers` without a depth test.  The
+input buffers are not modified: new device buffers are returned, as the
+reference's functional API returns new arrays.
+"""
+from __future__ import annotations
+
+from typing import Optional, Tuple
+
+import numpy as np
+import torch
+
+from . import jobs as _jobs
+from .geometry import Camera
+from .shader import kernel_id_of
+from .types import Buffers
+
+
+def default_device() -> torch.device:
+    if not torch.cuda.is_available():
+        raise RuntimeError("jaxrenderer_gb300 renders on a CUDA GPU only; none is visible")
+    return torch.device("cuda", torch.cuda.current_device())
+
+
+def _faces(face_indices):
+    if isinstance(face_indices, torch.Tensor):
+        return face_indices.to(torch.int32).reshape(-1, 3)
+    return np.ascontiguousarray(np.asarray(face_indices, dtype=np.int32).reshape(-1, 3))
+
+
+def render_job(spec: _jobs.JobSpec, zbuffer, canvas, device=None, count_ties: bool = False):
+    """Render one JobSpec; returns (zbuffer, canvas or None, prim_id, near_ties tensor or None)."""
+    device = device if device is not None else default_device()
+    packed = _jobs.pack([spec], [zbuffer], [canvas], device, want_prim_id=True, count_ties=count_ties)
+    _jobs.render_plain(packed)
+    z, c, p = _jobs.unpack(packed, [spec])[0]
+    return z, c, p, packed.near_ties
+
+
+def render_with_ids(camera: Camera, shader, buffers: Buffers, face_indices, extra,
+                    loop_unroll: int = 1, count_ties: bool = False):
+    """pipeline.render that also returns the winning-primitive buffer
+    ((W, H) int32, -1 where nothing was written) and the near-tie count."""
+    sid = kernel_id_of(shader)
+    zbuffer = buffers.zbuffer
+    width, height = int(zbuffer.shape[0]), int(zbuffer.shape[1])
+    spec = _jobs.job_from_extra(sid, camera, extra, width, height)
+    spec.faces = _faces(face_indices)
+    canvas = buffers.targets[0] if len(buffers.targets) > 0 else None
+    z, c, p, ties = render_job(spec, zbuffer, canvas, count_ties=count_ties)
+    targets = (c,) if c is not None else ()
+    return Buffers(zbuffer=z, targets=targets), p, ties
+
+
+def render(camera: Camera, shader, buffers: Buffers, face_indices, extra, loop_unroll: int = 1) -> Buffers:
+    """Render a scene with a built-in shader (pipeline.py:470-537).
+
+    `loop_unroll` is accepted for API compatibility; the CUDA kernels have
+    no row loop to unroll.
+    """
+    return render_with_ids(camera, shader, buffers, face_indices, extra, loop_unroll)[0]
+
+
+__all__ = ["render", "render_with_ids", "render_job", "default_device"]

@@ -1,0 +1,285 @@
+"""Seeded synthetic scenes for the benchmark workloads and the parity tests.
+
+The reference benchmarks on Brax Ant scenes it renders in notebooks; the
+workloads here are seeded stand-ins with the stated shapes: a ground plane
+plus 8-32 objects drawn from {box 12 tris, icosphere level 2 (320 tris),
+capsule 16x8 segments (~512 tris)} per 84x84 scene, and so on.  Generators
+use numpy's PCG64 with seed 20230701 + workload index.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass
+from typing import List, Optional, Sequence, Tuple
+
+import numpy as np
+
+from .geometry import Camera, normalise, transform_matrix_from_rotation
+from .model import Model, ModelObject
+from .shapes.cube import create_cube
+
+F32 = np.float32
+BASE_SEED = 20230701
+
+
+def icosphere(level: int) -> Tuple[np.ndarray, np.ndarray]:
+    """Unit icosphere: 20 * 4**level faces, shared vertices, CCW outward."""
+    t = (1.0 + 5.0 ** 0.5) / 2.0
+    v = [(-1, t, 0), (1, t, 0), (-1, -t, 0), (1, -t, 0), (0, -1, t), (0, 1, t), (0, -1, -t), (0, 1, -t),
+         (t, 0, -1), (t, 0, 1), (-t, 0, -1), (-t, 0, 1)]
+    f = [(0, 11, 5), (0, 5, 1), (0, 1, 7), (0, 7, 10), (0, 10, 11), (1, 5, 9), (5, 11, 4), (11, 10, 2),
+         (10, 7, 6), (7, 1, 8), (3, 9, 4), (3, 4, 2), (3, 2, 6), (3, 6, 8), (3, 8, 9), (4, 9, 5),
+         (2, 4, 11), (6, 2, 10), (8, 6, 7), (9, 8, 1)]
+    verts = [np.array(p, dtype=np.float64) / np.linalg.norm(p) for p in v]
+    faces = list(f)
+    for _ in range(level):
+        cache = {}
+
+        def mid(a, b):
+            key = (min(a, b), max(a, b))
+            if key not in cache:
+                m = verts[a] + verts[b]
+                verts.append(m / np.linalg.norm(m))
+                cache[key] = len(verts) - 1
+            return cache[key]
+
+        nf = []
+        for a, b, c in faces:
+            ab, bc, ca = mid(a, b), mid(b, c), mid(c, a)
+            nf += [(a, ab, ca), (b, bc, ab), (c, ca, bc), (ab, bc, ca)]
+        faces = nf
+    return np.asarray(verts, dtype=F32), np.asarray(faces, dtype=np.int32)
+
+
+def sphere_uv(verts: np.ndarray) -> np.ndarray:
+    u = 0.5 + np.arctan2(verts[:, 1], verts[:, 0]) / (2 * np.pi)
+    w = 0.5 + np.arcsin(np.clip(verts[:, 2], -1, 1)) / np.pi
+    return np.stack([u, w], axis=1).astype(F32)
+
+
+def capsule_mesh(segments: int = 16, rings: int = 8, half_height: float = 0.5) -> Tuple[np.ndarray, np.ndarray]:
+    """Capsule with `segments` around and `rings` latitude bands per hemisphere
+    plus a cylinder band; pole bands are fans: 16x8 -> 512 triangles."""
+    verts = []
+    lat = []
+    for r in range(rings + 1):  # north hemisphere, pole to equator
+        lat.append((np.pi / 2 * r / rings, +half_height))
+    for r in range(rings + 1):  # south hemisphere, equator to pole
+        lat.append((np.pi / 2 + np.pi / 2 * r / rings, -half_height))
+    for theta, dz in lat:
+        for s in range(segments):
+            phi = 2 * np.pi * s / segments
+            verts.append((np.sin(theta) * np.cos(phi), np.sin(theta) * np.sin(phi), np.cos(theta) + dz))
+    faces = []
+    nrow = len(lat)
+    for r in range(nrow - 1):
+        for s in range(segments):
+            a = r * segments + s
+            b = r * segments + (s + 1) % segments
+            c = (r + 1) * segments + s
+            d = (r + 1) * segments + (s + 1) % segments
+            if r == 0:  # north pole fan
+                faces.append((a, c, d))
+            elif r == nrow - 2:  # south pole fan
+                faces.append((a, c, b))
+            else:
+                faces.append((a, c, d))
+                faces.append((a, d, b))
+    return np.asarray(verts, dtype=F32), np.asarray(faces, dtype=np.int32)
+
+
+def _normals_of(verts: np.ndarray, centre_z: Optional[np.ndarray] = None) -> np.ndarray:
+    n = verts.astype(np.float64).copy()
+    if centre_z is not None:
+        n[:, 2] -= centre_z
+    return (n / np.linalg.norm(n, axis=1, keepdims=True)).astype(F32)
+
+
+_PRIMS = {}
+
+
+def primitive_model(kind: str, colour: np.ndarray, specular: float = 2.0) -> Model:
+    """One of the workload primitives with a 4x4 texture of `colour`."""
+    tex = np.broadcast_to(np.asarray(colour, F32), (4, 4, 3)).copy()
+    spec = np.full((4, 4), specular, F32)
+    if kind == "box":
+        return create_cube(np.ones(3, F32) * 0.5, np.ones(2, F32), tex, spec)
+    if kind not in _PRIMS:
+        if kind == "icosphere2":
+            v, f = icosphere(2)
+            v = v * F32(0.5)
+            _PRIMS[kind] = (v, _normals_of(v), sphere_uv(v), f)
+        elif kind == "capsule":
+            v, f = capsule_mesh(16, 8, 0.5)
+            cz = np.where(v[:, 2] > 0, 0.5, -0.5).astype(np.float64)
+            n = _normals_of(v, cz)
+            v = v * F32(0.4)
+            _PRIMS[kind] = (v.astype(F32), n, sphere_uv(n), f)
+        else:
+            raise ValueError(kind)
+    v, n, uv, f = _PRIMS[kind]
+    return Model(verts=v, norms=n, uvs=uv, faces=f, faces_norm=f, faces_uv=f, diffuse_map=tex, specular_map=spec)
+
+
+def random_rotation(rng: np.random.Generator) -> np.ndarray:
+    q = rng.normal(size=4)
+    q = q / np.linalg.norm(q)
+    return transform_matrix_from_rotation(q.astype(F32))
+
+
+@dataclass
+class BraxLikeScene:
+    objects: List[ModelObject]
+    camera_position: np.ndarray
+    n_faces: int
+
+
+def brax_like_scene(rng: np.random.Generator) -> BraxLikeScene:
+    """Ground plane (2 triangles, 10x10) plus 8..32 random objects, camera on
+    a radius-6 sphere at elevation U[20, 60] deg, azimuth U[0, 360) deg."""
+    objects = []
+    ground_tex = np.broadcast_to(rng.uniform(0, 1, 3).astype(F32), (4, 4, 3)).copy()
+    gv = np.array([(-5, -5, 0), (5, -5, 0), (5, 5, 0), (-5, 5, 0)], F32)
+    gf = np.array([(0, 1, 2), (0, 2, 3)], np.int32)
+    gn = np.tile(np.array([(0, 0, 1)], F32), (4, 1))
+    guv = np.array([(0, 0), (4, 0), (4, 4), (0, 4)], F32)
+    ground = Model(gv, gn, guv, gf, gf, gf, ground_tex, np.full((4, 4), 2.0, F32))
+    objects.append(ModelObject(model=ground))
+    n_obj = int(rng.integers(8, 33))
+    kinds = ("box", "icosphere2", "capsule")
+    nf = 2
+    for _ in range(n_obj):
+        kind = kinds[int(rng.integers(0, 3))]
+        model = primitive_model(kind, rng.uniform(0, 1, 3))
+        t = np.identity(4, dtype=F32)
+        t[:3, :3] = random_rotation(rng)
+        t[:3, 3] = (rng.uniform(-3, 3), rng.uniform(-3, 3), rng.uniform(0, 2))
+        s = F32(rng.uniform(0.2, 1.0))
+        objects.append(ModelObject(model=model, local_scaling=np.full(3, s, F32), transform=t))
+        nf += len(model.faces)
+    elev = np.deg2rad(rng.uniform(20, 60))
+    azim = np.deg2rad(rng.uniform(0, 360))
+    pos = 6.0 * np.array([np.cos(elev) * np.cos(azim), np.cos(elev) * np.sin(azim), np.sin(elev)])
+    return BraxLikeScene(objects=objects, camera_position=pos.astype(F32), n_faces=nf)
+
+
+def random_triangle_soup(rng: np.random.Generator, n_faces: int, spread: float = 1.5,
+                         size: float = 0.6, shared: bool = False) -> Tuple[np.ndarray, np.ndarray]:
+    """Random triangles around the origin, some crossing z = camera planes,
+    with duplicates (exact depth ties) and degenerate ones mixed in."""
+    centres = rng.uniform(-spread, spread, size=(n_faces, 1, 3))
+    offs = rng.normal(scale=size, size=(n_faces, 3, 3))
+    tri = (centres + offs).astype(F32)
+    if n_faces >= 8:
+        k = max(1, n_faces // 16)
+        tri[-k:] = tri[:k]  # exact duplicates: ties resolved by lowest id
+        tri[k, 2] = tri[k, 1]  # degenerate (zero area)
+    verts = tri.reshape(-1, 3)
+    faces = np.arange(verts.shape[0], dtype=np.int32).reshape(-1, 3)
+    return verts, faces
+
+
+__all__ = [
+    "icosphere",
+    "capsule_mesh",
+    "primitive_model",
+    "brax_like_scene",
+    "random_triangle_soup",
+    "BASE_SEED",
+]
+
+
+# --------------------------------------------------- batched Brax-like workload
+
+_KINDS = ("box", "icosphere2", "capsule")
+
+
+def _base_mesh(kind: str):
+    m = primitive_model(kind, np.zeros(3, F32))
+    return np.asarray(m.verts, F32), np.asarray(m.norms, F32), np.asarray(m.uvs, F32), np.asarray(m.faces, np.int32)
+
+
+@dataclass
+class FlatScenes:
+    """Many merged scenes, flattened per face corner, in flat arrays.
+
+    Scene s owns corner rows [corner_begin[s], corner_begin[s] + 3 * n_faces[s])
+    of position/normal/uv/texture_index, faces 3 * arange within them, and
+    texture rows [tex_begin[s], tex_begin[s] + 4 * n_objects[s]) of the 4x4
+    diffuse (RGB) and specular maps.
+    """
+
+    position: np.ndarray
+    normal: np.ndarray
+    uv: np.ndarray
+    texture_index: np.ndarray
+    texture: np.ndarray
+    specular_map: np.ndarray
+    corner_begin: np.ndarray
+    n_faces: np.ndarray
+    tex_begin: np.ndarray
+    n_objects: np.ndarray
+    camera_position: np.ndarray
+
+    @property
+    def n_scenes(self) -> int:
+        return int(self.n_faces.shape[0])
+
+
+def brax_like_batch(n_scenes: int, seed: int = BASE_SEED + 1) -> FlatScenes:
+    """`n_scenes` Brax-like scenes (see brax_like_scene), already merged and
+    flattened per face corner.  Object vertices are scaled, rotated and
+    translated; normals go through the rotation (the inverse-transpose of a
+    rotation times a uniform scale, normalised per vertex)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    bases = {k: _base_mesh(k) for k in _KINDS}
+    gv = np.array([(-5, -5, 0), (5, -5, 0), (5, 5, 0), (-5, 5, 0)], F32)
+    gf = np.array([(0, 1, 2), (0, 2, 3)], np.int32)
+    guv = np.array([(0, 0), (4, 0), (4, 4), (0, 4)], F32)
+    n_obj = rng.integers(8, 33, size=n_scenes)
+    kinds = [rng.integers(0, 3, size=int(k)) for k in n_obj]
+    quats = [rng.normal(size=(int(k), 4)) for k in n_obj]
+    trans = [np.stack([rng.uniform(-3, 3, int(k)), rng.uniform(-3, 3, int(k)), rng.uniform(0, 2, int(k))], 1) for k in n_obj]
+    scales = [rng.uniform(0.2, 1.0, int(k)) for k in n_obj]
+    colours = [rng.uniform(0, 1, (int(k) + 1, 3)) for k in n_obj]
+    elev = np.deg2rad(rng.uniform(20, 60, n_scenes))
+    azim = np.deg2rad(rng.uniform(0, 360, n_scenes))
+    cam = 6.0 * np.stack([np.cos(elev) * np.cos(azim), np.cos(elev) * np.sin(azim), np.sin(elev)], 1)
+    face_counts = {k: bases[k][3].shape[0] for k in _KINDS}
+    n_faces = np.array([2 + sum(face_counts[_KINDS[int(t)]] for t in ks) for ks in kinds], np.int64)
+    corner_begin = np.concatenate([[0], np.cumsum(3 * n_faces)[:-1]]).astype(np.int64)
+    total = int(3 * n_faces.sum())
+    position = np.empty((total, 3), F32)
+    normal = np.empty((total, 3), F32)
+    uv = np.empty((total, 2), F32)
+    tex_idx = np.empty(total, np.int32)
+    objs = n_obj + 1
+    tex_begin = np.concatenate([[0], np.cumsum(4 * objs)[:-1]]).astype(np.int64)
+    texture = np.empty((int(4 * objs.sum()), 4, 3), F32)
+    specular = np.full((int(4 * objs.sum()), 4), 2.0, F32)
+    for s in range(n_scenes):
+        row = corner_begin[s]
+        corners = gv[gf.reshape(-1)]
+        position[row : row + 6] = corners
+        normal[row : row + 6] = (0, 0, 1)
+        uv[row : row + 6] = guv[gf.reshape(-1)]
+        tex_idx[row : row + 6] = 0
+        row += 6
+        q = quats[s] / np.linalg.norm(quats[s], axis=1, keepdims=True)
+        for o, t in enumerate(kinds[s]):
+            v, n, u, f = bases[_KINDS[int(t)]]
+            R = transform_matrix_from_rotation(q[o].astype(F32)).astype(F32)
+            sc = F32(scales[s][o])
+            idx = f.reshape(-1)
+            p = (v[idx] * sc) @ R.T + trans[s][o].astype(F32)
+            nn = n[idx] @ R.T
+            nn = nn / np.linalg.norm(nn, axis=1, keepdims=True)
+            k = idx.size
+            position[row : row + k] = p
+            normal[row : row + k] = nn
+            uv[row : row + k] = u[idx]
+            tex_idx[row : row + k] = o + 1
+            row += k
+        tb = tex_begin[s]
+        texture[tb : tb + 4 * objs[s]] = np.repeat(colours[s], 4, axis=0)[:, None, :].astype(F32)
+    return FlatScenes(position, normal, uv, tex_idx, texture, specular, corner_begin, n_faces.astype(np.int32),
+                      tex_begin, objs.astype(np.int32), cam.astype(F32))
