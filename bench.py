@@ -50,6 +50,7 @@ def parse():
     p.add_argument("--scenes", type=int, default=N_SCENES)
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-plain", action="store_true")
     return p.parse_args()
 
 
@@ -172,14 +173,11 @@ def run_ours(args, rank, world, local):
     if world > 1:
         import torch.distributed as dist
 
-        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+        dist.init_process_group("nccl")
     _lib.load()
-    form = args.form
-    if form == "auto":
-        form = "tiled" if hasattr(_lib.load(), "rast_render_tiled") else "plain"
+    form = "tiled" if args.form == "auto" else args.form
     flat = synthetic.brax_like_batch(args.scenes, seed=synthetic.BASE_SEED + 1 + rank)
     sb = jb.scene_batch_from_flat(flat, W, H, shadow_size=SHADOW, device=dev)
-    runner = jb.BatchRunner(sb, form=form, want_prim_id=False)
     stream = torch.cuda.current_stream(dev)
 
     def barrier():
@@ -187,33 +185,50 @@ def run_ours(args, rank, world, local):
         if world > 1:
             torch.distributed.barrier()
 
-    for _ in range(args.warmup):
-        runner.run(stream)
-    barrier()
-    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with ClockSampler(local) as clk:
+    def timed(step_fn, steps, warmup, clocks=None):
+        for _ in range(warmup):
+            step_fn()
         barrier()
+        start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         start.record(stream)
-        for _ in range(args.steps):
-            runner.run(stream)
+        for _ in range(steps):
+            step_fn()
         stop.record(stream)
         barrier()
-    ms = start.elapsed_time(stop)
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    ms_per_step = ms / args.steps
-    value = world * args.scenes / (ms_per_step / 1e3)
+        ms = start.elapsed_time(stop)
+        if world > 1:
+            t = torch.tensor([ms], device=dev)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms / steps
 
-    # per-kernel durations: the same steps again with event timing inside the library
+    runner = jb.BatchRunner(sb, form=form, want_prim_id=False)
+    if form == "tiled":
+        runner.capture()
+        step = runner.replay
+    else:
+        step = lambda: runner.run(stream)  # noqa: E731
+    for _ in range(args.warmup):
+        step()
+    with ClockSampler(local) as clk:
+        ms_per_step = timed(step, args.steps, 0)
+    value = world * args.scenes / (ms_per_step / 1e3)
     prof = profile_kernels(runner, args.steps, stream)
+
+    comparison = {}
+    if form == "tiled" and not args.no_plain:
+        plain = jb.BatchRunner(sb, form="plain", want_prim_id=False)
+        pms = timed(lambda: plain.run(stream), max(1, min(args.steps, 3)), 1)
+        comparison = {"plain_fwd": world * args.scenes / (pms / 1e3), "plain_ms_per_step": pms,
+                      "tiled_over_plain": pms / ms_per_step}
+        del plain
+        torch.cuda.empty_cache()
 
     e2e = None
     if not args.no_e2e:
-        e2e = measure_e2e(flat, sb, runner, args, dev, stream, world)
+        e2e = measure_e2e(flat, sb, runner, step, args, dev, stream, world)
 
-    kernels_per_step = sum(1 for _ in prof["per_step_names"])
+    kernels_per_step = len(prof["per_step_names"])
     out = {
         "metric": METRIC,
         "value": value,
@@ -229,7 +244,8 @@ def run_ours(args, rank, world, local):
         "data": "synthetic (seeded Brax-like scenes; the reference's Brax fixtures are inputs-only pickles)",
         "config": {
             "workload": "brax-like 84x84 x 4096 scenes, phong_reflection_shadow + 128x128 depth pass",
-            "form": form,
+            "form": form + (" (CUDA graph replay)" if form == "tiled" else ""),
+            "tiled_config": {k: [c.tile_w, c.tile_h, int(c.bin_capacity)] for k, c in runner.configs.items()},
             "scenes": args.scenes,
             "mean_faces_per_scene": float(flat.n_faces.mean()),
             "resolution": [W, H],
@@ -237,7 +253,8 @@ def run_ours(args, rank, world, local):
             "l2": "inputs larger than L2 (per-corner pools %.2f GB)" % (flat.position.nbytes * 3 / 1e9),
             "parallelism": f"scene-sharded x{world} (no collective)",
         },
-        "roofline": roofline(prof, sb, flat),
+        "fwd_comparison": comparison,
+        "roofline": roofline(prof, sb, flat, runner),
         "kernels": prof["summary"],
         "gpu_launches": kernels_per_step * args.steps,
         "clocks": clk.summary(),
@@ -253,21 +270,16 @@ def run_ours(args, rank, world, local):
 
 
 def profile_kernels(runner, steps, stream):
-    import torch
+    """Per-kernel CUDA-event durations inside the library, same steps again."""
+    from jaxrenderer_gb300 import _lib
 
-    lib = runner.lib
     acc = {}
     names_order = []
     for _ in range(steps):
-        for key, b in (("shadow", runner.shadow_batch), ("main", runner.main_batch)):
-            if b is None:
-                continue
-            buf, nbytes = runner.ws[key]
-            prof = _lib_profile()
-            fn = lib.rast_render_plain_profiled if runner.form == "plain" else lib.rast_render_tiled_profiled
-            st = fn(ctypes.byref(b), buf.data_ptr(), nbytes, stream.cuda_stream, ctypes.byref(prof))
-            if st != 0:
-                raise RuntimeError(f"profiled render failed: {st}")
+        runner._reset(1.0)
+        for key, _b in runner.batches():
+            prof = _lib.RastProfile()
+            runner.launch(key, stream.cuda_stream, profile=prof)
             for k in range(prof.n):
                 name = f"{key}:{prof.names[k].decode()}"
                 if name not in acc:
@@ -287,31 +299,58 @@ def _lib_profile():
     return _lib.RastProfile()
 
 
-def roofline(prof, sb, flat):
+def kernel_bytes(kname, pass_name, sb, flat, runner):
+    """Algorithmic bytes one launch of `kname` must move (roofline):
+    inputs read once, outputs written once; re-reads served by caches are
+    not counted."""
+    F = int(flat.n_faces.sum())
+    corners = 3 * F
+    main = pass_name == "main"
+    pixels = sb.n_scenes * (W * H if main else SHADOW[0] * SHADOW[1])
+    entries = 0
+    if runner.form == "tiled":
+        entries = int(runner.stats(pass_name).bin_entries)
+    out_px = (4 + 12) if main else 4  # zbuffer (+ canvas) written
+    table = {
+        # plain form
+        "vertex_kernel": corners * (12 + (12 + 8 + 4 if main else 0)) + corners * (16 + (40 if main else 0)),
+        "setup_kernel": F * (12 + 3 * 16 + 64),
+        "scan_kernel": F * 48 + pixels * 4,
+        "shade_kernel": pixels * (4 + out_px + (4 if main else 0)),
+        # tiled form
+        "setup_bin_kernel": F * (12 + 36 + 64 + 8) + entries * 4,
+        "scan_kernels": runner_tiles(runner, pass_name) * 12,
+        "scatter_kernel": F * 8 + entries * 12,
+        "raster_kernel": F * 48 + entries * 4 + pixels * 4,
+        "tiled_shade_kernel": pixels * (4 + out_px + (4 if main else 0)),
+    }
+    return table.get(kname, 0), entries
+
+
+def runner_tiles(runner, pass_name):
+    if runner.form != "tiled":
+        return 0
+    return int(runner.stats(pass_name).tiles)
+
+
+def roofline(prof, sb, flat, runner):
     """HBM roofline of the dominant kernel: algorithmic bytes per launch /
-    average launch duration (bytes per unit stated in the design doc)."""
+    average launch duration (CUDA events inside the library)."""
     peak, kind = measured_peaks()
     summ = prof["summary"]
     dom = max(summ, key=lambda k: summ[k]["avg_ms"])
     ms = summ[dom]["avg_ms"]
     pass_name, kname = dom.split(":")
-    F = int(flat.n_faces.sum())
-    corners = 3 * F
-    if pass_name == "shadow":
-        pixels = sb.n_scenes * SHADOW[0] * SHADOW[1]
-    else:
-        pixels = sb.n_scenes * W * H
-    # algorithmic bytes per launch of each kernel
-    bytes_by_kernel = {
-        "vertex_kernel": corners * (12 + 12 + 8 + 4 + 16 + 40),
-        "setup_kernel": F * (12 + 3 * 16 + 64),
-        "scan_kernel": F * 64 * 1 + pixels * 4,
-        "shade_kernel": pixels * (4 + 4 + 12 + 4) + F * 64,
-    }
-    alg = bytes_by_kernel.get(kname, 0)
+    alg, entries = kernel_bytes(kname, pass_name, sb, flat, runner)
     achieved = alg / (ms / 1e3) / 1e9 if ms > 0 else 0.0
-    tests = pixels * (F / sb.n_scenes) * 1.0
-    return {
+    pixels = sb.n_scenes * (W * H if pass_name == "main" else SHADOW[0] * SHADOW[1])
+    per_kernel = {}
+    for name, v in summ.items():
+        pn, kn = name.split(":")
+        b, _ = kernel_bytes(kn, pn, sb, flat, runner)
+        per_kernel[name] = {"GB/s": b / (v["avg_ms"] / 1e3) / 1e9 if v["avg_ms"] > 0 else None,
+                            "frac": (b / (v["avg_ms"] / 1e3) / 1e9) / peak if v["avg_ms"] > 0 else None}
+    out = {
         "bound": "hbm",
         "kernel": dom,
         "achieved": achieved,
@@ -322,12 +361,17 @@ def roofline(prof, sb, flat):
         "traffic": None,
         "algorithmic_bytes_per_launch": alg,
         "avg_launch_ms": ms,
-        "pixel_triangle_tests_per_s": (pixels * float(flat.n_faces.mean()) / (ms / 1e3)) if kname == "scan_kernel" else None,
-        "note": "the plain scan kernel is FP32-issue bound, not HBM bound: see profiles/ for issue-slot utilisation",
+        "per_kernel": per_kernel,
     }
+    if kname in ("scan_kernel", "raster_kernel"):
+        tests = pixels * float(flat.n_faces.mean()) if kname == "scan_kernel" else None
+        out["coverage"] = {"pixel_triangle_tests_per_s": tests / (ms / 1e3) if tests else None,
+                           "bin_entries": entries or None,
+                           "note": "coverage is FP32-issue bound; issue-slot utilisation in profiles/"}
+    return out
 
 
-def measure_e2e(flat, sb, runner, args, dev, stream, world):
+def measure_e2e(flat, sb, runner, step, args, dev, stream, world):
     """Public-API path with host inputs: pinned host pools -> device, render,
     canvases -> pinned host, all inside the timed region."""
     import torch
@@ -342,20 +386,20 @@ def measure_e2e(flat, sb, runner, args, dev, stream, world):
     out_host = torch.empty(runner.canvas.shape, dtype=torch.float32, pin_memory=True)
     h2d = sum(host[n].numel() * host[n].element_size() for n in names)
     d2h = out_host.numel() * 4
-    steps = max(1, min(args.steps, 3))
-    for _ in range(1):
+
+    def e2e_step():
         for n in names:
             sb.pools[n].copy_(host[n], non_blocking=True)
-        runner.run(stream)
+        step()
         out_host.copy_(runner.canvas, non_blocking=True)
+
+    steps = max(1, min(args.steps, 5))
+    e2e_step()
     torch.cuda.synchronize(dev)
     start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     start.record(stream)
     for _ in range(steps):
-        for n in names:
-            sb.pools[n].copy_(host[n], non_blocking=True)
-        runner.run(stream)
-        out_host.copy_(runner.canvas, non_blocking=True)
+        e2e_step()
     stop.record(stream)
     torch.cuda.synchronize(dev)
     ms = start.elapsed_time(stop) / steps

@@ -168,6 +168,46 @@ typedef struct RastProfile {
 int rast_render_plain_profiled(const RastBatch* batch, void* workspace, size_t workspace_bytes,
                                void* stream, RastProfile* profile);
 
+/* Tiled form parameters (chosen by the autotuner).  Zero fields take the
+ * defaults: 8x8 tiles, bin capacity of 4 entries per face. */
+typedef struct RastTiledConfig {
+  int32_t tile_w;          /* tile width along x (buffer axis 0): 8, 16 or 32 */
+  int32_t tile_h;          /* tile height along y (buffer axis 1): 8, 16 or 32 */
+  uint64_t bin_capacity;   /* total (tile, primitive) bin entries reserved in the workspace */
+} RastTiledConfig;
+
+/* Workspace bytes rast_render_tiled needs for `batch` under `cfg` (NULL = defaults). */
+size_t rast_tiled_workspace_bytes(const RastBatch* batch, const RastTiledConfig* cfg);
+
+/* Tiled form for many scenes per call.  Per face: clip positions, set-up and
+ * a conservative tile range of its coverage (a superset of the pixels whose
+ * FP32 edge functions can pass); bin counts, exclusive prefix sum, scatter of
+ * primitive ids into per-tile bins; persistent warps rasterise one tile at a
+ * time with bin entries staged in shared memory (packed depth|id minimum per
+ * pixel); deferred shading of the winners.  Identical results to
+ * rast_render_plain.  Tiles whose bins exceed bin_capacity are rasterised by a
+ * scan over all primitives of their job (same results, slower).  Launches only
+ * kernels and memsets on `stream`: capturable in a CUDA graph. */
+int rast_render_tiled(const RastBatch* batch, const RastTiledConfig* cfg, void* workspace,
+                      size_t workspace_bytes, void* stream);
+
+/* rast_render_tiled with per-kernel timing (synchronises `stream`). */
+int rast_render_tiled_profiled(const RastBatch* batch, const RastTiledConfig* cfg, void* workspace,
+                               size_t workspace_bytes, void* stream, RastProfile* profile);
+
+/* Bin statistics of the last rast_render_tiled call that used `workspace`
+ * (synchronises `stream`; for autotuning and diagnostics). */
+typedef struct RastTiledStats {
+  uint64_t bin_entries;   /* (tile, primitive) pairs requested by the binning */
+  uint64_t bin_capacity;  /* entries reserved */
+  uint64_t tiles;         /* tile slots (jobs x tiles of the largest job) */
+  uint32_t overflow;      /* 1: some tiles exceeded the capacity and were full-scanned */
+  uint32_t reserved;
+} RastTiledStats;
+
+int rast_tiled_stats(const RastBatch* batch, const RastTiledConfig* cfg, const void* workspace,
+                     void* stream, RastTiledStats* out);
+
 /* Host-side validation of one job against pool sizes (no device access):
  * returns RAST_ERR_INVALID_ARGUMENT for inconsistent sizes. */
 int rast_validate_job(const RastJob* job);

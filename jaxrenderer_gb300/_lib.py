@@ -127,11 +127,26 @@ class RastProfile(ctypes.Structure):
     _fields_ = [("n", c_int32), ("ms", c_float * 16), ("names", ctypes.c_char_p * 16)]
 
 
+class RastTiledConfig(ctypes.Structure):
+    _fields_ = [("tile_w", c_int32), ("tile_h", c_int32), ("bin_capacity", c_uint64)]
+
+
+class RastTiledStats(ctypes.Structure):
+    _fields_ = [("bin_entries", c_uint64), ("bin_capacity", c_uint64), ("tiles", c_uint64),
+                ("overflow", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+
+
 # Exported symbols and their prototypes: (name, restype, argtypes).
 PROTOTYPES = [
     ("rast_plain_workspace_bytes", c_size_t, [POINTER(RastBatch)]),
     ("rast_render_plain", c_int, [POINTER(RastBatch), c_void_p, c_size_t, c_void_p]),
     ("rast_render_plain_profiled", c_int, [POINTER(RastBatch), c_void_p, c_size_t, c_void_p, POINTER(RastProfile)]),
+    ("rast_tiled_workspace_bytes", c_size_t, [POINTER(RastBatch), POINTER(RastTiledConfig)]),
+    ("rast_render_tiled", c_int, [POINTER(RastBatch), POINTER(RastTiledConfig), c_void_p, c_size_t, c_void_p]),
+    ("rast_render_tiled_profiled", c_int,
+     [POINTER(RastBatch), POINTER(RastTiledConfig), c_void_p, c_size_t, c_void_p, POINTER(RastProfile)]),
+    ("rast_tiled_stats", c_int,
+     [POINTER(RastBatch), POINTER(RastTiledConfig), c_void_p, c_void_p, POINTER(RastTiledStats)]),
     ("rast_validate_job", c_int, [POINTER(RastJob)]),
     ("rast_error_string", ctypes.c_char_p, [c_int]),
     ("rast_abi_version", c_int, []),
@@ -188,6 +203,8 @@ __all__ = [
     "RastPools",
     "RastBatch",
     "RastProfile",
+    "RastTiledConfig",
+    "RastTiledStats",
     "RastError",
     "PROTOTYPES",
     "load",

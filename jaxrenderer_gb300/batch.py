@@ -259,9 +259,17 @@ class BatchOutputs:
 
 
 class BatchRunner:
-    """Reusable outputs + workspaces for repeated renders of one SceneBatch."""
+    """Reusable outputs + workspaces for repeated renders of one SceneBatch.
 
-    def __init__(self, sb: SceneBatch, form: str = "plain", want_prim_id: bool = True, count_ties: bool = False):
+    form="plain": per-pixel scan over every primitive (rast_render_plain);
+    form="tiled": binned tiles (rast_render_tiled) with `tiled_config`
+    (tile shape, bin capacity) from the autotuner when not given.
+    `capture()` records one full render (buffer reset, depth pass, main pass)
+    into a CUDA graph that `replay()` re-issues with a single launch.
+    """
+
+    def __init__(self, sb: SceneBatch, form: str = "plain", want_prim_id: bool = True, count_ties: bool = False,
+                 tiled_config=None):
         self.sb = sb
         self.form = form
         dev = sb.device
@@ -273,6 +281,8 @@ class BatchRunner:
         self.shadow_map = None
         self.shadow_prim = None
         self.keep = []
+        self.graph = None
+        self._colour = torch.ones(3, dtype=torch.float32, device=dev)
         lib = _lib.load()
         self.lib = lib
         if sb.shadow_jobs is not None:
@@ -285,39 +295,94 @@ class BatchRunner:
             self.shadow_batch = None
             pools = sb.pools
         self.main_batch = _rast_batch(sb.main_jobs, pools, self.zbuffer, self.canvas, self.prim_id, self.ties, self.keep)
+        self.configs = {}
+        if form == "tiled":
+            from .autotune import tiled_config_for
+
+            for name, b, tbl in (("shadow", self.shadow_batch, sb.shadow_jobs), ("main", self.main_batch, sb.main_jobs)):
+                if b is not None:
+                    self.configs[name] = tiled_config if tiled_config is not None else tiled_config_for(self, name, b, tbl)
         self.ws = {}
         for name, b in (("shadow", self.shadow_batch), ("main", self.main_batch)):
             if b is None:
                 continue
-            nbytes = int(self._ws_bytes(b))
+            nbytes = int(self._ws_bytes(name, b))
             self.ws[name] = (torch.empty(max(nbytes, 256), dtype=torch.uint8, device=dev), nbytes)
 
-    def _ws_bytes(self, b) -> int:
+    def batches(self):
+        return [(n, b) for n, b in (("shadow", self.shadow_batch), ("main", self.main_batch)) if b is not None]
+
+    def _cfg(self, name):
+        c = self.configs.get(name)
+        return ctypes.byref(c) if c is not None else None
+
+    def _ws_bytes(self, name, b) -> int:
         if self.form == "plain":
             return self.lib.rast_plain_workspace_bytes(ctypes.byref(b))
-        return self.lib.rast_tiled_workspace_bytes(ctypes.byref(b))
+        return self.lib.rast_tiled_workspace_bytes(ctypes.byref(b), self._cfg(name))
 
-    def _launch(self, b, ws, stream) -> None:
-        buf, nbytes = ws
+    def launch(self, name, stream_handle, profile=None) -> None:
+        b = self.shadow_batch if name == "shadow" else self.main_batch
+        buf, nbytes = self.ws[name]
         if self.form == "plain":
-            st = self.lib.rast_render_plain(ctypes.byref(b), buf.data_ptr(), nbytes, stream)
+            if profile is None:
+                st = self.lib.rast_render_plain(ctypes.byref(b), buf.data_ptr(), nbytes, stream_handle)
+            else:
+                st = self.lib.rast_render_plain_profiled(ctypes.byref(b), buf.data_ptr(), nbytes, stream_handle,
+                                                         ctypes.byref(profile))
         else:
-            st = self.lib.rast_render_tiled(ctypes.byref(b), buf.data_ptr(), nbytes, stream)
+            if profile is None:
+                st = self.lib.rast_render_tiled(ctypes.byref(b), self._cfg(name), buf.data_ptr(), nbytes, stream_handle)
+            else:
+                st = self.lib.rast_render_tiled_profiled(ctypes.byref(b), self._cfg(name), buf.data_ptr(), nbytes,
+                                                         stream_handle, ctypes.byref(profile))
         _lib.check(st, f"rast_render_{self.form}")
 
-    def run(self, stream: Optional[torch.cuda.Stream] = None, zbuffer_default: float = 1.0,
-            colour_default=(1.0, 1.0, 1.0)) -> BatchOutputs:
+    def stats(self, name="main"):
+        """Bin statistics of the last tiled render of pass `name`."""
+        b = self.shadow_batch if name == "shadow" else self.main_batch
+        out = _lib.RastTiledStats()
+        buf, _ = self.ws[name]
+        s = torch.cuda.current_stream(self.sb.device)
+        _lib.check(self.lib.rast_tiled_stats(ctypes.byref(b), self._cfg(name), buf.data_ptr(), s.cuda_stream,
+                                             ctypes.byref(out)), "rast_tiled_stats")
+        return out
+
+    def _reset(self, zbuffer_default: float):
+        self.zbuffer.fill_(zbuffer_default)
+        self.canvas.copy_(self._colour.expand_as(self.canvas))
+        if self.shadow_map is not None:
+            self.shadow_map.fill_(float(np.finfo(np.float32).max))
+
+    def run(self, stream: Optional[torch.cuda.Stream] = None, zbuffer_default: float = 1.0) -> BatchOutputs:
         """Reset the buffers to their defaults and render every scene
         (depth pass, then main pass) on `stream`."""
         s = stream if stream is not None else torch.cuda.current_stream(self.sb.device)
         with torch.cuda.stream(s):
-            self.zbuffer.fill_(zbuffer_default)
-            self.canvas.copy_(torch.tensor(colour_default, dtype=torch.float32, device=self.sb.device).expand_as(self.canvas))
-            if self.shadow_batch is not None:
-                self.shadow_map.fill_(float(np.finfo(np.float32).max))
-                self._launch(self.shadow_batch, self.ws["shadow"], s.cuda_stream)
-            self._launch(self.main_batch, self.ws["main"], s.cuda_stream)
+            self._reset(zbuffer_default)
+            for name, _ in self.batches():
+                self.launch(name, s.cuda_stream)
+        return self.outputs()
+
+    def outputs(self) -> BatchOutputs:
         return BatchOutputs(self.canvas, self.zbuffer, self.prim_id, self.shadow_map, self.shadow_prim, self.ties)
+
+    def capture(self) -> None:
+        """Record run() into a CUDA graph (one launch per replay)."""
+        dev = self.sb.device
+        side = torch.cuda.Stream(dev)
+        side.wait_stream(torch.cuda.current_stream(dev))
+        self.run(side)
+        torch.cuda.current_stream(dev).wait_stream(side)
+        torch.cuda.synchronize(dev)
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            self.run(torch.cuda.current_stream(dev))
+        self.graph = g
+
+    def replay(self) -> BatchOutputs:
+        self.graph.replay()
+        return self.outputs()
 
 
 def render_batch(sb: SceneBatch, form: str = "plain", want_prim_id: bool = True) -> BatchOutputs:

@@ -314,6 +314,26 @@ def render_plain(packed: PackedBatch, stream: Optional[torch.cuda.Stream] = None
     _lib.check(st, "rast_render_plain")
 
 
+def render_tiled(packed: PackedBatch, tile=(8, 8), bin_capacity: int = 0,
+                 stream: Optional[torch.cuda.Stream] = None) -> "_lib.RastTiledStats":
+    """Run the tiled form on a packed batch; returns its bin statistics
+    (reading them synchronises the stream)."""
+    lib = _lib.load()
+    b = packed.batch
+    cfg = _lib.RastTiledConfig(int(tile[0]), int(tile[1]), int(bin_capacity))
+    nbytes = lib.rast_tiled_workspace_bytes(ctypes.byref(b), ctypes.byref(cfg))
+    dev = packed.zbuffer.device
+    ws = torch.empty(max(int(nbytes), 256), dtype=torch.uint8, device=dev)
+    packed.keep.append(ws)
+    s = stream if stream is not None else torch.cuda.current_stream(dev)
+    _lib.check(lib.rast_render_tiled(ctypes.byref(b), ctypes.byref(cfg), ws.data_ptr(), int(nbytes), s.cuda_stream),
+               "rast_render_tiled")
+    stats = _lib.RastTiledStats()
+    _lib.check(lib.rast_tiled_stats(ctypes.byref(b), ctypes.byref(cfg), ws.data_ptr(), s.cuda_stream,
+                                    ctypes.byref(stats)), "rast_tiled_stats")
+    return stats
+
+
 def unpack(packed: PackedBatch, specs: Sequence[JobSpec]):
     """Per-job views of the output pools: (zbuffer, canvas or None, prim_id or None)."""
     out = []
@@ -326,4 +346,4 @@ def unpack(packed: PackedBatch, specs: Sequence[JobSpec]):
     return out
 
 
-__all__ = ["JobSpec", "job_from_extra", "pack", "render_plain", "unpack", "PackedBatch"]
+__all__ = ["JobSpec", "job_from_extra", "pack", "render_plain", "render_tiled", "unpack", "PackedBatch"]

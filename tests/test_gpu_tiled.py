@@ -1,0 +1,114 @@
+"""GPU parity of the tiled form: identical results to the plain form and the
+oracle, for every tile shape, with bin overflow forced, and under CUDA-graph
+replay."""
+import numpy as np
+import pytest
+import torch
+
+import jaxrenderer_gb300 as jr
+from jaxrenderer_gb300 import _lib, batch as jb, synthetic
+from jaxrenderer_gb300.jobs import pack, render_plain, render_tiled, unpack
+from oracle import oracle
+from tests import scenes
+from tests.test_gpu_plain import assert_parity
+
+pytestmark = pytest.mark.gpu
+F32 = np.float32
+SHAPES = [(8, 8), (16, 8), (16, 16), (32, 8), (8, 32)]
+
+
+def _tiled_job(spec, z0, c0, device, tile=(8, 8), cap=0, ties=False):
+    packed = pack([spec], [z0], [c0], device, count_ties=ties)
+    stats = render_tiled(packed, tile=tile, bin_capacity=cap)
+    z, c, p = unpack(packed, [spec])[0]
+    return z, c, p, packed.near_ties, stats
+
+
+@pytest.mark.parametrize("shader", scenes.ALL_SHADERS)
+def test_tiled_random_scene_parity(cuda_device, shader):
+    spec = scenes.random_job(shader, seed=700 + shader, W=57, H=45, F=150, spread=2.0)
+    z0, c0 = scenes.initial_buffers(spec)
+    z, c, p, ties, stats = _tiled_job(spec, z0, c0, cuda_device, ties=True)
+    ref = oracle.render(spec, z0, c0)
+    assert_parity(z, c, p, ref, f"tiled shader {shader}")
+    assert int(ties.item()) == ref["near_ties"]
+    assert stats.overflow == 0
+
+
+@pytest.mark.parametrize("tile", SHAPES)
+def test_tile_shapes_and_unbounded_regions(cuda_device, tile):
+    # eye inside the soup: many primitives straddle w = 0, so their coverage
+    # regions are unbounded and must be clipped to the screen, not dropped
+    spec = scenes.random_job(_lib.SHADER_PHONG, seed=800, W=70, H=50, F=300, spread=3.0, eye=(0.2, 0.1, 0.6))
+    z0, c0 = scenes.initial_buffers(spec)
+    z, c, p, _, _ = _tiled_job(spec, z0, c0, cuda_device, tile=tile)
+    assert_parity(z, c, p, oracle.render(spec, z0, c0), f"tile {tile}")
+
+
+def test_bin_overflow_falls_back_to_full_scan(cuda_device):
+    spec = scenes.random_job(_lib.SHADER_GOURAUD, seed=801, W=64, H=64, F=400, spread=1.0)
+    z0, c0 = scenes.initial_buffers(spec)
+    z, c, p, _, stats = _tiled_job(spec, z0, c0, cuda_device, cap=64)
+    assert stats.overflow == 1 and stats.bin_entries > 64
+    assert_parity(z, c, p, oracle.render(spec, z0, c0), "overflow")
+
+
+def test_reference_smoke_scene_tiled(cuda_device):
+    spec = scenes.smoke_batched_triangles_job()
+    z0 = np.ones((1920, 1080), F32)
+    c0 = np.zeros((1920, 1080, 3), F32)
+    z, c, p, _, _ = _tiled_job(spec, z0, c0, cuda_device, tile=(16, 16))
+    scenes.smoke_batched_triangles_asserts(z.cpu().numpy(), c.cpu().numpy())
+    assert_parity(z, c, p, oracle.render(spec, z0, c0, n_threads=8), "smoke tiled")
+
+
+@pytest.fixture(scope="module")
+def brax_batch(cuda_device):
+    flat = synthetic.brax_like_batch(48, seed=synthetic.BASE_SEED + 21)
+    sb = jb.scene_batch_from_flat(flat, 84, 84, shadow_size=(128, 128), device=cuda_device)
+    return flat, sb
+
+
+def _copy(out):
+    keys = ("canvas", "zbuffer", "prim_id", "shadow_map", "shadow_prim_id")
+    return {k: getattr(out, k).clone() for k in keys}
+
+
+@pytest.mark.parametrize("tile", [(8, 8), (16, 16), (32, 8)])
+def test_tiled_batch_equals_plain_batch(cuda_device, brax_batch, tile):
+    flat, sb = brax_batch
+    plain = _copy(jb.BatchRunner(sb, form="plain").run())
+    cfg = _lib.RastTiledConfig(tile[0], tile[1], 0)
+    runner = jb.BatchRunner(sb, form="tiled", tiled_config=cfg)
+    tiled = _copy(runner.run())
+    torch.cuda.synchronize()
+    for k in ("prim_id", "shadow_prim_id"):
+        assert torch.equal(plain[k], tiled[k]), k
+    for k in ("zbuffer", "shadow_map", "canvas"):
+        assert torch.equal(plain[k].view(torch.int32), tiled[k].view(torch.int32)), k
+    assert runner.stats("main").overflow == 0
+
+
+def test_tiled_batch_matches_oracle_on_a_few_scenes(cuda_device, brax_batch):
+    flat, sb = brax_batch
+    out = jb.BatchRunner(sb, form="tiled", tiled_config=_lib.RastTiledConfig(8, 8, 0)).run()
+    torch.cuda.synchronize()
+    for s in (0, 17, 47):
+        dspec, mspec = scenes.specs_from_batch(flat, sb, s)
+        dref = oracle.render(dspec, np.full((128, 128), np.finfo(F32).max, F32))
+        np.testing.assert_array_equal(out.shadow_prim_id[s].cpu().numpy(), dref["prim_id"])
+        mspec.shadow_map = dref["zbuffer"]
+        ref = oracle.render(mspec, np.ones((84, 84), F32), np.ones((84, 84, 3), F32))
+        assert_parity(out.zbuffer[s], out.canvas[s], out.prim_id[s], ref, f"scene {s}")
+
+
+def test_graph_replay_matches_eager(cuda_device, brax_batch):
+    flat, sb = brax_batch
+    runner = jb.BatchRunner(sb, form="tiled", tiled_config=_lib.RastTiledConfig(8, 8, 0))
+    eager = _copy(runner.run())
+    runner.capture()
+    runner.canvas.zero_()
+    replayed = runner.replay()
+    torch.cuda.synchronize()
+    assert torch.equal(eager["canvas"].view(torch.int32), replayed.canvas.view(torch.int32))
+    assert torch.equal(eager["prim_id"], replayed.prim_id)
