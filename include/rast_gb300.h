@@ -208,6 +208,42 @@ typedef struct RastTiledStats {
 int rast_tiled_stats(const RastBatch* batch, const RastTiledConfig* cfg, const void* workspace,
                      void* stream, RastTiledStats* out);
 
+/* ---------------------------------------------------------------- backward
+ * Gradients of a rendered batch, visibility piecewise constant (as under
+ * jax.grad of the reference, tests/smoke_test_grad.py:92-128).  The batch
+ * must be the one just rendered (same pools) with pools.prim_id holding the
+ * forward's winning-primitive buffer; for PHONG_REFLECTION_SHADOW jobs
+ * pools.shadow_map holds the forward's shadow maps.  Every gradient array is
+ * ACCUMULATED into (the caller zeroes it); NULL arrays are skipped.
+ * RastGradPools arrays have the layout of the matching RastPools arrays. */
+#define RAST_GRAD_WORLD_TO_CLIP 0       /* 16: d/d Camera.world_to_clip (row-major) */
+#define RAST_GRAD_WORLD_TO_EYE_NORM 16  /* 16: d/d Camera.world_to_eye_norm */
+#define RAST_GRAD_LIGHT_DIRECTION 32    /* 3: d/d LightSource.direction */
+#define RAST_GRAD_LIGHT_COLOUR 35       /* 3: d/d LightSource.colour */
+#define RAST_GRAD_LIGHT_DIR_EYE 38      /* 3: d/d light_dir_eye (phong_reflection*) */
+#define RAST_GRAD_AMBIENT 41            /* 3 */
+#define RAST_GRAD_DIFFUSE 44            /* 3 */
+#define RAST_GRAD_SPECULAR 47           /* 3 */
+#define RAST_GRAD_SHADOW_STRENGTH 50    /* 3: d/d Shadow.strength */
+#define RAST_NPARAM 56                  /* per-job stride of job_params */
+
+typedef struct RastGradPools {
+  float* position;      /* (rows, 3) d/d vertex positions */
+  float* normal;        /* (rows, 3) d/d vertex normals */
+  float* colour;        /* (rows, 3) d/d vertex colours (gouraud) */
+  float* texture;       /* like RastPools.texture: d/d diffuse texels */
+  float* specular_map;  /* like RastPools.specular_map: d/d specular exponents */
+  float* job_params;    /* (n_jobs, RAST_NPARAM) per-job camera/light gradients */
+} RastGradPools;
+
+/* One thread per pixel whose fragment was kept: recompute, then reverse
+ * mode through fragment, interpolation, barycentrics, 3x3 inverse and clip
+ * transform.  uv gets no gradient (nearest texel: floor).  Not available for
+ * PHONG_DARBOUX (RAST_ERR_UNSUPPORTED).  grad_canvas (pixels, 3) and
+ * grad_zbuffer (pixels) may each be NULL. */
+int rast_backward(const RastBatch* batch, const float* grad_canvas, const float* grad_zbuffer,
+                  const RastGradPools* grads, void* stream);
+
 /* Host-side validation of one job against pool sizes (no device access):
  * returns RAST_ERR_INVALID_ARGUMENT for inconsistent sizes. */
 int rast_validate_job(const RastJob* job);

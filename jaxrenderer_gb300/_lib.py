@@ -136,6 +136,23 @@ class RastTiledStats(ctypes.Structure):
                 ("overflow", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
 
 
+GRAD_WORLD_TO_CLIP = 0
+GRAD_WORLD_TO_EYE_NORM = 16
+GRAD_LIGHT_DIRECTION = 32
+GRAD_LIGHT_COLOUR = 35
+GRAD_LIGHT_DIR_EYE = 38
+GRAD_AMBIENT = 41
+GRAD_DIFFUSE = 44
+GRAD_SPECULAR = 47
+GRAD_SHADOW_STRENGTH = 50
+NPARAM = 56
+
+
+class RastGradPools(ctypes.Structure):
+    _fields_ = [("position", c_void_p), ("normal", c_void_p), ("colour", c_void_p), ("texture", c_void_p),
+                ("specular_map", c_void_p), ("job_params", c_void_p)]
+
+
 # Exported symbols and their prototypes: (name, restype, argtypes).
 PROTOTYPES = [
     ("rast_plain_workspace_bytes", c_size_t, [POINTER(RastBatch)]),
@@ -147,6 +164,7 @@ PROTOTYPES = [
      [POINTER(RastBatch), POINTER(RastTiledConfig), c_void_p, c_size_t, c_void_p, POINTER(RastProfile)]),
     ("rast_tiled_stats", c_int,
      [POINTER(RastBatch), POINTER(RastTiledConfig), c_void_p, c_void_p, POINTER(RastTiledStats)]),
+    ("rast_backward", c_int, [POINTER(RastBatch), c_void_p, c_void_p, POINTER(RastGradPools), c_void_p]),
     ("rast_validate_job", c_int, [POINTER(RastJob)]),
     ("rast_error_string", ctypes.c_char_p, [c_int]),
     ("rast_abi_version", c_int, []),
@@ -205,6 +223,7 @@ __all__ = [
     "RastProfile",
     "RastTiledConfig",
     "RastTiledStats",
+    "RastGradPools",
     "RastError",
     "PROTOTYPES",
     "load",

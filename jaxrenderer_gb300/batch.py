@@ -187,6 +187,22 @@ def scene_batch_from_flat(flat, width: int = 84, height: int = 84,
                       t.main_jobs, t.shadow_jobs, device, flat.n_faces)
 
 
+def scene_batch_from_specs(specs, device=None) -> SceneBatch:
+    """A SceneBatch of N independent single-pass jobs (same size and shader,
+    no shadow pass) from JobSpecs, e.g. N differentiable scenes."""
+    from .jobs import pack
+
+    device = device if device is not None else torch.device("cuda", torch.cuda.current_device())
+    W, H = specs[0].width, specs[0].height
+    if any(s.width != W or s.height != H for s in specs):
+        raise ValueError("scene_batch_from_specs needs equal sizes")
+    z = [np.ones((W, H), F32)] * len(specs)
+    packed = pack(specs, z, [None] * len(specs), device, want_prim_id=False)
+    jobs = np.frombuffer(bytes(packed.jobs), dtype=JOB_DTYPE).copy()
+    n_faces = jobs["n_faces"].astype(np.int32)
+    return SceneBatch(len(specs), W, H, 0, 0, packed.pools, jobs, None, device, n_faces)
+
+
 def scene_job_specs(flat, tables, s: int):
     """The pipeline.render calls scene `s` of a flat batch makes, as JobSpecs
     with host arrays: (depth pass or None, main pass)."""
@@ -227,6 +243,7 @@ def _rast_batch(jobs: np.ndarray, pools: Dict[str, torch.Tensor], zbuffer: torch
                 canvas: Optional[torch.Tensor], prim_id: Optional[torch.Tensor], ties, keep: list):
     jt = torch.from_numpy(jobs.view(np.uint8).copy()).to(zbuffer.device)
     keep.append(jt)
+    keep.append(("jobs", id(jobs), jt))
     b = _lib.RastBatch()
     b.jobs = jt.data_ptr()
     b.n_jobs = len(jobs)
@@ -295,6 +312,8 @@ class BatchRunner:
             self.shadow_batch = None
             pools = sb.pools
         self.main_batch = _rast_batch(sb.main_jobs, pools, self.zbuffer, self.canvas, self.prim_id, self.ties, self.keep)
+        self.main_jobs_dev = self.keep[-1][2]  # device copy of the main job table (uint8)
+        self.pools = pools
         self.configs = {}
         if form == "tiled":
             from .autotune import tiled_config_for
@@ -337,6 +356,40 @@ class BatchRunner:
                 st = self.lib.rast_render_tiled_profiled(ctypes.byref(b), self._cfg(name), buf.data_ptr(), nbytes,
                                                          stream_handle, ctypes.byref(profile))
         _lib.check(st, f"rast_render_{self.form}")
+
+    def job_floats(self) -> torch.Tensor:
+        """The main pass's device job table viewed as (n_jobs, sizeof(RastJob)/4)
+        float32, for in-place updates of per-job matrices and light terms."""
+        return self.main_jobs_dev.view(torch.float32).view(self.sb.n_scenes, -1)
+
+    def backward(self, grad_canvas: Optional[torch.Tensor], grad_zbuffer: Optional[torch.Tensor] = None,
+                 stream: Optional[torch.cuda.Stream] = None) -> Dict[str, torch.Tensor]:
+        """Gradients of the last run() of the main pass (rast_backward):
+        per-vertex position/normal, per-texel texture/specular exponent and
+        per-scene camera/light terms (RAST_GRAD_* layout, (N, 56))."""
+        if self.prim_id is None:
+            raise RuntimeError("backward needs the winning-primitive buffer: build the runner with want_prim_id=True")
+        dev = self.sb.device
+        P = self.pools
+        g = {
+            "position": torch.zeros_like(P["position"]),
+            "normal": torch.zeros_like(P["normal"]),
+            "texture": torch.zeros_like(P["texture"]),
+            "specular_map": torch.zeros_like(P["specular_map"]),
+            "job_params": torch.zeros((self.sb.n_scenes, _lib.NPARAM), dtype=torch.float32, device=dev),
+        }
+        if "colour" in P:
+            g["colour"] = torch.zeros_like(P["colour"])
+        gp = _lib.RastGradPools()
+        for k, t in g.items():
+            setattr(gp, k, t.data_ptr())
+        gc = grad_canvas.contiguous() if grad_canvas is not None else None
+        gz = grad_zbuffer.contiguous() if grad_zbuffer is not None else None
+        s = stream if stream is not None else torch.cuda.current_stream(dev)
+        st = self.lib.rast_backward(ctypes.byref(self.main_batch), gc.data_ptr() if gc is not None else None,
+                                    gz.data_ptr() if gz is not None else None, ctypes.byref(gp), s.cuda_stream)
+        _lib.check(st, "rast_backward")
+        return g
 
     def stats(self, name="main"):
         """Bin statistics of the last tiled render of pass `name`."""
@@ -390,5 +443,6 @@ def render_batch(sb: SceneBatch, form: str = "plain", want_prim_id: bool = True)
     return BatchRunner(sb, form=form, want_prim_id=want_prim_id).run()
 
 
-__all__ = ["SceneBatch", "SceneTables", "scene_batch_tables", "scene_batch_from_flat", "scene_job_specs",
+__all__ = ["SceneBatch", "SceneTables", "scene_batch_tables", "scene_batch_from_flat", "scene_batch_from_specs",
+           "scene_job_specs",
            "flat_pools", "render_batch", "BatchRunner", "BatchOutputs", "job_table"]

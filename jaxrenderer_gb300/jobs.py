@@ -187,6 +187,8 @@ class PackedBatch:
     prim_id: Optional[torch.Tensor]
     near_ties: Optional[torch.Tensor]
     pixel_begin: List[int]
+    pools: dict = None  # name -> device tensor (RastPools inputs)
+    jobs: object = None  # ctypes array of RastJob (host copy)
 
 
 def pack(specs: Sequence[JobSpec], zbuffers: Sequence[Any], canvases: Sequence[Any], device,
@@ -298,7 +300,8 @@ def pack(specs: Sequence[JobSpec], zbuffers: Sequence[Any], canvases: Sequence[A
     P.canvas = _ptr(canvas)
     P.prim_id = _ptr(prim)
     b.near_ties = _ptr(ties)
-    return PackedBatch(b, keep, zbuf, canvas, prim, ties, pixel_begin)
+    return PackedBatch(b, keep, zbuf, canvas, prim, ties, pixel_begin,
+                       {k: v for k, v in tensors.items() if v is not None}, jobs)
 
 
 def render_plain(packed: PackedBatch, stream: Optional[torch.cuda.Stream] = None) -> None:

@@ -283,3 +283,39 @@ def brax_like_batch(n_scenes: int, seed: int = BASE_SEED + 1) -> FlatScenes:
         texture[tb : tb + 4 * objs[s]] = np.repeat(colours[s], 4, axis=0)[:, None, :].astype(F32)
     return FlatScenes(position, normal, uv, tex_idx, texture, specular, corner_begin, n_faces.astype(np.int32),
                       tex_begin, objs.astype(np.int32), cam.astype(F32))
+
+
+# ------------------------------------------------ differentiable phong batch
+
+@dataclass
+class PhongScene:
+    """One scene of the differentiable phong workload (PhongTextureShader)."""
+
+    base_position: np.ndarray  # (V, 3) unperturbed icosphere
+    position: np.ndarray  # (V, 3) displaced along the normal
+    normal: np.ndarray
+    uv: np.ndarray  # texel units
+    faces: np.ndarray
+    texture: np.ndarray  # (tw, th, 3)
+    light_direction: np.ndarray  # eye space
+    eye: np.ndarray  # camera position
+
+
+def phong_scene(rng: np.random.Generator, level: int = 4, texture_size: int = 64, sigma: float = 0.05,
+                radius: float = 4.0) -> PhongScene:
+    """Icosphere of `level` with per-vertex Gaussian displacement sigma along
+    the normal, a texture_size^2 RGB texture U[0, 1] sampled in texel units,
+    a random unit light direction (eye space, towards the viewer's side) and
+    a camera on a sphere of `radius` looking at the origin."""
+    v, f = icosphere(level)
+    n = v.copy()
+    disp = rng.normal(0.0, sigma, size=(len(v), 1)).astype(F32)
+    pos = (v * (F32(1) + disp)).astype(F32)
+    uv = (sphere_uv(v) * F32(texture_size)).astype(F32)
+    tex = rng.uniform(0, 1, (texture_size, texture_size, 3)).astype(F32)
+    l = rng.normal(size=3)
+    l[2] = abs(l[2]) + 0.5
+    l = (l / np.linalg.norm(l)).astype(F32)
+    e = rng.normal(size=3)
+    e = (radius * e / np.linalg.norm(e)).astype(F32)
+    return PhongScene(v, pos, n, uv, f, tex, l, e)
