@@ -38,6 +38,26 @@ __device__ __forceinline__ int find_job_by_setup(const RastJob* jobs, int n, int
   return find_job(jobs, n, row, [](const RastJob& j) { return j.setup_begin; });
 }
 
+// Job owning rows [row0, row0 + blockDim.x) of a flat per-row launch when
+// they all belong to one job (the common case: one binary search per block,
+// by thread 0), else -1 (each thread then searches for its own row).  Every
+// thread of the block must call it.
+template <typename Begin, typename Count>
+__device__ __forceinline__ int block_uniform_job(const RastJob* jobs, int n, int64_t row0, int64_t total,
+                                                 Begin begin, Count count, int* s_job) {
+  if (threadIdx.x == 0) {
+    int j = -1;
+    if (row0 < total) {
+      const int64_t last = min(row0 + static_cast<int64_t>(blockDim.x) - 1, total - 1);
+      const int f = find_job(jobs, n, row0, begin);
+      if (begin(jobs[f]) + count(jobs[f]) > last) j = f;
+    }
+    *s_job = j;
+  }
+  __syncthreads();
+  return *s_job;
+}
+
 // PerPrimitive.create (pipeline.py:80-113) from the three clip positions.
 // Record: [inv0..3] [inv4..7] [inv8 z0 z1 z2] [det flags 0 0].
 __device__ __forceinline__ void setup_from_clip(const float4* c, float* inv, float* det_out,
@@ -141,9 +161,9 @@ __device__ __forceinline__ void resolve_pixel(const RastJob& J, const RastPools&
       }
     } else {
       float clip[4];
-      vertex_shader(J, P, i0, clip, v0);
-      vertex_shader(J, P, i1, clip, v1);
-      vertex_shader(J, P, i2, clip, v2);
+      vertex_shader<false>(J, P, i0, clip, v0);
+      vertex_shader<false>(J, P, i1, clip, v1);
+      vertex_shader<false>(J, P, i2, clip, v2);
     }
   }
   const bool frag_keep = fragment_shader(J, P, v0, v1, v2, bary, front, r->colour);

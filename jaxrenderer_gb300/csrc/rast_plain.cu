@@ -24,10 +24,17 @@ namespace rast {
 
 __global__ void __launch_bounds__(256)
 vertex_kernel(RastBatch B, float4* __restrict__ clip_out, float* __restrict__ var_out, int vstride) {
-  const int64_t row = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  __shared__ RastJob sJ;
+  __shared__ int s_job;
+  const int64_t row0 = static_cast<int64_t>(blockIdx.x) * blockDim.x;
+  const int64_t row = row0 + threadIdx.x;
+  const int uj = block_uniform_job(B.jobs, B.n_jobs, row0, B.total_vout,
+                                   [](const RastJob& j) { return j.vout_begin; },
+                                   [](const RastJob& j) { return static_cast<int64_t>(j.n_verts); }, &s_job);
+  if (uj >= 0) load_job_to_shared(B.jobs + uj, &sJ);
+  __syncthreads();
   if (row >= B.total_vout) return;
-  const int jid = find_job_by_vout(B.jobs, B.n_jobs, row);
-  const RastJob& J = B.jobs[jid];
+  const RastJob& J = uj >= 0 ? sJ : B.jobs[find_job_by_vout(B.jobs, B.n_jobs, row)];
   const int v = static_cast<int>(row - J.vout_begin);
   float clip[4];
   float var[kMaxVarying];
@@ -39,10 +46,14 @@ vertex_kernel(RastBatch B, float4* __restrict__ clip_out, float* __restrict__ va
 
 __global__ void __launch_bounds__(256)
 setup_kernel(RastBatch B, const float4* __restrict__ clip, float4* __restrict__ setup) {
-  const int64_t row = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  __shared__ int s_job;
+  const int64_t row0 = static_cast<int64_t>(blockIdx.x) * blockDim.x;
+  const int64_t row = row0 + threadIdx.x;
+  const int uj = block_uniform_job(B.jobs, B.n_jobs, row0, B.total_setup,
+                                   [](const RastJob& j) { return j.setup_begin; },
+                                   [](const RastJob& j) { return static_cast<int64_t>(j.n_faces); }, &s_job);
   if (row >= B.total_setup) return;
-  const int jid = find_job_by_setup(B.jobs, B.n_jobs, row);
-  const RastJob& J = B.jobs[jid];
+  const RastJob& J = B.jobs[uj >= 0 ? uj : find_job_by_setup(B.jobs, B.n_jobs, row)];
   const int64_t f = row - J.setup_begin;
   const int32_t* face = B.pools.faces + (J.face_begin + f) * 3;
   float4 c[3];

@@ -41,12 +41,15 @@ __device__ __forceinline__ void load3(const float* p, int64_t row, float* out) {
 // depth.py:47-61, gouraud.py:119-149, gouraud_texture.py:253-286,
 // phong.py:430-456, phong_darboux.py:120-170, phong_reflection.py:104-132,
 // phong_reflection_shadow.py:373-408.
+// kClip = false skips gl_Position (the deferred shading re-run needs only
+// the varyings).
+template <bool kClip = true>
 __device__ __forceinline__ void vertex_shader(const RastJob& J, const RastPools& P, int v,
                                               float* clip, float* var) {
   const int64_t row = J.vert_begin + v;
   float pos[3];
   load3(P.position, row, pos);
-  to_clip(J.world_to_clip, pos[0], pos[1], pos[2], clip);
+  if (kClip) to_clip(J.world_to_clip, pos[0], pos[1], pos[2], clip);
   const int sh = J.shader;
   if (sh == RAST_SHADER_GOURAUD || sh == RAST_SHADER_GOURAUD_TEXTURE) {
     float nin[3], n[3], l[3];

@@ -151,10 +151,18 @@ __device__ __forceinline__ void face_clip(const RastJob& J, const RastPools& P, 
 __global__ void __launch_bounds__(kSetupThreads)
 setup_bin_kernel(RastBatch B, Geometry G, float4* __restrict__ setup, ushort4* __restrict__ bbox,
                  uint32_t* __restrict__ counts) {
-  const int64_t row = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  __shared__ RastJob sJ;
+  __shared__ int s_job;
+  const int64_t row0 = static_cast<int64_t>(blockIdx.x) * blockDim.x;
+  const int64_t row = row0 + threadIdx.x;
+  const int uj = block_uniform_job(B.jobs, B.n_jobs, row0, B.total_setup,
+                                   [](const RastJob& j) { return j.setup_begin; },
+                                   [](const RastJob& j) { return static_cast<int64_t>(j.n_faces); }, &s_job);
+  if (uj >= 0) load_job_to_shared(B.jobs + uj, &sJ);
+  __syncthreads();
   if (row >= B.total_setup) return;
-  const int jid = find_job_by_setup(B.jobs, B.n_jobs, row);
-  const RastJob& J = B.jobs[jid];
+  const int jid = uj >= 0 ? uj : find_job_by_setup(B.jobs, B.n_jobs, row);
+  const RastJob& J = uj >= 0 ? sJ : B.jobs[jid];
   const int64_t f = row - J.setup_begin;
   float4 c[3];
   face_clip(J, B.pools, f, c);
@@ -162,9 +170,13 @@ setup_bin_kernel(RastBatch B, Geometry G, float4* __restrict__ setup, ushort4* _
   int flags;
   setup_from_clip(c, inv, &det, &flags);
   float4* out = setup + row * 4;
-  out[0] = make_float4(inv[0], inv[1], inv[2], inv[3]);
-  out[1] = make_float4(inv[4], inv[5], inv[6], inv[7]);
-  out[2] = make_float4(inv[8], c[0].z, c[1].z, c[2].z);
+  // the inverse is read only for candidates (raster) and for face 0 (the
+  // chooser's fallback); the flags of every face are kept
+  if ((flags & kCandidate) == kCandidate || f == 0) {
+    out[0] = make_float4(inv[0], inv[1], inv[2], inv[3]);
+    out[1] = make_float4(inv[4], inv[5], inv[6], inv[7]);
+    out[2] = make_float4(inv[8], c[0].z, c[1].z, c[2].z);
+  }
   out[3] = make_float4(det, __int_as_float(flags), 0.0f, 0.0f);
   int i0, i1, j0, j1;
   ushort4 bb = make_ushort4(1, 1, 0, 0);  // empty: lo > hi
@@ -254,12 +266,20 @@ __global__ void __launch_bounds__(kSetupThreads)
 scatter_kernel(RastBatch B, Geometry G, const ushort4* __restrict__ bbox,
                const uint32_t* __restrict__ offsets, uint32_t* __restrict__ cursors,
                int32_t* __restrict__ bins) {
-  const int64_t row = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  __shared__ int s_job;
+  __shared__ int64_t s_begin;
+  const int64_t row0 = static_cast<int64_t>(blockIdx.x) * blockDim.x;
+  const int64_t row = row0 + threadIdx.x;
+  const int uj = block_uniform_job(B.jobs, B.n_jobs, row0, B.total_setup,
+                                   [](const RastJob& j) { return j.setup_begin; },
+                                   [](const RastJob& j) { return static_cast<int64_t>(j.n_faces); }, &s_job);
+  if (threadIdx.x == 0 && uj >= 0) s_begin = B.jobs[uj].setup_begin;
+  __syncthreads();
   if (row >= B.total_setup) return;
   const ushort4 bb = bbox[row];
   if (bb.x > bb.z) return;
-  const int jid = find_job_by_setup(B.jobs, B.n_jobs, row);
-  const int32_t fid = static_cast<int32_t>(row - B.jobs[jid].setup_begin);
+  const int jid = uj >= 0 ? uj : find_job_by_setup(B.jobs, B.n_jobs, row);
+  const int32_t fid = static_cast<int32_t>(row - (uj >= 0 ? s_begin : B.jobs[jid].setup_begin));
   const int64_t tb = static_cast<int64_t>(jid) * G.tiles_per_job;
   for (int ty = bb.y; ty <= bb.w; ++ty)
     for (int tx = bb.x; tx <= bb.z; ++tx) {
@@ -320,19 +340,35 @@ raster_kernel(RastBatch B, Geometry G, const float4* __restrict__ setup,
     const uint32_t off = offsets[t];
     const bool overflow = (off & kOverflow) != 0;
     const int n = overflow ? J.n_faces : static_cast<int>(counts[t]);
+    // entry `e` of the tile's list -> (record, id); ids of non-candidates
+    // (only met on the full-scan path) are -1 and their records unused
+    auto fetch = [&](int e, float4& r0, float4& r1, float4& r2, int& id) {
+      const int fid = overflow ? e : __ldg(bins + static_cast<int64_t>(off) + e);
+      const float4* r = jrec + static_cast<int64_t>(fid) * 4;
+      id = fid;
+      if (overflow && (__float_as_int(__ldg(r + 3).y) & kCandidate) != kCandidate) {
+        id = -1;
+        r0 = r1 = r2 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        return;
+      }
+      r0 = __ldg(r);
+      r1 = __ldg(r + 1);
+      r2 = __ldg(r + 2);
+    };
+    float4 n0, n1, n2;
+    int nid = -1;
+    if (lane < n) fetch(lane, n0, n1, n2, nid);
     for (int base = 0; base < n; base += kStage) {
       const int m = min(kStage, n - base);
       if (lane < m) {
-        const int fid = overflow ? base + lane : bins[static_cast<int64_t>(off) + base + lane];
-        const float4* r = jrec + static_cast<int64_t>(fid) * 4;
-        int id = fid;
-        if (overflow && (__float_as_int(__ldg(r + 3).y) & kCandidate) != kCandidate) id = -1;
-        rec[lane][0] = __ldg(r);
-        rec[lane][1] = __ldg(r + 1);
-        rec[lane][2] = __ldg(r + 2);
-        ids[lane] = id;
+        rec[lane][0] = n0;
+        rec[lane][1] = n1;
+        rec[lane][2] = n2;
+        ids[lane] = nid;
       }
       __syncwarp();
+      // prefetch the next chunk while this one is tested
+      if (base + kStage + lane < n) fetch(base + kStage + lane, n0, n1, n2, nid);
       for (int e = 0; e < m; ++e) {
         const float4 a = rec[e][0], b = rec[e][1], cz = rec[e][2];
 #pragma unroll
@@ -377,10 +413,18 @@ raster_kernel(RastBatch B, Geometry G, const float4* __restrict__ setup,
 // re-run for the three corners of the winning primitive only.
 __global__ void __launch_bounds__(256)
 tiled_shade_kernel(RastBatch B, const float4* __restrict__ setup, const int32_t* __restrict__ winner) {
-  const int64_t pix = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  __shared__ RastJob sJ;
+  __shared__ int s_job;
+  const int64_t row0 = static_cast<int64_t>(blockIdx.x) * blockDim.x;
+  const int64_t pix = row0 + threadIdx.x;
+  const int uj = block_uniform_job(B.jobs, B.n_jobs, row0, B.total_pixels,
+                                   [](const RastJob& j) { return j.pixel_begin; },
+                                   [](const RastJob& j) { return static_cast<int64_t>(j.width) * j.height; }, &s_job);
+  if (uj >= 0) load_job_to_shared(B.jobs + uj, &sJ);
+  __syncthreads();
   if (pix >= B.total_pixels) return;
-  const int jid = find_job(B.jobs, B.n_jobs, pix, [](const RastJob& j) { return j.pixel_begin; });
-  const RastJob& J = B.jobs[jid];
+  const RastJob& J = uj >= 0 ? sJ
+                             : B.jobs[find_job(B.jobs, B.n_jobs, pix, [](const RastJob& j) { return j.pixel_begin; })];
   const int64_t local = pix - J.pixel_begin;
   const int i = static_cast<int>(local / J.height), j = static_cast<int>(local % J.height);
   PixelResult r;
