@@ -51,6 +51,7 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-plain", action="store_true")
+    p.add_argument("--no-bwd", action="store_true")
     return p.parse_args()
 
 
@@ -224,6 +225,10 @@ def run_ours(args, rank, world, local):
         del plain
         torch.cuda.empty_cache()
 
+    fwd_bwd = {}
+    if not args.no_bwd:
+        fwd_bwd = measure_fwd_bwd(sb, args, stream, timed, world)
+
     e2e = None
     if not args.no_e2e:
         e2e = measure_e2e(flat, sb, runner, step, args, dev, stream, world)
@@ -254,6 +259,7 @@ def run_ours(args, rank, world, local):
             "parallelism": f"scene-sharded x{world} (no collective)",
         },
         "fwd_comparison": comparison,
+        "fwd_bwd": fwd_bwd,
         "roofline": roofline(prof, sb, flat, runner),
         "kernels": prof["summary"],
         "gpu_launches": kernels_per_step * args.steps,
@@ -267,6 +273,50 @@ def run_ours(args, rank, world, local):
         print(json.dumps(out), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def measure_fwd_bwd(sb, args, stream, timed, world):
+    """Forward + backward of an MSE loss against a fixed target image, per
+    step: render (prim-id buffer saved), dL/dcanvas, rast_backward into
+    reused gradient arrays (per-vertex, per-texel, per-scene camera/light)."""
+    import torch
+
+    from jaxrenderer_gb300 import batch as jb
+
+    out = {}
+    target = torch.rand((sb.n_scenes, W, H, 3), generator=torch.Generator().manual_seed(0)).to(sb.device)
+    scale = 2.0 / target.numel()
+    for form in ("tiled", "plain"):
+        if form == "plain" and args.no_plain:
+            continue
+        r = jb.BatchRunner(sb, form=form, want_prim_id=True)
+        grads = r.grad_buffers()
+        if form == "tiled":
+            r.capture()
+            fwd = r.replay
+        else:
+            fwd = lambda r=r: r.run(stream)  # noqa: E731
+
+        def step(r=r, fwd=fwd, grads=grads):
+            o = fwd()
+            g = (o.canvas - target) * scale
+            r.backward(g, out=grads)
+
+        steps = args.steps if form == "tiled" else max(1, min(args.steps, 3))
+        ms = timed(step, steps, 1 if form == "plain" else args.warmup)
+        out[form] = {"value": world * args.scenes / (ms / 1e3), "ms_per_step": ms, "steps": steps}
+        # backward alone
+        if form == "tiled":
+            fwd()
+            gc = (r.canvas - target) * scale
+            bms = timed(lambda: r.backward(gc, out=grads), steps, 1)
+            out["backward_ms"] = bms
+        del r, grads
+        torch.cuda.empty_cache()
+    if "plain" in out:
+        out["tiled_over_plain"] = out["plain"]["ms_per_step"] / out["tiled"]["ms_per_step"]
+    out["unit"] = UNIT
+    return out
 
 
 def profile_kernels(runner, steps, stream):

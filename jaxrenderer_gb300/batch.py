@@ -362,13 +362,8 @@ class BatchRunner:
         float32, for in-place updates of per-job matrices and light terms."""
         return self.main_jobs_dev.view(torch.float32).view(self.sb.n_scenes, -1)
 
-    def backward(self, grad_canvas: Optional[torch.Tensor], grad_zbuffer: Optional[torch.Tensor] = None,
-                 stream: Optional[torch.cuda.Stream] = None) -> Dict[str, torch.Tensor]:
-        """Gradients of the last run() of the main pass (rast_backward):
-        per-vertex position/normal, per-texel texture/specular exponent and
-        per-scene camera/light terms (RAST_GRAD_* layout, (N, 56))."""
-        if self.prim_id is None:
-            raise RuntimeError("backward needs the winning-primitive buffer: build the runner with want_prim_id=True")
+    def grad_buffers(self) -> Dict[str, torch.Tensor]:
+        """Zeroed gradient arrays matching the batch's pools (for backward(out=...))."""
         dev = self.sb.device
         P = self.pools
         g = {
@@ -380,6 +375,24 @@ class BatchRunner:
         }
         if "colour" in P:
             g["colour"] = torch.zeros_like(P["colour"])
+        return g
+
+    def backward(self, grad_canvas: Optional[torch.Tensor], grad_zbuffer: Optional[torch.Tensor] = None,
+                 stream: Optional[torch.cuda.Stream] = None,
+                 out: Optional[Dict[str, torch.Tensor]] = None) -> Dict[str, torch.Tensor]:
+        """Gradients of the last run() of the main pass (rast_backward):
+        per-vertex position/normal, per-texel texture/specular exponent and
+        per-scene camera/light terms (RAST_GRAD_* layout, (N, 56)).  With
+        `out` (from grad_buffers()) the arrays are zeroed and reused."""
+        if self.prim_id is None:
+            raise RuntimeError("backward needs the winning-primitive buffer: build the runner with want_prim_id=True")
+        dev = self.sb.device
+        if out is None:
+            g = self.grad_buffers()
+        else:
+            g = out
+            for t in g.values():
+                t.zero_()
         gp = _lib.RastGradPools()
         for k, t in g.items():
             setattr(gp, k, t.data_ptr())
