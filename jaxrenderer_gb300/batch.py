@@ -366,15 +366,8 @@ class BatchRunner:
         """Zeroed gradient arrays matching the batch's pools (for backward(out=...))."""
         dev = self.sb.device
         P = self.pools
-        g = {
-            "position": torch.zeros_like(P["position"]),
-            "normal": torch.zeros_like(P["normal"]),
-            "texture": torch.zeros_like(P["texture"]),
-            "specular_map": torch.zeros_like(P["specular_map"]),
-            "job_params": torch.zeros((self.sb.n_scenes, _lib.NPARAM), dtype=torch.float32, device=dev),
-        }
-        if "colour" in P:
-            g["colour"] = torch.zeros_like(P["colour"])
+        g = {k: torch.zeros_like(P[k]) for k in ("position", "normal", "colour", "texture", "specular_map") if k in P}
+        g["job_params"] = torch.zeros((self.sb.n_scenes, _lib.NPARAM), dtype=torch.float32, device=dev)
         return g
 
     def backward(self, grad_canvas: Optional[torch.Tensor], grad_zbuffer: Optional[torch.Tensor] = None,

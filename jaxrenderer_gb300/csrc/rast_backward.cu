@@ -59,7 +59,25 @@ __device__ __forceinline__ void add_texel_grad(float* g, int64_t base, int ch, c
   }
 }
 
-__global__ void __launch_bounds__(kThreads)
+// Per-scene parameters a shader's backward can touch (bit k = RAST_GRAD index k).
+__host__ __device__ constexpr unsigned long long range_bits(int lo, int n) {
+  return ((n >= 64 ? ~0ull : ((1ull << n) - 1ull)) << lo);
+}
+__host__ __device__ constexpr unsigned long long param_bits(int sh) {
+  return sh == RAST_SHADER_DEPTH ? range_bits(RAST_GRAD_WORLD_TO_CLIP, 16)
+       : (sh == RAST_SHADER_GOURAUD || sh == RAST_SHADER_GOURAUD_TEXTURE)
+           ? range_bits(RAST_GRAD_WORLD_TO_CLIP, 16) | range_bits(RAST_GRAD_LIGHT_DIRECTION, 6)
+       : sh == RAST_SHADER_PHONG
+           ? range_bits(RAST_GRAD_WORLD_TO_CLIP, 32) | range_bits(RAST_GRAD_LIGHT_DIRECTION, 6)
+       : (sh == RAST_SHADER_PHONG_REFLECTION || sh == RAST_SHADER_PHONG_REFLECTION_SHADOW)
+           ? range_bits(RAST_GRAD_WORLD_TO_CLIP, 32) | range_bits(RAST_GRAD_LIGHT_COLOUR, 18)
+       : range_bits(0, RAST_NPARAM);
+}
+
+// SH: the shader of every job of the launch, or -1 for a batch that mixes
+// shaders (every path compiled in, selected per job).
+template <int SH>
+__global__ void __launch_bounds__(kThreads, 2)
 backward_kernel(RastBatch B, const float* __restrict__ grad_canvas, const float* __restrict__ grad_zbuffer,
                 RastGradPools G) {
   __shared__ RastJob sJ;
@@ -73,7 +91,7 @@ backward_kernel(RastBatch B, const float* __restrict__ grad_canvas, const float*
   ParamGrad pg;
 #pragma unroll
   for (int k = 0; k < RAST_NPARAM; ++k) pg.v[k] = 0.0f;
-  const int sh = J.shader;
+  const int sh = SH >= 0 ? SH : J.shader;
   bool active = local < npix && J.n_faces > 0;
   int p = -1;
   int64_t pix = 0;
@@ -283,9 +301,9 @@ backward_kernel(RastBatch B, const float* __restrict__ grad_canvas, const float*
       } else if (sh == RAST_SHADER_PHONG_REFLECTION || sh == RAST_SHADER_PHONG_REFLECTION_SHADOW) {
         const bool shadowed = sh == RAST_SHADER_PHONG_REFLECTION_SHADOW;
         float v0[kMaxVarying], v1[kMaxVarying], v2[kMaxVarying], dummy[4];
-        vertex_shader(J, P, vid[0], dummy, v0);
-        vertex_shader(J, P, vid[1], dummy, v1);
-        vertex_shader(J, P, vid[2], dummy, v2);
+        vertex_shader<false>(J, P, vid[0], dummy, v0);
+        vertex_shader<false>(J, P, vid[1], dummy, v1);
+        vertex_shader<false>(J, P, vid[2], dummy, v2);
         float shadow[3] = {1.0f, 1.0f, 1.0f};
         bool lit = true;
         if (shadowed) {
@@ -466,9 +484,14 @@ backward_kernel(RastBatch B, const float* __restrict__ grad_canvas, const float*
   }
   // ---- per-scene parameter gradients: warp then block reduction
   if (G.job_params) {
+    constexpr unsigned long long bits = param_bits(SH);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 #pragma unroll
     for (int k = 0; k < RAST_NPARAM; ++k) {
+      if (!((bits >> k) & 1ull)) {
+        if (lane == 0) s_red[warp][k] = 0.0f;
+        continue;
+      }
       float v = pg.v[k];
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -500,6 +523,21 @@ extern "C" int rast_backward(const RastBatch* batch, const float* grad_canvas, c
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   const int64_t max_px = static_cast<int64_t>(b.max_width) * b.max_height;
   const dim3 grid(static_cast<unsigned>((max_px + bwd::kThreads - 1) / bwd::kThreads), static_cast<unsigned>(b.n_jobs));
-  bwd::backward_kernel<<<grid, bwd::kThreads, 0, s>>>(b, grad_canvas, grad_zbuffer, *grads);
+  const int mask = b.shader_mask;
+  auto only = [&](int sh) { return mask == (1 << sh); };
+  if (only(RAST_SHADER_DEPTH))
+    bwd::backward_kernel<RAST_SHADER_DEPTH><<<grid, bwd::kThreads, 0, s>>>(b, grad_canvas, grad_zbuffer, *grads);
+  else if (only(RAST_SHADER_GOURAUD))
+    bwd::backward_kernel<RAST_SHADER_GOURAUD><<<grid, bwd::kThreads, 0, s>>>(b, grad_canvas, grad_zbuffer, *grads);
+  else if (only(RAST_SHADER_GOURAUD_TEXTURE))
+    bwd::backward_kernel<RAST_SHADER_GOURAUD_TEXTURE><<<grid, bwd::kThreads, 0, s>>>(b, grad_canvas, grad_zbuffer, *grads);
+  else if (only(RAST_SHADER_PHONG))
+    bwd::backward_kernel<RAST_SHADER_PHONG><<<grid, bwd::kThreads, 0, s>>>(b, grad_canvas, grad_zbuffer, *grads);
+  else if (only(RAST_SHADER_PHONG_REFLECTION))
+    bwd::backward_kernel<RAST_SHADER_PHONG_REFLECTION><<<grid, bwd::kThreads, 0, s>>>(b, grad_canvas, grad_zbuffer, *grads);
+  else if (only(RAST_SHADER_PHONG_REFLECTION_SHADOW))
+    bwd::backward_kernel<RAST_SHADER_PHONG_REFLECTION_SHADOW><<<grid, bwd::kThreads, 0, s>>>(b, grad_canvas, grad_zbuffer, *grads);
+  else
+    bwd::backward_kernel<-1><<<grid, bwd::kThreads, 0, s>>>(b, grad_canvas, grad_zbuffer, *grads);
   return cudaGetLastError() == cudaSuccess ? RAST_OK : RAST_ERR_CUDA;
 }
