@@ -22,38 +22,36 @@ namespace rast {
 
 // -------------------------------------------------------------- kernels
 
+// Grid: (ceil(max_verts / 256), n_jobs).
 __global__ void __launch_bounds__(256)
 vertex_kernel(RastBatch B, float4* __restrict__ clip_out, float* __restrict__ var_out, int vstride) {
   __shared__ RastJob sJ;
-  __shared__ int s_job;
-  const int64_t row0 = static_cast<int64_t>(blockIdx.x) * blockDim.x;
-  const int64_t row = row0 + threadIdx.x;
-  const int uj = block_uniform_job(B.jobs, B.n_jobs, row0, B.total_vout,
-                                   [](const RastJob& j) { return j.vout_begin; },
-                                   [](const RastJob& j) { return static_cast<int64_t>(j.n_verts); }, &s_job);
-  if (uj >= 0) load_job_to_shared(B.jobs + uj, &sJ);
+  const int jid = blockIdx.y;
+  const int nv = __ldg(&B.jobs[jid].n_verts);
+  if (static_cast<int64_t>(blockIdx.x) * 256 >= nv) return;
+  load_job_to_shared(B.jobs + jid, &sJ);
   __syncthreads();
-  if (row >= B.total_vout) return;
-  const RastJob& J = uj >= 0 ? sJ : B.jobs[find_job_by_vout(B.jobs, B.n_jobs, row)];
+  const RastJob& J = sJ;
+  const int64_t v0 = static_cast<int64_t>(blockIdx.x) * 256 + threadIdx.x;
+  if (v0 >= nv) return;
+  const int64_t row = J.vout_begin + v0;
   const int v = static_cast<int>(row - J.vout_begin);
   float clip[4];
   float var[kMaxVarying];
   vertex_shader(J, B.pools, v, clip, var);
   clip_out[row] = make_float4(clip[0], clip[1], clip[2], clip[3]);
-  const int nv = varying_count(J.shader);
-  for (int k = 0; k < nv; ++k) var_out[row * vstride + k] = var[k];
+  const int nvar = varying_count(J.shader);
+  for (int k = 0; k < nvar; ++k) var_out[row * vstride + k] = var[k];
 }
 
+// Grid: (ceil(max_faces / 256), n_jobs).
 __global__ void __launch_bounds__(256)
 setup_kernel(RastBatch B, const float4* __restrict__ clip, float4* __restrict__ setup) {
-  __shared__ int s_job;
-  const int64_t row0 = static_cast<int64_t>(blockIdx.x) * blockDim.x;
-  const int64_t row = row0 + threadIdx.x;
-  const int uj = block_uniform_job(B.jobs, B.n_jobs, row0, B.total_setup,
-                                   [](const RastJob& j) { return j.setup_begin; },
-                                   [](const RastJob& j) { return static_cast<int64_t>(j.n_faces); }, &s_job);
-  if (row >= B.total_setup) return;
-  const RastJob& J = B.jobs[uj >= 0 ? uj : find_job_by_setup(B.jobs, B.n_jobs, row)];
+  const int jid = blockIdx.y;
+  const RastJob& J = B.jobs[jid];
+  const int64_t f0 = static_cast<int64_t>(blockIdx.x) * 256 + threadIdx.x;
+  if (f0 >= J.n_faces) return;
+  const int64_t row = J.setup_begin + f0;
   const int64_t f = row - J.setup_begin;
   const int32_t* face = B.pools.faces + (J.face_begin + f) * 3;
   float4 c[3];
@@ -199,12 +197,12 @@ static int render_plain(const RastBatch* batch, void* workspace, size_t workspac
   Profiler prof(profile, s);
 
   if (b.total_vout > 0) {
-    const unsigned grid = static_cast<unsigned>((b.total_vout + 255) / 256);
+    const dim3 grid(static_cast<unsigned>((b.max_verts + 255) / 256), static_cast<unsigned>(b.n_jobs));
     vertex_kernel<<<grid, 256, 0, s>>>(b, clip, var, L.vstride);
     prof.mark("vertex_kernel");
   }
   if (b.total_setup > 0) {
-    const unsigned grid = static_cast<unsigned>((b.total_setup + 255) / 256);
+    const dim3 grid(static_cast<unsigned>((b.max_faces + 255) / 256), static_cast<unsigned>(b.n_jobs));
     setup_kernel<<<grid, 256, 0, s>>>(b, clip, setup);
     prof.mark("setup_kernel");
   }

@@ -148,21 +148,20 @@ __device__ __forceinline__ void face_clip(const RastJob& J, const RastPools& P, 
   }
 }
 
+// Grid: (ceil(max_faces / kSetupThreads), n_jobs); blockIdx.y is the job.
 __global__ void __launch_bounds__(kSetupThreads)
 setup_bin_kernel(RastBatch B, Geometry G, float4* __restrict__ setup, ushort4* __restrict__ bbox,
                  uint32_t* __restrict__ counts) {
   __shared__ RastJob sJ;
-  __shared__ int s_job;
-  const int64_t row0 = static_cast<int64_t>(blockIdx.x) * blockDim.x;
-  const int64_t row = row0 + threadIdx.x;
-  const int uj = block_uniform_job(B.jobs, B.n_jobs, row0, B.total_setup,
-                                   [](const RastJob& j) { return j.setup_begin; },
-                                   [](const RastJob& j) { return static_cast<int64_t>(j.n_faces); }, &s_job);
-  if (uj >= 0) load_job_to_shared(B.jobs + uj, &sJ);
+  const int jid = blockIdx.y;
+  const int nf = __ldg(&B.jobs[jid].n_faces);
+  if (static_cast<int64_t>(blockIdx.x) * kSetupThreads >= nf) return;
+  load_job_to_shared(B.jobs + jid, &sJ);
   __syncthreads();
-  if (row >= B.total_setup) return;
-  const int jid = uj >= 0 ? uj : find_job_by_setup(B.jobs, B.n_jobs, row);
-  const RastJob& J = uj >= 0 ? sJ : B.jobs[jid];
+  const RastJob& J = sJ;
+  const int64_t f0 = static_cast<int64_t>(blockIdx.x) * kSetupThreads + threadIdx.x;
+  if (f0 >= nf) return;
+  const int64_t row = J.setup_begin + f0;
   const int64_t f = row - J.setup_begin;
   float4 c[3];
   face_clip(J, B.pools, f, c);
@@ -266,20 +265,14 @@ __global__ void __launch_bounds__(kSetupThreads)
 scatter_kernel(RastBatch B, Geometry G, const ushort4* __restrict__ bbox,
                const uint32_t* __restrict__ offsets, uint32_t* __restrict__ cursors,
                int32_t* __restrict__ bins) {
-  __shared__ int s_job;
-  __shared__ int64_t s_begin;
-  const int64_t row0 = static_cast<int64_t>(blockIdx.x) * blockDim.x;
-  const int64_t row = row0 + threadIdx.x;
-  const int uj = block_uniform_job(B.jobs, B.n_jobs, row0, B.total_setup,
-                                   [](const RastJob& j) { return j.setup_begin; },
-                                   [](const RastJob& j) { return static_cast<int64_t>(j.n_faces); }, &s_job);
-  if (threadIdx.x == 0 && uj >= 0) s_begin = B.jobs[uj].setup_begin;
-  __syncthreads();
-  if (row >= B.total_setup) return;
+  const int jid = blockIdx.y;
+  const int nf = __ldg(&B.jobs[jid].n_faces);
+  const int64_t f0 = static_cast<int64_t>(blockIdx.x) * kSetupThreads + threadIdx.x;
+  if (f0 >= nf) return;
+  const int64_t row = __ldg(&B.jobs[jid].setup_begin) + f0;
   const ushort4 bb = bbox[row];
   if (bb.x > bb.z) return;
-  const int jid = uj >= 0 ? uj : find_job_by_setup(B.jobs, B.n_jobs, row);
-  const int32_t fid = static_cast<int32_t>(row - (uj >= 0 ? s_begin : B.jobs[jid].setup_begin));
+  const int32_t fid = static_cast<int32_t>(f0);
   const int64_t tb = static_cast<int64_t>(jid) * G.tiles_per_job;
   for (int ty = bb.y; ty <= bb.w; ++ty)
     for (int tx = bb.x; tx <= bb.z; ++tx) {
@@ -411,20 +404,19 @@ raster_kernel(RastBatch B, Geometry G, const float4* __restrict__ setup,
 
 // Deferred shading: one thread per pixel of every job; the vertex shader is
 // re-run for the three corners of the winning primitive only.
+// Grid: (ceil(max pixels per job / 256), n_jobs).
 __global__ void __launch_bounds__(256)
 tiled_shade_kernel(RastBatch B, const float4* __restrict__ setup, const int32_t* __restrict__ winner) {
   __shared__ RastJob sJ;
-  __shared__ int s_job;
-  const int64_t row0 = static_cast<int64_t>(blockIdx.x) * blockDim.x;
-  const int64_t pix = row0 + threadIdx.x;
-  const int uj = block_uniform_job(B.jobs, B.n_jobs, row0, B.total_pixels,
-                                   [](const RastJob& j) { return j.pixel_begin; },
-                                   [](const RastJob& j) { return static_cast<int64_t>(j.width) * j.height; }, &s_job);
-  if (uj >= 0) load_job_to_shared(B.jobs + uj, &sJ);
+  const int jid = blockIdx.y;
+  const int64_t npx = static_cast<int64_t>(__ldg(&B.jobs[jid].width)) * __ldg(&B.jobs[jid].height);
+  if (static_cast<int64_t>(blockIdx.x) * 256 >= npx) return;
+  load_job_to_shared(B.jobs + jid, &sJ);
   __syncthreads();
-  if (pix >= B.total_pixels) return;
-  const RastJob& J = uj >= 0 ? sJ
-                             : B.jobs[find_job(B.jobs, B.n_jobs, pix, [](const RastJob& j) { return j.pixel_begin; })];
+  const RastJob& J = sJ;
+  const int64_t local0 = static_cast<int64_t>(blockIdx.x) * 256 + threadIdx.x;
+  if (local0 >= npx) return;
+  const int64_t pix = J.pixel_begin + local0;
   const int64_t local = pix - J.pixel_begin;
   const int i = static_cast<int>(local / J.height), j = static_cast<int>(local % J.height);
   PixelResult r;
@@ -514,7 +506,8 @@ static int render(const RastBatch* batch, const RastTiledConfig* cfg, void* work
   if (cudaMemsetAsync(misc, 0, 256, s) != cudaSuccess) return RAST_ERR_CUDA;
   prof.mark("memset");
   if (b.total_setup > 0) {
-    const unsigned grid = static_cast<unsigned>((b.total_setup + kSetupThreads - 1) / kSetupThreads);
+    const dim3 grid(static_cast<unsigned>((b.max_faces + kSetupThreads - 1) / kSetupThreads),
+                    static_cast<unsigned>(b.n_jobs));
     setup_bin_kernel<<<grid, kSetupThreads, 0, s>>>(b, L.G, setup, bbox, counts);
     prof.mark("setup_bin_kernel");
     scan_local_kernel<<<static_cast<unsigned>(L.n_scan_blocks), 256, 0, s>>>(counts, offsets, bsums, L.n_tiles);
@@ -545,8 +538,9 @@ static int render(const RastBatch* batch, const RastTiledConfig* cfg, void* work
         return RAST_ERR_CUDA;
     }
     prof.mark("raster_kernel");
-    const unsigned grid = static_cast<unsigned>((b.total_pixels + 255) / 256);
-    tiled_shade_kernel<<<grid, 256, 0, s>>>(b, setup, winner);
+    const int64_t max_px = static_cast<int64_t>(b.max_width) * b.max_height;
+    const dim3 sgrid(static_cast<unsigned>((max_px + 255) / 256), static_cast<unsigned>(b.n_jobs));
+    tiled_shade_kernel<<<sgrid, 256, 0, s>>>(b, setup, winner);
     prof.mark("tiled_shade_kernel");
   }
   const cudaError_t e = cudaGetLastError();

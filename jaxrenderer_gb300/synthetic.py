@@ -319,3 +319,56 @@ def phong_scene(rng: np.random.Generator, level: int = 4, texture_size: int = 64
     e = rng.normal(size=3)
     e = (radius * e / np.linalg.norm(e)).astype(F32)
     return PhongScene(v, pos, n, uv, f, tex, l, e)
+
+
+# ------------------------------------------- large overlapping single scene
+
+def overdraw_scene(rng: np.random.Generator, width: int = 960, height: int = 540,
+                   n_l4: int = 64, n_l5: int = 3, texture_size: int = 512):
+    """Single gouraud_texture scene of 64 level-4 + 3 level-5 icospheres
+    (389,120 triangles) at random overlapping placements in front of the
+    camera, a 512x512x3 U[0, 1] texture sampled in texel units, and a few
+    exact duplicate spheres (equal depths: ties resolved by lowest index).
+    Returns (JobSpec fields as a dict, estimated mean overdraw)."""
+    from .geometry import Camera
+
+    meshes = []
+    v4, f4 = icosphere(4)
+    v5, f5 = icosphere(5)
+    positions, normals, uvs, faces = [], [], [], []
+    offset = 0
+    centres, radii = [], []
+    kinds = [4] * n_l4 + [5] * n_l5
+    for k, lvl in enumerate(kinds):
+        v, f = (v4, f4) if lvl == 4 else (v5, f5)
+        if k >= 4 and k % 16 == 0:
+            c, r = centres[k - 4], radii[k - 4]  # exact duplicate of an earlier sphere
+        else:
+            c = rng.uniform((-2.2, -1.2, -1.5), (2.2, 1.2, 1.5))
+            r = rng.uniform(2.2, 3.6)
+        centres.append(c)
+        radii.append(r)
+        p = (v.astype(np.float64) * r + c).astype(F32)
+        positions.append(p)
+        normals.append(v.copy())
+        uvs.append((sphere_uv(v) * texture_size * rng.uniform(0.5, 2.0)).astype(F32))
+        faces.append(f + offset)
+        offset += len(v)
+    eye = np.array((0.0, 0.0, 9.0), F32)
+    view = Camera.view_matrix(eye, np.zeros(3, F32), np.array((0, 1, 0), F32))
+    proj = Camera.perspective_projection_matrix(45.0, width / height, 0.1, 100.0)
+    vp = Camera.viewport_matrix(np.zeros(2, np.int32), np.array((width, height)), 1.0)
+    cam = Camera.create(view, proj, vp)
+    # projected disc area estimate: f_px * r / depth
+    fpx = (height / 2) / np.tan(np.radians(22.5))
+    area = sum(np.pi * (fpx * r / (9.0 - c[2])) ** 2 for c, r in zip(centres, radii))
+    light = rng.normal(size=3)
+    light = (light / np.linalg.norm(light)).astype(F32)
+    spec = dict(
+        width=width, height=height, viewport=cam.viewport, world_to_clip=cam.world_to_clip,
+        world_to_eye_norm=cam.world_to_eye_norm, position=np.concatenate(positions),
+        normal=np.concatenate(normals), uv=np.concatenate(uvs), faces=np.concatenate(faces).astype(np.int32),
+        texture=rng.uniform(0, 1, (texture_size, texture_size, 3)).astype(F32),
+        light_direction=-light if light[2] < 0 else light, light_colour=np.ones(3, F32),
+    )
+    return spec, float(area / (width * height))
