@@ -58,7 +58,9 @@ typedef enum RastStatus {
   RAST_ERR_UNSUPPORTED = 4,
   RAST_ERR_TIMEOUT = 5,            /* a bounded device-side wait ran out */
   RAST_ERR_BIN_OVERFLOW = 6,       /* tiled form: a bin exceeded its capacity */
-  RAST_ERR_INDEX_OUT_OF_RANGE = 7  /* validation found a face index outside its vertex range */
+  RAST_ERR_INDEX_OUT_OF_RANGE = 7, /* validation found a face index outside its vertex range */
+  RAST_ERR_STATIC_SCRATCH_TOO_SMALL = 8 /* rast_render_tiled_static: batch needs more than
+                                           RAST_STATIC_SCRATCH_BYTES of workspace */
 } RastStatus;
 
 /* One pipeline.render call.  Offsets are element rows into RastPools
@@ -194,6 +196,31 @@ int rast_render_tiled(const RastBatch* batch, const RastTiledConfig* cfg, void* 
 /* rast_render_tiled with per-kernel timing (synchronises `stream`). */
 int rast_render_tiled_profiled(const RastBatch* batch, const RastTiledConfig* cfg, void* workspace,
                                size_t workspace_bytes, void* stream, RastProfile* profile);
+
+/* Tiled form for callers that cannot allocate device memory.
+ *
+ * No counterpart in the reference.  Some callers cannot call cudaMalloc
+ * where they render: code recording into a CUDA graph or running inside a
+ * framework callback that forbids allocation, real-time render threads
+ * that must not hit the allocator, plugins whose host owns all device
+ * memory.  This entry point takes no workspace: it runs rast_render_tiled
+ * out of one file-scope __device__ array of RAST_STATIC_SCRATCH_BYTES
+ * (64 MiB) that every GPU loading this library holds until the process
+ * exits.  It calls no cudaMalloc, cudaFree or allocating library routine.
+ *
+ *  - The first call on a device looks up the array's device address
+ *    (cudaGetSymbolAddress, with that device current) and caches it; make
+ *    that first call before any stream capture on that device.
+ *  - Batches whose tiled workspace (rast_tiled_workspace_bytes) exceeds
+ *    RAST_STATIC_SCRATCH_BYTES are rejected with
+ *    RAST_ERR_STATIC_SCRATCH_TOO_SMALL; nothing is launched.
+ *  - Every call shares the one array, which keeps the last call's contents
+ *    (counters that must start at zero are cleared on `stream` each call).
+ *    Calls whose work overlaps on the GPU (different streams, or
+ *    different host threads without ordering) race on it: serialise them.
+ * Outputs, statuses and results are those of rast_render_tiled. */
+#define RAST_STATIC_SCRATCH_BYTES (64u << 20)
+int rast_render_tiled_static(const RastBatch* batch, const RastTiledConfig* cfg, void* stream);
 
 /* Bin statistics of the last rast_render_tiled call that used `workspace`
  * (synchronises `stream`; for autotuning and diagnostics). */

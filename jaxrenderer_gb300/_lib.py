@@ -31,7 +31,9 @@ STATUS_NAMES = {
     5: "RAST_ERR_TIMEOUT",
     6: "RAST_ERR_BIN_OVERFLOW",
     7: "RAST_ERR_INDEX_OUT_OF_RANGE",
+    8: "RAST_ERR_STATIC_SCRATCH_TOO_SMALL",
 }
+STATIC_SCRATCH_BYTES = 64 << 20
 
 F16 = c_float * 16
 F3 = c_float * 3
@@ -162,6 +164,7 @@ PROTOTYPES = [
     ("rast_render_tiled", c_int, [POINTER(RastBatch), POINTER(RastTiledConfig), c_void_p, c_size_t, c_void_p]),
     ("rast_render_tiled_profiled", c_int,
      [POINTER(RastBatch), POINTER(RastTiledConfig), c_void_p, c_size_t, c_void_p, POINTER(RastProfile)]),
+    ("rast_render_tiled_static", c_int, [POINTER(RastBatch), POINTER(RastTiledConfig), c_void_p]),
     ("rast_tiled_stats", c_int,
      [POINTER(RastBatch), POINTER(RastTiledConfig), c_void_p, c_void_p, POINTER(RastTiledStats)]),
     ("rast_backward", c_int, [POINTER(RastBatch), c_void_p, c_void_p, POINTER(RastGradPools), c_void_p]),

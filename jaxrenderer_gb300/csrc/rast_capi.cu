@@ -12,6 +12,7 @@ extern "C" const char* rast_error_string(int status) {
     case RAST_ERR_TIMEOUT: return "device-side wait ran out of iterations";
     case RAST_ERR_BIN_OVERFLOW: return "tile bin capacity exceeded";
     case RAST_ERR_INDEX_OUT_OF_RANGE: return "index out of range";
+    case RAST_ERR_STATIC_SCRATCH_TOO_SMALL: return "batch exceeds the static scratch of rast_render_tiled_static";
     default: return "unknown status";
   }
 }

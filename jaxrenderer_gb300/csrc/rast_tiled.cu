@@ -17,6 +17,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <mutex>
 
 #include "rast_internal.cuh"
 
@@ -588,4 +589,45 @@ extern "C" int rast_render_tiled_profiled(const RastBatch* batch, const RastTile
                                           void* workspace, size_t workspace_bytes, void* stream,
                                           RastProfile* profile) {
   return tiled::render(batch, cfg, workspace, workspace_bytes, stream, profile);
+}
+
+// ------------------------------------------------ allocation-free variant
+
+namespace {
+
+// Workspace of rast_render_tiled_static: one per GPU that loads the library,
+// held until process exit.
+static __device__ __align__(256) unsigned char g_static_scratch[RAST_STATIC_SCRATCH_BYTES];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_static_mutex;
+void* g_static_ptr[kMaxDevices] = {};
+
+// Device address of g_static_scratch on the current device (host code sees
+// only a host-side stand-in for the symbol).  Looked up once per device.
+int static_scratch(void** out) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return RAST_ERR_CUDA;
+  if (dev < 0 || dev >= kMaxDevices) return RAST_ERR_UNSUPPORTED;
+  std::lock_guard<std::mutex> lock(g_static_mutex);
+  if (!g_static_ptr[dev]) {
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_static_scratch) != cudaSuccess || !p) return RAST_ERR_CUDA;
+    g_static_ptr[dev] = p;
+  }
+  *out = g_static_ptr[dev];
+  return RAST_OK;
+}
+
+}  // namespace
+
+extern "C" int rast_render_tiled_static(const RastBatch* batch, const RastTiledConfig* cfg, void* stream) {
+  int st = check_batch(batch);
+  if (st != RAST_OK) return st;
+  const size_t need = rast_tiled_workspace_bytes(batch, cfg);
+  if (need > RAST_STATIC_SCRATCH_BYTES) return RAST_ERR_STATIC_SCRATCH_TOO_SMALL;
+  void* scratch = nullptr;
+  st = static_scratch(&scratch);
+  if (st != RAST_OK) return st;
+  return tiled::render(batch, cfg, scratch, RAST_STATIC_SCRATCH_BYTES, stream, nullptr);
 }
