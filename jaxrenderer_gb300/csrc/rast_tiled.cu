@@ -316,7 +316,7 @@ raster_kernel(RastBatch B, Geometry G, const float4* __restrict__ setup,
     if (tx * TW >= W || ty * TH >= H) continue;
     const float sx = J.viewport[0], ox = J.viewport[3], sy = J.viewport[5], oy = J.viewport[7];
     const float vp22 = J.viewport[10], vp23 = J.viewport[11];
-    float x[PPL], y[PPL];
+    float x[PPL], y[PPL], best_z[PPL];
     int pi[PPL], pj[PPL];
     unsigned long long best[PPL];
     uint32_t second[PPL];
@@ -328,6 +328,7 @@ raster_kernel(RastBatch B, Geometry G, const float4* __restrict__ setup,
       x[q] = (static_cast<float>(pi[q]) - ox) / sx;
       y[q] = (static_cast<float>(pj[q]) - oy) / sy;
       best[q] = kEmptyKey;
+      best_z[q] = 0.0f;
       second[q] = 0xffffffffu;
     }
     const float4* jrec = setup + J.setup_begin * 4;
@@ -378,6 +379,7 @@ raster_kernel(RastBatch B, Geometry G, const float4* __restrict__ setup,
               if (key < best[q]) {
                 second[q] = min(second[q], static_cast<uint32_t>(best[q] >> 32));
                 best[q] = key;
+                best_z[q] = z;
               } else {
                 second[q] = min(second[q], static_cast<uint32_t>(key >> 32));
               }
@@ -387,13 +389,38 @@ raster_kernel(RastBatch B, Geometry G, const float4* __restrict__ setup,
       }
       __syncwarp();
     }
+    const bool depth_only = J.shader == RAST_SHADER_DEPTH;
 #pragma unroll
     for (int q = 0; q < PPL; ++q) {
       if (pi[q] < W && pj[q] < H) {
         const uint32_t o1 = static_cast<uint32_t>(best[q] >> 32);
-        winner[J.pixel_begin + static_cast<int64_t>(pi[q]) * H + pj[q]] =
-            (best[q] == kEmptyKey || o1 == kInfOrder) ? -1 : static_cast<int32_t>(best[q] & 0xffffffffu);
+        const bool found = !(best[q] == kEmptyKey || o1 == kInfOrder);
+        const int64_t pix = J.pixel_begin + static_cast<int64_t>(pi[q]) * H + pj[q];
         if (is_near_tie(best[q], second[q])) ++tie_count;
+        if (!depth_only) {
+          winner[pix] = found ? static_cast<int32_t>(best[q] & 0xffffffffu) : -1;
+          continue;
+        }
+        // DepthShader: the fragment keeps everything and writes the default
+        // depth, so the pixel resolves here (same operations as
+        // resolve_pixel): the winner's depth, or primitive 0's chooser fallback.
+        bool keep = found;
+        float z = best_z[q];
+        int prim = found ? static_cast<int>(best[q] & 0xffffffffu) : 0;
+        if (!found && J.n_faces > 0) {
+          const float4 a = __ldg(jrec), b = __ldg(jrec + 1), cz = __ldg(jrec + 2), d = __ldg(jrec + 3);
+          const float c0 = (x[q] * a.x + y[q] * a.w) + b.z;
+          const float c1 = (x[q] * a.y + y[q] * b.x) + b.w;
+          const float c2 = (x[q] * a.z + y[q] * b.y) + cz.x;
+          keep = (__float_as_int(d.y) & kKeep) && c0 >= 0.0f && c1 >= 0.0f && c2 >= 0.0f;
+          z = ((c0 * cz.y + c1 * cz.z) + c2 * cz.w) * vp22 + vp23;
+        }
+        PixelResult r;
+        r.keep = keep;
+        r.z = z;
+        r.prim = keep ? prim : -1;
+        r.colour[0] = r.colour[1] = r.colour[2] = 0.0f;
+        store_pixel(J, B.pools, pix, r);
       }
     }
   }
@@ -407,11 +434,13 @@ raster_kernel(RastBatch B, Geometry G, const float4* __restrict__ setup,
 // re-run for the three corners of the winning primitive only.
 // Grid: (ceil(max pixels per job / 256), n_jobs).
 __global__ void __launch_bounds__(256)
-tiled_shade_kernel(RastBatch B, const float4* __restrict__ setup, const int32_t* __restrict__ winner) {
+tiled_shade_kernel(RastBatch B, const float4* __restrict__ setup, const int32_t* __restrict__ winner,
+                   bool depth_resolved) {
   __shared__ RastJob sJ;
   const int jid = blockIdx.y;
   const int64_t npx = static_cast<int64_t>(__ldg(&B.jobs[jid].width)) * __ldg(&B.jobs[jid].height);
   if (static_cast<int64_t>(blockIdx.x) * 256 >= npx) return;
+  if (depth_resolved && __ldg(&B.jobs[jid].shader) == RAST_SHADER_DEPTH) return;  // done by the raster kernel
   load_job_to_shared(B.jobs + jid, &sJ);
   __syncthreads();
   const RastJob& J = sJ;
@@ -541,8 +570,10 @@ static int render(const RastBatch* batch, const RastTiledConfig* cfg, void* work
     prof.mark("raster_kernel");
     const int64_t max_px = static_cast<int64_t>(b.max_width) * b.max_height;
     const dim3 sgrid(static_cast<unsigned>((max_px + 255) / 256), static_cast<unsigned>(b.n_jobs));
-    tiled_shade_kernel<<<sgrid, 256, 0, s>>>(b, setup, winner);
-    prof.mark("tiled_shade_kernel");
+    if (b.shader_mask != (1 << RAST_SHADER_DEPTH) || b.total_setup == 0) {
+      tiled_shade_kernel<<<sgrid, 256, 0, s>>>(b, setup, winner, b.total_setup > 0);
+      prof.mark("tiled_shade_kernel");
+    }
   }
   const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return RAST_ERR_CUDA;
