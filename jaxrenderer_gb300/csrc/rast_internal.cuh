@@ -105,9 +105,11 @@ __device__ __forceinline__ void load_job_to_shared(const RastJob* job, RastJob* 
 // Where the vertex varyings of a face come from: the vertex kernel's output
 // (plain form) or a recomputation of the vertex shader (tiled form).
 struct VaryingSource {
-  const float* var;   // nullptr: recompute
+  const float* var;   // per-vertex varyings (plain form), or nullptr
   int vstride;
   int64_t vout_begin;
+  const float* fvar = nullptr;  // per-face varyings of visible faces (tiled form): 3 rows of vstride per face
+  int64_t setup_begin = 0;
 };
 
 struct PixelResult {
@@ -150,14 +152,25 @@ __device__ __forceinline__ void resolve_pixel(const RastJob& J, const RastPools&
     const int i0 = gather_clamp(face[0], J.n_verts);
     const int i1 = gather_clamp(face[1], J.n_verts);
     const int i2 = gather_clamp(face[2], J.n_verts);
-    if (src.var) {
-      const float* r0 = src.var + (src.vout_begin + i0) * src.vstride;
-      const float* r1 = src.var + (src.vout_begin + i1) * src.vstride;
-      const float* r2 = src.var + (src.vout_begin + i2) * src.vstride;
-      for (int k = 0; k < nv; ++k) {
-        v0[k] = r0[k];
-        v1[k] = r1[k];
-        v2[k] = r2[k];
+    if (src.fvar || src.var) {
+      const float *r0, *r1, *r2;
+      if (src.fvar) {
+        r0 = src.fvar + ((src.setup_begin + p) * 3) * src.vstride;
+        r1 = r0 + src.vstride;
+        r2 = r1 + src.vstride;
+      } else {
+        r0 = src.var + (src.vout_begin + i0) * src.vstride;
+        r1 = src.var + (src.vout_begin + i1) * src.vstride;
+        r2 = src.var + (src.vout_begin + i2) * src.vstride;
+      }
+      // constant indices keep the three rows in registers
+#pragma unroll
+      for (int k = 0; k < kMaxVarying; ++k) {
+        if (k < nv) {
+          v0[k] = __ldg(r0 + k);
+          v1[k] = __ldg(r1 + k);
+          v2[k] = __ldg(r2 + k);
+        }
       }
     } else {
       float clip[4];

@@ -172,6 +172,17 @@ __device__ __forceinline__ void inv3(const float* m, float* out) {
   }
 }
 
+// min that propagates NaN (PTX min.NaN): min_nan(a, min_nan(b, c)) >= 0 is
+// exactly (a >= 0 && b >= 0 && c >= 0), NaN failing as in the reference.
+__device__ __forceinline__ float min_nan(float a, float b) {
+  float r;
+  asm("min.NaN.f32 %0, %1, %2;" : "=f"(r) : "f"(a), "f"(b));
+  return r;
+}
+__device__ __forceinline__ bool all_nonneg(float a, float b, float c) {
+  return min_nan(a, min_nan(b, c)) >= 0.0f;
+}
+
 // max(x, 0) of jnp.maximum / lax.max: NaN propagates, -0 -> +0.
 __device__ __forceinline__ float max0(float x) {
   return (x != x) ? x : (x > 0.0f ? x : 0.0f);

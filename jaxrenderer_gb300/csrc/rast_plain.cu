@@ -96,7 +96,7 @@ scan_kernel(RastBatch B, const float4* __restrict__ setup, int32_t* __restrict__
       const float c0 = (x * a.x + y * a.w) + b.z;
       const float c1 = (x * a.y + y * b.x) + b.w;
       const float c2 = (x * a.z + y * b.y) + cz.x;
-      if (c0 >= 0.0f && c1 >= 0.0f && c2 >= 0.0f) {
+      if (all_nonneg(c0, c1, c2)) {
         if ((s_flag[p] & kCandidate) == kCandidate) {
           const float z = ((c0 * cz.y + c1 * cz.z) + c2 * cz.w) * vp22 + vp23;
           const unsigned long long key = pack_key(z, base + p);

@@ -295,7 +295,7 @@ __global__ void __launch_bounds__(32 * kRasterWarps)
 raster_kernel(RastBatch B, Geometry G, const float4* __restrict__ setup,
               const uint32_t* __restrict__ counts, const uint32_t* __restrict__ offsets,
               const int32_t* __restrict__ bins, int32_t* __restrict__ winner,
-              unsigned int* __restrict__ work, int64_t n_tiles) {
+              unsigned int* __restrict__ work, int64_t n_tiles, unsigned char* __restrict__ visible) {
   constexpr int PPL = TW * TH / 32;
   __shared__ float4 s_rec[kRasterWarps][kStage][3];
   __shared__ int s_id[kRasterWarps][kStage];
@@ -316,17 +316,18 @@ raster_kernel(RastBatch B, Geometry G, const float4* __restrict__ setup,
     if (tx * TW >= W || ty * TH >= H) continue;
     const float sx = J.viewport[0], ox = J.viewport[3], sy = J.viewport[5], oy = J.viewport[7];
     const float vp22 = J.viewport[10], vp23 = J.viewport[11];
-    float x[PPL], y[PPL], best_z[PPL];
-    int pi[PPL], pj[PPL];
+    // lane -> one column j of the tile (TH divides 32) and PPL rows i:
+    // every pixel of a lane shares y, so y * inv[1][k] is computed once per
+    // entry (the same rounded product each pixel would compute).
+    constexpr int LPC = 32 / TH;
+    const int pj = ty * TH + lane % TH;
+    const float y = (static_cast<float>(pj) - oy) / sy;
+    float x[PPL], best_z[PPL];
     unsigned long long best[PPL];
     uint32_t second[PPL];
 #pragma unroll
     for (int q = 0; q < PPL; ++q) {
-      const int p = q * 32 + lane;  // pixel of the tile, y fastest
-      pj[q] = ty * TH + (p % TH);
-      pi[q] = tx * TW + (p / TH);
-      x[q] = (static_cast<float>(pi[q]) - ox) / sx;
-      y[q] = (static_cast<float>(pj[q]) - oy) / sy;
+      x[q] = (static_cast<float>(tx * TW + q * LPC + lane / TH) - ox) / sx;
       best[q] = kEmptyKey;
       best_z[q] = 0.0f;
       second[q] = 0xffffffffu;
@@ -366,12 +367,13 @@ raster_kernel(RastBatch B, Geometry G, const float4* __restrict__ setup,
       if (base + kStage + lane < n) fetch(base + kStage + lane, n0, n1, n2, nid);
       for (int e = 0; e < m; ++e) {
         const float4 a = rec[e][0], b = rec[e][1], cz = rec[e][2];
+        const float y0 = y * a.w, y1 = y * b.x, y2 = y * b.y;
 #pragma unroll
         for (int q = 0; q < PPL; ++q) {
-          const float c0 = (x[q] * a.x + y[q] * a.w) + b.z;
-          const float c1 = (x[q] * a.y + y[q] * b.x) + b.w;
-          const float c2 = (x[q] * a.z + y[q] * b.y) + cz.x;
-          if (c0 >= 0.0f && c1 >= 0.0f && c2 >= 0.0f) {
+          const float c0 = (x[q] * a.x + y0) + b.z;
+          const float c1 = (x[q] * a.y + y1) + b.w;
+          const float c2 = (x[q] * a.z + y2) + cz.x;
+          if (all_nonneg(c0, c1, c2)) {
             const int id = ids[e];
             if (id >= 0) {
               const float z = ((c0 * cz.y + c1 * cz.z) + c2 * cz.w) * vp22 + vp23;
@@ -392,13 +394,18 @@ raster_kernel(RastBatch B, Geometry G, const float4* __restrict__ setup,
     const bool depth_only = J.shader == RAST_SHADER_DEPTH;
 #pragma unroll
     for (int q = 0; q < PPL; ++q) {
-      if (pi[q] < W && pj[q] < H) {
+      const int pi = tx * TW + q * LPC + lane / TH;
+      if (pi < W && pj < H) {
         const uint32_t o1 = static_cast<uint32_t>(best[q] >> 32);
         const bool found = !(best[q] == kEmptyKey || o1 == kInfOrder);
-        const int64_t pix = J.pixel_begin + static_cast<int64_t>(pi[q]) * H + pj[q];
+        const int64_t pix = J.pixel_begin + static_cast<int64_t>(pi) * H + pj;
         if (is_near_tie(best[q], second[q])) ++tie_count;
         if (!depth_only) {
-          winner[pix] = found ? static_cast<int32_t>(best[q] & 0xffffffffu) : -1;
+          const int32_t w = found ? static_cast<int32_t>(best[q] & 0xffffffffu) : -1;
+          winner[pix] = w;
+          // faces whose varyings the shade needs: winners, and face 0 for the
+          // chooser's fallback
+          if (visible && J.n_faces > 0) visible[J.setup_begin + (w < 0 ? 0 : w)] = 1;
           continue;
         }
         // DepthShader: the fragment keeps everything and writes the default
@@ -409,10 +416,10 @@ raster_kernel(RastBatch B, Geometry G, const float4* __restrict__ setup,
         int prim = found ? static_cast<int>(best[q] & 0xffffffffu) : 0;
         if (!found && J.n_faces > 0) {
           const float4 a = __ldg(jrec), b = __ldg(jrec + 1), cz = __ldg(jrec + 2), d = __ldg(jrec + 3);
-          const float c0 = (x[q] * a.x + y[q] * a.w) + b.z;
-          const float c1 = (x[q] * a.y + y[q] * b.x) + b.w;
-          const float c2 = (x[q] * a.z + y[q] * b.y) + cz.x;
-          keep = (__float_as_int(d.y) & kKeep) && c0 >= 0.0f && c1 >= 0.0f && c2 >= 0.0f;
+          const float c0 = (x[q] * a.x + y * a.w) + b.z;
+          const float c1 = (x[q] * a.y + y * b.x) + b.w;
+          const float c2 = (x[q] * a.z + y * b.y) + cz.x;
+          keep = (__float_as_int(d.y) & kKeep) && all_nonneg(c0, c1, c2);
           z = ((c0 * cz.y + c1 * cz.z) + c2 * cz.w) * vp22 + vp23;
         }
         PixelResult r;
@@ -430,12 +437,37 @@ raster_kernel(RastBatch B, Geometry G, const float4* __restrict__ setup,
   }
 }
 
-// Deferred shading: one thread per pixel of every job; the vertex shader is
-// re-run for the three corners of the winning primitive only.
+// Vertex varyings of the three corners of every face some pixel needs
+// (marked by the raster kernel), stored per face: the shade then reads them
+// instead of re-running the vertex shader per pixel.
+// Grid: (ceil(max_faces / 128), n_jobs).
+__global__ void __launch_bounds__(128)
+face_varyings_kernel(RastBatch B, const unsigned char* __restrict__ visible, float* __restrict__ fvar,
+                     int vstride) {
+  const int jid = blockIdx.y;
+  const RastJob& J = B.jobs[jid];
+  const int64_t f0 = static_cast<int64_t>(blockIdx.x) * 128 + threadIdx.x;
+  if (f0 >= __ldg(&J.n_faces)) return;
+  const int64_t row = __ldg(&J.setup_begin) + f0;
+  if (!visible[row]) return;
+  if (J.shader == RAST_SHADER_DEPTH) return;
+  const int32_t* face = B.pools.faces + (J.face_begin + f0) * 3;
+  const int nv = varying_count(J.shader);
+  float* out = fvar + row * 3 * vstride;
+#pragma unroll 1
+  for (int k = 0; k < 3; ++k) {
+    float var[kMaxVarying], clip[4];
+    vertex_shader<false>(J, B.pools, gather_clamp(__ldg(face + k), J.n_verts), clip, var);
+    for (int q = 0; q < nv; ++q) out[k * vstride + q] = var[q];
+  }
+}
+
+// Deferred shading: one thread per pixel of every job, reading the winner's
+// corner varyings computed once per visible face.
 // Grid: (ceil(max pixels per job / 256), n_jobs).
 __global__ void __launch_bounds__(256)
 tiled_shade_kernel(RastBatch B, const float4* __restrict__ setup, const int32_t* __restrict__ winner,
-                   bool depth_resolved) {
+                   bool depth_resolved, const float* __restrict__ fvar, int vstride) {
   __shared__ RastJob sJ;
   const int jid = blockIdx.y;
   const int64_t npx = static_cast<int64_t>(__ldg(&B.jobs[jid].width)) * __ldg(&B.jobs[jid].height);
@@ -450,7 +482,8 @@ tiled_shade_kernel(RastBatch B, const float4* __restrict__ setup, const int32_t*
   const int64_t local = pix - J.pixel_begin;
   const int i = static_cast<int>(local / J.height), j = static_cast<int>(local % J.height);
   PixelResult r;
-  resolve_pixel(J, B.pools, setup + J.setup_begin * 4, i, j, winner[pix], VaryingSource{nullptr, 0, 0}, &r);
+  VaryingSource src{nullptr, vstride, 0, fvar, J.setup_begin};
+  resolve_pixel(J, B.pools, setup + J.setup_begin * 4, i, j, winner[pix], src, &r);
   store_pixel(J, B.pools, pix, r);
 }
 
@@ -465,7 +498,8 @@ inline uint64_t default_bin_capacity(const RastBatch& b) {
 
 struct Layout {
   size_t setup_off, bbox_off, counts_off, offsets_off, cursors_off, bsums_off, bins_off, winner_off,
-      misc_off, total;
+      vis_off, fvar_off, misc_off, total;
+  int vstride;
   int64_t n_tiles, n_scan_blocks;
   uint64_t bin_capacity;
   Geometry G;
@@ -495,6 +529,13 @@ static Layout layout(const RastBatch& b, TileShape ts, uint64_t bin_capacity) {
   L.bsums_off = take(static_cast<size_t>(L.n_scan_blocks) * 4);
   L.bins_off = take(static_cast<size_t>(bin_capacity) * 4);
   L.winner_off = take(static_cast<size_t>(b.total_pixels) * 4);
+  int vstride = 0;
+  for (int sh = 0; sh < 7; ++sh)
+    if (b.shader_mask & (1 << sh)) vstride = std::max(vstride, varying_count(sh));
+  L.vstride = vstride;
+  const bool shading = vstride > 0;
+  L.vis_off = take(shading ? static_cast<size_t>(b.total_setup) : 0);
+  L.fvar_off = take(shading ? static_cast<size_t>(b.total_setup) * 3 * vstride * sizeof(float) : 0);
   L.misc_off = take(256);
   L.total = off;
   return L;
@@ -534,6 +575,10 @@ static int render(const RastBatch* batch, const RastTiledConfig* cfg, void* work
   // counts and cursors are adjacent: one memset clears both, plus the counters
   if (cudaMemsetAsync(counts, 0, L.offsets_off - L.counts_off, s) != cudaSuccess) return RAST_ERR_CUDA;
   if (cudaMemsetAsync(misc, 0, 256, s) != cudaSuccess) return RAST_ERR_CUDA;
+  unsigned char* vis = L.vstride > 0 ? reinterpret_cast<unsigned char*>(ws + L.vis_off) : nullptr;
+  float* fvar = L.vstride > 0 ? reinterpret_cast<float*>(ws + L.fvar_off) : nullptr;
+  if (vis && b.total_setup > 0 && cudaMemsetAsync(vis, 0, static_cast<size_t>(b.total_setup), s) != cudaSuccess)
+    return RAST_ERR_CUDA;
   prof.mark("memset");
   if (b.total_setup > 0) {
     const dim3 grid(static_cast<unsigned>((b.max_faces + kSetupThreads - 1) / kSetupThreads),
@@ -554,15 +599,15 @@ static int render(const RastBatch* batch, const RastTiledConfig* cfg, void* work
     if (b.total_setup > 0) {
       const unsigned grid = static_cast<unsigned>(std::max(sms, 1) * 8);
       if (ts.tw == 8 && ts.th == 8)
-        raster_kernel<8, 8><<<grid, 32 * kRasterWarps, 0, s>>>(b, L.G, setup, counts, offsets, bins, winner, misc, L.n_tiles);
+        raster_kernel<8, 8><<<grid, 32 * kRasterWarps, 0, s>>>(b, L.G, setup, counts, offsets, bins, winner, misc, L.n_tiles, vis);
       else if (ts.tw == 16 && ts.th == 16)
-        raster_kernel<16, 16><<<grid, 32 * kRasterWarps, 0, s>>>(b, L.G, setup, counts, offsets, bins, winner, misc, L.n_tiles);
+        raster_kernel<16, 16><<<grid, 32 * kRasterWarps, 0, s>>>(b, L.G, setup, counts, offsets, bins, winner, misc, L.n_tiles, vis);
       else if (ts.tw == 32 && ts.th == 8)
-        raster_kernel<32, 8><<<grid, 32 * kRasterWarps, 0, s>>>(b, L.G, setup, counts, offsets, bins, winner, misc, L.n_tiles);
+        raster_kernel<32, 8><<<grid, 32 * kRasterWarps, 0, s>>>(b, L.G, setup, counts, offsets, bins, winner, misc, L.n_tiles, vis);
       else if (ts.tw == 8 && ts.th == 32)
-        raster_kernel<8, 32><<<grid, 32 * kRasterWarps, 0, s>>>(b, L.G, setup, counts, offsets, bins, winner, misc, L.n_tiles);
+        raster_kernel<8, 32><<<grid, 32 * kRasterWarps, 0, s>>>(b, L.G, setup, counts, offsets, bins, winner, misc, L.n_tiles, vis);
       else
-        raster_kernel<16, 8><<<grid, 32 * kRasterWarps, 0, s>>>(b, L.G, setup, counts, offsets, bins, winner, misc, L.n_tiles);
+        raster_kernel<16, 8><<<grid, 32 * kRasterWarps, 0, s>>>(b, L.G, setup, counts, offsets, bins, winner, misc, L.n_tiles, vis);
     } else {
       if (cudaMemsetAsync(winner, 0xff, static_cast<size_t>(b.total_pixels) * 4, s) != cudaSuccess)
         return RAST_ERR_CUDA;
@@ -571,7 +616,14 @@ static int render(const RastBatch* batch, const RastTiledConfig* cfg, void* work
     const int64_t max_px = static_cast<int64_t>(b.max_width) * b.max_height;
     const dim3 sgrid(static_cast<unsigned>((max_px + 255) / 256), static_cast<unsigned>(b.n_jobs));
     if (b.shader_mask != (1 << RAST_SHADER_DEPTH) || b.total_setup == 0) {
-      tiled_shade_kernel<<<sgrid, 256, 0, s>>>(b, setup, winner, b.total_setup > 0);
+      const bool pre = fvar != nullptr && b.total_setup > 0;
+      if (pre) {
+        const dim3 fgrid(static_cast<unsigned>((b.max_faces + 127) / 128), static_cast<unsigned>(b.n_jobs));
+        face_varyings_kernel<<<fgrid, 128, 0, s>>>(b, vis, fvar, L.vstride);
+        prof.mark("face_varyings_kernel");
+      }
+      tiled_shade_kernel<<<sgrid, 256, 0, s>>>(b, setup, winner, b.total_setup > 0, pre ? fvar : nullptr,
+                                               L.vstride);
       prof.mark("tiled_shade_kernel");
     }
   }
