@@ -305,12 +305,17 @@ def measure_fwd_bwd(sb, args, stream, timed, world):
         steps = args.steps if form == "tiled" else max(1, min(args.steps, 3))
         ms = timed(step, steps, 1 if form == "plain" else args.warmup)
         out[form] = {"value": world * args.scenes / (ms / 1e3), "ms_per_step": ms, "steps": steps}
-        # backward alone
+        # backward alone, and its kernels (CUDA events inside the library)
         if form == "tiled":
+            from jaxrenderer_gb300 import _lib
+
             fwd()
             gc = (r.canvas - target) * scale
             bms = timed(lambda: r.backward(gc, out=grads), steps, 1)
             out["backward_ms"] = bms
+            prof = _lib.RastProfile()
+            r.backward(gc, out=grads, profile=prof)
+            out["backward_kernels_ms"] = {prof.names[k].decode(): prof.ms[k] for k in range(prof.n)}
         del r, grads
         torch.cuda.empty_cache()
     if "plain" in out:

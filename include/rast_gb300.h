@@ -263,13 +263,23 @@ typedef struct RastGradPools {
   float* job_params;    /* (n_jobs, RAST_NPARAM) per-job camera/light gradients */
 } RastGradPools;
 
-/* One thread per pixel whose fragment was kept: recompute, then reverse
- * mode through fragment, interpolation, barycentrics, 3x3 inverse and clip
- * transform.  uv gets no gradient (nearest texel: floor).  Not available for
- * PHONG_DARBOUX (RAST_ERR_UNSUPPORTED).  grad_canvas (pixels, 3) and
- * grad_zbuffer (pixels) may each be NULL. */
+/* Workspace rast_backward needs for `batch` (256-byte aligned base). */
+size_t rast_backward_workspace_bytes(const RastBatch* batch);
+
+/* Reverse mode, split by dependency: per visible face (3x3 inverse of the
+ * [x, y, w] clip rows), per corner vertex (vertex shader varyings), per kept
+ * pixel (fragment and interpolation backward, accumulating dL/d inverse and
+ * dL/d varyings), then per face (inverse and clip transform backward) and
+ * per vertex (vertex shader backward).  uv gets no gradient (nearest texel:
+ * floor).  Not available for PHONG_DARBOUX (RAST_ERR_UNSUPPORTED).
+ * grad_canvas (pixels, 3) and grad_zbuffer (pixels) may each be NULL. */
 int rast_backward(const RastBatch* batch, const float* grad_canvas, const float* grad_zbuffer,
-                  const RastGradPools* grads, void* stream);
+                  const RastGradPools* grads, void* workspace, size_t workspace_bytes, void* stream);
+
+/* rast_backward with per-kernel timing (synchronises `stream`). */
+int rast_backward_profiled(const RastBatch* batch, const float* grad_canvas, const float* grad_zbuffer,
+                           const RastGradPools* grads, void* workspace, size_t workspace_bytes, void* stream,
+                           RastProfile* profile);
 
 /* Host-side validation of one job against pool sizes (no device access):
  * returns RAST_ERR_INVALID_ARGUMENT for inconsistent sizes. */

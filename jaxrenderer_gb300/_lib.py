@@ -167,7 +167,12 @@ PROTOTYPES = [
     ("rast_render_tiled_static", c_int, [POINTER(RastBatch), POINTER(RastTiledConfig), c_void_p]),
     ("rast_tiled_stats", c_int,
      [POINTER(RastBatch), POINTER(RastTiledConfig), c_void_p, c_void_p, POINTER(RastTiledStats)]),
-    ("rast_backward", c_int, [POINTER(RastBatch), c_void_p, c_void_p, POINTER(RastGradPools), c_void_p]),
+    ("rast_backward_workspace_bytes", c_size_t, [POINTER(RastBatch)]),
+    ("rast_backward", c_int,
+     [POINTER(RastBatch), c_void_p, c_void_p, POINTER(RastGradPools), c_void_p, c_size_t, c_void_p]),
+    ("rast_backward_profiled", c_int,
+     [POINTER(RastBatch), c_void_p, c_void_p, POINTER(RastGradPools), c_void_p, c_size_t, c_void_p,
+      POINTER(RastProfile)]),
     ("rast_validate_job", c_int, [POINTER(RastJob)]),
     ("rast_error_string", ctypes.c_char_p, [c_int]),
     ("rast_abi_version", c_int, []),

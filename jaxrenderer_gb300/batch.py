@@ -372,7 +372,7 @@ class BatchRunner:
 
     def backward(self, grad_canvas: Optional[torch.Tensor], grad_zbuffer: Optional[torch.Tensor] = None,
                  stream: Optional[torch.cuda.Stream] = None,
-                 out: Optional[Dict[str, torch.Tensor]] = None) -> Dict[str, torch.Tensor]:
+                 out: Optional[Dict[str, torch.Tensor]] = None, profile=None) -> Dict[str, torch.Tensor]:
         """Gradients of the last run() of the main pass (rast_backward):
         per-vertex position/normal, per-texel texture/specular exponent and
         per-scene camera/light terms (RAST_GRAD_* layout, (N, 56)).  With
@@ -392,8 +392,16 @@ class BatchRunner:
         gc = grad_canvas.contiguous() if grad_canvas is not None else None
         gz = grad_zbuffer.contiguous() if grad_zbuffer is not None else None
         s = stream if stream is not None else torch.cuda.current_stream(dev)
-        st = self.lib.rast_backward(ctypes.byref(self.main_batch), gc.data_ptr() if gc is not None else None,
-                                    gz.data_ptr() if gz is not None else None, ctypes.byref(gp), s.cuda_stream)
+        nbytes = int(self.lib.rast_backward_workspace_bytes(ctypes.byref(self.main_batch)))
+        if getattr(self, "_bwd_ws", None) is None or self._bwd_ws.numel() < nbytes:
+            self._bwd_ws = torch.empty(max(nbytes, 256), dtype=torch.uint8, device=dev)
+        args = (ctypes.byref(self.main_batch), gc.data_ptr() if gc is not None else None,
+                gz.data_ptr() if gz is not None else None, ctypes.byref(gp), self._bwd_ws.data_ptr(), nbytes,
+                s.cuda_stream)
+        if profile is None:
+            st = self.lib.rast_backward(*args)
+        else:
+            st = self.lib.rast_backward_profiled(*args, ctypes.byref(profile))
         _lib.check(st, "rast_backward")
         return g
 
