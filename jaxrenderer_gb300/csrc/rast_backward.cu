@@ -68,6 +68,47 @@ __device__ __forceinline__ void add_texel_grad(float* g, int64_t base, int ch, c
   }
 }
 
+// ---- warp-aggregated atomics: lanes hold (key, value); lanes whose keys
+// are equal and adjacent form a segment; the segment's last lane adds the
+// segment's sum.  Every lane of the warp must call these.
+constexpr unsigned kFull = 0xffffffffu;
+
+struct Seg {
+  int start;    // first lane of this lane's segment
+  bool tail;    // last lane of its segment (and active)
+  int levels;   // shuffle levels that cover the longest segment of the warp
+};
+
+__device__ __forceinline__ Seg segment(long long key, bool active) {
+  const int lane = threadIdx.x & 31;
+  const long long k = active ? key : -2 - lane;  // inactive lanes stand alone
+  const long long prev = __shfl_up_sync(kFull, k, 1);
+  const long long next = __shfl_down_sync(kFull, k, 1);
+  const bool head = lane == 0 || prev != k;
+  const bool tail = lane == 31 || next != k;
+  const unsigned heads = __ballot_sync(kFull, head);
+  const unsigned upto = heads & (0xffffffffu >> (31 - lane));
+  Seg s;
+  s.start = 31 - __clz(upto);
+  s.tail = tail && active;
+  const unsigned len = tail ? static_cast<unsigned>(lane - s.start + 1) : 0u;
+  const unsigned longest = __reduce_max_sync(kFull, len);
+  s.levels = 0;
+  while ((1u << s.levels) < longest) ++s.levels;
+  return s;
+}
+
+// Inclusive segmented sum up to this lane (the tail lane holds the total).
+__device__ __forceinline__ float seg_sum(float v, const Seg& s) {
+  const int lane = threadIdx.x & 31;
+  for (int l = 0; l < s.levels; ++l) {
+    const int d = 1 << l;
+    const float o = __shfl_up_sync(kFull, v, d);
+    if (lane - d >= s.start) v += o;
+  }
+  return v;
+}
+
 __host__ __device__ constexpr unsigned long long range_bits(int lo, int n) {
   return ((n >= 64 ? ~0ull : ((1ull << n) - 1ull)) << lo);
 }
@@ -196,10 +237,21 @@ __global__ void __launch_bounds__(kThreads) vertex_prep_kernel(RastBatch B, Work
 // corner varying rows r0..r2, barycentrics b, dL/dcolour.  Out: g_interp
 // (dL/d of the interpolated carried varying: eye normal or colour), texel
 // gradients (atomics), per-scene light terms into pg.
+// Texel-side outputs of one pixel's fragment backward: dL/d texel (gt at
+// texture element tb, ch channels) and dL/d specular exponent (gs at sidx);
+// keys < 0 mean none.
+struct TexGrad {
+  int64_t tb = -1;
+  int ch = 3;
+  float gt[3] = {0.0f, 0.0f, 0.0f};
+  int64_t sidx = -1;
+  float gs = 0.0f;
+};
+
 template <int SH>
 __device__ __forceinline__ void fragment_bwd(const RastJob& J, const RastPools& P, const RastGradPools& G,
                                              const float* r0, const float* r1, const float* r2, const float* b,
-                                             const float* gcv, float* g_interp, ParamGrad& pg) {
+                                             const float* gcv, float* g_interp, ParamGrad& pg, TexGrad& tg) {
   const int sh = SH >= 0 ? SH : J.shader;
   g_interp[0] = g_interp[1] = g_interp[2] = 0.0f;
   if (sh == RAST_SHADER_GOURAUD) {
@@ -211,18 +263,15 @@ __device__ __forceinline__ void fragment_bwd(const RastJob& J, const RastPools& 
     const float u = interp1(b, r0[kVUvG], r1[kVUvG], r2[kVUvG]);
     const float v = interp1(b, r0[kVUvG + 1], r1[kVUvG + 1], r2[kVUvG + 1]);
     const int ui = pymod(f2i(floorf(u)), J.tex_w), wi = pymod(f2i(floorf(v)), J.tex_h);
-    float tc[3], lcol[3], gt[3];
+    float tc[3], lcol[3];
     texel3(P.texture + J.texture_begin, J.tex_w, J.tex_h, J.tex_c, ui, wi, tc);
 #pragma unroll
     for (int q = 0; q < 3; ++q) {
       lcol[q] = interp1(b, r0[kVColour + q], r1[kVColour + q], r2[kVColour + q]);
       g_interp[q] = gcv[q] * tc[q];
-      gt[q] = gcv[q] * lcol[q];
+      tg.gt[q] = gcv[q] * lcol[q];
     }
-    int64_t tb;
-    int ch;
-    texel_index(J, ui, wi, &tb, &ch);
-    add_texel_grad(G.texture, tb, ch, gt);
+    texel_index(J, ui, wi, &tg.tb, &tg.ch);
     return;
   }
   if (sh == RAST_SHADER_DEPTH || sh == RAST_SHADER_PHONG_DARBOUX) return;
@@ -251,18 +300,15 @@ __device__ __forceinline__ void fragment_bwd(const RastJob& J, const RastPools& 
       nonneg = nonneg && lc[q] >= 0.0f;
     }
     if (!nonneg) return;
-    int64_t tb;
-    int ch;
-    texel_index(J, ui, wi, &tb, &ch);
-    float gt[3], gd = 0.0f;
+    texel_index(J, ui, wi, &tg.tb, &tg.ch);
+    float gd = 0.0f;
 #pragma unroll
     for (int q = 0; q < 3; ++q) {
-      gt[q] = gcv[q] * lc[q];
+      tg.gt[q] = gcv[q] * lc[q];
       const float glc = gcv[q] * tc[q];
       pg.v[RAST_GRAD_LIGHT_COLOUR + q] += glc * d;
       gd += glc * J.light_colour[q];
     }
-    add_texel_grad(G.texture, tb, ch, gt);
     float gl[3], gL[3];
 #pragma unroll
     for (int q = 0; q < 3; ++q) {
@@ -325,12 +371,12 @@ __device__ __forceinline__ void fragment_bwd(const RastJob& J, const RastPools& 
     const float sexp = __ldg(P.specular_map + sidx);
     const float rz = max0(rn[2]);
     const float spec = powf(rz, sexp);
-    float gdif = 0.0f, gspec = 0.0f, gt[3];
+    float gdif = 0.0f, gspec = 0.0f;
 #pragma unroll
     for (int q = 0; q < 3; ++q) {
       const float K = J.diffuse[q] * dif + J.specular[q] * spec;
       const float lc = J.light_colour[q];
-      gt[q] = gcv[q] * (J.ambient[q] + shadow[q] * K * lc);
+      tg.gt[q] = gcv[q] * (J.ambient[q] + shadow[q] * K * lc);
       pg.v[RAST_GRAD_AMBIENT + q] += gcv[q] * tc[q];
       const float gK = gcv[q] * shadow[q] * tc[q] * lc;
       pg.v[RAST_GRAD_DIFFUSE + q] += gK * dif;
@@ -340,12 +386,12 @@ __device__ __forceinline__ void fragment_bwd(const RastJob& J, const RastPools& 
       gdif += gK * J.diffuse[q];
       gspec += gK * J.specular[q];
     }
-    int64_t tb;
-    int ch;
-    texel_index(J, ui, wi, &tb, &ch);
-    add_texel_grad(G.texture, tb, ch, gt);
+    texel_index(J, ui, wi, &tg.tb, &tg.ch);
     // spec = rz ** s: d/dx = s x^(s-1) (0 when s == 0), d/ds = log(x) x^s with log(0) -> 0
-    if (G.specular_map && rz > 0.0f) atomicAdd(G.specular_map + sidx, gspec * spec * logf(rz));
+    if (rz > 0.0f) {
+      tg.sidx = sidx;
+      tg.gs = gspec * spec * logf(rz);
+    }
     const float dspec_drz = (sexp == 0.0f) ? 0.0f : sexp * powf(rz, sexp - 1.0f);
     const float grn[3] = {0.0f, 0.0f, gspec * dspec_drz * dmax0(rn[2])};
     float gr[3];
@@ -392,6 +438,16 @@ pixel_kernel(RastBatch B, Work w, const float* __restrict__ grad_canvas, const f
     pix = J.pixel_begin + local;
     p = P.prim_id[pix];
   }
+  // per-pixel contributions, added with warp-aggregated atomics below
+  int64_t frow = -1;
+  float fval[12];
+  float vval[9];
+#pragma unroll
+  for (int k = 0; k < 12; ++k) fval[k] = 0.0f;
+#pragma unroll
+  for (int k = 0; k < 9; ++k) vval[k] = 0.0f;
+  int64_t vrows[3] = {0, 0, 0};
+  TexGrad tg;
   if (p >= 0) {
     const int i = static_cast<int>(local / J.height), j = static_cast<int>(local % J.height);
     const float x = (static_cast<float>(i) - J.viewport[3]) / J.viewport[0];
@@ -401,6 +457,13 @@ pixel_kernel(RastBatch B, Work w, const float* __restrict__ grad_canvas, const f
     const float4 a = fr[0], bb = fr[1], cz = fr[2];
     const float m[9] = {a.x, a.y, a.z, a.w, bb.x, bb.y, bb.z, bb.w, cz.x};
     const float zc[3] = {cz.y, cz.z, cz.w};
+    {
+      // corner vertex rows: the same for every pixel of the face (the key of
+      // the aggregated vertex accumulation)
+      const int32_t* face = P.faces + (J.face_begin + p) * 3;
+#pragma unroll
+      for (int k = 0; k < 3; ++k) vrows[k] = J.vout_begin + gather_clamp(__ldg(face + k), J.n_verts);
+    }
     float c[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) c[k] = (x * m[k] + y * m[3 + k]) + m[6 + k];
@@ -421,10 +484,7 @@ pixel_kernel(RastBatch B, Work w, const float* __restrict__ grad_canvas, const f
                           grad_canvas ? grad_canvas[pix * 3 + 1] : 0.0f,
                           grad_canvas ? grad_canvas[pix * 3 + 2] : 0.0f};
     if (sh != RAST_SHADER_DEPTH && (gcv[0] != 0.0f || gcv[1] != 0.0f || gcv[2] != 0.0f)) {
-      const int32_t* face = P.faces + (J.face_begin + p) * 3;
-      int64_t vr[3];
-#pragma unroll
-      for (int k = 0; k < 3; ++k) vr[k] = J.vout_begin + gather_clamp(__ldg(face + k), J.n_verts);
+      const int64_t* vr = vrows;
       float r0[kMaxVarying], r1[kMaxVarying], r2[kMaxVarying];
       const int nv = varying_count(sh);
 #pragma unroll
@@ -436,7 +496,7 @@ pixel_kernel(RastBatch B, Work w, const float* __restrict__ grad_canvas, const f
         }
       }
       float gi[3];
-      fragment_bwd<SH>(J, P, G, r0, r1, r2, b, gcv, gi, pg);
+      fragment_bwd<SH>(J, P, G, r0, r1, r2, b, gcv, gi, pg, tg);
       if (gi[0] != 0.0f || gi[1] != 0.0f || gi[2] != 0.0f) {
         // interpolated = sum_k b_k v_k over the carried varying (offset 0 in
         // both families: eye normal or colour)
@@ -446,10 +506,9 @@ pixel_kernel(RastBatch B, Work w, const float* __restrict__ grad_canvas, const f
         gb[2] = (gi[0] * r2[0] + gi[1] * r2[1]) + gi[2] * r2[2];
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
-          float* acc = w.vacc + vr[k] * 3;
-          atomicAdd(acc + 0, b[k] * gi[0]);
-          atomicAdd(acc + 1, b[k] * gi[1]);
-          atomicAdd(acc + 2, b[k] * gi[2]);
+          vval[3 * k + 0] = b[k] * gi[0];
+          vval[3 * k + 1] = b[k] * gi[1];
+          vval[3 * k + 2] = b[k] * gi[2];
         }
         // b = c / sum(c)
         const float s = (gb[0] * b[0] + gb[1] * b[1]) + gb[2] * b[2];
@@ -458,16 +517,42 @@ pixel_kernel(RastBatch B, Work w, const float* __restrict__ grad_canvas, const f
       }
     }
     // ---- c_k = x m[k] + y m[3+k] + m[6+k]: dL/dm, dL/dz_clip per face
-    float* facc = w.facc + row * 12;
+    frow = row;
     const float xy1[3] = {x, y, 1.0f};
 #pragma unroll
     for (int r = 0; r < 3; ++r)
 #pragma unroll
-      for (int k = 0; k < 3; ++k)
-        if (gc[k] != 0.0f) atomicAdd(facc + 3 * r + k, xy1[r] * gc[k]);
+      for (int k = 0; k < 3; ++k) fval[3 * r + k] = xy1[r] * gc[k];
 #pragma unroll
-    for (int k = 0; k < 3; ++k)
-      if (gzc[k] != 0.0f) atomicAdd(facc + 9 + k, gzc[k]);
+    for (int k = 0; k < 3; ++k) fval[9 + k] = gzc[k];
+  }
+  // ---- warp-aggregated accumulation (pixels of a warp run along a column,
+  // so neighbours usually share the face and the texel)
+  {
+    const Seg sf = segment(frow, frow >= 0);
+    float* facc = w.facc + (frow >= 0 ? frow : 0) * 12;
+#pragma unroll
+    for (int k = 0; k < 12; ++k) {
+      const float v = seg_sum(fval[k], sf);
+      if (sf.tail && v != 0.0f) atomicAdd(facc + k, v);
+    }
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+      const float v = seg_sum(vval[k], sf);
+      if (sf.tail && v != 0.0f) atomicAdd(w.vacc + vrows[k / 3] * 3 + (k % 3), v);
+    }
+  }
+  if (G.texture) {
+    const Seg st = segment(tg.tb, tg.tb >= 0);
+    float g3[3];
+#pragma unroll
+    for (int q = 0; q < 3; ++q) g3[q] = seg_sum(tg.gt[q], st);
+    if (st.tail) add_texel_grad(G.texture, tg.tb, tg.ch, g3);
+  }
+  if (G.specular_map) {
+    const Seg ss = segment(tg.sidx, tg.sidx >= 0);
+    const float v = seg_sum(tg.gs, ss);
+    if (ss.tail && v != 0.0f) atomicAdd(G.specular_map + tg.sidx, v);
   }
   reduce_params<pixel_bits(SH)>(pg, G.job_params);
 }
