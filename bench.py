@@ -1,14 +1,26 @@
-"""Benchmark: frames/s of the rasterisation path at 84x84 x 4096 scenes.
+"""Benchmark: frames/s of the rasterisation path, tiled-batched vs plain GPU.
 
-Workload (the reference's Brax-style 84x84 benchmark, seeded synthetic
-stand-in): 4096 scenes, each a ground plane plus 8-32 objects drawn from
-{box 12 tris, icosphere level 2 320 tris, capsule 16x8 512 tris}, uneven
-triangle counts (mean ~5.7k per scene), PhongReflectionShadowTextureShader
-with a 128x128 light-space depth map.  One step renders every scene once:
-the depth pass of all scenes, then the main pass of all scenes.  One frame is
-one scene's final canvas.
+Default workload (`--workload brax84`, the headline): the reference's
+Brax-style 84x84 benchmark as a seeded synthetic stand-in: 4096 scenes, each a
+ground plane plus 8-32 objects drawn from {box 12 tris, icosphere level 2 320
+tris, capsule 16x8 512 tris}, uneven triangle counts (mean ~5.7k per scene),
+PhongReflectionShadowTextureShader with a 128x128 light-space depth map.  One
+step renders every scene once: the depth pass of all scenes, then the main
+pass of all scenes.  One frame is one scene's final canvas.
 
-    python bench.py [--steps K] [--warmup W] [--form plain|tiled] [--impl ours|reference]
+Other workloads (one JSON line each, same keys):
+  cube640     one 640x480 create_cube image, phong_reflection (fwd only)
+  overdraw960 one 960x540 scene of 389,120 triangles, gouraud_texture,
+              mean overdraw ~18 (fwd only)
+  phong128    256 differentiable 128x128 phong scenes (icosphere level 4 with
+              Gaussian displacement, 64x64 textures): fwd, and fwd+bwd of an
+              MSE loss against images of the unperturbed meshes with
+              gradients w.r.t. positions, texture, light and camera position
+  mixed1024   1024 scenes at {32x32, 84x84, 480x270} with 100..100k cube
+              triangles (log-uniform), half with a shadow pass, one CUDA graph
+              over the three resolution classes, fwd and fwd+bwd
+
+    python bench.py [--workload W] [--steps K] [--warmup W] [--form plain|tiled] [--impl ours|reference]
 
 Prints one JSON line (rank 0).  `value` is device-resident throughput; `e2e`
 is the same work through the public batch API with the scene inputs copied
@@ -19,14 +31,16 @@ JAX path) on a bounded sample of the same workload, with all host threads.
 from __future__ import annotations
 
 import argparse
-import ctypes
+import copy
 import json
 import os
 import statistics
 import subprocess
 import sys
 import time
+from dataclasses import dataclass, field
 from pathlib import Path
+from typing import Callable, List, Optional
 
 import numpy as np
 
@@ -35,9 +49,10 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "frames/s @84x84x4096 scenes fwd and fwd+bwd, tiled-batched vs plain GPU"
 UNIT = "frames/s"
-N_SCENES = 4096
-W = H = 84
-SHADOW = (128, 128)
+L2_BYTES = 129 * 1024 * 1024
+MIXED_CLASSES = [(32, 32), (84, 84), (480, 270)]
+WORKLOADS = ("brax84", "cube640", "overdraw960", "phong128", "mixed1024")
+DEFAULT_SCENES = {"brax84": 4096, "cube640": 1, "overdraw960": 1, "phong128": 256, "mixed1024": 1024}
 
 
 def parse():
@@ -46,13 +61,18 @@ def parse():
     p.add_argument("--steps", type=int, default=5)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--workload", choices=WORKLOADS, default="brax84")
     p.add_argument("--form", choices=["plain", "tiled", "auto"], default="auto")
-    p.add_argument("--scenes", type=int, default=N_SCENES)
+    p.add_argument("--scenes", type=int, default=None)
+    p.add_argument("--cpu-budget", type=float, default=12.0, help="seconds of oracle work for cpu_baseline")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-plain", action="store_true")
     p.add_argument("--no-bwd", action="store_true")
-    return p.parse_args()
+    a = p.parse_args()
+    if a.scenes is None:
+        a.scenes = DEFAULT_SCENES[a.workload]
+    return a
 
 
 def dist_env():
@@ -62,42 +82,186 @@ def dist_env():
     return rank, world, local
 
 
+# --------------------------------------------------------------- workloads
+
+@dataclass
+class Workload:
+    key: str
+    desc: str
+    frames: int  # frames (scene canvases) per step
+    chain: Callable[[int], tuple]  # scene k -> (depth JobSpec or None, main JobSpec), for the oracle
+    work: np.ndarray  # per scene: pixel-triangle pairs of its passes (oracle cost model)
+    groups: list = field(default_factory=list)  # SceneBatches on the device
+    bwd: Optional[str] = "mse"  # fwd+bwd loss: "mse" against a fixed image, "phong", or None
+    oracle_crop: int = 1  # the oracle renders width // oracle_crop columns of a frame
+    config: dict = field(default_factory=dict)
+    phong: Optional[dict] = None
+
+
+def _pass_work(spec) -> float:
+    return float(spec.width) * spec.height * spec.n_faces if spec is not None else 0.0
+
+
+def build_brax84(n, rank, dev):
+    from jaxrenderer_gb300 import batch as jb, synthetic
+
+    W = H = 84
+    shadow = (128, 128)
+    flat = synthetic.brax_like_batch(n, seed=synthetic.BASE_SEED + 1 + rank)
+    tables = jb.scene_batch_tables(flat, W, H, shadow_size=shadow)
+    work = flat.n_faces.astype(np.float64) * (W * H + shadow[0] * shadow[1])
+    groups = [jb.scene_batch_from_flat(flat, W, H, shadow_size=shadow, device=dev)] if dev is not None else []
+    return Workload("brax84", "brax-like 84x84 x 4096 scenes, phong_reflection_shadow + 128x128 depth pass", n,
+                    lambda k: jb.scene_job_specs(flat, tables, k % n), work, groups,
+                    config={"scenes": n, "mean_faces_per_scene": float(flat.n_faces.mean()),
+                            "resolution": [W, H], "shadow_map": list(shadow)})
+
+
+def build_cube640(n, rank, dev):
+    import jaxrenderer_gb300 as jr
+    from jaxrenderer_gb300 import _lib, batch as jb
+    from jaxrenderer_gb300.jobs import job_from_extra
+
+    W, H = 640, 480
+    F32 = np.float32
+    cube = jr.create_cube(np.ones(3, F32), np.ones(2, F32), np.zeros((2, 2, 3), F32) + np.array([0, 0, 1], F32),
+                          np.ones((2, 2), F32) * 2.0)
+    params = jr.CameraParameters(viewWidth=W, viewHeight=H, position=np.array([2.0, 4.0, 1.0], F32))
+    cam = jr.Renderer.create_camera_from_parameters(params)
+    extra, fi = jr.Renderer._extra(jr.merge_objects([jr.ModelObject(model=cube)]), jr.LightParameters(), cam)
+    spec = job_from_extra(_lib.SHADER_PHONG_REFLECTION, cam, extra, W, H)
+    spec.faces = fi
+    groups = [jb.scene_batch_from_specs([spec] * n, dev)] if dev is not None else []
+    return Workload("cube640", f"create_cube 640x480 x {n}, phong_reflection (Renderer.get_camera_image)", n,
+                    lambda k: (None, spec), np.full(n, _pass_work(spec)), groups, bwd=None,
+                    config={"scenes": n, "faces": 12, "resolution": [W, H]})
+
+
+def build_overdraw960(n, rank, dev):
+    from jaxrenderer_gb300 import _lib, batch as jb, synthetic
+    from jaxrenderer_gb300.jobs import JobSpec
+
+    rng = np.random.Generator(np.random.PCG64(synthetic.BASE_SEED + 3 + rank))
+    d, overdraw = synthetic.overdraw_scene(rng)
+    spec = JobSpec(shader=_lib.SHADER_GOURAUD_TEXTURE, **d)
+    groups = [jb.scene_batch_from_specs([spec] * n, dev)] if dev is not None else []
+    return Workload("overdraw960", f"960x540 x {n}, 64 level-4 + 3 level-5 icospheres (389,120 tris), "
+                    "gouraud_texture, 512x512 texture", n, lambda k: (None, spec), np.full(n, _pass_work(spec)),
+                    groups, bwd=None, oracle_crop=16,
+                    config={"scenes": n, "faces": int(spec.n_faces), "resolution": [spec.width, spec.height],
+                            "estimated_overdraw": round(overdraw, 2)})
+
+
+def build_phong128(n, rank, dev):
+    from jaxrenderer_gb300 import batch as jb, synthetic
+
+    rng = np.random.Generator(np.random.PCG64(synthetic.BASE_SEED + 40 + rank))
+    scenes = [synthetic.phong_scene(rng, level=4, texture_size=64, sigma=0.05, radius=4.0) for _ in range(n)]
+    specs = [synthetic.phong_job_spec(sc) for sc in scenes]
+    groups = [jb.scene_batch_from_specs(specs, dev)] if dev is not None else []
+    phong = None
+    if dev is not None:
+        base = jb.scene_batch_from_specs([synthetic.phong_job_spec(sc, position=sc.base_position) for sc in scenes],
+                                         dev)
+        phong = {"scenes": scenes, "base": base}
+    return Workload("phong128", f"{n} x 128x128 phong (icosphere L4 + displacement, 64x64 texture), "
+                    "MSE vs unperturbed render, grads wrt positions/texture/light/camera", n,
+                    lambda k: (None, specs[k % n]), np.array([_pass_work(s) for s in specs]), groups, bwd="phong",
+                    config={"scenes": n, "faces": 5120, "resolution": [128, 128], "texture": [64, 64]},
+                    phong=phong)
+
+
+def build_mixed1024(n, rank, dev):
+    from jaxrenderer_gb300 import batch as jb, synthetic
+
+    flat = synthetic.cube_scene_batch(n, seed=synthetic.BASE_SEED + 5 + rank)
+    rng = np.random.Generator(np.random.PCG64(synthetic.BASE_SEED + 6 + rank))
+    res = rng.integers(0, len(MIXED_CLASSES), n)
+    shadow = rng.random(n) < 0.5
+    px = np.array([w * h for w, h in MIXED_CLASSES], np.float64)[res]
+    work = flat.n_faces.astype(np.float64) * px * np.where(shadow, 2.0, 1.0)
+    host = {}
+
+    def chain(k):
+        k = k % n
+        c = int(res[k])
+        if c not in host:
+            idx = np.nonzero(res == c)[0]
+            sub = synthetic.flat_subset(flat, idx)
+            w, h = MIXED_CLASSES[c]
+            host[c] = (sub, jb.scene_batch_tables(sub, w, h, shadow_size=(w, h), shadow_mask=shadow[idx]),
+                       {int(s): i for i, s in enumerate(idx)})
+        sub, tables, local = host[c]
+        return jb.scene_job_specs(sub, tables, local[k])
+
+    groups = []
+    if dev is not None:
+        groups = [sb for _, sb in jb.mixed_scene_batches(flat, res, MIXED_CLASSES, shadow, device=dev)]
+    counts = {f"{w}x{h}": int((res == c).sum()) for c, (w, h) in enumerate(MIXED_CLASSES)}
+    return Workload("mixed1024", f"{n} mixed scenes {{32x32, 84x84, 480x270}}, 100..100k cube tris log-uniform, "
+                    "50% phong_reflection / 50% phong_reflection_shadow, one CUDA graph", n, chain, work, groups,
+                    config={"scenes": n, "per_class": counts, "mean_faces_per_scene": float(flat.n_faces.mean()),
+                            "shadow_scenes": int(shadow.sum()), "shadow_map": "canvas size (Renderer.render)"})
+
+
+BUILDERS = {"brax84": build_brax84, "cube640": build_cube640, "overdraw960": build_overdraw960,
+            "phong128": build_phong128, "mixed1024": build_mixed1024}
+
+
 # ------------------------------------------------------------ CPU baseline
 
-def _oracle_frame(flat, sb_tables, s, threads):
+def oracle_frame(wl: Workload, k: int, threads: int) -> float:
+    """Render scene k's passes with the oracle (main pass cropped to
+    width // oracle_crop columns); returns the pixel-triangle pairs done."""
     from oracle import oracle
 
-    dspec, mspec = sb_tables(s)
-    smap = oracle.render(dspec, np.full(SHADOW, np.finfo(np.float32).max, np.float32), n_threads=threads)["zbuffer"]
-    mspec.shadow_map = smap
-    oracle.render(mspec, np.ones((W, H), np.float32), np.ones((W, H, 3), np.float32), n_threads=threads)
+    depth, main = wl.chain(k)
+    done = 0.0
+    if wl.oracle_crop > 1:
+        main = copy.copy(main)
+        main.width = max(1, main.width // wl.oracle_crop)
+    if depth is not None:
+        f32max = np.finfo(np.float32).max
+        smap = oracle.render(depth, np.full((depth.width, depth.height), f32max, np.float32),
+                             n_threads=threads)["zbuffer"]
+        main = copy.copy(main)
+        main.shadow_map = smap
+        done += _pass_work(depth)
+    oracle.render(main, np.ones((main.width, main.height), np.float32),
+                  np.ones((main.width, main.height, 3), np.float32), n_threads=threads)
+    return done + _pass_work(main)
 
 
-def time_oracle(flat, tables_fn, budget_s: float, threads: int):
-    """Render consecutive scenes with the oracle until `budget_s` is spent."""
-    done = 0
+def time_oracle(wl: Workload, budget_s: float, threads: int, start: int = 0):
+    """Consecutive scenes with the oracle until `budget_s` is spent.
+    Returns (scenes, seconds, pixel-triangle pairs done)."""
+    done, work = 0, 0.0
     t0 = time.perf_counter()
     while True:
-        _oracle_frame(flat, tables_fn, done % flat.n_scenes, threads)
+        work += oracle_frame(wl, start + done, threads)
         done += 1
         el = time.perf_counter() - t0
         if el >= budget_s:
-            return done, el
+            return done, el, work
 
 
-class HostTables:
-    """Job tables of a FlatScenes batch without a device (for the oracle)."""
+def oracle_rate(wl: Workload, budget_s: float, threads: int, start: int = 0):
+    """Frames/s of the whole workload extrapolated from a timed sample:
+    sample pixel-triangle pairs per second, applied to the workload's total
+    (exact for equal scenes, cost-weighted for uneven ones)."""
+    done, el, work = time_oracle(wl, budget_s, threads, start)
+    rate = work / el
+    fps = wl.frames / (float(wl.work.sum()) / rate)
+    return fps, done, el
 
-    def __init__(self, flat):
-        from jaxrenderer_gb300 import batch as jb
 
-        self.flat = flat
-        self.tables = jb.scene_batch_tables(flat, W, H, shadow_size=SHADOW)
-
-    def __call__(self, s):
-        from jaxrenderer_gb300 import batch as jb
-
-        return jb.scene_job_specs(self.flat, self.tables, s)
+def cpu_baseline_line(wl: Workload, budget_s: float):
+    threads = len(os.sched_getaffinity(0))
+    fps, done, el = oracle_rate(wl, budget_s, threads)
+    crop = f", main pass cropped to 1/{wl.oracle_crop} of the columns" if wl.oracle_crop > 1 else ""
+    return {"value": fps, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{done} consecutive scenes of the workload{crop}, oracle C restatement, OpenMP over pixel "
+                      f"columns, {el:.1f} s; frames/s = sample pixel-triangle rate applied to the whole workload"}
 
 
 # ------------------------------------------------------------------ clocks
@@ -164,10 +328,68 @@ def measured_peaks():
 
 # ------------------------------------------------------------------- ours
 
+INPUT_POOLS = ("position", "normal", "uv", "colour", "texture_index", "texture", "specular_map")
+
+
+def input_bytes(groups) -> int:
+    return sum(sb.pools[k].numel() * sb.pools[k].element_size() for sb in groups for k in INPUT_POOLS
+               if k in sb.pools)
+
+
+class Timer:
+    """Device time of repeated steps: CUDA events on the launching stream,
+    a barrier + synchronize on both sides, max over ranks.  With `flush`
+    (inputs smaller than L2), a buffer larger than L2 is written before each
+    step, outside the events."""
+
+    def __init__(self, dev, stream, world, flush: bool):
+        import torch
+
+        self.torch = torch
+        self.dev, self.stream, self.world = dev, stream, world
+        self.scratch = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=dev) if flush else None
+
+    def barrier(self):
+        self.torch.cuda.synchronize(self.dev)
+        if self.world > 1:
+            self.torch.distributed.barrier()
+
+    def __call__(self, step_fn, steps, warmup):
+        torch = self.torch
+        for _ in range(warmup):
+            step_fn()
+        self.barrier()
+        ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
+        if self.scratch is None:
+            start, stop = ev(), ev()
+            start.record(self.stream)
+            for _ in range(steps):
+                step_fn()
+            stop.record(self.stream)
+            self.barrier()
+            ms = start.elapsed_time(stop)
+        else:
+            pairs = []
+            for k in range(steps):
+                self.scratch.fill_(float(k))
+                a, b = ev(), ev()
+                a.record(self.stream)
+                step_fn()
+                b.record(self.stream)
+                pairs.append((a, b))
+            self.barrier()
+            ms = sum(a.elapsed_time(b) for a, b in pairs)
+        if self.world > 1:
+            t = torch.tensor([ms], device=self.dev)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms / steps
+
+
 def run_ours(args, rank, world, local):
     import torch
 
-    from jaxrenderer_gb300 import _lib, batch as jb, synthetic
+    from jaxrenderer_gb300 import _lib, batch as jb
 
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
@@ -177,63 +399,44 @@ def run_ours(args, rank, world, local):
         dist.init_process_group("nccl")
     _lib.load()
     form = "tiled" if args.form == "auto" else args.form
-    flat = synthetic.brax_like_batch(args.scenes, seed=synthetic.BASE_SEED + 1 + rank)
-    sb = jb.scene_batch_from_flat(flat, W, H, shadow_size=SHADOW, device=dev)
+    wl = BUILDERS[args.workload](args.scenes, rank, dev)
     stream = torch.cuda.current_stream(dev)
+    in_bytes = input_bytes(wl.groups)
+    flush = in_bytes < 2 * L2_BYTES
+    timed = Timer(dev, stream, world, flush)
 
-    def barrier():
-        torch.cuda.synchronize(dev)
-        if world > 1:
-            torch.distributed.barrier()
-
-    def timed(step_fn, steps, warmup, clocks=None):
-        for _ in range(warmup):
-            step_fn()
-        barrier()
-        start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        start.record(stream)
-        for _ in range(steps):
-            step_fn()
-        stop.record(stream)
-        barrier()
-        ms = start.elapsed_time(stop)
-        if world > 1:
-            t = torch.tensor([ms], device=dev)
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            ms = float(t.item())
-        return ms / steps
-
-    runner = jb.BatchRunner(sb, form=form, want_prim_id=False)
+    mr = jb.MultiRunner(wl.groups, form=form, want_prim_id=False)
     if form == "tiled":
-        runner.capture()
-        step = runner.replay
+        mr.capture()
+        step = mr.replay
     else:
-        step = lambda: runner.run(stream)  # noqa: E731
+        step = lambda: mr.run(stream)  # noqa: E731
     for _ in range(args.warmup):
         step()
     with ClockSampler(local) as clk:
         ms_per_step = timed(step, args.steps, 0)
-    value = world * args.scenes / (ms_per_step / 1e3)
-    prof = profile_kernels(runner, args.steps, stream)
+    value = world * wl.frames / (ms_per_step / 1e3)
+    prof = profile_kernels(mr, args.steps, stream)
+    visible = count_visible(mr)
 
     comparison = {}
     if form == "tiled" and not args.no_plain:
-        plain = jb.BatchRunner(sb, form="plain", want_prim_id=False)
+        plain = jb.MultiRunner(wl.groups, form="plain", want_prim_id=False)
         pms = timed(lambda: plain.run(stream), max(1, min(args.steps, 3)), 1)
-        comparison = {"plain_fwd": world * args.scenes / (pms / 1e3), "plain_ms_per_step": pms,
+        comparison = {"plain_fwd": world * wl.frames / (pms / 1e3), "plain_ms_per_step": pms,
                       "tiled_over_plain": pms / ms_per_step}
         del plain
         torch.cuda.empty_cache()
 
     fwd_bwd = {}
-    if not args.no_bwd:
-        fwd_bwd = measure_fwd_bwd(sb, args, stream, timed, world)
+    if not args.no_bwd and wl.bwd is not None:
+        fwd_bwd = measure_fwd_bwd(wl, args, stream, timed, world)
 
     e2e = None
     if not args.no_e2e:
-        e2e = measure_e2e(flat, sb, runner, step, args, dev, stream, world)
+        e2e = measure_e2e(wl, mr, step, args, dev, stream, world)
 
-    kernels_per_step = len(prof["per_step_names"])
+    kernels_per_step = prof["launches_per_step"]
     out = {
         "metric": METRIC,
         "value": value,
@@ -246,21 +449,21 @@ def run_ours(args, rank, world, local):
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f32",
-        "data": "synthetic (seeded Brax-like scenes; the reference's Brax fixtures are inputs-only pickles)",
-        "config": {
-            "workload": "brax-like 84x84 x 4096 scenes, phong_reflection_shadow + 128x128 depth pass",
+        "data": "synthetic (seeded stand-ins with the stated shapes; the reference's Brax fixtures are "
+                "inputs-only pickles)",
+        "config": dict({
+            "workload": wl.desc,
             "form": form + (" (CUDA graph replay)" if form == "tiled" else ""),
-            "tiled_config": {k: [c.tile_w, c.tile_h, int(c.bin_capacity)] for k, c in runner.configs.items()},
-            "scenes": args.scenes,
-            "mean_faces_per_scene": float(flat.n_faces.mean()),
-            "resolution": [W, H],
-            "shadow_map": list(SHADOW),
-            "l2": "inputs larger than L2 (per-corner pools %.2f GB)" % (flat.position.nbytes * 3 / 1e9),
+            "tiled_config": {name: [c.tile_w, c.tile_h, int(c.bin_capacity)] for name, r, p in prof["passes"]
+                             for c in [r.configs.get(p)] if c is not None},
+            "l2": ("inputs larger than L2 (input pools %.2f GB)" % (in_bytes / 1e9)) if not flush else
+                  ("L2 flushed between timed steps (a %d MB buffer written; input pools %.1f MB)"
+                   % (2 * L2_BYTES >> 20, in_bytes / 1e6)),
             "parallelism": f"scene-sharded x{world} (no collective)",
-        },
+        }, **wl.config),
         "fwd_comparison": comparison,
         "fwd_bwd": fwd_bwd,
-        "roofline": roofline(prof, sb, flat, runner),
+        "roofline": roofline(prof, visible),
         "kernels": prof["summary"],
         "gpu_launches": kernels_per_step * args.steps,
         "clocks": clk.summary(),
@@ -268,55 +471,96 @@ def run_ours(args, rank, world, local):
     if e2e is not None:
         out["e2e"] = e2e
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        out["cpu_baseline"] = cpu_baseline_line(flat, budget_s=12.0)
+        out["cpu_baseline"] = cpu_baseline_line(wl, budget_s=args.cpu_budget)
     if rank == 0:
         print(json.dumps(out), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
 
 
-def measure_fwd_bwd(sb, args, stream, timed, world):
-    """Forward + backward of an MSE loss against a fixed target image, per
-    step: render (prim-id buffer saved), dL/dcanvas, rast_backward into
-    reused gradient arrays (per-vertex, per-texel, per-scene camera/light)."""
+def count_visible(mr):
+    """Faces that win at least one pixel of a main pass (the faces whose
+    varyings the tiled form computes), per runner, from one prim-id render."""
     import torch
 
     from jaxrenderer_gb300 import batch as jb
 
+    out = []
+    for r in mr.runners:
+        rr = jb.BatchRunner(r.sb, form=r.form, want_prim_id=True, tiled_config=r.configs.get("main"))
+        rr.run()
+        pid = rr.prim_id.reshape(r.sb.n_scenes, -1).to(torch.int64)
+        key = torch.arange(r.sb.n_scenes, device=pid.device)[:, None] * (1 << 32) + pid
+        out.append(int(torch.unique(key[pid >= 0]).numel()))
+        del rr, pid, key
+    torch.cuda.empty_cache()
+    return out
+
+
+def measure_fwd_bwd(wl: Workload, args, stream, timed, world):
+    """Forward + backward per step.  "mse": MSE against a fixed image per
+    scene: render (prim-id buffer saved), dL/dcanvas, rast_backward into
+    reused gradient arrays (per-vertex, per-texel, per-scene camera/light).
+    "phong": the differentiable phong batch through DifferentiableBatch and
+    torch autograd: camera matrices from eye positions, render, MSE against
+    the unperturbed meshes' images, backward to positions, texture, light
+    direction and camera position."""
+    import torch
+
+    from jaxrenderer_gb300 import _lib, batch as jb
+
     out = {}
-    target = torch.rand((sb.n_scenes, W, H, 3), generator=torch.Generator().manual_seed(0)).to(sb.device)
-    scale = 2.0 / target.numel()
     for form in ("tiled", "plain"):
         if form == "plain" and args.no_plain:
             continue
-        r = jb.BatchRunner(sb, form=form, want_prim_id=True)
-        grads = r.grad_buffers()
-        if form == "tiled":
-            r.capture()
-            fwd = r.replay
-        else:
-            fwd = lambda r=r: r.run(stream)  # noqa: E731
-
-        def step(r=r, fwd=fwd, grads=grads):
-            o = fwd()
-            g = (o.canvas - target) * scale
-            r.backward(g, out=grads)
-
         steps = args.steps if form == "tiled" else max(1, min(args.steps, 3))
-        ms = timed(step, steps, 1 if form == "plain" else args.warmup)
-        out[form] = {"value": world * args.scenes / (ms / 1e3), "ms_per_step": ms, "steps": steps}
-        # backward alone, and its kernels (CUDA events inside the library)
-        if form == "tiled":
-            from jaxrenderer_gb300 import _lib
+        warm = args.warmup if form == "tiled" else 1
+        if wl.bwd == "phong":
+            step, r, extra = phong_step(wl, form)
+            runners = [r]
+        else:
+            mr = jb.MultiRunner(wl.groups, form=form, want_prim_id=True)
+            grads = mr.grad_buffers()
+            gen = torch.Generator().manual_seed(0)
+            targets = [torch.rand(r.canvas.shape, generator=gen).to(r.canvas.device) for r in mr.runners]
+            scales = [2.0 / t.numel() for t in targets]
+            if form == "tiled":
+                mr.capture()
+                fwd = mr.replay
+            else:
+                fwd = lambda mr=mr: mr.run(stream)  # noqa: E731
 
-            fwd()
-            gc = (r.canvas - target) * scale
-            bms = timed(lambda: r.backward(gc, out=grads), steps, 1)
-            out["backward_ms"] = bms
-            prof = _lib.RastProfile()
-            r.backward(gc, out=grads, profile=prof)
-            out["backward_kernels_ms"] = {prof.names[k].decode(): prof.ms[k] for k in range(prof.n)}
-        del r, grads
+            def step(mr=mr, fwd=fwd, grads=grads):
+                outs = fwd()
+                mr.backward([(o.canvas - t) * s for o, t, s in zip(outs, targets, scales)], out=grads)
+
+            runners = mr.runners
+            mr = None
+        ms = timed(step, steps, warm)
+        out[form] = {"value": world * wl.frames / (ms / 1e3), "ms_per_step": ms, "steps": steps}
+        if form == "tiled":
+            # backward alone, and its kernels (CUDA events inside the library)
+            step()
+            torch.cuda.synchronize()
+            gcs = [(r.canvas - r.canvas.detach().mean()) * 1e-3 for r in runners]
+            gbs = [r.grad_buffers() for r in runners]
+
+            def bwd():
+                for r, g, b in zip(runners, gcs, gbs):
+                    r.backward(g, out=b)
+
+            out["backward_ms"] = timed(bwd, steps, 1)
+            kms = {}
+            for r, g, b in zip(runners, gcs, gbs):
+                prof = _lib.RastProfile()
+                r.backward(g, out=b, profile=prof)
+                for k in range(prof.n):
+                    name = prof.names[k].decode()
+                    kms[name] = kms.get(name, 0.0) + prof.ms[k]
+            out["backward_kernels_ms"] = kms
+            if wl.bwd == "phong":
+                out["grads"] = extra()
+        del step, runners
         torch.cuda.empty_cache()
     if "plain" in out:
         out["tiled_over_plain"] = out["plain"]["ms_per_step"] / out["tiled"]["ms_per_step"]
@@ -324,87 +568,164 @@ def measure_fwd_bwd(sb, args, stream, timed, world):
     return out
 
 
-def profile_kernels(runner, steps, stream):
-    """Per-kernel CUDA-event durations inside the library, same steps again."""
+def phong_step(wl: Workload, form: str):
+    """One fwd+bwd step of the differentiable phong batch (see measure_fwd_bwd)."""
+    import torch
+
+    from jaxrenderer_gb300 import batch as jb, synthetic
+    from jaxrenderer_gb300.autograd import DifferentiableBatch, camera_matrices
+
+    sb = wl.groups[0]
+    dev = sb.device
+    scenes = wl.phong["scenes"]
+    tr = jb.BatchRunner(wl.phong["base"], form=form, want_prim_id=False)
+    target = tr.run().canvas.clone()
+    del tr
+    db = DifferentiableBatch(sb, form=form)
+    params = synthetic.phong_camera_params(scenes[0].eye)
+    eye = torch.tensor(np.stack([sc.eye for sc in scenes]), dtype=torch.float32, device=dev, requires_grad=True)
+    light = torch.tensor(np.stack([sc.light_direction for sc in scenes]), dtype=torch.float32, device=dev,
+                         requires_grad=True)
+    pos = sb.pools["position"].clone().requires_grad_(True)
+    tex = sb.pools["texture"].clone().requires_grad_(True)
+    leaves = (eye, light, pos, tex)
+
+    def step():
+        for t in leaves:
+            t.grad = None
+        w2c, w2e, _ = camera_matrices(eye, params)
+        canvas, _ = db.render(position=pos, texture=tex, world_to_clip=w2c, world_to_eye_norm=w2e,
+                              light_direction=light)
+        loss = ((canvas - target) ** 2).mean()
+        loss.backward()
+
+    def extra():
+        return {k: float(t.grad.abs().sum()) if t.grad is not None else None
+                for k, t in zip(("camera_position", "light_direction", "position", "texture"), leaves)}
+
+    return step, db.runner, extra
+
+
+def profile_kernels(mr, steps, stream):
+    """Per-kernel CUDA-event durations inside the library, same steps again.
+    Kernel names are "pass:kernel", prefixed by "WxH/" for multi-class runs."""
     from jaxrenderer_gb300 import _lib
 
-    acc = {}
-    names_order = []
-    for _ in range(steps):
-        runner._reset(1.0)
-        for key, _b in runner.batches():
-            prof = _lib.RastProfile()
-            runner.launch(key, stream.cuda_stream, profile=prof)
-            for k in range(prof.n):
-                name = f"{key}:{prof.names[k].decode()}"
-                if name not in acc:
-                    acc[name] = []
-                    names_order.append(name)
-                acc[name].append(prof.ms[k])
+    acc, names_order, passes, where = {}, [], [], {}
+    multi = len(mr.runners) > 1
+    launches = 0
+    for it in range(steps):
+        for r in mr.runners:
+            r._reset(1.0)
+            prefix = f"{r.sb.width}x{r.sb.height}/" if multi else ""
+            for key, _b in r.batches():
+                if it == 0:
+                    passes.append((prefix + key, r, key))
+                prof = _lib.RastProfile()
+                r.launch(key, stream.cuda_stream, profile=prof)
+                for k in range(prof.n):
+                    kname = prof.names[k].decode()
+                    name = f"{prefix}{key}:{kname}"
+                    if name not in acc:
+                        acc[name] = []
+                        names_order.append(name)
+                        where[name] = (r, key, kname)
+                    acc[name].append(prof.ms[k])
+                    if it == 0 and kname != "memset":
+                        launches += 2 if kname == "scan_kernels" else 1
     summary = {n: {"avg_ms": float(np.mean(v)), "launches": len(v)} for n, v in acc.items()}
     total = sum(v["avg_ms"] for v in summary.values())
     for v in summary.values():
         v["share"] = v["avg_ms"] / total if total > 0 else 0.0
-    return {"summary": summary, "per_step_names": names_order}
+    return {"summary": summary, "order": names_order, "where": where, "passes": passes,
+            "launches_per_step": launches}
 
 
-def _lib_profile():
-    from jaxrenderer_gb300 import _lib
+# bytes a face corner's vertex inputs take, and texel bytes a pixel reads, per shader id
+_CORNER_IN = {0: 12, 1: 36, 2: 32, 3: 32, 4: 32, 5: 36, 6: 36}
+_TEXEL = {0: 0, 1: 0, 2: 12, 3: 12, 4: 24, 5: 16, 6: 20}
+_VARYINGS = {0: 0, 1: 3, 2: 5, 3: 5, 4: 20, 5: 6, 6: 10}  # floats per corner (rast_shaders.cuh varying_count)
 
-    return _lib.RastProfile()
 
-
-def kernel_bytes(kname, pass_name, sb, flat, runner):
-    """Algorithmic bytes one launch of `kname` must move (roofline):
-    inputs read once, outputs written once; re-reads served by caches are
-    not counted."""
-    F = int(flat.n_faces.sum())
-    corners = 3 * F
-    main = pass_name == "main"
-    pixels = sb.n_scenes * (W * H if main else SHADOW[0] * SHADOW[1])
-    entries = 0
+def pass_info(runner, pass_name):
+    jobs = runner.sb.shadow_jobs if pass_name == "shadow" else runner.sb.main_jobs
+    sh = jobs["shader"].astype(np.int64)
+    px = jobs["width"].astype(np.int64) * jobs["height"]
+    nv = jobs["n_verts"].astype(np.int64)
+    info = {
+        "F": float(jobs["n_faces"].astype(np.int64).sum()),
+        "P": float(px.sum()),
+        "Ptex": float(sum(px[k] * _TEXEL[int(sh[k])] for k in range(len(sh)))),
+        "corners": float(nv.sum()),
+        "cin": float(sum(nv[k] * _CORNER_IN[int(sh[k])] for k in range(len(sh)))),
+        "vs": max(_VARYINGS[int(s)] for s in np.unique(sh)),
+        "tests": float((px * jobs["n_faces"].astype(np.int64)).sum()),
+        "main": bool((sh != 0).any()),
+        "E": 0.0,
+        "T": 0.0,
+    }
     if runner.form == "tiled":
-        entries = int(runner.stats(pass_name).bin_entries)
-    out_px = (4 + 12) if main else 4  # zbuffer (+ canvas) written
+        st = runner.stats(pass_name)
+        info["E"], info["T"] = float(st.bin_entries), float(st.tiles)
+    return info
+
+
+def kernel_bytes(kname, info, visible):
+    """Algorithmic bytes one launch of `kname` must move: inputs read once,
+    outputs written once; re-reads served by caches are not counted.
+    F faces, P pixels, E bin entries, T tiles, V faces visible in the main
+    pass, vs varyings per corner."""
+    F, P, E, T, vs = info["F"], info["P"], info["E"], info["T"], info["vs"]
+    V = float(visible) if info["main"] else 0.0
+    out_px = 16 if info["main"] else 4  # zbuffer (+ canvas) written
     table = {
         # plain form
-        "vertex_kernel": corners * (12 + (12 + 8 + 4 if main else 0)) + corners * (16 + (40 if main else 0)),
+        "vertex_kernel": info["cin"] + info["corners"] * (16 + 4 * vs),
         "setup_kernel": F * (12 + 3 * 16 + 64),
-        "scan_kernel": F * 48 + pixels * 4,
-        "shade_kernel": pixels * (4 + out_px + (4 if main else 0)),
+        "scan_kernel": F * 48 + P * 4,
+        "shade_kernel": P * (4 + out_px) + info["Ptex"] + V * (64 + 3 * (16 + 4 * vs)),
         # tiled form
-        "setup_bin_kernel": F * (12 + 36 + 64 + 8) + entries * 4,
-        "scan_kernels": runner_tiles(runner, pass_name) * 12,
-        "scatter_kernel": F * 8 + entries * 12,
-        "raster_kernel": F * 48 + entries * 4 + pixels * 4,
-        "tiled_shade_kernel": pixels * (4 + out_px + (4 if main else 0)),
+        "setup_bin_kernel": F * (12 + 36 + 64 + 8) + E * 4,
+        "scan_kernels": T * 12,
+        "scatter_kernel": F * 8 + E * 12,
+        "raster_kernel": F * 48 + E * 4 + P * 4,
+        "face_varyings_kernel": F + V * (12 + 3 * (info["cin"] / max(info["corners"], 1)) + 3 * 4 * vs),
+        "tiled_shade_kernel": P * (4 + out_px) + info["Ptex"] + V * (64 + 3 * 4 * vs),
     }
-    return table.get(kname, 0), entries
+    return table.get(kname, 0.0)
 
 
-def runner_tiles(runner, pass_name):
-    if runner.form != "tiled":
-        return 0
-    return int(runner.stats(pass_name).tiles)
-
-
-def roofline(prof, sb, flat, runner):
+def roofline(prof, visible):
     """HBM roofline of the dominant kernel: algorithmic bytes per launch /
     average launch duration (CUDA events inside the library)."""
     peak, kind = measured_peaks()
     summ = prof["summary"]
-    dom = max(summ, key=lambda k: summ[k]["avg_ms"])
+    infos = {}
+    vis_of = {}
+    runners = []
+    for name, r, p in prof["passes"]:
+        if r not in runners:
+            runners.append(r)
+    for r, v in zip(runners, visible):
+        vis_of[id(r)] = v
+
+    def bytes_of(name):
+        r, p, kn = prof["where"][name]
+        if (id(r), p) not in infos:
+            infos[(id(r), p)] = pass_info(r, p)
+        return kernel_bytes(kn, infos[(id(r), p)], vis_of.get(id(r), 0)), infos[(id(r), p)]
+
+    cands = [n for n in summ if not n.endswith(":memset")]
+    dom = max(cands, key=lambda k: summ[k]["avg_ms"])
     ms = summ[dom]["avg_ms"]
-    pass_name, kname = dom.split(":")
-    alg, entries = kernel_bytes(kname, pass_name, sb, flat, runner)
+    alg, info = bytes_of(dom)
     achieved = alg / (ms / 1e3) / 1e9 if ms > 0 else 0.0
-    pixels = sb.n_scenes * (W * H if pass_name == "main" else SHADOW[0] * SHADOW[1])
     per_kernel = {}
-    for name, v in summ.items():
-        pn, kn = name.split(":")
-        b, _ = kernel_bytes(kn, pn, sb, flat, runner)
-        per_kernel[name] = {"GB/s": b / (v["avg_ms"] / 1e3) / 1e9 if v["avg_ms"] > 0 else None,
-                            "frac": (b / (v["avg_ms"] / 1e3) / 1e9) / peak if v["avg_ms"] > 0 else None}
+    for name in cands:
+        b, _ = bytes_of(name)
+        v = summ[name]
+        gbs = b / (v["avg_ms"] / 1e3) / 1e9 if v["avg_ms"] > 0 else None
+        per_kernel[name] = {"bytes": b, "GB/s": gbs, "frac": gbs / peak if gbs is not None else None}
     out = {
         "bound": "hbm",
         "kernel": dom,
@@ -418,35 +739,44 @@ def roofline(prof, sb, flat, runner):
         "avg_launch_ms": ms,
         "per_kernel": per_kernel,
     }
+    kname = prof["where"][dom][2]
     if kname in ("scan_kernel", "raster_kernel"):
-        tests = pixels * float(flat.n_faces.mean()) if kname == "scan_kernel" else None
+        tests = info["tests"] if kname == "scan_kernel" else None
         out["coverage"] = {"pixel_triangle_tests_per_s": tests / (ms / 1e3) if tests else None,
-                           "bin_entries": entries or None,
+                           "bin_entries": info["E"] or None,
                            "note": "coverage is FP32-issue bound; issue-slot utilisation in profiles/"}
     return out
 
 
-def measure_e2e(flat, sb, runner, step, args, dev, stream, world):
+def measure_e2e(wl: Workload, mr, step, args, dev, stream, world):
     """Public-API path with host inputs: pinned host pools -> device, render,
     canvases -> pinned host, all inside the timed region."""
     import torch
 
-    names = ["position", "normal", "uv", "texture_index", "texture", "specular_map"]
-    host = {}
-    for n in names:
-        t = sb.pools[n]
-        h = torch.empty(t.shape, dtype=t.dtype, pin_memory=True)
-        h.copy_(t)
-        host[n] = h
-    out_host = torch.empty(runner.canvas.shape, dtype=torch.float32, pin_memory=True)
-    h2d = sum(host[n].numel() * host[n].element_size() for n in names)
-    d2h = out_host.numel() * 4
+    host, outs = [], []
+    h2d = d2h = 0
+    for r in mr.runners:
+        hp = {}
+        for n in INPUT_POOLS:
+            if n not in r.sb.pools:
+                continue
+            t = r.sb.pools[n]
+            h = torch.empty(t.shape, dtype=t.dtype, pin_memory=True)
+            h.copy_(t)
+            hp[n] = h
+            h2d += h.numel() * h.element_size()
+        host.append(hp)
+        oh = torch.empty(r.canvas.shape, dtype=torch.float32, pin_memory=True)
+        outs.append(oh)
+        d2h += oh.numel() * 4
 
     def e2e_step():
-        for n in names:
-            sb.pools[n].copy_(host[n], non_blocking=True)
+        for r, hp in zip(mr.runners, host):
+            for n, h in hp.items():
+                r.sb.pools[n].copy_(h, non_blocking=True)
         step()
-        out_host.copy_(runner.canvas, non_blocking=True)
+        for r, oh in zip(mr.runners, outs):
+            oh.copy_(r.canvas, non_blocking=True)
 
     steps = max(1, min(args.steps, 5))
     e2e_step()
@@ -458,18 +788,8 @@ def measure_e2e(flat, sb, runner, step, args, dev, stream, world):
     stop.record(stream)
     torch.cuda.synchronize(dev)
     ms = start.elapsed_time(stop) / steps
-    return {"value": world * args.scenes / (ms / 1e3), "unit": UNIT, "ms_per_step": ms,
+    return {"value": world * wl.frames / (ms / 1e3), "unit": UNIT, "ms_per_step": ms,
             "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h), "steps": steps}
-
-
-def cpu_baseline_line(flat, budget_s: float):
-    threads = len(os.sched_getaffinity(0))
-    tables = HostTables(flat)
-    _oracle_frame(flat, tables, 0, threads)  # build + warm
-    done, el = time_oracle(flat, tables, budget_s, threads)
-    return {"value": done / el, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{done} consecutive scenes of the workload (depth + main pass each), oracle C restatement, "
-                      f"OpenMP over pixel columns, {el:.1f} s"}
 
 
 # ------------------------------------------------------------- reference arm
@@ -477,21 +797,26 @@ def cpu_baseline_line(flat, budget_s: float):
 def run_reference(args, rank, world, local):
     if rank != 0:
         return
-    from jaxrenderer_gb300 import synthetic
-
-    flat = synthetic.brax_like_batch(min(args.scenes, 256), seed=synthetic.BASE_SEED + 1)
+    n = args.scenes
+    if args.workload == "brax84":
+        n = min(n, 256)  # scenes the sample draws from (the workload's first 256)
+    wl = BUILDERS[args.workload](n, 0, None)
+    wl.frames = args.scenes
+    if len(wl.work) != args.scenes:
+        wl.work = np.resize(wl.work, args.scenes)
     threads = len(os.sched_getaffinity(0))
-    tables = HostTables(flat)
-    _oracle_frame(flat, tables, 0, threads)
     per_step = []
     budget = 6.0
+    start = 0
     for k in range(args.warmup + args.steps):
-        done, el = time_oracle(flat, tables, budget, threads)
+        fps, done, el = oracle_rate(wl, budget, threads, start)
+        start += done
         if k >= args.warmup:
-            per_step.append((done, el))
-    frames = sum(d for d, _ in per_step)
-    secs = sum(e for _, e in per_step)
-    value = frames / secs
+            per_step.append((fps, done, el))
+    value = float(np.mean([p[0] for p in per_step]))
+    frames = sum(p[1] for p in per_step)
+    secs = sum(p[2] for p in per_step)
+    crop = f", main pass cropped to 1/{wl.oracle_crop} of the columns" if wl.oracle_crop > 1 else ""
     out = {
         "metric": METRIC,
         "value": value,
@@ -505,9 +830,9 @@ def run_reference(args, rank, world, local):
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f32",
-        "data": "synthetic (seeded Brax-like scenes)",
-        "config": {"workload": "brax-like 84x84 x 4096 scenes, phong_reflection_shadow + 128x128 depth pass",
-                   "sample_per_step": f"~{budget:.0f} s of consecutive scenes"},
+        "data": "synthetic (seeded stand-ins with the stated shapes)",
+        "config": dict({"workload": wl.desc, "sample_per_step": f"~{budget:.0f} s of consecutive scenes{crop}"},
+                       **wl.config),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": f"{frames} scenes over {len(per_step)} steps; JAX is not installable, so the "
                                    "CPU path timed is the C restatement of the reference (oracle/)"},

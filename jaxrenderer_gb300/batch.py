@@ -15,7 +15,7 @@ from __future__ import annotations
 
 import ctypes
 from dataclasses import dataclass, field
-from typing import Dict, Optional, Sequence
+from typing import Dict, List, Optional, Sequence, Tuple
 
 import numpy as np
 import torch
@@ -48,16 +48,20 @@ class SceneBatch:
     shadow_jobs: Optional[np.ndarray]  # RastJob table of the depth pass, or None
     device: torch.device
     n_faces: np.ndarray = field(default=None)
+    shadow_index: Optional[np.ndarray] = None  # scene -> shadow job row or -1
 
     @property
     def total_faces(self) -> int:
         return int(self.n_faces.sum())
 
 
-def _cameras(positions: np.ndarray, params: CameraParameters):
+def _cameras(positions: np.ndarray, params: CameraParameters, targets=None):
     w2c, w2e, view = [], [], []
-    for p in positions:
-        cam = Renderer.create_camera_from_parameters(params._replace(position=p))
+    for k, p in enumerate(positions):
+        prm = params._replace(position=p)
+        if targets is not None:
+            prm = prm._replace(target=targets[k])
+        cam = Renderer.create_camera_from_parameters(prm)
         w2c.append(cam.world_to_clip)
         w2e.append(cam.world_to_eye_norm)
         view.append(cam.view)
@@ -74,47 +78,55 @@ class SceneTables:
     height: int
     shadow_width: int
     shadow_height: int
+    shadow_index: Optional[np.ndarray] = None  # scene -> row of shadow_jobs, -1 without a shadow pass
 
 
 def scene_batch_tables(flat, width: int = 84, height: int = 84,
                        light: LightParameters = LightParameters(),
                        shadow_param: Optional[ShadowParameters] = ShadowParameters(),
-                       shadow_size=(128, 128), camera_params: Optional[CameraParameters] = None) -> SceneTables:
+                       shadow_size=(128, 128), camera_params: Optional[CameraParameters] = None,
+                       shadow_mask: Optional[np.ndarray] = None) -> SceneTables:
     """RastJob tables of a synthetic.FlatScenes batch.
 
     Each scene: PhongReflection(Shadow)TextureShader over its corners
     (Renderer.render, renderer.py:254-385); with `shadow_param`, a DepthShader
     pass into a shadow_size map seen through an orthographic light camera
     with viewport shadow_size (the low-level Shadow.render_shadow_map API).
+    `shadow_mask` (N,) selects the scenes that get the shadow pass (all by
+    default); the others render with PhongReflectionTextureShader.
     """
     n = flat.n_scenes
+    T = int(getattr(flat, "tex_size", 4))
     params = camera_params or CameraParameters(viewWidth=width, viewHeight=height, near=0.01, far=1000.0,
                                                hfov=58.0, vfov=58.0, target=np.zeros(3, F32))
-    w2c, w2e, views, viewport = _cameras(flat.camera_position, params)
+    w2c, w2e, views, viewport = _cameras(flat.camera_position, params, getattr(flat, "camera_target", None))
     light_dir = normalise(np.asarray(light.direction, F32))
     light_dir_eye = np.stack([Camera.apply_vec(light_dir, v) for v in views])
 
     shadow = shadow_param is not None
+    mask = np.ones(n, bool) if shadow_mask is None else np.asarray(shadow_mask, bool)
+    if not shadow:
+        mask = np.zeros(n, bool)
     main = job_table(n)
-    main["shader"] = _lib.SHADER_PHONG_REFLECTION_SHADOW if shadow else _lib.SHADER_PHONG_REFLECTION
+    main["shader"] = np.where(mask, _lib.SHADER_PHONG_REFLECTION_SHADOW, _lib.SHADER_PHONG_REFLECTION)
     main["width"], main["height"] = width, height
     main["n_verts"] = 3 * flat.n_faces
     main["n_faces"] = flat.n_faces
     main["n_objects"] = flat.n_objects
-    main["texture_offset"] = 4
+    main["texture_offset"] = T
     main["vert_begin"] = flat.corner_begin
     main["face_begin"] = 0
     main["pixel_begin"] = np.arange(n, dtype=np.int64) * width * height
     main["vout_begin"] = flat.corner_begin
     main["setup_begin"] = np.concatenate([[0], np.cumsum(flat.n_faces.astype(np.int64))[:-1]])
-    main["texture_begin"] = flat.tex_begin * 4 * 3
-    main["specular_begin"] = flat.tex_begin * 4
+    main["texture_begin"] = flat.tex_begin * T * 3
+    main["specular_begin"] = flat.tex_begin * T
     obj_begin = np.concatenate([[0], np.cumsum(flat.n_objects.astype(np.int64))[:-1]])
     main["texture_shape_begin"] = obj_begin
-    main["tex_w"] = 4 * flat.n_objects
-    main["tex_h"], main["tex_c"] = 4, 3
-    main["spec_w"] = 4 * flat.n_objects
-    main["spec_h"] = 4
+    main["tex_w"] = T * flat.n_objects
+    main["tex_h"], main["tex_c"] = T, 3
+    main["spec_w"] = T * flat.n_objects
+    main["spec_h"] = T
     main["viewport"] = np.broadcast_to(viewport.reshape(16), (n, 16))
     main["world_to_clip"] = w2c.reshape(n, 16)
     main["world_to_eye_norm"] = w2e.reshape(n, 16)
@@ -129,23 +141,33 @@ def scene_batch_tables(flat, width: int = 84, height: int = 84,
     if shadow:
         svp = Camera.viewport_matrix(np.zeros(2, np.int32), np.array((sw, sh)), 1.0)
         scam = Shadow.light_camera(np.asarray(light.direction, F32), svp, shadow_param.centre, shadow_param.up)
-        shadow_jobs = job_table(n)
+        sel = np.nonzero(mask)[0]
+        shadow_jobs = job_table(len(sel))
         shadow_jobs["shader"] = _lib.SHADER_DEPTH
         shadow_jobs["width"], shadow_jobs["height"] = sw, sh
-        for k in ("n_verts", "n_faces", "vert_begin", "face_begin", "vout_begin", "setup_begin"):
-            shadow_jobs[k] = main[k]
-        shadow_jobs["pixel_begin"] = np.arange(n, dtype=np.int64) * sw * sh
+        for k in ("n_verts", "n_faces", "vert_begin", "face_begin"):
+            shadow_jobs[k] = main[k][sel]
+        nf = shadow_jobs["n_faces"].astype(np.int64)
+        nvt = shadow_jobs["n_verts"].astype(np.int64)
+        shadow_jobs["setup_begin"] = np.concatenate([[0], np.cumsum(nf)[:-1]])
+        shadow_jobs["vout_begin"] = np.concatenate([[0], np.cumsum(nvt)[:-1]])
+        shadow_jobs["pixel_begin"] = np.arange(len(sel), dtype=np.int64) * sw * sh
         shadow_jobs["viewport"] = svp.reshape(16)
         shadow_jobs["world_to_clip"] = scam.world_to_clip.reshape(16)
         shadow_jobs["world_to_eye_norm"] = scam.world_to_eye_norm.reshape(16)
         shadow_jobs["depth_offset"] = np.float32(shadow_param.offset)
         shadow_jobs["flags"] = _lib.JOB_APPLY_DEPTH_OFFSET
-        main["shadow_begin"] = shadow_jobs["pixel_begin"]
-        main["shadow_w"], main["shadow_h"] = sw, sh
-        main["shadow_viewport"] = scam.viewport.reshape(16)
-        main["shadow_world_to_clip"] = scam.world_to_clip.reshape(16)
-        main["shadow_strength"] = np.asarray(shadow_param.strength, F32)
-    return SceneTables(main, shadow_jobs, width, height, sw, sh)
+        main["shadow_begin"][sel] = shadow_jobs["pixel_begin"]
+        main["shadow_w"][sel], main["shadow_h"][sel] = sw, sh
+        main["shadow_viewport"][sel] = scam.viewport.reshape(16)
+        main["shadow_world_to_clip"][sel] = scam.world_to_clip.reshape(16)
+        main["shadow_strength"][sel] = np.asarray(shadow_param.strength, F32)
+    if shadow_jobs is not None and len(shadow_jobs) == 0:
+        shadow_jobs = None
+    index = np.full(n, -1, np.int64)
+    if shadow_jobs is not None:
+        index[np.nonzero(mask)[0]] = np.arange(len(shadow_jobs))
+    return SceneTables(main, shadow_jobs, width, height, sw, sh, index)
 
 
 def flat_pools(flat, device) -> Dict[str, torch.Tensor]:
@@ -164,7 +186,8 @@ def flat_pools(flat, device) -> Dict[str, torch.Tensor]:
         "faces": T(faces, torch.int32),
         "texture": T(flat.texture),
         "specular_map": T(flat.specular_map),
-        "texture_shape": T(np.tile(np.array([[4, 4]], np.int32), (int(flat.n_objects.sum()), 1)), torch.int32),
+        "texture_shape": T(np.tile(np.array([[getattr(flat, "tex_size", 4)] * 2], np.int32),
+                                   (int(flat.n_objects.sum()), 1)), torch.int32),
     }
 
 
@@ -172,10 +195,11 @@ def scene_batch_from_flat(flat, width: int = 84, height: int = 84,
                           light: LightParameters = LightParameters(),
                           shadow_param: Optional[ShadowParameters] = ShadowParameters(),
                           shadow_size=(128, 128), device=None,
-                          camera_params: Optional[CameraParameters] = None) -> SceneBatch:
+                          camera_params: Optional[CameraParameters] = None,
+                          shadow_mask: Optional[np.ndarray] = None) -> SceneBatch:
     """Upload a synthetic.FlatScenes batch and build its job tables."""
     device = device if device is not None else torch.device("cuda", torch.cuda.current_device())
-    t = scene_batch_tables(flat, width, height, light, shadow_param, shadow_size, camera_params)
+    t = scene_batch_tables(flat, width, height, light, shadow_param, shadow_size, camera_params, shadow_mask)
     lib = _lib.load()
     for tbl in (t.main_jobs, t.shadow_jobs):
         if tbl is None:
@@ -184,7 +208,7 @@ def scene_batch_from_flat(flat, width: int = 84, height: int = 84,
             job = _lib.RastJob.from_buffer_copy(tbl[k].tobytes())
             _lib.check(lib.rast_validate_job(ctypes.byref(job)), f"job {k}")
     return SceneBatch(flat.n_scenes, width, height, t.shadow_width, t.shadow_height, flat_pools(flat, device),
-                      t.main_jobs, t.shadow_jobs, device, flat.n_faces)
+                      t.main_jobs, t.shadow_jobs, device, flat.n_faces, t.shadow_index)
 
 
 def scene_batch_from_specs(specs, device=None) -> SceneBatch:
@@ -209,6 +233,7 @@ def scene_job_specs(flat, tables, s: int):
     from .jobs import JobSpec
 
     m = tables.main_jobs[s]
+    T = int(getattr(flat, "tex_size", 4))
     cb, F = int(flat.corner_begin[s]), int(flat.n_faces[s])
     tb, no = int(flat.tex_begin[s]), int(flat.n_objects[s])
     faces = np.arange(3 * F, dtype=np.int32).reshape(F, 3)
@@ -220,15 +245,17 @@ def scene_job_specs(flat, tables, s: int):
     main.normal = flat.normal[rows]
     main.uv = flat.uv[rows]
     main.texture_index = flat.texture_index[rows]
-    main.texture = flat.texture[tb : tb + 4 * no]
-    main.specular_map = flat.specular_map[tb : tb + 4 * no]
-    main.texture_shape = np.tile(np.array([[4, 4]], np.int32), (no, 1))
-    main.texture_offset = 4
+    main.texture = flat.texture[tb : tb + T * no]
+    main.specular_map = flat.specular_map[tb : tb + T * no]
+    main.texture_shape = np.tile(np.array([[T, T]], np.int32), (no, 1))
+    main.texture_offset = T
     for k in ("light_direction", "light_colour", "light_dir_eye", "ambient", "diffuse", "specular"):
         setattr(main, k, np.asarray(m[k], F32))
     depth = None
-    if tables.shadow_jobs is not None:
-        d = tables.shadow_jobs[s]
+    index = getattr(tables, "shadow_index", None)
+    srow = s if index is None else int(index[s])
+    if tables.shadow_jobs is not None and srow >= 0:
+        d = tables.shadow_jobs[srow]
         depth = JobSpec(shader=_lib.SHADER_DEPTH, width=int(d["width"]), height=int(d["height"]),
                         viewport=d["viewport"].reshape(4, 4), world_to_clip=d["world_to_clip"].reshape(4, 4),
                         world_to_eye_norm=d["world_to_eye_norm"].reshape(4, 4), position=flat.position[rows],
@@ -303,7 +330,8 @@ class BatchRunner:
         lib = _lib.load()
         self.lib = lib
         if sb.shadow_jobs is not None:
-            self.shadow_map = torch.empty((n, sb.shadow_width, sb.shadow_height), dtype=torch.float32, device=dev)
+            self.shadow_map = torch.empty((len(sb.shadow_jobs), sb.shadow_width, sb.shadow_height),
+                                          dtype=torch.float32, device=dev)
             self.shadow_prim = torch.empty_like(self.shadow_map, dtype=torch.int32) if want_prim_id else None
             self.shadow_batch = _rast_batch(sb.shadow_jobs, sb.pools, self.shadow_map, None, self.shadow_prim, None, self.keep)
             pools = dict(sb.pools)
@@ -452,11 +480,88 @@ class BatchRunner:
         return self.outputs()
 
 
+class MultiRunner:
+    """Several SceneBatches (e.g. one per resolution class of a mixed batch),
+    each with its own BatchRunner and autotuned tiled config, rendered in
+    order on one stream; `capture()` records all of them into ONE CUDA graph
+    so a replay re-issues the whole mixed batch with a single launch."""
+
+    def __init__(self, batches: Sequence[SceneBatch], form: str = "tiled", want_prim_id: bool = True,
+                 tiled_config=None):
+        if not batches:
+            raise ValueError("MultiRunner needs at least one SceneBatch")
+        self.runners = [BatchRunner(sb, form=form, want_prim_id=want_prim_id, tiled_config=tiled_config)
+                        for sb in batches]
+        self.form = form
+        self.device = batches[0].device
+        self.graph = None
+
+    @property
+    def n_scenes(self) -> int:
+        return sum(r.sb.n_scenes for r in self.runners)
+
+    def run(self, stream: Optional[torch.cuda.Stream] = None) -> List[BatchOutputs]:
+        s = stream if stream is not None else torch.cuda.current_stream(self.device)
+        return [r.run(s) for r in self.runners]
+
+    def capture(self) -> None:
+        dev = self.device
+        side = torch.cuda.Stream(dev)
+        side.wait_stream(torch.cuda.current_stream(dev))
+        self.run(side)
+        torch.cuda.current_stream(dev).wait_stream(side)
+        torch.cuda.synchronize(dev)
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            self.run(torch.cuda.current_stream(dev))
+        self.graph = g
+
+    def replay(self) -> List[BatchOutputs]:
+        self.graph.replay()
+        return [r.outputs() for r in self.runners]
+
+    def grad_buffers(self) -> List[Dict[str, torch.Tensor]]:
+        return [r.grad_buffers() for r in self.runners]
+
+    def backward(self, grad_canvases: Sequence[torch.Tensor], out=None,
+                 stream: Optional[torch.cuda.Stream] = None) -> List[Dict[str, torch.Tensor]]:
+        outs = out if out is not None else [None] * len(self.runners)
+        return [r.backward(g, stream=stream, out=o) for r, g, o in zip(self.runners, grad_canvases, outs)]
+
+
+def mixed_scene_batches(flat, resolutions: np.ndarray, classes: Sequence[Tuple[int, int]],
+                        shadow_mask: Optional[np.ndarray] = None, light: LightParameters = LightParameters(),
+                        shadow_param: Optional[ShadowParameters] = ShadowParameters(), device=None,
+                        camera_params: Optional[CameraParameters] = None):
+    """Split a FlatScenes batch by resolution class: scene s renders at
+    classes[resolutions[s]].  Scenes with shadow_mask[s] get the depth pass
+    (a map of their own canvas size, as Renderer.render makes it,
+    renderer.py:343-365) and PhongReflectionShadowTextureShader, the others
+    PhongReflectionTextureShader.  Returns [(scene indices, SceneBatch)] per
+    non-empty class, in class order."""
+    from .synthetic import flat_subset
+
+    res = np.asarray(resolutions)
+    mask = np.ones(flat.n_scenes, bool) if shadow_mask is None else np.asarray(shadow_mask, bool)
+    out = []
+    for c, (w, h) in enumerate(classes):
+        idx = np.nonzero(res == c)[0]
+        if idx.size == 0:
+            continue
+        sub = flat_subset(flat, idx)
+        prm = None
+        if camera_params is not None:
+            prm = camera_params._replace(viewWidth=w, viewHeight=h)
+        sb = scene_batch_from_flat(sub, w, h, light, shadow_param, (w, h), device, prm, mask[idx])
+        out.append((idx, sb))
+    return out
+
+
 def render_batch(sb: SceneBatch, form: str = "plain", want_prim_id: bool = True) -> BatchOutputs:
     """Render every scene of `sb` (see BatchRunner)."""
     return BatchRunner(sb, form=form, want_prim_id=want_prim_id).run()
 
 
 __all__ = ["SceneBatch", "SceneTables", "scene_batch_tables", "scene_batch_from_flat", "scene_batch_from_specs",
-           "scene_job_specs",
+           "scene_job_specs", "MultiRunner", "mixed_scene_batches",
            "flat_pools", "render_batch", "BatchRunner", "BatchOutputs", "job_table"]

@@ -219,6 +219,8 @@ class FlatScenes:
     tex_begin: np.ndarray
     n_objects: np.ndarray
     camera_position: np.ndarray
+    tex_size: int = 4  # every object's diffuse/specular map is tex_size x tex_size
+    camera_target: Optional[np.ndarray] = None  # (N, 3); origin when None
 
     @property
     def n_scenes(self) -> int:
@@ -321,6 +323,34 @@ def phong_scene(rng: np.random.Generator, level: int = 4, texture_size: int = 64
     return PhongScene(v, pos, n, uv, f, tex, l, e)
 
 
+def phong_camera_params(eye, width: int = 128, height: int = 128):
+    """Camera of the differentiable phong workload: at `eye`, looking at the
+    origin, +Z up, 40 degree field of view, near 0.1, far 100."""
+    from .renderer import CameraParameters
+
+    return CameraParameters(viewWidth=width, viewHeight=height, near=0.1, far=100.0, hfov=40.0, vfov=40.0,
+                            position=np.asarray(eye, F32), target=np.zeros(3, F32))
+
+
+def phong_job_spec(sc: PhongScene, width: int = 128, height: int = 128, position: Optional[np.ndarray] = None):
+    """JobSpec of PhongTextureShader (phong.py) rendering `sc` (its displaced
+    positions unless `position` is given) through phong_camera_params."""
+    from . import _lib
+    from .jobs import JobSpec
+    from .renderer import Renderer
+
+    cam = Renderer.create_camera_from_parameters(phong_camera_params(sc.eye, width, height))
+    spec = JobSpec(shader=_lib.SHADER_PHONG, width=width, height=height, viewport=cam.viewport,
+                   world_to_clip=cam.world_to_clip, world_to_eye_norm=cam.world_to_eye_norm,
+                   position=np.asarray(sc.position if position is None else position, F32), faces=sc.faces)
+    spec.normal = sc.normal
+    spec.uv = sc.uv
+    spec.texture = sc.texture
+    spec.light_direction = sc.light_direction
+    spec.light_colour = np.ones(3, F32)
+    return spec
+
+
 # ------------------------------------------- large overlapping single scene
 
 def overdraw_scene(rng: np.random.Generator, width: int = 960, height: int = 540,
@@ -372,3 +402,80 @@ def overdraw_scene(rng: np.random.Generator, width: int = 960, height: int = 540
         light_direction=-light if light[2] < 0 else light, light_colour=np.ones(3, F32),
     )
     return spec, float(area / (width * height))
+
+
+def _quat_matrices(q: np.ndarray) -> np.ndarray:
+    """(K, 3, 3) rotation matrices of (K, 4) unit (w, x, y, z) quaternions,
+    the same convention as geometry.transform_matrix_from_rotation."""
+    w, x, y, z = q[:, 0], q[:, 1], q[:, 2], q[:, 3]
+    return np.stack([
+        np.stack([1 - 2 * (y * y + z * z), 2 * (x * y - w * z), 2 * (x * z + w * y)], -1),
+        np.stack([2 * (x * y + w * z), 1 - 2 * (x * x + z * z), 2 * (y * z - w * x)], -1),
+        np.stack([2 * (x * z - w * y), 2 * (y * z + w * x), 1 - 2 * (x * x + y * y)], -1),
+    ], -2)
+
+
+def cube_scene_batch(n_scenes: int, seed: int = BASE_SEED + 5, f_min: int = 100, f_max: int = 100_000,
+                     chunk: int = 65536) -> FlatScenes:
+    """Scenes built from the config-1 primitive (create_cube, 12 triangles,
+    24 vertices with normals and UVs): triangle counts log-uniform in
+    [f_min, f_max] (rounded to whole cubes), cubes at uniform positions in a
+    box of half-extent 1.5 * cubes^(1/3), random unit-quaternion rotations,
+    scales U[0.3, 0.8], one RGB diffuse U[0, 1] per cube on a 4x4 map,
+    specular 2.0; the camera at 3.2 half-extents on a random direction above
+    the box's mid-plane, looking at the origin."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    cube = create_cube(np.ones(3, F32), np.ones(2, F32), np.zeros((4, 4, 3), F32), np.full((4, 4), 2.0, F32))
+    idx = np.asarray(cube.faces, np.int32).reshape(-1)
+    cv = np.asarray(cube.verts, F32)[idx]
+    cn = np.asarray(cube.norms, F32)[idx]
+    cu = np.asarray(cube.uvs, F32)[idx]
+    n_cubes = np.maximum(1, np.round(np.exp(rng.uniform(np.log(f_min), np.log(f_max), n_scenes)) / 12)).astype(np.int64)
+    K = int(n_cubes.sum())
+    scene_of = np.repeat(np.arange(n_scenes), n_cubes)
+    half = 1.5 * n_cubes.astype(np.float64) ** (1.0 / 3.0)
+    centres = rng.uniform(-1.0, 1.0, (K, 3)) * half[scene_of, None]
+    q = rng.normal(size=(K, 4))
+    q /= np.linalg.norm(q, axis=1, keepdims=True)
+    scale = rng.uniform(0.3, 0.8, K)
+    colour = rng.uniform(0, 1, (K, 3))
+    d = rng.normal(size=(n_scenes, 3))
+    d[:, 2] = np.abs(d[:, 2]) + 0.3
+    cams = (3.2 * half[:, None] * d / np.linalg.norm(d, axis=1, keepdims=True)).astype(F32)
+    position = np.empty((36 * K, 3), F32)
+    normal = np.empty((36 * K, 3), F32)
+    for a in range(0, K, chunk):
+        b = min(K, a + chunk)
+        R = _quat_matrices(q[a:b])
+        position[36 * a : 36 * b] = (np.einsum("kij,vj->kvi", R * scale[a:b, None, None], cv)
+                                     + centres[a:b, None, :]).reshape(-1, 3)
+        normal[36 * a : 36 * b] = np.einsum("kij,vj->kvi", R, cn).reshape(-1, 3)
+    uv = np.tile(cu, (K, 1))
+    cube_begin = np.concatenate([[0], np.cumsum(n_cubes)[:-1]])
+    tex_idx = (np.arange(K, dtype=np.int64) - cube_begin[scene_of]).astype(np.int32).repeat(36)
+    texture = np.repeat(colour, 4, axis=0)[:, None, :].repeat(4, axis=1).astype(F32)
+    specular = np.full((4 * K, 4), 2.0, F32)
+    n_faces = (12 * n_cubes).astype(np.int32)
+    corner_begin = 36 * cube_begin
+    return FlatScenes(position, normal, uv, tex_idx, texture, specular, corner_begin.astype(np.int64), n_faces,
+                      (4 * cube_begin).astype(np.int64), n_cubes.astype(np.int32), cams, 4,
+                      np.zeros((n_scenes, 3), F32))
+
+
+def flat_subset(flat: FlatScenes, scenes: Sequence[int]) -> FlatScenes:
+    """The scenes `scenes` of a FlatScenes batch as a FlatScenes of their own
+    (corner and texture rows gathered, offsets rebased)."""
+    sel = np.asarray(scenes, np.int64)
+    T = flat.tex_size
+    nf = flat.n_faces[sel].astype(np.int64)
+    no = flat.n_objects[sel].astype(np.int64)
+    rows = np.concatenate([np.arange(c, c + 3 * f) for c, f in zip(flat.corner_begin[sel], nf)]) if len(sel) else \
+        np.zeros(0, np.int64)
+    trows = np.concatenate([np.arange(t, t + T * o) for t, o in zip(flat.tex_begin[sel], no)]) if len(sel) else \
+        np.zeros(0, np.int64)
+    corner_begin = np.concatenate([[0], np.cumsum(3 * nf)[:-1]]).astype(np.int64)
+    tex_begin = np.concatenate([[0], np.cumsum(T * no)[:-1]]).astype(np.int64)
+    target = None if flat.camera_target is None else flat.camera_target[sel]
+    return FlatScenes(flat.position[rows], flat.normal[rows], flat.uv[rows], flat.texture_index[rows],
+                      flat.texture[trows], flat.specular_map[trows], corner_begin, flat.n_faces[sel].copy(),
+                      tex_begin, flat.n_objects[sel].copy(), flat.camera_position[sel].copy(), T, target)

@@ -1,0 +1,150 @@
+"""GPU parity on the benchmark workloads beyond the 84x84 batch: the
+389,120-triangle overdraw scene (tiled == plain bit-exact on the full frame,
+the oracle on a band of columns) and the mixed-resolution / mixed-shader
+batch rendered through one MultiRunner graph (tiled == plain, the oracle on
+a few scenes of every resolution class, backward of both forms)."""
+import copy
+
+import numpy as np
+import pytest
+import torch
+
+from jaxrenderer_gb300 import _lib, batch as jb, synthetic
+from jaxrenderer_gb300.jobs import JobSpec, pack, render_plain, render_tiled, unpack
+from oracle import oracle
+from tests.test_gpu_plain import assert_parity
+
+pytestmark = pytest.mark.gpu
+F32 = np.float32
+CLASSES = [(32, 32), (84, 84), (480, 270)]
+
+
+@pytest.fixture(scope="module")
+def overdraw(cuda_device):
+    rng = np.random.Generator(np.random.PCG64(synthetic.BASE_SEED + 3))
+    d, est = synthetic.overdraw_scene(rng)
+    spec = JobSpec(shader=_lib.SHADER_GOURAUD_TEXTURE, **d)
+    assert spec.n_faces == 389_120 and est > 10
+    z0 = np.ones((spec.width, spec.height), F32)
+    c0 = np.ones((spec.width, spec.height, 3), F32)
+    out = {}
+    for form in ("plain", "tiled"):
+        packed = pack([spec], [z0], [c0], cuda_device, count_ties=True)
+        if form == "plain":
+            render_plain(packed)
+        else:
+            stats = render_tiled(packed, tile=(8, 8))
+            assert stats.overflow == 0
+        z, c, p = unpack(packed, [spec])[0]
+        out[form] = (z.clone(), c.clone(), p.clone(), int(packed.near_ties.item()))
+    return spec, z0, c0, out
+
+
+def test_overdraw_scene_tiled_equals_plain(overdraw):
+    spec, _, _, out = overdraw
+    (zp, cp, pp, tp), (zt, ct, pt, tt) = out["plain"], out["tiled"]
+    assert torch.equal(pp, pt)
+    assert torch.equal(zp.view(torch.int32), zt.view(torch.int32))
+    assert torch.equal(cp.view(torch.int32), ct.view(torch.int32))
+    assert tp == tt
+    assert (pp >= 0).float().mean() > 0.5  # the spheres cover most of the frame
+
+
+def band(spec: JobSpec, i0: int, w: int) -> JobSpec:
+    """Columns [i0, i0 + w) of `spec` as a job of width w: the viewport's x
+    offset moves by -i0 (exact in FP32 for these integers), so pixel i of the
+    band computes what pixel i0 + i of the full frame does."""
+    b = copy.copy(spec)
+    b.width = w
+    vp = np.array(spec.viewport, F32, copy=True)
+    vp[0, 3] = F32(vp[0, 3] - F32(i0))
+    assert float(vp[0, 3]) == float(spec.viewport[0, 3]) - i0
+    b.viewport = vp
+    return b
+
+
+def test_overdraw_scene_band_matches_oracle(overdraw):
+    spec, z0, c0, out = overdraw
+    z, c, p, _ = out["tiled"]
+    i0, w = 468, 24  # the middle of the frame, where the spheres pile up
+    ref = oracle.render(band(spec, i0, w), z0[i0 : i0 + w], c0[i0 : i0 + w])
+    assert_parity(z[i0 : i0 + w], c[i0 : i0 + w], p[i0 : i0 + w], ref, "overdraw band")
+
+
+@pytest.fixture(scope="module")
+def mixed(cuda_device):
+    n = 36
+    flat = synthetic.cube_scene_batch(n, seed=synthetic.BASE_SEED + 15, f_min=100, f_max=20_000)
+    rng = np.random.Generator(np.random.PCG64(synthetic.BASE_SEED + 16))
+    res = np.arange(n) % 3
+    rng.shuffle(res)
+    shadow = rng.random(n) < 0.5
+    groups = jb.mixed_scene_batches(flat, res, CLASSES, shadow, device=cuda_device)
+    assert len(groups) == 3
+    return flat, res, shadow, groups
+
+
+def _outputs(outs):
+    return [{k: (None if getattr(o, k) is None else getattr(o, k).clone())
+             for k in ("canvas", "zbuffer", "prim_id", "shadow_map", "shadow_prim_id")} for o in outs]
+
+
+def test_mixed_batch_graph_tiled_equals_plain(mixed):
+    _, _, _, groups = mixed
+    sbs = [sb for _, sb in groups]
+    tiled = jb.MultiRunner(sbs, form="tiled")
+    tiled.capture()
+    got = _outputs(tiled.replay())
+    want = _outputs(jb.MultiRunner(sbs, form="plain").run())
+    torch.cuda.synchronize()
+    for g, w in zip(got, want):
+        for k in g:
+            if w[k] is None:
+                assert g[k] is None
+                continue
+            a, b = g[k], w[k]
+            if a.dtype == torch.float32:
+                a, b = a.view(torch.int32), b.view(torch.int32)
+            assert torch.equal(a, b), k
+
+
+def test_mixed_batch_matches_oracle(mixed):
+    flat, res, shadow, groups = mixed
+    for c, (idx, sb) in enumerate(groups):
+        w, h = CLASSES[c]
+        sub = synthetic.flat_subset(flat, idx)
+        tables = jb.scene_batch_tables(sub, w, h, shadow_size=(w, h), shadow_mask=shadow[idx])
+        out = jb.MultiRunner([sb], form="tiled").run()[0]
+        # the cheapest scene with and the cheapest without a shadow pass
+        picks = []
+        for want in (True, False):
+            cand = [k for k in np.argsort(sub.n_faces) if bool(shadow[idx[k]]) == want]
+            if cand:
+                picks.append(int(cand[0]))
+        for k in picks:
+            dspec, mspec = jb.scene_job_specs(sub, tables, k)
+            if dspec is not None:
+                dref = oracle.render(dspec, np.full((w, h), np.finfo(F32).max, F32))
+                srow = int(tables.shadow_index[k])
+                np.testing.assert_array_equal(out.shadow_map[srow].cpu().numpy().view(np.uint32),
+                                              dref["zbuffer"].view(np.uint32))
+                mspec.shadow_map = dref["zbuffer"]
+            ref = oracle.render(mspec, np.ones((w, h), F32), np.ones((w, h, 3), F32))
+            assert_parity(out.zbuffer[k], out.canvas[k], out.prim_id[k], ref, f"class {w}x{h} scene {k}")
+
+
+def test_mixed_batch_backward_tiled_matches_plain(mixed):
+    _, _, _, groups = mixed
+    sbs = [sb for _, sb in groups]
+    grads = {}
+    for form in ("tiled", "plain"):
+        mr = jb.MultiRunner(sbs, form=form)
+        outs = mr.run()
+        gen = torch.Generator().manual_seed(3)
+        gc = [torch.randn(o.canvas.shape, generator=gen).to(o.canvas.device) for o in outs]
+        grads[form] = [{k: v.clone() for k, v in g.items()} for g in mr.backward(gc)]
+    torch.cuda.synchronize()
+    for gt, gp in zip(grads["tiled"], grads["plain"]):
+        for k in gt:
+            torch.testing.assert_close(gt[k], gp[k], rtol=1e-4, atol=1e-5, msg=k)
+        assert gt["position"].abs().sum() > 0

@@ -133,3 +133,18 @@ def test_double_twin_agrees_with_float():
     same = a["prim_id"] == b["prim_id"]
     assert same.mean() > 0.97
     np.testing.assert_allclose(a["canvas"][same], b["canvas"][same], atol=2e-3)
+
+
+def test_column_band_equals_full_frame_columns():
+    """The band-of-columns job the large-scene GPU test compares against
+    (viewport x offset moved by -i0) renders exactly the full frame's columns."""
+    from tests.test_gpu_workloads import band
+
+    spec = scenes.random_job(_lib.SHADER_GOURAUD_TEXTURE, seed=5, W=64, H=40, F=200)
+    z0, c0 = scenes.initial_buffers(spec)
+    full = oracle.render(spec, z0, c0)
+    for i0, w in ((0, 10), (20, 24), (50, 14)):
+        b = oracle.render(band(spec, i0, w), z0[i0 : i0 + w], c0[i0 : i0 + w])
+        np.testing.assert_array_equal(b["prim_id"], full["prim_id"][i0 : i0 + w])
+        np.testing.assert_array_equal(b["zbuffer"].view(np.uint32), full["zbuffer"][i0 : i0 + w].view(np.uint32))
+        np.testing.assert_array_equal(b["canvas"], full["canvas"][i0 : i0 + w])
