@@ -589,21 +589,35 @@ def phong_step(wl: Workload, form: str):
     pos = sb.pools["position"].clone().requires_grad_(True)
     tex = sb.pools["texture"].clone().requires_grad_(True)
     leaves = (eye, light, pos, tex)
+    look_at = torch.zeros(3, dtype=torch.float32, device=dev)
+    up = torch.tensor(np.asarray(params.up, np.float32), device=dev)
 
     def step():
         for t in leaves:
             t.grad = None
-        w2c, w2e, _ = camera_matrices(eye, params)
+        w2c, w2e, _ = camera_matrices(eye, params, target=look_at, up=up)
         canvas, _ = db.render(position=pos, texture=tex, world_to_clip=w2c, world_to_eye_norm=w2e,
                               light_direction=light)
         loss = ((canvas - target) ** 2).mean()
         loss.backward()
 
+    # the whole step (camera matrices, render, loss, backward) as one CUDA graph
+    side = torch.cuda.Stream(dev)
+    side.wait_stream(torch.cuda.current_stream(dev))
+    with torch.cuda.stream(side):
+        for _ in range(3):
+            step()
+    torch.cuda.current_stream(dev).wait_stream(side)
+    torch.cuda.synchronize(dev)
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph):
+        step()
+
     def extra():
         return {k: float(t.grad.abs().sum()) if t.grad is not None else None
                 for k, t in zip(("camera_position", "light_direction", "position", "texture"), leaves)}
 
-    return step, db.runner, extra
+    return graph.replay, db.runner, extra
 
 
 def profile_kernels(mr, steps, stream):

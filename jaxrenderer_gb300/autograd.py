@@ -68,36 +68,52 @@ def view_matrix_inv(eye: torch.Tensor, centre: torch.Tensor, up: torch.Tensor) -
     up = torch.cross(side, forward, dim=-1)
     rot = torch.stack([side, up, -forward], dim=-1)  # columns
     top = torch.cat([rot, eye.unsqueeze(-1)], -1)
-    bottom = torch.zeros_like(top[..., :1, :])
-    bottom = bottom + torch.tensor([0.0, 0.0, 0.0, 1.0], dtype=eye.dtype, device=eye.device)
+    zero = torch.zeros_like(top[..., :1, :3])
+    bottom = torch.cat([zero, torch.ones_like(zero[..., :1])], -1)  # (0, 0, 0, 1), no host copy
     return torch.cat([top, bottom], dim=-2)
 
 
 def perspective_projection_matrix(fovy: float, aspect: float, z_near: float, z_far: float, dtype=torch.float32,
                                   device=None) -> torch.Tensor:
     """gluPerspective (geometry.py:638-684)."""
-    f = 1.0 / np.tan(np.radians(fovy) / 2.0)
+    f = float(1.0 / np.tan(np.radians(fovy) / 2.0))
     p = torch.zeros((4, 4), dtype=dtype, device=device)
-    p[0, 0] = f / aspect
+    p[0, 0] = float(f / aspect)
     p[1, 1] = f
-    p[2, 2] = (z_far + z_near) / (z_near - z_far)
-    p[2, 3] = 2.0 * z_far * z_near / (z_near - z_far)
+    p[2, 2] = float((z_far + z_near) / (z_near - z_far))
+    p[2, 3] = float(2.0 * z_far * z_near / (z_near - z_far))
     p[3, 2] = -1.0
     return p
 
 
 def camera_matrices(eye: torch.Tensor, params, target=None, up=None) -> Tuple[torch.Tensor, torch.Tensor, torch.Tensor]:
     """(world_to_clip, world_to_eye_norm, view) of cameras at `eye` (N, 3)
-    built as Renderer.create_camera_from_parameters does."""
+    built as Renderer.create_camera_from_parameters does.  With `target` and
+    `up` given as tensors on eye's device, calls after the first for the same
+    camera parameters copy nothing from the host, so they can be captured in
+    a CUDA graph."""
     dt, dev = eye.dtype, eye.device
-    target = torch.as_tensor(np.asarray(params.target if target is None else target, np.float64), dtype=dt, device=dev)
-    up = torch.as_tensor(np.asarray(params.up if up is None else up, np.float64), dtype=dt, device=dev)
+
+    def vec(x, default):
+        if isinstance(x, torch.Tensor):
+            return x.to(dtype=dt, device=dev)
+        return torch.as_tensor(np.asarray(default if x is None else x, np.float64), dtype=dt, device=dev)
+
+    target = vec(target, params.target)
+    up = vec(up, params.up)
     target = target.expand_as(eye)
     v = view_matrix(eye, target, up)
     vinv = view_matrix_inv(eye, target, up)
     aspect = np.tan(np.radians(params.hfov) / 2.0) / np.tan(np.radians(params.vfov) / 2.0)
-    p = perspective_projection_matrix(params.vfov, aspect, params.near, params.far, dtype=dt, device=dev)
+    key = (float(params.vfov), float(aspect), float(params.near), float(params.far), dt, dev)
+    p = _PROJECTIONS.get(key)
+    if p is None:  # built once per camera and device: later calls copy nothing from the host
+        p = perspective_projection_matrix(params.vfov, aspect, params.near, params.far, dtype=dt, device=dev)
+        _PROJECTIONS[key] = p
     return p @ v, vinv.transpose(-1, -2), v
+
+
+_PROJECTIONS: dict = {}
 
 
 def apply_vec(vec: torch.Tensor, m: torch.Tensor) -> torch.Tensor:

@@ -5,11 +5,12 @@
 // pass.
 //
 //   job_tiles_kernel   per-job tile grid (fixed stride: tiles of the largest job)
-//   setup_bin_kernel   one thread per face: clip positions, det/keep/inverse,
+//   setup_bin_kernel   one thread per face: clip positions, det/keep/inverse;
+//                      then one thread per candidate (queued in shared memory):
 //                      conservative tile range of its coverage region, bin counts
 //   scan_local_kernel  \  exclusive prefix sum of bin counts -> bin offsets;
 //   scan_apply_kernel  /  tiles whose bins exceed the capacity are marked
-//   scatter_kernel     one thread per face: face id into every bin it overlaps
+//   scatter_kernel     one warp per 32 faces: face id into every bin it overlaps
 //   raster_kernel      persistent warps, one tile each: bin entries staged in
 //                      shared memory, per-pixel packed (depth | id) minimum
 //   tiled_shade_kernel one thread per pixel: deferred shading of the winner,
@@ -40,29 +41,72 @@ __host__ __device__ inline int ceil_div(int a, int b) { return (a + b - 1) / b; 
 
 // --------------------------------------------------------- conservative bins
 
-// Clip a convex polygon (n <= 8 vertices) against a*x + b*y + c >= 0.
-__device__ __forceinline__ int clip_poly(const float* px, const float* py, int n, float a, float b,
-                                         float c, float* ox, float* oy) {
-  int m = 0;
-  for (int k = 0; k < n; ++k) {
-    const int k2 = (k + 1 == n) ? 0 : k + 1;
-    const float x0 = px[k], y0 = py[k], x1 = px[k2], y1 = py[k2];
-    const float d0 = a * x0 + b * y0 + c;
-    const float d1 = a * x1 + b * y1 + c;
-    const bool in0 = d0 >= 0.0f, in1 = d1 >= 0.0f;
-    if (in0 && m < 8) {
-      ox[m] = x0;
-      oy[m] = y0;
-      ++m;
+// Sutherland-Hodgman clipping in its re-entrant (streaming) form: the
+// rectangle's corners pass through three clip stages one at a time and the
+// survivors update a bounding box, so no polygon array is kept.  For an edge
+// S -> E a stage passes on the crossing point S + t (E - S),
+// t = d_S / (d_S - d_E), when the edge crosses its line, then E when
+// d_E >= 0; the closing edge (last -> first) is passed at the end.
+struct ClipBox {
+  float mnx, mxx, mny, mxy;
+  int n;
+};
+
+struct ClipStage {
+  float a, b, c;                 // the half-plane a x + b y + c >= 0
+  float fx, fy, fd, sx, sy, sd;  // first and previous vertex, with their values
+  bool any;
+};
+
+__device__ __forceinline__ void clip_sink(ClipBox& box, float x, float y) {
+  box.mnx = fminf(box.mnx, x);
+  box.mxx = fmaxf(box.mxx, x);
+  box.mny = fminf(box.mny, y);
+  box.mxy = fmaxf(box.mxy, y);
+  ++box.n;
+}
+
+__device__ __forceinline__ void clip_push2(ClipStage& s, ClipBox& box, float x, float y) {
+  const float d = s.a * x + s.b * y + s.c;
+  if (s.any) {
+    if ((s.sd >= 0.0f) != (d >= 0.0f)) {
+      const float t = s.sd / (s.sd - d);  // no cancellation: opposite signs
+      clip_sink(box, s.sx + t * (x - s.sx), s.sy + t * (y - s.sy));
     }
-    if (in0 != in1 && m < 8) {
-      const float t = d0 / (d0 - d1);  // no cancellation: d0, d1 of opposite signs
-      ox[m] = x0 + t * (x1 - x0);
-      oy[m] = y0 + t * (y1 - y0);
-      ++m;
-    }
+    if (d >= 0.0f) clip_sink(box, x, y);
+  } else {
+    s.fx = x, s.fy = y, s.fd = d, s.any = true;
   }
-  return m;
+  s.sx = x, s.sy = y, s.sd = d;
+}
+
+__device__ __forceinline__ void clip_push1(ClipStage& s, ClipStage& s2, ClipBox& box, float x, float y) {
+  const float d = s.a * x + s.b * y + s.c;
+  if (s.any) {
+    if ((s.sd >= 0.0f) != (d >= 0.0f)) {
+      const float t = s.sd / (s.sd - d);
+      clip_push2(s2, box, s.sx + t * (x - s.sx), s.sy + t * (y - s.sy));
+    }
+    if (d >= 0.0f) clip_push2(s2, box, x, y);
+  } else {
+    s.fx = x, s.fy = y, s.fd = d, s.any = true;
+  }
+  s.sx = x, s.sy = y, s.sd = d;
+}
+
+__device__ __forceinline__ void clip_push0(ClipStage& s, ClipStage& s1, ClipStage& s2, ClipBox& box, float x,
+                                           float y) {
+  const float d = s.a * x + s.b * y + s.c;
+  if (s.any) {
+    if ((s.sd >= 0.0f) != (d >= 0.0f)) {
+      const float t = s.sd / (s.sd - d);
+      clip_push1(s1, s2, box, s.sx + t * (x - s.sx), s.sy + t * (y - s.sy));
+    }
+    if (d >= 0.0f) clip_push1(s1, s2, box, x, y);
+  } else {
+    s.fx = x, s.fy = y, s.fd = d, s.any = true;
+  }
+  s.sx = x, s.sy = y, s.sd = d;
 }
 
 // Pixel range [i0, i1] x [j0, j1] that contains every pixel whose FP32 edge
@@ -91,25 +135,37 @@ __device__ __forceinline__ bool coverage_bbox(const float* inv, const RastJob& J
   const float ya = (-1.0f - oy) / sy, yb = (static_cast<float>(H) - oy) / sy;
   const float xl = fminf(xa, xb), xh = fmaxf(xa, xb), yl = fminf(ya, yb), yh = fmaxf(ya, yb);
   const float X = fmaxf(fabsf(xl), fabsf(xh)), Y = fmaxf(fabsf(yl), fabsf(yh));
-  float px[8] = {xl, xh, xh, xl}, py[8] = {yl, yl, yh, yh};
-  float qx[8], qy[8];
-  int n = 4;
-#pragma unroll
-  for (int k = 0; k < 3; ++k) {
-    const float a = inv[k], b = inv[3 + k], c = inv[6 + k];
-    const float eps = 64.0f * 5.9604645e-08f * (X * fabsf(a) + Y * fabsf(b) + fabsf(c));
-    if (k == 1) n = clip_poly(qx, qy, n, a, b, c + eps, px, py);
-    else n = clip_poly(px, py, n, a, b, c + eps, qx, qy);
-    if (n == 0) return false;
+  // edge k: a_k x + b_k y + (c_k + eps_k), kept in scalars (no arrays: the
+  // clip stages below capture them)
+  bool small = true;  // |c_k| < 1e37 on the rectangle: no overflow below
+  auto widened = [&](float a, float b, float c) {
+    const float bound = X * fabsf(a) + Y * fabsf(b) + fabsf(c);
+    small = small && bound < 1e37f;
+    return c + 64.0f * 5.9604645e-08f * bound;
+  };
+  const float a0 = inv[0], b0 = inv[3], c0 = widened(inv[0], inv[3], inv[6]);
+  const float a1 = inv[1], b1 = inv[4], c1 = widened(inv[1], inv[4], inv[7]);
+  const float a2 = inv[2], b2 = inv[5], c2 = widened(inv[2], inv[5], inv[8]);
+  if (!small) {
+    *i0 = 0;
+    *i1 = W - 1;
+    *j0 = 0;
+    *j1 = H - 1;
+    return true;  // edge functions too large to evaluate safely: every pixel
   }
-  // result is in qx/qy after clips 0 (p->q), 1 (q->p), 2 (p->q)
-  float mnx = qx[0], mxx = qx[0], mny = qy[0], mxy = qy[0];
-  for (int k = 1; k < n; ++k) {
-    mnx = fminf(mnx, qx[k]);
-    mxx = fmaxf(mxx, qx[k]);
-    mny = fminf(mny, qy[k]);
-    mxy = fmaxf(mxy, qy[k]);
-  }
+  ClipStage s0{a0, b0, c0, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, false};
+  ClipStage s1{a1, b1, c1, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, false};
+  ClipStage s2{a2, b2, c2, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, false};
+  ClipBox box{kInf, -kInf, kInf, -kInf, 0};
+#pragma unroll 1
+  for (int k = 0; k < 4; ++k) clip_push0(s0, s1, s2, box, (k == 1 || k == 2) ? xh : xl, k >= 2 ? yh : yl);
+  // closing edges, stage by stage: re-sending a stage's first vertex closes it
+  clip_push0(s0, s1, s2, box, s0.fx, s0.fy);
+  if (s1.any) clip_push1(s1, s2, box, s1.fx, s1.fy);
+  if (s2.any) clip_push2(s2, box, s2.fx, s2.fy);
+  const int n_out = box.n;
+  const float mnx = box.mnx, mxx = box.mxx, mny = box.mny, mxy = box.mxy;
+  if (n_out == 0) return false;
   // NDC -> pixel index: i = x * sx + ox (monotone in x with the sign of sx)
   const float pa = mnx * sx + ox, pb = mxx * sx + ox;
   const float qa = mny * sy + oy, qb = mxy * sy + oy;
@@ -149,45 +205,128 @@ __device__ __forceinline__ void face_clip(const RastJob& J, const RastPools& P, 
   }
 }
 
+// Visits every (lane, tile) pair of the tile rectangles the 32 lanes of a
+// warp hold ([tx0, tx1] x [ty0, ty1], empty when tx0 > tx1), 32 pairs per
+// round spread over all lanes, so one large face does not serialise on one
+// thread.  fn(owner lane, tile index within the job, valid) runs on every
+// lane each round; valid is false past the last pair.  All 32 lanes must call.
+template <class Fn>
+__device__ __forceinline__ void warp_tiles(int tx0, int ty0, int tx1, int ty1, int tiles_x, Fn&& fn) {
+  const int lane = threadIdx.x & 31;
+  const int w = tx1 - tx0 + 1;
+  const int n = (tx0 <= tx1 && ty0 <= ty1) ? w * (ty1 - ty0 + 1) : 0;
+  int incl = n;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const int v = __shfl_up_sync(0xffffffffu, incl, d);
+    if (lane >= d) incl += v;
+  }
+  const int excl = incl - n;
+  const int total = __shfl_sync(0xffffffffu, incl, 31);
+  for (int base = 0; base < total; base += 32) {
+    const int k = base + lane;
+    int owner = 0;  // lanes whose pairs all precede pair k
+#pragma unroll
+    for (int step = 16; step > 0; step >>= 1) {
+      const int v = __shfl_sync(0xffffffffu, incl, owner + step - 1);
+      if (v <= k) owner += step;
+    }
+    const int o_excl = __shfl_sync(0xffffffffu, excl, owner);
+    const int o_tx0 = __shfl_sync(0xffffffffu, tx0, owner);
+    const int o_ty0 = __shfl_sync(0xffffffffu, ty0, owner);
+    const int o_w = __shfl_sync(0xffffffffu, w, owner);
+    const bool valid = k < total;
+    int tile = 0;
+    if (valid) {
+      const int local = k - o_excl;
+      const int r = local / o_w;
+      tile = (o_ty0 + r) * tiles_x + o_tx0 + (local - r * o_w);
+    }
+    fn(owner, tile, valid);
+  }
+}
+
+__device__ __forceinline__ unsigned lanemask_lt() { return (1u << (threadIdx.x & 31)) - 1u; }
+
+// Phase 1, one thread per face: clip positions, determinant, keep/front
+// flags and inverse -> setup record.  Candidates (kept, front-facing) are
+// queued in shared memory; phase 2, one thread per queued candidate:
+// conservative coverage rectangle -> bbox, then the warp adds the tile counts
+// with one atomic per distinct tile per round (lanes hitting the same tile
+// are merged with __match_any_sync).
 // Grid: (ceil(max_faces / kSetupThreads), n_jobs); blockIdx.y is the job.
 __global__ void __launch_bounds__(kSetupThreads)
 setup_bin_kernel(RastBatch B, Geometry G, float4* __restrict__ setup, ushort4* __restrict__ bbox,
                  uint32_t* __restrict__ counts) {
   __shared__ RastJob sJ;
+  __shared__ float s_inv[9][kSetupThreads];
+  __shared__ int s_face[kSetupThreads];
+  __shared__ int s_qn;
   const int jid = blockIdx.y;
   const int nf = __ldg(&B.jobs[jid].n_faces);
   if (static_cast<int64_t>(blockIdx.x) * kSetupThreads >= nf) return;
   load_job_to_shared(B.jobs + jid, &sJ);
+  if (threadIdx.x == 0) s_qn = 0;
   __syncthreads();
   const RastJob& J = sJ;
-  const int64_t f0 = static_cast<int64_t>(blockIdx.x) * kSetupThreads + threadIdx.x;
-  if (f0 >= nf) return;
-  const int64_t row = J.setup_begin + f0;
-  const int64_t f = row - J.setup_begin;
-  float4 c[3];
-  face_clip(J, B.pools, f, c);
-  float inv[9], det;
-  int flags;
-  setup_from_clip(c, inv, &det, &flags);
-  float4* out = setup + row * 4;
-  // the inverse is read only for candidates (raster) and for face 0 (the
-  // chooser's fallback); the flags of every face are kept
-  if ((flags & kCandidate) == kCandidate || f == 0) {
-    out[0] = make_float4(inv[0], inv[1], inv[2], inv[3]);
-    out[1] = make_float4(inv[4], inv[5], inv[6], inv[7]);
-    out[2] = make_float4(inv[8], c[0].z, c[1].z, c[2].z);
+  const int f = static_cast<int>(blockIdx.x) * kSetupThreads + static_cast<int>(threadIdx.x);
+  bool cand = false;
+  float inv[9];
+  if (f < nf) {
+    const int64_t row = J.setup_begin + f;
+    float4 c[3];
+    face_clip(J, B.pools, f, c);
+    float det;
+    int flags;
+    setup_from_clip(c, inv, &det, &flags);
+    float4* out = setup + row * 4;
+    cand = (flags & kCandidate) == kCandidate;
+    // the inverse is read only for candidates (raster) and for face 0 (the
+    // chooser's fallback); the flags of every face are kept
+    if (cand || f == 0) {
+      out[0] = make_float4(inv[0], inv[1], inv[2], inv[3]);
+      out[1] = make_float4(inv[4], inv[5], inv[6], inv[7]);
+      out[2] = make_float4(inv[8], c[0].z, c[1].z, c[2].z);
+    }
+    out[3] = make_float4(det, __int_as_float(flags), 0.0f, 0.0f);
+    if (!cand) bbox[row] = make_ushort4(1, 1, 0, 0);  // empty: lo > hi
   }
-  out[3] = make_float4(det, __int_as_float(flags), 0.0f, 0.0f);
-  int i0, i1, j0, j1;
-  ushort4 bb = make_ushort4(1, 1, 0, 0);  // empty: lo > hi
-  if ((flags & kCandidate) == kCandidate && coverage_bbox(inv, J, &i0, &i1, &j0, &j1)) {
-    const int tx0 = i0 / G.tw, tx1 = i1 / G.tw, ty0 = j0 / G.th, ty1 = j1 / G.th;
-    bb = make_ushort4(tx0, ty0, tx1, ty1);
-    uint32_t* cnt = counts + static_cast<int64_t>(jid) * G.tiles_per_job;
-    for (int ty = ty0; ty <= ty1; ++ty)
-      for (int tx = tx0; tx <= tx1; ++tx) atomicAdd(cnt + ty * G.tiles_x + tx, 1u);
+  const unsigned m = __ballot_sync(0xffffffffu, cand);
+  int base = 0;
+  if ((threadIdx.x & 31) == 0 && m) base = atomicAdd(&s_qn, __popc(m));
+  base = __shfl_sync(0xffffffffu, base, 0);
+  if (cand) {
+    const int q = base + __popc(m & lanemask_lt());
+    s_face[q] = f;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) s_inv[k][q] = inv[k];
   }
-  bbox[row] = bb;
+  __syncthreads();
+  const int qn = s_qn;
+  if (static_cast<int>(threadIdx.x & ~31u) >= qn) return;  // the whole warp is past the queue
+  const int q = threadIdx.x;
+  int tx0 = 1, ty0 = 1, tx1 = 0, ty1 = 0;
+  if (q < qn) {
+    const int fq = s_face[q];
+    float iv[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) iv[k] = s_inv[k][q];
+    int i0, i1, j0, j1;
+    ushort4 bb = make_ushort4(1, 1, 0, 0);
+    if (coverage_bbox(iv, J, &i0, &i1, &j0, &j1)) {
+      tx0 = i0 / G.tw;
+      tx1 = i1 / G.tw;
+      ty0 = j0 / G.th;
+      ty1 = j1 / G.th;
+      bb = make_ushort4(tx0, ty0, tx1, ty1);
+    }
+    bbox[J.setup_begin + fq] = bb;
+  }
+  uint32_t* cnt = counts + static_cast<int64_t>(jid) * G.tiles_per_job;
+  warp_tiles(tx0, ty0, tx1, ty1, G.tiles_x, [&](int, int tile, bool valid) {
+    const unsigned peers = __match_any_sync(0xffffffffu, valid ? tile : -1);
+    if (valid && __popc(peers & lanemask_lt()) == 0) atomicAdd(cnt + tile, static_cast<unsigned>(__popc(peers)));
+  });
 }
 
 // Block-local exclusive scan of counts -> offsets, block sums out.
@@ -262,27 +401,33 @@ scan_apply_kernel(const uint32_t* __restrict__ counts, uint32_t* __restrict__ of
   }
 }
 
+// Face ids into the bins of the tiles their rectangles cover, one warp per
+// 32 faces with the (face, tile) pairs spread over its lanes; lanes writing
+// to the same tile take their slots with one atomic (__match_any_sync).
+// Grid: (ceil(max_faces / kSetupThreads), n_jobs).
 __global__ void __launch_bounds__(kSetupThreads)
 scatter_kernel(RastBatch B, Geometry G, const ushort4* __restrict__ bbox,
                const uint32_t* __restrict__ offsets, uint32_t* __restrict__ cursors,
                int32_t* __restrict__ bins) {
   const int jid = blockIdx.y;
   const int nf = __ldg(&B.jobs[jid].n_faces);
-  const int64_t f0 = static_cast<int64_t>(blockIdx.x) * kSetupThreads + threadIdx.x;
-  if (f0 >= nf) return;
-  const int64_t row = __ldg(&B.jobs[jid].setup_begin) + f0;
-  const ushort4 bb = bbox[row];
-  if (bb.x > bb.z) return;
-  const int32_t fid = static_cast<int32_t>(f0);
+  const int f = static_cast<int>(blockIdx.x) * kSetupThreads + static_cast<int>(threadIdx.x);
+  if (f - static_cast<int>(threadIdx.x & 31) >= nf) return;  // the whole warp is past the faces
+  ushort4 bb = make_ushort4(1, 1, 0, 0);
+  if (f < nf) bb = bbox[__ldg(&B.jobs[jid].setup_begin) + f];
   const int64_t tb = static_cast<int64_t>(jid) * G.tiles_per_job;
-  for (int ty = bb.y; ty <= bb.w; ++ty)
-    for (int tx = bb.x; tx <= bb.z; ++tx) {
-      const int64_t t = tb + ty * G.tiles_x + tx;
-      const uint32_t o = offsets[t];
-      if (o & kOverflow) continue;
-      const uint32_t slot = atomicAdd(cursors + t, 1u);
-      bins[static_cast<int64_t>(o) + slot] = fid;
-    }
+  const int lane = threadIdx.x & 31;
+  warp_tiles(bb.x, bb.y, bb.z, bb.w, G.tiles_x, [&](int owner, int tile, bool valid) {
+    const uint32_t o = valid ? offsets[tb + tile] : kOverflow;
+    const bool write = !(o & kOverflow);
+    const unsigned peers = __match_any_sync(0xffffffffu, write ? tile : -1);
+    const int leader = __ffs(peers) - 1;
+    uint32_t slot = 0;
+    if (write && lane == leader) slot = atomicAdd(cursors + tb + tile, static_cast<unsigned>(__popc(peers)));
+    slot = __shfl_sync(0xffffffffu, slot, leader) + __popc(peers & lanemask_lt());
+    const int fid = __shfl_sync(0xffffffffu, f, owner);
+    if (write) bins[static_cast<int64_t>(o) + slot] = fid;
+  });
 }
 
 // Persistent warps: each takes one tile (of any job) at a time.  Lane l owns
