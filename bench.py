@@ -280,7 +280,7 @@ class ClockSampler:
                  "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
             self.fh = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
-                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                          "--format=csv,noheader,nounits", "-lms", "20"],
                                          stdout=self.fh, stderr=subprocess.DEVNULL)
         except (OSError, FileNotFoundError):
             self.proc = None
@@ -411,9 +411,10 @@ def run_ours(args, rank, world, local):
         step = mr.replay
     else:
         step = lambda: mr.run(stream)  # noqa: E731
-    for _ in range(args.warmup):
-        step()
-    with ClockSampler(local) as clk:
+    with ClockSampler(local) as clk:  # sampled over the warm-up and the timed steps
+        time.sleep(0.2)
+        for _ in range(args.warmup):
+            step()
         ms_per_step = timed(step, args.steps, 0)
     value = world * wl.frames / (ms_per_step / 1e3)
     prof = profile_kernels(mr, args.steps, stream)

@@ -136,17 +136,23 @@ struct ParamGrad {
 
 // Block reduction of the parameters in BITS, added to this block's scene.
 // Every thread of the block must call it.
+// `active`: this thread contributed; warps without a contributing thread
+// skip their shuffles and add zeros.
 template <unsigned long long BITS>
-__device__ __forceinline__ void reduce_params(const ParamGrad& pg, float* job_params) {
+__device__ __forceinline__ void reduce_params(const ParamGrad& pg, float* job_params, bool active, int job) {
   __shared__ float s_red[kThreads / 32][RAST_NPARAM];
   if (BITS == 0ull || !job_params) return;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const bool warp_active = __any_sync(0xffffffffu, active);
 #pragma unroll
   for (int k = 0; k < RAST_NPARAM; ++k) {
     if (!((BITS >> k) & 1ull)) continue;
-    float v = pg.v[k];
+    float v = 0.0f;
+    if (warp_active) {
+      v = pg.v[k];
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    }
     if (lane == 0) s_red[warp][k] = v;
   }
   __syncthreads();
@@ -154,7 +160,7 @@ __device__ __forceinline__ void reduce_params(const ParamGrad& pg, float* job_pa
     float v = 0.0f;
 #pragma unroll
     for (int w = 0; w < kThreads / 32; ++w) v += s_red[w][threadIdx.x];
-    if (v != 0.0f) atomicAdd(job_params + static_cast<int64_t>(blockIdx.y) * RAST_NPARAM + threadIdx.x, v);
+    if (v != 0.0f) atomicAdd(job_params + static_cast<int64_t>(job) * RAST_NPARAM + threadIdx.x, v);
   }
 }
 
@@ -167,6 +173,8 @@ struct Work {
   float* vvar;          // per vertex: varyings (vstride)
   float* vacc;          // per vertex: dL/d(eye normal or colour varying) (3)
   int vstride;
+  const int2* fmap;     // face block map (kThreads faces per block)
+  const int2* vmap;     // vertex block map
 };
 
 // --------------------------------------------------------------- kernels
@@ -183,12 +191,24 @@ __global__ void __launch_bounds__(kThreads) mark_kernel(RastBatch B, Work w) {
   if (p >= 0) w.fvis[J.setup_begin + p] = 1;
 }
 
+// The per-face and per-corner kernels queue the block's visible faces (or
+// flagged corners) in shared memory first, so only they occupy lanes.
 __global__ void __launch_bounds__(kThreads) face_prep_kernel(RastBatch B, Work w) {
-  const RastJob& J = B.jobs[blockIdx.y];
-  const int64_t f = static_cast<int64_t>(blockIdx.x) * kThreads + threadIdx.x;
-  if (f >= J.n_faces) return;
+  __shared__ RastJob sJ;
+  __shared__ int s_q[kThreads];
+  __shared__ int s_n;
+  const int2 blk = w.fmap[blockIdx.x];
+  if (blk.x < 0) return;
+  const int nf = __ldg(&B.jobs[blk.x].n_faces);
+  load_job_to_shared(B.jobs + blk.x, &sJ);
+  if (threadIdx.x == 0) s_n = 0;
+  __syncthreads();
+  const RastJob& J = sJ;
+  const int f0 = blk.y + static_cast<int>(threadIdx.x);
+  const int n = block_queue(f0 < nf && w.fvis[J.setup_begin + f0], f0, s_q, &s_n);
+  if (static_cast<int>(threadIdx.x) >= n) return;
+  const int f = s_q[threadIdx.x];
   const int64_t row = J.setup_begin + f;
-  if (!w.fvis[row]) return;
   const int32_t* face = B.pools.faces + (J.face_begin + f) * 3;
   float M[9], zc[3];
 #pragma unroll
@@ -215,15 +235,25 @@ __global__ void __launch_bounds__(kThreads) face_prep_kernel(RastBatch B, Work w
 }
 
 __global__ void __launch_bounds__(kThreads) vertex_prep_kernel(RastBatch B, Work w) {
-  const RastJob& J = B.jobs[blockIdx.y];
-  const int64_t v = static_cast<int64_t>(blockIdx.x) * kThreads + threadIdx.x;
-  if (v >= J.n_verts) return;
+  __shared__ RastJob sJ;
+  __shared__ int s_q[kThreads];
+  __shared__ int s_n;
+  const int2 blk = w.vmap[blockIdx.x];
+  if (blk.x < 0) return;
+  const int nvt = __ldg(&B.jobs[blk.x].n_verts);
+  load_job_to_shared(B.jobs + blk.x, &sJ);
+  if (threadIdx.x == 0) s_n = 0;
+  __syncthreads();
+  const RastJob& J = sJ;
+  const int v0 = blk.y + static_cast<int>(threadIdx.x);
+  const int n = block_queue(v0 < nvt && w.vvis[J.vout_begin + v0], v0, s_q, &s_n);
+  if (static_cast<int>(threadIdx.x) >= n) return;
+  const int v = s_q[threadIdx.x];
   const int64_t row = J.vout_begin + v;
-  if (!w.vvis[row]) return;
   const int nv = varying_count(J.shader);
   if (nv > 0) {
     float var[kMaxVarying], clip[4];
-    vertex_shader<false>(J, B.pools, static_cast<int>(v), clip, var);
+    vertex_shader<false>(J, B.pools, v, clip, var);
 #pragma unroll
     for (int k = 0; k < kMaxVarying; ++k)
       if (k < nv) w.vvar[row * w.vstride + k] = var[k];
@@ -449,7 +479,8 @@ pixel_kernel(RastBatch B, Work w, const float* __restrict__ grad_canvas, const f
   int64_t vrows[3] = {0, 0, 0};
   TexGrad tg;
   if (p >= 0) {
-    const int i = static_cast<int>(local / J.height), j = static_cast<int>(local % J.height);
+    int i, j;
+    pixel_of(local, npx, J.height, &i, &j);
     const float x = (static_cast<float>(i) - J.viewport[3]) / J.viewport[0];
     const float y = (static_cast<float>(j) - J.viewport[7]) / J.viewport[5];
     const int64_t row = J.setup_begin + p;
@@ -512,8 +543,9 @@ pixel_kernel(RastBatch B, Work w, const float* __restrict__ grad_canvas, const f
         }
         // b = c / sum(c)
         const float s = (gb[0] * b[0] + gb[1] * b[1]) + gb[2] * b[2];
+        const float rw = __frcp_rn(wr);
 #pragma unroll
-        for (int k = 0; k < 3; ++k) gc[k] += (gb[k] - s) / wr;
+        for (int k = 0; k < 3; ++k) gc[k] += (gb[k] - s) * rw;
       }
     }
     // ---- c_k = x m[k] + y m[3+k] + m[6+k]: dL/dm, dL/dz_clip per face
@@ -531,8 +563,10 @@ pixel_kernel(RastBatch B, Work w, const float* __restrict__ grad_canvas, const f
   {
     const Seg sf = segment(frow, frow >= 0);
     float* facc = w.facc + (frow >= 0 ? frow : 0) * 12;
+    const int nf = grad_zbuffer ? 12 : 9;  // dL/dz_clip only with a depth gradient
 #pragma unroll
     for (int k = 0; k < 12; ++k) {
+      if (k >= nf) break;
       const float v = seg_sum(fval[k], sf);
       if (sf.tail && v != 0.0f) atomicAdd(facc + k, v);
     }
@@ -554,22 +588,31 @@ pixel_kernel(RastBatch B, Work w, const float* __restrict__ grad_canvas, const f
     const float v = seg_sum(tg.gs, ss);
     if (ss.tail && v != 0.0f) atomicAdd(G.specular_map + tg.sidx, v);
   }
-  reduce_params<pixel_bits(SH)>(pg, G.job_params);
+  reduce_params<pixel_bits(SH)>(pg, G.job_params, p >= 0, blockIdx.y);
 }
 
 // dL/dM = -m^T (dL/dm) m^T for the [x, y, w] rows of the clip positions,
 // then clip_k = A [p_k, 1]: dL/dA (per scene) and dL/dp_k (atomics).
 __global__ void __launch_bounds__(kThreads) face_post_kernel(RastBatch B, Work w, RastGradPools G) {
   __shared__ RastJob sJ;
-  load_job_to_shared(B.jobs + blockIdx.y, &sJ);
+  __shared__ int s_q[kThreads];
+  __shared__ int s_n;
+  const int2 blk = w.fmap[blockIdx.x];
+  if (blk.x < 0) return;
+  const int nf = __ldg(&B.jobs[blk.x].n_faces);
+  load_job_to_shared(B.jobs + blk.x, &sJ);
+  if (threadIdx.x == 0) s_n = 0;
   __syncthreads();
   const RastJob& J = sJ;
-  const int64_t f = static_cast<int64_t>(blockIdx.x) * kThreads + threadIdx.x;
+  const int f0 = blk.y + static_cast<int>(threadIdx.x);
+  const int n = block_queue(f0 < nf && w.fvis[J.setup_begin + f0], f0, s_q, &s_n);
+  const bool active = static_cast<int>(threadIdx.x) < n;
+  const int f = active ? s_q[threadIdx.x] : 0;
   ParamGrad pg;
 #pragma unroll
   for (int k = 0; k < 16; ++k) pg.v[RAST_GRAD_WORLD_TO_CLIP + k] = 0.0f;
   const int64_t row = J.setup_begin + f;
-  if (f < J.n_faces && w.fvis[row]) {
+  if (active) {
     const float4* fr = w.frec + row * 3;
     const float4 a = fr[0], bb = fr[1], cz = fr[2];
     const float m[9] = {a.x, a.y, a.z, a.w, bb.x, bb.y, bb.z, bb.w, cz.x};
@@ -609,7 +652,7 @@ __global__ void __launch_bounds__(kThreads) face_post_kernel(RastBatch B, Work w
       }
     }
   }
-  reduce_params<kClipBits>(pg, G.job_params);
+  reduce_params<kClipBits>(pg, G.job_params, active, blk.x);
 }
 
 // Reverse mode of the vertex shader: Gouraud lighting or the eye-space
@@ -617,17 +660,26 @@ __global__ void __launch_bounds__(kThreads) face_post_kernel(RastBatch B, Work w
 template <int SH>
 __global__ void __launch_bounds__(kThreads) vertex_post_kernel(RastBatch B, Work w, RastGradPools G) {
   __shared__ RastJob sJ;
-  load_job_to_shared(B.jobs + blockIdx.y, &sJ);
+  __shared__ int s_q[kThreads];
+  __shared__ int s_n;
+  const int2 blk = w.vmap[blockIdx.x];
+  if (blk.x < 0) return;
+  const int nvt = __ldg(&B.jobs[blk.x].n_verts);
+  load_job_to_shared(B.jobs + blk.x, &sJ);
+  if (threadIdx.x == 0) s_n = 0;
   __syncthreads();
   const RastJob& J = sJ;
   const RastPools& P = B.pools;
   const int sh = SH >= 0 ? SH : J.shader;
-  const int64_t v = static_cast<int64_t>(blockIdx.x) * kThreads + threadIdx.x;
+  const int v0 = blk.y + static_cast<int>(threadIdx.x);
+  const int n = block_queue(v0 < nvt && w.vvis[J.vout_begin + v0], v0, s_q, &s_n);
+  const bool active = static_cast<int>(threadIdx.x) < n && sh != RAST_SHADER_DEPTH && sh != RAST_SHADER_PHONG_DARBOUX;
+  const int v = active ? s_q[threadIdx.x] : 0;
   ParamGrad pg;
 #pragma unroll
   for (int k = 0; k < RAST_NPARAM; ++k) pg.v[k] = 0.0f;
   const int64_t row = J.vout_begin + v;
-  if (v < J.n_verts && w.vvis[row] && sh != RAST_SHADER_DEPTH && sh != RAST_SHADER_PHONG_DARBOUX) {
+  if (active) {
     const float g[3] = {w.vacc[row * 3 + 0], w.vacc[row * 3 + 1], w.vacc[row * 3 + 2]};
     const int64_t vrow = J.vert_begin + v;
     float N[3];
@@ -689,14 +741,15 @@ __global__ void __launch_bounds__(kThreads) vertex_post_kernel(RastBatch B, Work
       for (int q = 0; q < 3; ++q) atomicAdd(G.normal + vrow * 3 + q, gN[q]);
     }
   }
-  reduce_params<vertex_bits(SH)>(pg, G.job_params);
+  reduce_params<vertex_bits(SH)>(pg, G.job_params, active, blk.x);
 }
 
 // ------------------------------------------------------------------ layout
 
 struct Layout {
-  size_t fvis_off, frec_off, facc_off, vvis_off, vvar_off, vacc_off, total;
+  size_t fvis_off, frec_off, facc_off, vvis_off, vvar_off, vacc_off, fmap_off, vmap_off, total;
   int vstride;
+  unsigned fblocks, vblocks;
 };
 
 static Layout layout(const RastBatch& b) {
@@ -718,17 +771,22 @@ static Layout layout(const RastBatch& b) {
   L.vvis_off = take(V);
   L.vvar_off = take(V * vstride * sizeof(float));
   L.vacc_off = take(V * 3 * sizeof(float));
+  L.fblocks = block_map_capacity(b.total_setup, b.n_jobs, kThreads);
+  L.vblocks = block_map_capacity(b.total_vout, b.n_jobs, kThreads);
+  L.fmap_off = take(static_cast<size_t>(L.fblocks) * sizeof(int2));
+  L.vmap_off = take(static_cast<size_t>(L.vblocks) * sizeof(int2));
   L.total = off;
   return L;
 }
 
 template <int SH>
-static void launch_all(const RastBatch& b, const Work& w, const float* gc, const float* gz, const RastGradPools& G,
-                       cudaStream_t s, Profiler& prof) {
+static void launch_all(const RastBatch& b, const Work& w, const Layout& L, const float* gc, const float* gz,
+                       const RastGradPools& G, cudaStream_t s, Profiler& prof) {
   const int64_t max_px = static_cast<int64_t>(b.max_width) * b.max_height;
   const dim3 pgrid(static_cast<unsigned>((max_px + kThreads - 1) / kThreads), static_cast<unsigned>(b.n_jobs));
-  const dim3 fgrid(static_cast<unsigned>((b.max_faces + kThreads - 1) / kThreads), static_cast<unsigned>(b.n_jobs));
-  const dim3 vgrid(static_cast<unsigned>((b.max_verts + kThreads - 1) / kThreads), static_cast<unsigned>(b.n_jobs));
+  const unsigned fgrid = L.fblocks, vgrid = L.vblocks;
+  build_block_map(b, kMapFaces, kThreads, const_cast<int2*>(w.fmap), s);
+  build_block_map(b, kMapVertices, kThreads, const_cast<int2*>(w.vmap), s);
   mark_kernel<<<pgrid, kThreads, 0, s>>>(b, w);
   face_prep_kernel<<<fgrid, kThreads, 0, s>>>(b, w);
   vertex_prep_kernel<<<vgrid, kThreads, 0, s>>>(b, w);
@@ -757,23 +815,24 @@ static int run(const RastBatch* batch, const float* grad_canvas, const float* gr
   char* ws = static_cast<char*>(workspace);
   Work w{reinterpret_cast<unsigned char*>(ws + L.fvis_off), reinterpret_cast<float4*>(ws + L.frec_off),
          reinterpret_cast<float*>(ws + L.facc_off), reinterpret_cast<unsigned char*>(ws + L.vvis_off),
-         reinterpret_cast<float*>(ws + L.vvar_off), reinterpret_cast<float*>(ws + L.vacc_off), L.vstride};
+         reinterpret_cast<float*>(ws + L.vvar_off), reinterpret_cast<float*>(ws + L.vacc_off), L.vstride,
+         reinterpret_cast<const int2*>(ws + L.fmap_off), reinterpret_cast<const int2*>(ws + L.vmap_off)};
   Profiler prof(profile, s);
   if (cudaMemsetAsync(w.fvis, 0, static_cast<size_t>(b.total_setup), s) != cudaSuccess) return RAST_ERR_CUDA;
   if (cudaMemsetAsync(w.vvis, 0, static_cast<size_t>(b.total_vout), s) != cudaSuccess) return RAST_ERR_CUDA;
   const int mask = b.shader_mask;
   auto only = [&](int sh) { return mask == (1 << sh); };
-  if (only(RAST_SHADER_DEPTH)) launch_all<RAST_SHADER_DEPTH>(b, w, grad_canvas, grad_zbuffer, *grads, s, prof);
-  else if (only(RAST_SHADER_GOURAUD)) launch_all<RAST_SHADER_GOURAUD>(b, w, grad_canvas, grad_zbuffer, *grads, s, prof);
+  if (only(RAST_SHADER_DEPTH)) launch_all<RAST_SHADER_DEPTH>(b, w, L, grad_canvas, grad_zbuffer, *grads, s, prof);
+  else if (only(RAST_SHADER_GOURAUD)) launch_all<RAST_SHADER_GOURAUD>(b, w, L, grad_canvas, grad_zbuffer, *grads, s, prof);
   else if (only(RAST_SHADER_GOURAUD_TEXTURE))
-    launch_all<RAST_SHADER_GOURAUD_TEXTURE>(b, w, grad_canvas, grad_zbuffer, *grads, s, prof);
-  else if (only(RAST_SHADER_PHONG)) launch_all<RAST_SHADER_PHONG>(b, w, grad_canvas, grad_zbuffer, *grads, s, prof);
+    launch_all<RAST_SHADER_GOURAUD_TEXTURE>(b, w, L, grad_canvas, grad_zbuffer, *grads, s, prof);
+  else if (only(RAST_SHADER_PHONG)) launch_all<RAST_SHADER_PHONG>(b, w, L, grad_canvas, grad_zbuffer, *grads, s, prof);
   else if (only(RAST_SHADER_PHONG_REFLECTION))
-    launch_all<RAST_SHADER_PHONG_REFLECTION>(b, w, grad_canvas, grad_zbuffer, *grads, s, prof);
+    launch_all<RAST_SHADER_PHONG_REFLECTION>(b, w, L, grad_canvas, grad_zbuffer, *grads, s, prof);
   else if (only(RAST_SHADER_PHONG_REFLECTION_SHADOW))
-    launch_all<RAST_SHADER_PHONG_REFLECTION_SHADOW>(b, w, grad_canvas, grad_zbuffer, *grads, s, prof);
+    launch_all<RAST_SHADER_PHONG_REFLECTION_SHADOW>(b, w, L, grad_canvas, grad_zbuffer, *grads, s, prof);
   else
-    launch_all<-1>(b, w, grad_canvas, grad_zbuffer, *grads, s, prof);
+    launch_all<-1>(b, w, L, grad_canvas, grad_zbuffer, *grads, s, prof);
   if (cudaGetLastError() != cudaSuccess) return RAST_ERR_CUDA;
   return prof.finish();
 }

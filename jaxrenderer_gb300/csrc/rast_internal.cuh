@@ -94,6 +94,89 @@ __device__ __forceinline__ void count_near_tie(unsigned long long* counter, bool
     atomicAdd(counter, static_cast<unsigned long long>(__popc(m)));
 }
 
+__device__ __forceinline__ unsigned lanemask_lt() { return (1u << (threadIdx.x & 31)) - 1u; }
+
+// Block-wide compaction: every thread offers `idx` when `flag`; the flagged
+// indices land in s_q (order unspecified) and the count is returned.  *s_n
+// must be zero and visible to the block on entry; every thread must call.
+__device__ __forceinline__ int block_queue(bool flag, int idx, int* s_q, int* s_n) {
+  const unsigned m = __ballot_sync(0xffffffffu, flag);
+  int base = 0;
+  if ((threadIdx.x & 31) == 0 && m) base = atomicAdd(s_n, __popc(m));
+  base = __shfl_sync(0xffffffffu, base, 0);
+  if (flag) s_q[base + __popc(m & lanemask_lt())] = idx;
+  __syncthreads();
+  return *s_n;
+}
+
+// ---- block maps: grids over the faces (or vertices) of every job with no
+// empty blocks.  Entry b of the map is (job, first item of the block) for
+// the b-th block of the concatenated per-job block ranges, (-1, 0) past the
+// end.  A batch needs at most floor(total / per_block) + n_jobs blocks.
+constexpr int kMapFaces = 0, kMapVertices = 1;
+
+__host__ __device__ inline unsigned block_map_capacity(int64_t total, int n_jobs, int per_block) {
+  return static_cast<unsigned>(total / per_block + n_jobs);
+}
+
+// One block of 1024 threads; thread t owns a contiguous run of jobs.
+template <int kField>
+__global__ void __launch_bounds__(1024)
+block_map_kernel(const RastJob* __restrict__ jobs, int n_jobs, int per_block, int2* __restrict__ map,
+                 unsigned capacity) {
+  __shared__ unsigned s_sum[1024];
+  const int t = threadIdx.x;
+  const int per_thread = (n_jobs + 1023) / 1024;
+  const int j0 = min(n_jobs, t * per_thread), j1 = min(n_jobs, j0 + per_thread);
+  auto blocks_of = [&](int j) {
+    const int n = kField == kMapFaces ? __ldg(&jobs[j].n_faces) : __ldg(&jobs[j].n_verts);
+    return n > 0 ? static_cast<unsigned>((n + per_block - 1) / per_block) : 0u;
+  };
+  unsigned mine = 0;
+  for (int j = j0; j < j1; ++j) mine += blocks_of(j);
+  s_sum[t] = mine;
+  __syncthreads();
+  for (int off = 1; off < 1024; off <<= 1) {
+    const unsigned add = t >= off ? s_sum[t - off] : 0u;
+    __syncthreads();
+    s_sum[t] += add;
+    __syncthreads();
+  }
+  unsigned at = s_sum[t] - mine;
+  for (int j = j0; j < j1; ++j) {
+    const unsigned nb = blocks_of(j);
+    for (unsigned b = 0; b < nb && at + b < capacity; ++b)
+      map[at + b] = make_int2(j, static_cast<int>(b) * per_block);
+    at += nb;
+  }
+  for (unsigned k = s_sum[1023] + t; k < capacity; k += 1024) map[k] = make_int2(-1, 0);
+}
+
+// Builds the map of `field` for batch b on stream s.
+inline cudaError_t build_block_map(const RastBatch& b, int field, int per_block, int2* map, cudaStream_t s) {
+  const int64_t total = field == kMapFaces ? b.total_setup : b.total_vout;
+  const unsigned cap = block_map_capacity(total, b.n_jobs, per_block);
+  if (cap == 0) return cudaSuccess;
+  if (field == kMapFaces)
+    block_map_kernel<kMapFaces><<<1, 1024, 0, s>>>(b.jobs, b.n_jobs, per_block, map, cap);
+  else
+    block_map_kernel<kMapVertices><<<1, 1024, 0, s>>>(b.jobs, b.n_jobs, per_block, map, cap);
+  return cudaGetLastError();
+}
+
+// Pixel (i, j) of a job from its x-major local index i * H + j; 32-bit
+// division when the job's pixel count fits (every job in practice).
+__device__ __forceinline__ void pixel_of(int64_t local, int64_t npx, int H, int* i, int* j) {
+  if (npx <= 0x7fffffff) {
+    const int l = static_cast<int>(local);
+    *i = l / H;
+    *j = l - *i * H;
+  } else {
+    *i = static_cast<int>(local / H);
+    *j = static_cast<int>(local - static_cast<int64_t>(*i) * H);
+  }
+}
+
 __device__ __forceinline__ void load_job_to_shared(const RastJob* job, RastJob* dst) {
   const int nthreads = blockDim.x * blockDim.y;
   const int tid = threadIdx.y * blockDim.x + threadIdx.x;

@@ -246,30 +246,29 @@ __device__ __forceinline__ void warp_tiles(int tx0, int ty0, int tx1, int ty1, i
   }
 }
 
-__device__ __forceinline__ unsigned lanemask_lt() { return (1u << (threadIdx.x & 31)) - 1u; }
-
 // Phase 1, one thread per face: clip positions, determinant, keep/front
 // flags and inverse -> setup record.  Candidates (kept, front-facing) are
 // queued in shared memory; phase 2, one thread per queued candidate:
 // conservative coverage rectangle -> bbox, then the warp adds the tile counts
 // with one atomic per distinct tile per round (lanes hitting the same tile
 // are merged with __match_any_sync).
-// Grid: (ceil(max_faces / kSetupThreads), n_jobs); blockIdx.y is the job.
+// Grid: one block per kSetupThreads faces of a job (face block map).
 __global__ void __launch_bounds__(kSetupThreads)
-setup_bin_kernel(RastBatch B, Geometry G, float4* __restrict__ setup, ushort4* __restrict__ bbox,
-                 uint32_t* __restrict__ counts) {
+setup_bin_kernel(RastBatch B, Geometry G, const int2* __restrict__ fmap, float4* __restrict__ setup,
+                 ushort4* __restrict__ bbox, uint32_t* __restrict__ counts) {
   __shared__ RastJob sJ;
   __shared__ float s_inv[9][kSetupThreads];
   __shared__ int s_face[kSetupThreads];
   __shared__ int s_qn;
-  const int jid = blockIdx.y;
+  const int2 blk = fmap[blockIdx.x];
+  if (blk.x < 0) return;
+  const int jid = blk.x;
   const int nf = __ldg(&B.jobs[jid].n_faces);
-  if (static_cast<int64_t>(blockIdx.x) * kSetupThreads >= nf) return;
   load_job_to_shared(B.jobs + jid, &sJ);
   if (threadIdx.x == 0) s_qn = 0;
   __syncthreads();
   const RastJob& J = sJ;
-  const int f = static_cast<int>(blockIdx.x) * kSetupThreads + static_cast<int>(threadIdx.x);
+  const int f = blk.y + static_cast<int>(threadIdx.x);
   bool cand = false;
   float inv[9];
   if (f < nf) {
@@ -404,14 +403,16 @@ scan_apply_kernel(const uint32_t* __restrict__ counts, uint32_t* __restrict__ of
 // Face ids into the bins of the tiles their rectangles cover, one warp per
 // 32 faces with the (face, tile) pairs spread over its lanes; lanes writing
 // to the same tile take their slots with one atomic (__match_any_sync).
-// Grid: (ceil(max_faces / kSetupThreads), n_jobs).
+// Grid: one block per kSetupThreads faces of a job (face block map).
 __global__ void __launch_bounds__(kSetupThreads)
-scatter_kernel(RastBatch B, Geometry G, const ushort4* __restrict__ bbox,
+scatter_kernel(RastBatch B, Geometry G, const int2* __restrict__ fmap, const ushort4* __restrict__ bbox,
                const uint32_t* __restrict__ offsets, uint32_t* __restrict__ cursors,
                int32_t* __restrict__ bins) {
-  const int jid = blockIdx.y;
+  const int2 blk = fmap[blockIdx.x];
+  if (blk.x < 0) return;
+  const int jid = blk.x;
   const int nf = __ldg(&B.jobs[jid].n_faces);
-  const int f = static_cast<int>(blockIdx.x) * kSetupThreads + static_cast<int>(threadIdx.x);
+  const int f = blk.y + static_cast<int>(threadIdx.x);
   if (f - static_cast<int>(threadIdx.x & 31) >= nf) return;  // the whole warp is past the faces
   ushort4 bb = make_ushort4(1, 1, 0, 0);
   if (f < nf) bb = bbox[__ldg(&B.jobs[jid].setup_begin) + f];
@@ -584,26 +585,40 @@ raster_kernel(RastBatch B, Geometry G, const float4* __restrict__ setup,
 
 // Vertex varyings of the three corners of every face some pixel needs
 // (marked by the raster kernel), stored per face: the shade then reads them
-// instead of re-running the vertex shader per pixel.
-// Grid: (ceil(max_faces / 128), n_jobs).
-__global__ void __launch_bounds__(128)
-face_varyings_kernel(RastBatch B, const unsigned char* __restrict__ visible, float* __restrict__ fvar,
-                     int vstride) {
-  const int jid = blockIdx.y;
-  const RastJob& J = B.jobs[jid];
-  const int64_t f0 = static_cast<int64_t>(blockIdx.x) * 128 + threadIdx.x;
-  if (f0 >= __ldg(&J.n_faces)) return;
-  const int64_t row = __ldg(&J.setup_begin) + f0;
-  if (!visible[row]) return;
-  if (J.shader == RAST_SHADER_DEPTH) return;
-  const int32_t* face = B.pools.faces + (J.face_begin + f0) * 3;
+// instead of re-running the vertex shader per pixel.  The block queues its
+// visible faces in shared memory, then one thread per (visible face, corner)
+// runs the vertex shader, so faces nobody sees leave no idle lanes.
+// Grid: one block per kFaceThreads faces of a job (face block map).
+constexpr int kFaceThreads = kSetupThreads;
+
+__global__ void __launch_bounds__(kFaceThreads)
+face_varyings_kernel(RastBatch B, const int2* __restrict__ fmap, const unsigned char* __restrict__ visible,
+                     float* __restrict__ fvar, int vstride) {
+  __shared__ RastJob sJ;
+  __shared__ int s_face[kFaceThreads];
+  __shared__ int s_n;
+  const int2 blk = fmap[blockIdx.x];
+  if (blk.x < 0) return;
+  const int jid = blk.x;
+  const int nf = __ldg(&B.jobs[jid].n_faces);
+  if (__ldg(&B.jobs[jid].shader) == RAST_SHADER_DEPTH) return;
+  load_job_to_shared(B.jobs + jid, &sJ);
+  if (threadIdx.x == 0) s_n = 0;
+  __syncthreads();
+  const RastJob& J = sJ;
+  const int f = blk.y + static_cast<int>(threadIdx.x);
+  const int pairs = 3 * block_queue(f < nf && visible[J.setup_begin + f], f, s_face, &s_n);
   const int nv = varying_count(J.shader);
-  float* out = fvar + row * 3 * vstride;
-#pragma unroll 1
-  for (int k = 0; k < 3; ++k) {
+  for (int t = threadIdx.x; t < pairs; t += kFaceThreads) {
+    const int q = t / 3, k = t - 3 * q;
+    const int fq = s_face[q];
+    const int32_t* face = B.pools.faces + (J.face_begin + fq) * 3;
     float var[kMaxVarying], clip[4];
     vertex_shader<false>(J, B.pools, gather_clamp(__ldg(face + k), J.n_verts), clip, var);
-    for (int q = 0; q < nv; ++q) out[k * vstride + q] = var[q];
+    float* out = fvar + ((J.setup_begin + fq) * 3 + k) * vstride;
+#pragma unroll
+    for (int v = 0; v < kMaxVarying; ++v)
+      if (v < nv) out[v] = var[v];
   }
 }
 
@@ -624,8 +639,8 @@ tiled_shade_kernel(RastBatch B, const float4* __restrict__ setup, const int32_t*
   const int64_t local0 = static_cast<int64_t>(blockIdx.x) * 256 + threadIdx.x;
   if (local0 >= npx) return;
   const int64_t pix = J.pixel_begin + local0;
-  const int64_t local = pix - J.pixel_begin;
-  const int i = static_cast<int>(local / J.height), j = static_cast<int>(local % J.height);
+  int i, j;
+  pixel_of(local0, npx, J.height, &i, &j);
   PixelResult r;
   VaryingSource src{nullptr, vstride, 0, fvar, J.setup_begin};
   resolve_pixel(J, B.pools, setup + J.setup_begin * 4, i, j, winner[pix], src, &r);
@@ -643,7 +658,8 @@ inline uint64_t default_bin_capacity(const RastBatch& b) {
 
 struct Layout {
   size_t setup_off, bbox_off, counts_off, offsets_off, cursors_off, bsums_off, bins_off, winner_off,
-      vis_off, fvar_off, misc_off, total;
+      vis_off, fvar_off, fmap_off, misc_off, total;
+  unsigned fmap_blocks;
   int vstride;
   int64_t n_tiles, n_scan_blocks;
   uint64_t bin_capacity;
@@ -681,6 +697,8 @@ static Layout layout(const RastBatch& b, TileShape ts, uint64_t bin_capacity) {
   const bool shading = vstride > 0;
   L.vis_off = take(shading ? static_cast<size_t>(b.total_setup) : 0);
   L.fvar_off = take(shading ? static_cast<size_t>(b.total_setup) * 3 * vstride * sizeof(float) : 0);
+  L.fmap_blocks = block_map_capacity(b.total_setup, b.n_jobs, kSetupThreads);
+  L.fmap_off = take(static_cast<size_t>(L.fmap_blocks) * sizeof(int2));
   L.misc_off = take(256);
   L.total = off;
   return L;
@@ -725,16 +743,18 @@ static int render(const RastBatch* batch, const RastTiledConfig* cfg, void* work
   if (vis && b.total_setup > 0 && cudaMemsetAsync(vis, 0, static_cast<size_t>(b.total_setup), s) != cudaSuccess)
     return RAST_ERR_CUDA;
   prof.mark("memset");
+  int2* fmap = reinterpret_cast<int2*>(ws + L.fmap_off);
   if (b.total_setup > 0) {
-    const dim3 grid(static_cast<unsigned>((b.max_faces + kSetupThreads - 1) / kSetupThreads),
-                    static_cast<unsigned>(b.n_jobs));
-    setup_bin_kernel<<<grid, kSetupThreads, 0, s>>>(b, L.G, setup, bbox, counts);
+    if (build_block_map(b, kMapFaces, kSetupThreads, fmap, s) != cudaSuccess) return RAST_ERR_CUDA;
+    prof.mark("block_map_kernel");
+    const unsigned grid = L.fmap_blocks;
+    setup_bin_kernel<<<grid, kSetupThreads, 0, s>>>(b, L.G, fmap, setup, bbox, counts);
     prof.mark("setup_bin_kernel");
     scan_local_kernel<<<static_cast<unsigned>(L.n_scan_blocks), 256, 0, s>>>(counts, offsets, bsums, L.n_tiles);
     scan_apply_kernel<<<static_cast<unsigned>(L.n_scan_blocks), 256, 0, s>>>(counts, offsets, bsums, L.n_tiles,
                                                                               L.bin_capacity, misc + 1);
     prof.mark("scan_kernels");
-    scatter_kernel<<<grid, kSetupThreads, 0, s>>>(b, L.G, bbox, offsets, cursors, bins);
+    scatter_kernel<<<grid, kSetupThreads, 0, s>>>(b, L.G, fmap, bbox, offsets, cursors, bins);
     prof.mark("scatter_kernel");
   }
   if (b.total_pixels > 0) {
@@ -763,8 +783,7 @@ static int render(const RastBatch* batch, const RastTiledConfig* cfg, void* work
     if (b.shader_mask != (1 << RAST_SHADER_DEPTH) || b.total_setup == 0) {
       const bool pre = fvar != nullptr && b.total_setup > 0;
       if (pre) {
-        const dim3 fgrid(static_cast<unsigned>((b.max_faces + 127) / 128), static_cast<unsigned>(b.n_jobs));
-        face_varyings_kernel<<<fgrid, 128, 0, s>>>(b, vis, fvar, L.vstride);
+        face_varyings_kernel<<<L.fmap_blocks, kFaceThreads, 0, s>>>(b, fmap, vis, fvar, L.vstride);
         prof.mark("face_varyings_kernel");
       }
       tiled_shade_kernel<<<sgrid, 256, 0, s>>>(b, setup, winner, b.total_setup > 0, pre ? fvar : nullptr,
