@@ -96,6 +96,8 @@ class Workload:
     oracle_crop: int = 1  # the oracle renders width // oracle_crop columns of a frame
     config: dict = field(default_factory=dict)
     phong: Optional[dict] = None
+    merges: list = field(default_factory=list)  # instancing.DeviceMerge per group (instanced workloads)
+    instances: object = None  # instancing.InstancedScenes
 
 
 def _pass_work(spec) -> float:
@@ -107,14 +109,22 @@ def build_brax84(n, rank, dev):
 
     W = H = 84
     shadow = (128, 128)
-    flat = synthetic.brax_like_batch(n, seed=synthetic.BASE_SEED + 1 + rank)
-    tables = jb.scene_batch_tables(flat, W, H, shadow_size=shadow)
-    work = flat.n_faces.astype(np.float64) * (W * H + shadow[0] * shadow[1])
-    groups = [jb.scene_batch_from_flat(flat, W, H, shadow_size=shadow, device=dev)] if dev is not None else []
+    inst = synthetic.brax_like_instances(n, seed=synthetic.BASE_SEED + 1 + rank)
+    n_faces = inst.n_faces
+    work = n_faces.astype(np.float64) * (W * H + shadow[0] * shadow[1])
+
+    def chain(k):  # the host reference path for one scene: merge_objects + flatten_corners
+        sub = inst.host_flat([k % n])
+        return jb.scene_job_specs(sub, jb.scene_batch_tables(sub, W, H, shadow_size=shadow), 0)
+
+    groups, merges = [], []
+    if dev is not None:
+        sb, merge = jb.scene_batch_from_instances(inst, W, H, shadow_size=shadow, device=dev)
+        groups, merges = [sb], [merge]
     return Workload("brax84", "brax-like 84x84 x 4096 scenes, phong_reflection_shadow + 128x128 depth pass", n,
-                    lambda k: jb.scene_job_specs(flat, tables, k % n), work, groups,
-                    config={"scenes": n, "mean_faces_per_scene": float(flat.n_faces.mean()),
-                            "resolution": [W, H], "shadow_map": list(shadow)})
+                    chain, work, groups, merges=merges, instances=inst,
+                    config={"scenes": n, "mean_faces_per_scene": float(n_faces.mean()),
+                            "objects": int(inst.n_instances), "resolution": [W, H], "shadow_map": list(shadow)})
 
 
 def build_cube640(n, rank, dev):
@@ -764,28 +774,40 @@ def roofline(prof, visible):
 
 
 def measure_e2e(wl: Workload, mr, step, args, dev, stream, world):
-    """Public-API path with host inputs: pinned host pools -> device, render,
-    canvases -> pinned host, all inside the timed region."""
+    """Public-API path with host inputs, all inside the timed region:
+    instanced workloads copy the objects' transforms and scalings (pinned
+    host -> device), rebuild the per-corner pools with rast_merge_objects and
+    render; the others copy every per-corner input pool and render; then
+    the canvases go to pinned host memory."""
     import torch
 
     host, outs = [], []
     h2d = d2h = 0
+    if wl.merges:
+        inst = wl.instances
+        tr = torch.from_numpy(np.ascontiguousarray(inst.transforms)).pin_memory()
+        sc = torch.from_numpy(np.ascontiguousarray(inst.local_scaling)).pin_memory()
+        h2d = tr.numel() * 4 + sc.numel() * 4
+    else:
+        for r in mr.runners:
+            hp = {}
+            for n in INPUT_POOLS:
+                if n not in r.sb.pools:
+                    continue
+                t = r.sb.pools[n]
+                h = torch.empty(t.shape, dtype=t.dtype, pin_memory=True)
+                h.copy_(t)
+                hp[n] = h
+                h2d += h.numel() * h.element_size()
+            host.append(hp)
     for r in mr.runners:
-        hp = {}
-        for n in INPUT_POOLS:
-            if n not in r.sb.pools:
-                continue
-            t = r.sb.pools[n]
-            h = torch.empty(t.shape, dtype=t.dtype, pin_memory=True)
-            h.copy_(t)
-            hp[n] = h
-            h2d += h.numel() * h.element_size()
-        host.append(hp)
         oh = torch.empty(r.canvas.shape, dtype=torch.float32, pin_memory=True)
         outs.append(oh)
         d2h += oh.numel() * 4
 
     def e2e_step():
+        if wl.merges:
+            wl.merges[0].merge(tr, sc, stream)
         for r, hp in zip(mr.runners, host):
             for n, h in hp.items():
                 r.sb.pools[n].copy_(h, non_blocking=True)
@@ -803,8 +825,19 @@ def measure_e2e(wl: Workload, mr, step, args, dev, stream, world):
     stop.record(stream)
     torch.cuda.synchronize(dev)
     ms = start.elapsed_time(stop) / steps
-    return {"value": world * wl.frames / (ms / 1e3), "unit": UNIT, "ms_per_step": ms,
-            "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h), "steps": steps}
+    out = {"value": world * wl.frames / (ms / 1e3), "unit": UNIT, "ms_per_step": ms,
+           "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h), "steps": steps,
+           "inputs": ("object transforms + local scalings; per-corner pools rebuilt on the device "
+                      "(rast_merge_objects)") if wl.merges else "per-corner input pools"}
+    if wl.merges:
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(steps):
+            wl.merges[0].merge(stream=stream)
+        b.record(stream)
+        torch.cuda.synchronize(dev)
+        out["device_merge_ms"] = a.elapsed_time(b) / steps
+    return out
 
 
 # ------------------------------------------------------------- reference arm

@@ -281,6 +281,84 @@ int rast_backward_profiled(const RastBatch* batch, const float* grad_canvas, con
                            const RastGradPools* grads, void* workspace, size_t workspace_bytes, void* stream,
                            RastProfile* profile);
 
+/* ---------------------------------------------------------------------
+ * Device-side merge_objects + per-corner flattening (instanced scenes).
+ *
+ * Replaces the host work the reference does per frame before rendering:
+ * renderer/model.py:447-555 merge_objects (object vertices scaled and
+ * transformed with apply_pos, normals with apply_vec by the inverse
+ * transpose of the transform, faces offset into the merged arrays) and
+ * renderer/renderer.py:277-295 (positions, normals, uvs and texture indices
+ * gathered per face corner).  Meshes are uploaded once; per frame only the
+ * objects' transforms and local scalings change.  No counterpart entry point
+ * exists in the reference (it merges on the host inside the traced call).
+ *
+ * Scenes are contiguous runs of instances; an instance's rows in its
+ * scene's merged vertex / normal / uv arrays start at vert_offset /
+ * norm_offset / uv_offset (the sums over the scene's earlier instances),
+ * and its 3 * n_faces output corners at corner_begin.  Gathers follow the
+ * reference's: indices wrap once if negative, then clamp to the scene's
+ * merged array.  Global vector norms (normalise over a whole normal array)
+ * are summed sequentially in index order.
+ * --------------------------------------------------------------------- */
+typedef struct RastMesh {
+  int64_t vert_begin;    /* rows into mesh_verts */
+  int64_t norm_begin;    /* rows into mesh_norms */
+  int64_t uv_begin;      /* rows into mesh_uvs */
+  int64_t face_begin;    /* rows into mesh_faces / mesh_faces_norm / mesh_faces_uv */
+  int32_t n_verts, n_norms, n_uvs, n_faces;
+} RastMesh;
+
+typedef struct RastInstance {
+  int32_t mesh;          /* index into the mesh table */
+  int32_t scene_first;   /* first instance of this instance's scene */
+  int32_t scene_count;   /* instances in the scene */
+  int32_t vert_offset;   /* merged-row offsets of this instance in its scene */
+  int32_t norm_offset;
+  int32_t uv_offset;
+  int32_t scene_verts;   /* merged-row totals of the scene */
+  int32_t scene_norms;
+  int32_t scene_uvs;
+  int32_t reserved;
+  int64_t corner_begin;  /* first output corner row */
+  int64_t vert_row;      /* first row of this instance in the batch's merged */
+  int64_t norm_row;      /* vertex / normal / uv arrays (all scenes back to back) */
+  int64_t uv_row;
+} RastInstance;
+
+typedef struct RastMergeBatch {
+  const RastMesh* meshes;          /* device, n_meshes */
+  int32_t n_meshes;
+  int32_t n_instances;
+  const RastInstance* instances;   /* device, n_instances */
+  const float* transforms;         /* device (n_instances, 16): ModelObject.transform, row-major */
+  const float* local_scaling;      /* device (n_instances, 3) */
+  const float* mesh_verts;         /* (rows, 3) */
+  const float* mesh_norms;         /* (rows, 3) */
+  const float* mesh_uvs;           /* (rows, 2) */
+  const int32_t* mesh_faces;       /* (rows, 3) each, local to the mesh */
+  const int32_t* mesh_faces_norm;
+  const int32_t* mesh_faces_uv;
+  int64_t total_faces;             /* sums over instances of their mesh's n_faces, */
+  int64_t total_verts;             /* n_verts, n_norms and n_uvs (workspace sizing) */
+  int64_t total_norms;
+  int64_t total_uvs;
+  float* position;                 /* out (corners, 3) */
+  float* normal;                   /* out (corners, 3), may be NULL */
+  float* uv;                       /* out (corners, 2), may be NULL */
+  int32_t* texture_index;          /* out (corners), may be NULL */
+} RastMergeBatch;
+
+/* Workspace rast_merge_objects needs (256-byte aligned base): the merged
+ * per-scene vertex, normal and uv arrays of the whole batch (36 bytes per
+ * merged vertex + normal + uv row) plus per-instance bookkeeping. */
+size_t rast_merge_workspace_bytes(const RastMergeBatch* batch);
+
+/* Merge every scene's instances and write the per-corner pools the render
+ * entry points read (vert_begin of a scene's job = the corner_begin of its
+ * first instance, faces = 3 * arange).  Stream-ordered, graph-capturable. */
+int rast_merge_objects(const RastMergeBatch* batch, void* workspace, size_t workspace_bytes, void* stream);
+
 /* Host-side validation of one job against pool sizes (no device access):
  * returns RAST_ERR_INVALID_ARGUMENT for inconsistent sizes. */
 int rast_validate_job(const RastJob* job);

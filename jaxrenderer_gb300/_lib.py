@@ -156,6 +156,29 @@ class RastGradPools(ctypes.Structure):
 
 
 # Exported symbols and their prototypes: (name, restype, argtypes).
+class RastMesh(ctypes.Structure):
+    _fields_ = [("vert_begin", c_int64), ("norm_begin", c_int64), ("uv_begin", c_int64), ("face_begin", c_int64),
+                ("n_verts", c_int32), ("n_norms", c_int32), ("n_uvs", c_int32), ("n_faces", c_int32)]
+
+
+class RastInstance(ctypes.Structure):
+    _fields_ = [("mesh", c_int32), ("scene_first", c_int32), ("scene_count", c_int32),
+                ("vert_offset", c_int32), ("norm_offset", c_int32), ("uv_offset", c_int32),
+                ("scene_verts", c_int32), ("scene_norms", c_int32), ("scene_uvs", c_int32),
+                ("reserved", c_int32), ("corner_begin", c_int64), ("vert_row", c_int64), ("norm_row", c_int64),
+                ("uv_row", c_int64)]
+
+
+class RastMergeBatch(ctypes.Structure):
+    _fields_ = [("meshes", c_void_p), ("n_meshes", c_int32), ("n_instances", c_int32), ("instances", c_void_p),
+                ("transforms", c_void_p), ("local_scaling", c_void_p), ("mesh_verts", c_void_p),
+                ("mesh_norms", c_void_p), ("mesh_uvs", c_void_p), ("mesh_faces", c_void_p),
+                ("mesh_faces_norm", c_void_p), ("mesh_faces_uv", c_void_p), ("total_faces", c_int64),
+                ("total_verts", c_int64), ("total_norms", c_int64), ("total_uvs", c_int64),
+                ("position", c_void_p), ("normal", c_void_p),
+                ("uv", c_void_p), ("texture_index", c_void_p)]
+
+
 PROTOTYPES = [
     ("rast_plain_workspace_bytes", c_size_t, [POINTER(RastBatch)]),
     ("rast_render_plain", c_int, [POINTER(RastBatch), c_void_p, c_size_t, c_void_p]),
@@ -173,6 +196,8 @@ PROTOTYPES = [
     ("rast_backward_profiled", c_int,
      [POINTER(RastBatch), c_void_p, c_void_p, POINTER(RastGradPools), c_void_p, c_size_t, c_void_p,
       POINTER(RastProfile)]),
+    ("rast_merge_workspace_bytes", c_size_t, [POINTER(RastMergeBatch)]),
+    ("rast_merge_objects", c_int, [POINTER(RastMergeBatch), c_void_p, c_size_t, c_void_p]),
     ("rast_validate_job", c_int, [POINTER(RastJob)]),
     ("rast_error_string", ctypes.c_char_p, [c_int]),
     ("rast_abi_version", c_int, []),

@@ -211,6 +211,29 @@ def scene_batch_from_flat(flat, width: int = 84, height: int = 84,
                       t.main_jobs, t.shadow_jobs, device, flat.n_faces, t.shadow_index)
 
 
+def scene_batch_from_instances(inst, width: int = 84, height: int = 84,
+                               light: LightParameters = LightParameters(),
+                               shadow_param: Optional[ShadowParameters] = ShadowParameters(),
+                               shadow_size=(128, 128), device=None,
+                               camera_params: Optional[CameraParameters] = None,
+                               shadow_mask: Optional[np.ndarray] = None):
+    """A SceneBatch of an instancing.InstancedScenes batch whose per-corner
+    pools are built on the device; returns (SceneBatch, DeviceMerge) after
+    one merge.  Later frames: `merge.merge(transforms, local_scaling)` then
+    render again."""
+    from .instancing import DeviceMerge, instanced_pools
+
+    device = device if device is not None else torch.device("cuda", torch.cuda.current_device())
+    shell = inst.shell()
+    t = scene_batch_tables(shell, width, height, light, shadow_param, shadow_size, camera_params, shadow_mask)
+    pools = instanced_pools(inst, device)
+    merge = DeviceMerge(inst, pools, device)
+    merge.merge()
+    sb = SceneBatch(inst.n_scenes, width, height, t.shadow_width, t.shadow_height, pools, t.main_jobs,
+                    t.shadow_jobs, device, shell.n_faces, t.shadow_index)
+    return sb, merge
+
+
 def scene_batch_from_specs(specs, device=None) -> SceneBatch:
     """A SceneBatch of N independent single-pass jobs (same size and shader,
     no shadow pass) from JobSpecs, e.g. N differentiable scenes."""
@@ -563,5 +586,5 @@ def render_batch(sb: SceneBatch, form: str = "plain", want_prim_id: bool = True)
 
 
 __all__ = ["SceneBatch", "SceneTables", "scene_batch_tables", "scene_batch_from_flat", "scene_batch_from_specs",
-           "scene_job_specs", "MultiRunner", "mixed_scene_batches",
+           "scene_job_specs", "MultiRunner", "mixed_scene_batches", "scene_batch_from_instances",
            "flat_pools", "render_batch", "BatchRunner", "BatchOutputs", "job_table"]

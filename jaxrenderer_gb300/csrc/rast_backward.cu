@@ -175,6 +175,7 @@ struct Work {
   int vstride;
   const int2* fmap;     // face block map (kThreads faces per block)
   const int2* vmap;     // vertex block map
+  unsigned* starts;     // per-job block starts of both maps (2 x (n_jobs + 1))
 };
 
 // --------------------------------------------------------------- kernels
@@ -747,7 +748,7 @@ __global__ void __launch_bounds__(kThreads) vertex_post_kernel(RastBatch B, Work
 // ------------------------------------------------------------------ layout
 
 struct Layout {
-  size_t fvis_off, frec_off, facc_off, vvis_off, vvar_off, vacc_off, fmap_off, vmap_off, total;
+  size_t fvis_off, frec_off, facc_off, vvis_off, vvar_off, vacc_off, fmap_off, vmap_off, start_off, total;
   int vstride;
   unsigned fblocks, vblocks;
 };
@@ -775,6 +776,7 @@ static Layout layout(const RastBatch& b) {
   L.vblocks = block_map_capacity(b.total_vout, b.n_jobs, kThreads);
   L.fmap_off = take(static_cast<size_t>(L.fblocks) * sizeof(int2));
   L.vmap_off = take(static_cast<size_t>(L.vblocks) * sizeof(int2));
+  L.start_off = take(2 * block_start_bytes(b.n_jobs));
   L.total = off;
   return L;
 }
@@ -785,8 +787,8 @@ static void launch_all(const RastBatch& b, const Work& w, const Layout& L, const
   const int64_t max_px = static_cast<int64_t>(b.max_width) * b.max_height;
   const dim3 pgrid(static_cast<unsigned>((max_px + kThreads - 1) / kThreads), static_cast<unsigned>(b.n_jobs));
   const unsigned fgrid = L.fblocks, vgrid = L.vblocks;
-  build_block_map(b, kMapFaces, kThreads, const_cast<int2*>(w.fmap), s);
-  build_block_map(b, kMapVertices, kThreads, const_cast<int2*>(w.vmap), s);
+  build_block_map(b, kMapFaces, kThreads, const_cast<int2*>(w.fmap), w.starts, s);
+  build_block_map(b, kMapVertices, kThreads, const_cast<int2*>(w.vmap), w.starts + b.n_jobs + 1, s);
   mark_kernel<<<pgrid, kThreads, 0, s>>>(b, w);
   face_prep_kernel<<<fgrid, kThreads, 0, s>>>(b, w);
   vertex_prep_kernel<<<vgrid, kThreads, 0, s>>>(b, w);
@@ -816,7 +818,8 @@ static int run(const RastBatch* batch, const float* grad_canvas, const float* gr
   Work w{reinterpret_cast<unsigned char*>(ws + L.fvis_off), reinterpret_cast<float4*>(ws + L.frec_off),
          reinterpret_cast<float*>(ws + L.facc_off), reinterpret_cast<unsigned char*>(ws + L.vvis_off),
          reinterpret_cast<float*>(ws + L.vvar_off), reinterpret_cast<float*>(ws + L.vacc_off), L.vstride,
-         reinterpret_cast<const int2*>(ws + L.fmap_off), reinterpret_cast<const int2*>(ws + L.vmap_off)};
+         reinterpret_cast<const int2*>(ws + L.fmap_off), reinterpret_cast<const int2*>(ws + L.vmap_off),
+         reinterpret_cast<unsigned*>(ws + L.start_off)};
   Profiler prof(profile, s);
   if (cudaMemsetAsync(w.fvis, 0, static_cast<size_t>(b.total_setup), s) != cudaSuccess) return RAST_ERR_CUDA;
   if (cudaMemsetAsync(w.vvis, 0, static_cast<size_t>(b.total_vout), s) != cudaSuccess) return RAST_ERR_CUDA;

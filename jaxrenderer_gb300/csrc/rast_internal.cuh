@@ -119,21 +119,23 @@ __host__ __device__ inline unsigned block_map_capacity(int64_t total, int n_jobs
   return static_cast<unsigned>(total / per_block + n_jobs);
 }
 
-// One block of 1024 threads; thread t owns a contiguous run of jobs.
+template <int kField>
+__device__ __forceinline__ unsigned blocks_of_job(const RastJob* jobs, int j, int per_block) {
+  const int n = kField == kMapFaces ? __ldg(&jobs[j].n_faces) : __ldg(&jobs[j].n_verts);
+  return n > 0 ? static_cast<unsigned>((n + per_block - 1) / per_block) : 0u;
+}
+
+// Exclusive prefix of per-job block counts -> start[0..n_jobs] (start[n_jobs]
+// = total).  One block of 1024 threads; thread t owns a contiguous run of jobs.
 template <int kField>
 __global__ void __launch_bounds__(1024)
-block_map_kernel(const RastJob* __restrict__ jobs, int n_jobs, int per_block, int2* __restrict__ map,
-                 unsigned capacity) {
+block_prefix_kernel(const RastJob* __restrict__ jobs, int n_jobs, int per_block, unsigned* __restrict__ start) {
   __shared__ unsigned s_sum[1024];
   const int t = threadIdx.x;
   const int per_thread = (n_jobs + 1023) / 1024;
   const int j0 = min(n_jobs, t * per_thread), j1 = min(n_jobs, j0 + per_thread);
-  auto blocks_of = [&](int j) {
-    const int n = kField == kMapFaces ? __ldg(&jobs[j].n_faces) : __ldg(&jobs[j].n_verts);
-    return n > 0 ? static_cast<unsigned>((n + per_block - 1) / per_block) : 0u;
-  };
   unsigned mine = 0;
-  for (int j = j0; j < j1; ++j) mine += blocks_of(j);
+  for (int j = j0; j < j1; ++j) mine += blocks_of_job<kField>(jobs, j, per_block);
   s_sum[t] = mine;
   __syncthreads();
   for (int off = 1; off < 1024; off <<= 1) {
@@ -144,25 +146,48 @@ block_map_kernel(const RastJob* __restrict__ jobs, int n_jobs, int per_block, in
   }
   unsigned at = s_sum[t] - mine;
   for (int j = j0; j < j1; ++j) {
-    const unsigned nb = blocks_of(j);
-    for (unsigned b = 0; b < nb && at + b < capacity; ++b)
-      map[at + b] = make_int2(j, static_cast<int>(b) * per_block);
-    at += nb;
+    start[j] = at;
+    at += blocks_of_job<kField>(jobs, j, per_block);
   }
-  for (unsigned k = s_sum[1023] + t; k < capacity; k += 1024) map[k] = make_int2(-1, 0);
+  if (t == 1023) start[n_jobs] = s_sum[1023];
 }
 
-// Builds the map of `field` for batch b on stream s.
-inline cudaError_t build_block_map(const RastBatch& b, int field, int per_block, int2* map, cudaStream_t s) {
+// One thread per job writes its blocks' entries; the threads past the jobs
+// fill the tail of the map (entries >= total) with (-1, 0).
+template <int kField>
+__global__ void __launch_bounds__(256)
+block_fill_kernel(const RastJob* __restrict__ jobs, int n_jobs, int per_block, const unsigned* __restrict__ start,
+                  int2* __restrict__ map, unsigned capacity) {
+  const int j = blockIdx.x * 256 + threadIdx.x;
+  if (j < n_jobs) {
+    const unsigned a = start[j], nb = start[j + 1] - a;
+    for (unsigned b = 0; b < nb && a + b < capacity; ++b) map[a + b] = make_int2(j, static_cast<int>(b) * per_block);
+  }
+  const unsigned total = start[n_jobs];
+  const unsigned stride = gridDim.x * 256u;
+  for (unsigned k = total + static_cast<unsigned>(j); k < capacity; k += stride) map[k] = make_int2(-1, 0);
+}
+
+// Builds the map of `field` for batch b on stream s.  `start` holds
+// n_jobs + 1 unsigned.
+inline cudaError_t build_block_map(const RastBatch& b, int field, int per_block, int2* map, unsigned* start,
+                                   cudaStream_t s) {
   const int64_t total = field == kMapFaces ? b.total_setup : b.total_vout;
   const unsigned cap = block_map_capacity(total, b.n_jobs, per_block);
-  if (cap == 0) return cudaSuccess;
-  if (field == kMapFaces)
-    block_map_kernel<kMapFaces><<<1, 1024, 0, s>>>(b.jobs, b.n_jobs, per_block, map, cap);
-  else
-    block_map_kernel<kMapVertices><<<1, 1024, 0, s>>>(b.jobs, b.n_jobs, per_block, map, cap);
+  if (cap == 0 || b.n_jobs <= 0) return cudaSuccess;
+  const unsigned grid = static_cast<unsigned>((b.n_jobs + 255) / 256);
+  if (field == kMapFaces) {
+    block_prefix_kernel<kMapFaces><<<1, 1024, 0, s>>>(b.jobs, b.n_jobs, per_block, start);
+    block_fill_kernel<kMapFaces><<<grid, 256, 0, s>>>(b.jobs, b.n_jobs, per_block, start, map, cap);
+  } else {
+    block_prefix_kernel<kMapVertices><<<1, 1024, 0, s>>>(b.jobs, b.n_jobs, per_block, start);
+    block_fill_kernel<kMapVertices><<<grid, 256, 0, s>>>(b.jobs, b.n_jobs, per_block, start, map, cap);
+  }
   return cudaGetLastError();
 }
+
+// Bytes of the per-job block starts that build_block_map needs.
+inline size_t block_start_bytes(int n_jobs) { return (static_cast<size_t>(n_jobs) + 1) * sizeof(unsigned); }
 
 // Pixel (i, j) of a job from its x-major local index i * H + j; 32-bit
 // division when the job's pixel count fits (every job in practice).

@@ -658,7 +658,7 @@ inline uint64_t default_bin_capacity(const RastBatch& b) {
 
 struct Layout {
   size_t setup_off, bbox_off, counts_off, offsets_off, cursors_off, bsums_off, bins_off, winner_off,
-      vis_off, fvar_off, fmap_off, misc_off, total;
+      vis_off, fvar_off, fmap_off, fstart_off, misc_off, total;
   unsigned fmap_blocks;
   int vstride;
   int64_t n_tiles, n_scan_blocks;
@@ -699,6 +699,7 @@ static Layout layout(const RastBatch& b, TileShape ts, uint64_t bin_capacity) {
   L.fvar_off = take(shading ? static_cast<size_t>(b.total_setup) * 3 * vstride * sizeof(float) : 0);
   L.fmap_blocks = block_map_capacity(b.total_setup, b.n_jobs, kSetupThreads);
   L.fmap_off = take(static_cast<size_t>(L.fmap_blocks) * sizeof(int2));
+  L.fstart_off = take(block_start_bytes(b.n_jobs));
   L.misc_off = take(256);
   L.total = off;
   return L;
@@ -745,7 +746,9 @@ static int render(const RastBatch* batch, const RastTiledConfig* cfg, void* work
   prof.mark("memset");
   int2* fmap = reinterpret_cast<int2*>(ws + L.fmap_off);
   if (b.total_setup > 0) {
-    if (build_block_map(b, kMapFaces, kSetupThreads, fmap, s) != cudaSuccess) return RAST_ERR_CUDA;
+    if (build_block_map(b, kMapFaces, kSetupThreads, fmap, reinterpret_cast<unsigned*>(ws + L.fstart_off), s) !=
+        cudaSuccess)
+      return RAST_ERR_CUDA;
     prof.mark("block_map_kernel");
     const unsigned grid = L.fmap_blocks;
     setup_bin_kernel<<<grid, kSetupThreads, 0, s>>>(b, L.G, fmap, setup, bbox, counts);

@@ -54,13 +54,15 @@ def matvec(m: np.ndarray, v: np.ndarray) -> np.ndarray:
 
 
 def _sum_sq(v: np.ndarray) -> np.ndarray:
+    """Sum of squares of every element, accumulated sequentially in index
+    order (the order the device-side merge uses for the same global norms)."""
     flat = v.reshape(-1)
     if flat.size <= 4:
         acc = flat[0] * flat[0]
         for k in range(1, flat.size):
             acc = acc + flat[k] * flat[k]
         return acc
-    return np.sum(flat * flat, dtype=v.dtype)
+    return np.add.accumulate(flat * flat, dtype=v.dtype)[-1]
 
 
 def normalise(vector) -> np.ndarray:

@@ -479,3 +479,46 @@ def flat_subset(flat: FlatScenes, scenes: Sequence[int]) -> FlatScenes:
     return FlatScenes(flat.position[rows], flat.normal[rows], flat.uv[rows], flat.texture_index[rows],
                       flat.texture[trows], flat.specular_map[trows], corner_begin, flat.n_faces[sel].copy(),
                       tex_begin, flat.n_objects[sel].copy(), flat.camera_position[sel].copy(), T, target)
+
+
+def brax_like_instances(n_scenes: int, seed: int = BASE_SEED + 1):
+    """`n_scenes` Brax-like scenes as instances of four meshes (ground plane,
+    box, level-2 icosphere, 16x8 capsule): the ground (identity transform)
+    plus 8..32 objects with ModelObject transforms [R | t] (random unit
+    quaternion, t in [-3, 3]^2 x [0, 2]), uniform local scaling U[0.2, 1],
+    one RGB colour U[0, 1] per object on a 4x4 map, specular 2.0; camera on a
+    radius-6 sphere at elevation U[20, 60] deg, azimuth U[0, 360) deg."""
+    from .instancing import InstancedScenes, MeshLibrary
+
+    rng = np.random.Generator(np.random.PCG64(seed))
+    gv = np.array([(-5, -5, 0), (5, -5, 0), (5, 5, 0), (-5, 5, 0)], F32)
+    gf = np.array([(0, 1, 2), (0, 2, 3)], np.int32)
+    gn = np.tile(np.array([(0, 0, 1)], F32), (4, 1))
+    guv = np.array([(0, 0), (4, 0), (4, 4), (0, 4)], F32)
+    blank = np.zeros((4, 4, 3), F32)
+    ground = Model(gv, gn, guv, gf, gf, gf, blank, np.full((4, 4), 2.0, F32))
+    library = MeshLibrary.from_models([ground] + [primitive_model(k, np.zeros(3, F32)) for k in _KINDS])
+    n_obj = rng.integers(8, 33, size=n_scenes)
+    counts = n_obj + 1
+    I = int(counts.sum())
+    scene_begin = np.concatenate([[0], np.cumsum(counts)]).astype(np.int64)
+    is_ground = np.zeros(I, bool)
+    is_ground[scene_begin[:-1]] = True
+    mesh = np.zeros(I, np.int32)
+    mesh[~is_ground] = 1 + rng.integers(0, 3, size=I - n_scenes)
+    q = rng.normal(size=(I, 4))
+    q /= np.linalg.norm(q, axis=1, keepdims=True)
+    transforms = np.tile(np.identity(4, F32), (I, 1, 1))
+    transforms[~is_ground, :3, :3] = _quat_matrices(q[~is_ground]).astype(F32)
+    k = I - n_scenes
+    transforms[~is_ground, :3, 3] = np.stack([rng.uniform(-3, 3, k), rng.uniform(-3, 3, k), rng.uniform(0, 2, k)],
+                                             1).astype(F32)
+    scale = np.ones((I, 3), F32)
+    scale[~is_ground] = rng.uniform(0.2, 1.0, (k, 1)).astype(F32)
+    colour = rng.uniform(0, 1, (I, 3)).astype(F32)
+    diffuse = np.broadcast_to(colour[:, None, None, :], (I, 4, 4, 3)).copy()
+    specular = np.full((I, 4, 4), 2.0, F32)
+    elev = np.deg2rad(rng.uniform(20, 60, n_scenes))
+    azim = np.deg2rad(rng.uniform(0, 360, n_scenes))
+    cam = 6.0 * np.stack([np.cos(elev) * np.cos(azim), np.cos(elev) * np.sin(azim), np.sin(elev)], 1)
+    return InstancedScenes(library, mesh, scene_begin, transforms, scale, diffuse, specular, cam.astype(F32))

@@ -66,7 +66,8 @@ def _c_layout(tmp_path, struct, fields):
     return {k: int(v) for k, v in (line.split() for line in out.strip().splitlines())}
 
 
-@pytest.mark.parametrize("struct", ["RastJob", "RastPools", "RastBatch"])
+@pytest.mark.parametrize("struct", ["RastJob", "RastPools", "RastBatch", "RastMesh", "RastInstance", "RastMergeBatch",
+                                    "RastTiledConfig", "RastTiledStats", "RastGradPools"])
 def test_struct_layout_matches_c(tmp_path, struct):
     cls = getattr(_lib, struct)
     names = [f[0] for f in cls._fields_]
