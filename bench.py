@@ -51,8 +51,8 @@ METRIC = "frames/s @84x84x4096 scenes fwd and fwd+bwd, tiled-batched vs plain GP
 UNIT = "frames/s"
 L2_BYTES = 129 * 1024 * 1024
 MIXED_CLASSES = [(32, 32), (84, 84), (480, 270)]
-WORKLOADS = ("brax84", "cube640", "overdraw960", "phong128", "mixed1024")
-DEFAULT_SCENES = {"brax84": 4096, "cube640": 1, "overdraw960": 1, "phong128": 256, "mixed1024": 1024}
+WORKLOADS = ("brax84", "ant84", "cube640", "overdraw960", "phong128", "mixed1024")
+DEFAULT_SCENES = {"brax84": 4096, "ant84": 200, "cube640": 1, "overdraw960": 1, "phong128": 256, "mixed1024": 1024}
 
 
 def parse():
@@ -98,6 +98,9 @@ class Workload:
     phong: Optional[dict] = None
     merges: list = field(default_factory=list)  # instancing.DeviceMerge per group (instanced workloads)
     instances: object = None  # instancing.InstancedScenes
+    notebook: bool = False  # step = device merge + render + uint8 display epilogue, as the notebooks time it
+    published: Optional[float] = None  # the reference's published frames/s for this configuration
+    display: object = None  # uint8 display images of the notebook step
 
 
 def _pass_work(spec) -> float:
@@ -214,7 +217,42 @@ def build_mixed1024(n, rank, dev):
                             "shadow_scenes": int(shadow.sum()), "shadow_map": "canvas size (Renderer.render)"})
 
 
-BUILDERS = {"brax84": build_brax84, "cube640": build_cube640, "overdraw960": build_overdraw960,
+def build_ant84(n, rank, dev):
+    """The notebooks' benchmark (84x84/A100.ipynb cells 4-7): Brax Ant
+    frames -- here the seeded stand-in synthetic.ant_like_batched in the same
+    batched format, 18 objects / 3,276 triangles per frame, 30 frames
+    repeated to the batch -- rendered into 84x84 canvases through the
+    pickled 960x540 camera with the notebook's light and per-frame shadow
+    centre, then clamped, scaled to uint8 and transposed for display."""
+    from jaxrenderer_gb300 import batch as jb, brax, synthetic
+
+    W = H = 84
+    objects, camera, target = synthetic.ant_like_batched(30, seed=synthetic.BASE_SEED + 7 + rank)
+    frames = [k % 30 for k in range(n)]
+    bb = brax.scenes_from_batched(objects, camera, target, frames=frames)
+    inst = bb.scenes
+    work = inst.n_faces.astype(np.float64) * (2 * W * H)
+
+    def chain(k):
+        k = k % n
+        sub = inst.host_flat([k])
+        shadow = bb.shadow._replace(centre=bb.shadow.centre[k : k + 1])
+        t = jb.scene_batch_tables(sub, W, H, bb.light, shadow, (W, H), bb.camera, shadow_viewport="camera")
+        return jb.scene_job_specs(sub, t, 0)
+
+    groups, merges = [], []
+    if dev is not None:
+        sb, merge = brax.scene_batch(bb, W, H, dev)
+        groups, merges = [sb], [merge]
+    return Workload("ant84", f"Brax-Ant-like 84x84 x {n} frames (18 objects, 3,276 tris; 960x540 camera), "
+                    "phong_reflection_shadow, device merge + render + uint8 display per step", n, chain, work,
+                    groups, merges=merges, instances=inst, notebook=True, published=888.6 if n == 200 else None,
+                    config={"scenes": n, "faces_per_scene": 3276, "resolution": [W, H],
+                            "camera_viewport": [960, 540], "shadow_map": [W, H],
+                            "published": "888.6 frames/s, A100, batch 200 (notebooks/84x84/A100.ipynb:1308)"})
+
+
+BUILDERS = {"ant84": build_ant84, "brax84": build_brax84, "cube640": build_cube640, "overdraw960": build_overdraw960,
             "phong128": build_phong128, "mixed1024": build_mixed1024}
 
 
@@ -416,7 +454,9 @@ def run_ours(args, rank, world, local):
     timed = Timer(dev, stream, world, flush)
 
     mr = jb.MultiRunner(wl.groups, form=form, want_prim_id=False)
-    if form == "tiled":
+    if wl.notebook:
+        step, wl.display = notebook_step(wl, mr, dev, capture=form == "tiled")
+    elif form == "tiled":
         mr.capture()
         step = mr.replay
     else:
@@ -458,7 +498,7 @@ def run_ours(args, rank, world, local):
         "ms_per_step": ms_per_step,
         "higher_is_better": True,
         "scaling": "weak",
-        "vs_baseline": None,
+        "vs_baseline": (value / wl.published) if wl.published else None,
         "dtype": "f32",
         "data": "synthetic (seeded stand-ins with the stated shapes; the reference's Brax fixtures are "
                 "inputs-only pickles)",
@@ -487,6 +527,37 @@ def run_ours(args, rank, world, local):
         print(json.dumps(out), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def notebook_step(wl: Workload, mr, dev, capture: bool):
+    """One step as the notebooks time it: rebuild the per-corner pools from
+    the resident transforms (rast_merge_objects), render, and the uint8
+    display epilogue (rast_display_u8); as one CUDA graph when `capture`."""
+    import torch
+
+    from jaxrenderer_gb300.utils import display_u8
+
+    r = mr.runners[0]
+    n, w, h, c = r.canvas.shape
+    display = torch.empty((n, h, w, c), dtype=torch.uint8, device=dev)
+
+    def step(stream=None):
+        s = stream if stream is not None else torch.cuda.current_stream(dev)
+        wl.merges[0].merge(stream=s)
+        mr.run(s)
+        display_u8(r.canvas, out=display, stream=s)
+
+    if not capture:
+        return step, display
+    side = torch.cuda.Stream(dev)
+    side.wait_stream(torch.cuda.current_stream(dev))
+    step(side)
+    torch.cuda.current_stream(dev).wait_stream(side)
+    torch.cuda.synchronize(dev)
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        step()
+    return g.replay, display
 
 
 def count_visible(mr):
@@ -800,20 +871,24 @@ def measure_e2e(wl: Workload, mr, step, args, dev, stream, world):
                 hp[n] = h
                 h2d += h.numel() * h.element_size()
             host.append(hp)
-    for r in mr.runners:
-        oh = torch.empty(r.canvas.shape, dtype=torch.float32, pin_memory=True)
+    results = [wl.display] if wl.notebook else [r.canvas for r in mr.runners]
+    for t in results:
+        oh = torch.empty(t.shape, dtype=t.dtype, pin_memory=True)
         outs.append(oh)
-        d2h += oh.numel() * 4
+        d2h += oh.numel() * oh.element_size()
 
     def e2e_step():
-        if wl.merges:
+        if wl.notebook:  # the step itself merges
+            wl.merges[0].transforms.copy_(tr.reshape(-1, 16), non_blocking=True)
+            wl.merges[0].local_scaling.copy_(sc.reshape(-1, 3), non_blocking=True)
+        elif wl.merges:
             wl.merges[0].merge(tr, sc, stream)
         for r, hp in zip(mr.runners, host):
             for n, h in hp.items():
                 r.sb.pools[n].copy_(h, non_blocking=True)
         step()
-        for r, oh in zip(mr.runners, outs):
-            oh.copy_(r.canvas, non_blocking=True)
+        for t, oh in zip(results, outs):
+            oh.copy_(t, non_blocking=True)
 
     steps = max(1, min(args.steps, 5))
     e2e_step()
@@ -828,7 +903,8 @@ def measure_e2e(wl: Workload, mr, step, args, dev, stream, world):
     out = {"value": world * wl.frames / (ms / 1e3), "unit": UNIT, "ms_per_step": ms,
            "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h), "steps": steps,
            "inputs": ("object transforms + local scalings; per-corner pools rebuilt on the device "
-                      "(rast_merge_objects)") if wl.merges else "per-corner input pools"}
+                      "(rast_merge_objects)") if wl.merges else "per-corner input pools",
+           "outputs": "uint8 display images" if wl.notebook else "float32 canvases"}
     if wl.merges:
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         a.record(stream)

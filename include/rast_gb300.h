@@ -359,6 +359,15 @@ size_t rast_merge_workspace_bytes(const RastMergeBatch* batch);
  * first instance, faces = 3 * arange).  Stream-ordered, graph-capturable. */
 int rast_merge_objects(const RastMergeBatch* batch, void* workspace, size_t workspace_bytes, void* stream);
 
+/* Display epilogue of the reference's notebooks: transpose_for_display(
+ * (clamp(canvas, 0, 1) * 255).astype(uint8)) (renderer/utils.py:79-96).
+ * canvas (n_images, width, height, channels) float, x-major as rendered ->
+ * out (n_images, height, width, channels) uint8, row 0 the top when
+ * flip_vertical.  Values are clamped with NaN -> 0 and truncated toward
+ * zero. */
+int rast_display_u8(const float* canvas, int64_t n_images, int32_t width, int32_t height, int32_t channels,
+                    int32_t flip_vertical, uint8_t* out, void* stream);
+
 /* Host-side validation of one job against pool sizes (no device access):
  * returns RAST_ERR_INVALID_ARGUMENT for inconsistent sizes. */
 int rast_validate_job(const RastJob* job);

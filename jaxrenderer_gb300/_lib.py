@@ -198,6 +198,7 @@ PROTOTYPES = [
       POINTER(RastProfile)]),
     ("rast_merge_workspace_bytes", c_size_t, [POINTER(RastMergeBatch)]),
     ("rast_merge_objects", c_int, [POINTER(RastMergeBatch), c_void_p, c_size_t, c_void_p]),
+    ("rast_display_u8", c_int, [c_void_p, c_int64, c_int32, c_int32, c_int32, c_int32, c_void_p, c_void_p]),
     ("rast_validate_job", c_int, [POINTER(RastJob)]),
     ("rast_error_string", ctypes.c_char_p, [c_int]),
     ("rast_abi_version", c_int, []),

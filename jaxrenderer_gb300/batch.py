@@ -85,7 +85,7 @@ def scene_batch_tables(flat, width: int = 84, height: int = 84,
                        light: LightParameters = LightParameters(),
                        shadow_param: Optional[ShadowParameters] = ShadowParameters(),
                        shadow_size=(128, 128), camera_params: Optional[CameraParameters] = None,
-                       shadow_mask: Optional[np.ndarray] = None) -> SceneTables:
+                       shadow_mask: Optional[np.ndarray] = None, shadow_viewport: str = "map") -> SceneTables:
     """RastJob tables of a synthetic.FlatScenes batch.
 
     Each scene: PhongReflection(Shadow)TextureShader over its corners
@@ -94,9 +94,13 @@ def scene_batch_tables(flat, width: int = 84, height: int = 84,
     with viewport shadow_size (the low-level Shadow.render_shadow_map API).
     `shadow_mask` (N,) selects the scenes that get the shadow pass (all by
     default); the others render with PhongReflectionTextureShader.
+    `shadow_param.centre` may hold one centre per scene (N, 3);
+    `shadow_viewport="camera"` gives the depth pass the scene camera's
+    viewport, as Renderer.render does (renderer.py:343-365).
     """
     n = flat.n_scenes
     T = int(getattr(flat, "tex_size", 4))
+    Ts = int(getattr(flat, "spec_size", None) or T)
     params = camera_params or CameraParameters(viewWidth=width, viewHeight=height, near=0.01, far=1000.0,
                                                hfov=58.0, vfov=58.0, target=np.zeros(3, F32))
     w2c, w2e, views, viewport = _cameras(flat.camera_position, params, getattr(flat, "camera_target", None))
@@ -119,14 +123,14 @@ def scene_batch_tables(flat, width: int = 84, height: int = 84,
     main["pixel_begin"] = np.arange(n, dtype=np.int64) * width * height
     main["vout_begin"] = flat.corner_begin
     main["setup_begin"] = np.concatenate([[0], np.cumsum(flat.n_faces.astype(np.int64))[:-1]])
-    main["texture_begin"] = flat.tex_begin * T * 3
-    main["specular_begin"] = flat.tex_begin * T
     obj_begin = np.concatenate([[0], np.cumsum(flat.n_objects.astype(np.int64))[:-1]])
+    main["texture_begin"] = obj_begin * T * T * 3
+    main["specular_begin"] = obj_begin * Ts * Ts
     main["texture_shape_begin"] = obj_begin
     main["tex_w"] = T * flat.n_objects
     main["tex_h"], main["tex_c"] = T, 3
-    main["spec_w"] = T * flat.n_objects
-    main["spec_h"] = T
+    main["spec_w"] = Ts * flat.n_objects
+    main["spec_h"] = Ts
     main["viewport"] = np.broadcast_to(viewport.reshape(16), (n, 16))
     main["world_to_clip"] = w2c.reshape(n, 16)
     main["world_to_eye_norm"] = w2e.reshape(n, 16)
@@ -139,8 +143,20 @@ def scene_batch_tables(flat, width: int = 84, height: int = 84,
     shadow_jobs = None
     sw, sh = shadow_size
     if shadow:
-        svp = Camera.viewport_matrix(np.zeros(2, np.int32), np.array((sw, sh)), 1.0)
-        scam = Shadow.light_camera(np.asarray(light.direction, F32), svp, shadow_param.centre, shadow_param.up)
+        # shadow_viewport "map": the low-level API with a viewport of the map's
+        # size; "camera": Renderer.render, the scene camera's viewport
+        svp = viewport if shadow_viewport == "camera" else \
+            Camera.viewport_matrix(np.zeros(2, np.int32), np.array((sw, sh)), 1.0)
+        centre = np.asarray(shadow_param.centre, F32)
+        if centre.ndim == 2:  # one shadow centre per scene
+            cams = [Shadow.light_camera(np.asarray(light.direction, F32), svp, c, shadow_param.up) for c in centre]
+            s_w2c = np.stack([c.world_to_clip for c in cams])
+            s_w2e = np.stack([c.world_to_eye_norm for c in cams])
+            scam = cams[0]
+        else:
+            scam = Shadow.light_camera(np.asarray(light.direction, F32), svp, centre, shadow_param.up)
+            s_w2c = np.broadcast_to(scam.world_to_clip, (n, 4, 4))
+            s_w2e = np.broadcast_to(scam.world_to_eye_norm, (n, 4, 4))
         sel = np.nonzero(mask)[0]
         shadow_jobs = job_table(len(sel))
         shadow_jobs["shader"] = _lib.SHADER_DEPTH
@@ -153,14 +169,14 @@ def scene_batch_tables(flat, width: int = 84, height: int = 84,
         shadow_jobs["vout_begin"] = np.concatenate([[0], np.cumsum(nvt)[:-1]])
         shadow_jobs["pixel_begin"] = np.arange(len(sel), dtype=np.int64) * sw * sh
         shadow_jobs["viewport"] = svp.reshape(16)
-        shadow_jobs["world_to_clip"] = scam.world_to_clip.reshape(16)
-        shadow_jobs["world_to_eye_norm"] = scam.world_to_eye_norm.reshape(16)
+        shadow_jobs["world_to_clip"] = s_w2c[sel].reshape(-1, 16)
+        shadow_jobs["world_to_eye_norm"] = s_w2e[sel].reshape(-1, 16)
         shadow_jobs["depth_offset"] = np.float32(shadow_param.offset)
         shadow_jobs["flags"] = _lib.JOB_APPLY_DEPTH_OFFSET
         main["shadow_begin"][sel] = shadow_jobs["pixel_begin"]
         main["shadow_w"][sel], main["shadow_h"][sel] = sw, sh
         main["shadow_viewport"][sel] = scam.viewport.reshape(16)
-        main["shadow_world_to_clip"][sel] = scam.world_to_clip.reshape(16)
+        main["shadow_world_to_clip"][sel] = s_w2c[sel].reshape(-1, 16)
         main["shadow_strength"][sel] = np.asarray(shadow_param.strength, F32)
     if shadow_jobs is not None and len(shadow_jobs) == 0:
         shadow_jobs = None
@@ -186,9 +202,15 @@ def flat_pools(flat, device) -> Dict[str, torch.Tensor]:
         "faces": T(faces, torch.int32),
         "texture": T(flat.texture),
         "specular_map": T(flat.specular_map),
-        "texture_shape": T(np.tile(np.array([[getattr(flat, "tex_size", 4)] * 2], np.int32),
-                                   (int(flat.n_objects.sum()), 1)), torch.int32),
+        "texture_shape": T(_texture_shapes(flat), torch.int32),
     }
+
+
+def _texture_shapes(flat) -> np.ndarray:
+    ts = getattr(flat, "texture_shape", None)
+    if ts is not None:
+        return np.asarray(ts, np.int32).reshape(-1, 2)
+    return np.tile(np.array([[getattr(flat, "tex_size", 4)] * 2], np.int32), (int(flat.n_objects.sum()), 1))
 
 
 def scene_batch_from_flat(flat, width: int = 84, height: int = 84,
@@ -216,7 +238,7 @@ def scene_batch_from_instances(inst, width: int = 84, height: int = 84,
                                shadow_param: Optional[ShadowParameters] = ShadowParameters(),
                                shadow_size=(128, 128), device=None,
                                camera_params: Optional[CameraParameters] = None,
-                               shadow_mask: Optional[np.ndarray] = None):
+                               shadow_mask: Optional[np.ndarray] = None, shadow_viewport: str = "map"):
     """A SceneBatch of an instancing.InstancedScenes batch whose per-corner
     pools are built on the device; returns (SceneBatch, DeviceMerge) after
     one merge.  Later frames: `merge.merge(transforms, local_scaling)` then
@@ -225,7 +247,8 @@ def scene_batch_from_instances(inst, width: int = 84, height: int = 84,
 
     device = device if device is not None else torch.device("cuda", torch.cuda.current_device())
     shell = inst.shell()
-    t = scene_batch_tables(shell, width, height, light, shadow_param, shadow_size, camera_params, shadow_mask)
+    t = scene_batch_tables(shell, width, height, light, shadow_param, shadow_size, camera_params, shadow_mask,
+                           shadow_viewport)
     pools = instanced_pools(inst, device)
     merge = DeviceMerge(inst, pools, device)
     merge.merge()
@@ -257,8 +280,10 @@ def scene_job_specs(flat, tables, s: int):
 
     m = tables.main_jobs[s]
     T = int(getattr(flat, "tex_size", 4))
+    Ts = int(getattr(flat, "spec_size", None) or T)
     cb, F = int(flat.corner_begin[s]), int(flat.n_faces[s])
-    tb, no = int(flat.tex_begin[s]), int(flat.n_objects[s])
+    no = int(flat.n_objects[s])
+    ob = int(np.sum(flat.n_objects[:s], dtype=np.int64))
     faces = np.arange(3 * F, dtype=np.int32).reshape(F, 3)
     rows = slice(cb, cb + 3 * F)
     main = JobSpec(shader=int(m["shader"]), width=int(m["width"]), height=int(m["height"]),
@@ -268,9 +293,9 @@ def scene_job_specs(flat, tables, s: int):
     main.normal = flat.normal[rows]
     main.uv = flat.uv[rows]
     main.texture_index = flat.texture_index[rows]
-    main.texture = flat.texture[tb : tb + T * no]
-    main.specular_map = flat.specular_map[tb : tb + T * no]
-    main.texture_shape = np.tile(np.array([[T, T]], np.int32), (no, 1))
+    main.texture = flat.texture[ob * T : (ob + no) * T]
+    main.specular_map = flat.specular_map[ob * Ts : (ob + no) * Ts]
+    main.texture_shape = _texture_shapes(flat)[ob : ob + no]
     main.texture_offset = T
     for k in ("light_direction", "light_colour", "light_dir_eye", "ambient", "diffuse", "specular"):
         setattr(main, k, np.asarray(m[k], F32))

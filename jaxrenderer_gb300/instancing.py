@@ -78,10 +78,11 @@ class InstancedScenes:
     scene_begin: np.ndarray  # (S + 1,) int64
     transforms: np.ndarray  # (I, 4, 4) float32
     local_scaling: np.ndarray  # (I, 3) float32
-    diffuse: np.ndarray  # (I, T, T, 3) float32
-    specular: np.ndarray  # (I, T, T) float32
+    diffuse: np.ndarray  # (I, T, T, 3) float32, zero-padded at the end of each axis
+    specular: np.ndarray  # (I, Ts, Ts) float32
     camera_position: np.ndarray  # (S, 3)
     camera_target: Optional[np.ndarray] = None
+    texture_shape: Optional[np.ndarray] = None  # (I, 2) the diffuse maps' own sizes; (T, T) when None
 
     @property
     def n_scenes(self) -> int:
@@ -94,6 +95,26 @@ class InstancedScenes:
     @property
     def tex_size(self) -> int:
         return int(self.diffuse.shape[1])
+
+    @property
+    def spec_size(self) -> int:
+        return int(self.specular.shape[1])
+
+    def shapes(self) -> np.ndarray:
+        if self.texture_shape is not None:
+            return np.asarray(self.texture_shape, np.int32).reshape(-1, 2)
+        return np.tile(np.array([[self.tex_size] * 2], np.int32), (self.n_instances, 1))
+
+    def check_maps(self) -> None:
+        """merge_maps pads a scene's maps to the scene's largest; the batch
+        layout pads to the batch's, so every scene must hold a map of the
+        batch's (T, T) size (as with a textured ground in every scene)."""
+        sh = self.shapes()
+        T = self.tex_size
+        for s in range(self.n_scenes):
+            a, b = int(self.scene_begin[s]), int(self.scene_begin[s + 1])
+            if b > a and (sh[a:b, 0].max() != T or sh[a:b, 1].max() != T):
+                raise ValueError(f"scene {s}: its largest diffuse map is not {T}x{T}")
 
     def _mesh_counts(self, field: str) -> np.ndarray:
         return self.library.table[field][self.mesh].astype(np.int64)
@@ -136,7 +157,8 @@ class InstancedScenes:
         out = []
         for i in range(int(self.scene_begin[s]), int(self.scene_begin[s + 1])):
             m = self.library.models[int(self.mesh[i])]
-            model = m._replace(diffuse_map=self.diffuse[i], specular_map=self.specular[i])
+            w, h = (int(x) for x in self.shapes()[i])
+            model = m._replace(diffuse_map=self.diffuse[i][:w, :h], specular_map=self.specular[i])
             out.append(ModelObject(model=model, local_scaling=self.local_scaling[i], transform=self.transforms[i]))
         return out
 
@@ -144,12 +166,15 @@ class InstancedScenes:
         """A FlatScenes with the batch's bookkeeping and no per-corner arrays."""
         from .synthetic import FlatScenes
 
+        self.check_maps()
         T = self.tex_size
         counts = np.diff(self.scene_begin)
-        return FlatScenes(None, None, None, None, self.diffuse.reshape(-1, T, 3), self.specular.reshape(-1, T),
-                          self.corner_begin(), self.n_faces, (T * self.scene_begin[:-1]).astype(np.int64),
-                          counts.astype(np.int32), np.asarray(self.camera_position, F32), T,
-                          None if self.camera_target is None else np.asarray(self.camera_target, F32))
+        return FlatScenes(None, None, None, None, self.diffuse.reshape(-1, T, 3),
+                          self.specular.reshape(-1, self.spec_size), self.corner_begin(), self.n_faces,
+                          (T * self.scene_begin[:-1]).astype(np.int64), counts.astype(np.int32),
+                          np.asarray(self.camera_position, F32), T,
+                          None if self.camera_target is None else np.asarray(self.camera_target, F32),
+                          self.shapes(), self.spec_size)
 
     def host_flat(self, scenes: Sequence[int]):
         """FlatScenes of `scenes` built by the host reference path:
@@ -164,18 +189,20 @@ class InstancedScenes:
             p, n, u, t, _ = Renderer.flatten_corners(merged)
             pos.append(p), nrm.append(n), uv.append(u), tix.append(t)
             tex.append(np.asarray(merged.diffuse_map, F32).reshape(-1, T, 3))
-            spec.append(np.asarray(merged.specular_map, F32).reshape(-1, T))
+            spec.append(np.asarray(merged.specular_map, F32).reshape(-1, self.spec_size))
             nf.append(len(p) // 3)
             no.append(int(self.scene_begin[s + 1] - self.scene_begin[s]))
         nf = np.asarray(nf, np.int32)
         no = np.asarray(no, np.int32)
         sel = np.asarray(scenes, np.int64)
+        shapes = np.concatenate([self.shapes()[int(self.scene_begin[s]):int(self.scene_begin[s + 1])] for s in scenes])
         return FlatScenes(np.concatenate(pos), np.concatenate(nrm), np.concatenate(uv),
                           np.concatenate(tix).astype(np.int32), np.concatenate(tex), np.concatenate(spec),
                           np.concatenate([[0], np.cumsum(3 * nf.astype(np.int64))[:-1]]), nf,
                           np.concatenate([[0], np.cumsum(T * no.astype(np.int64))[:-1]]), no,
                           np.asarray(self.camera_position, F32)[sel], T,
-                          None if self.camera_target is None else np.asarray(self.camera_target, F32)[sel])
+                          None if self.camera_target is None else np.asarray(self.camera_target, F32)[sel],
+                          shapes, self.spec_size)
 
 
 class DeviceMerge:
@@ -241,7 +268,6 @@ def instanced_pools(inst: InstancedScenes, device) -> dict:
     corners = int(3 * inst.n_faces.astype(np.int64).sum())
     max_f = int(inst.n_faces.max()) if inst.n_scenes else 0
     T = inst.tex_size
-    n_obj = inst.n_instances
     return {
         "position": torch.empty((corners, 3), dtype=torch.float32, device=device),
         "normal": torch.empty((corners, 3), dtype=torch.float32, device=device),
@@ -249,8 +275,8 @@ def instanced_pools(inst: InstancedScenes, device) -> dict:
         "texture_index": torch.empty(corners, dtype=torch.int32, device=device),
         "faces": torch.arange(3 * max_f, dtype=torch.int32, device=device).reshape(-1, 3),
         "texture": torch.as_tensor(inst.diffuse.reshape(-1, T, 3)).to(device),
-        "specular_map": torch.as_tensor(inst.specular.reshape(-1, T)).to(device),
-        "texture_shape": torch.as_tensor(np.tile(np.array([[T, T]], np.int32), (n_obj, 1))).to(device),
+        "specular_map": torch.as_tensor(inst.specular.reshape(-1, inst.spec_size)).to(device),
+        "texture_shape": torch.as_tensor(inst.shapes()).to(device),
     }
 
 

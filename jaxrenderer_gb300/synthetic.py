@@ -204,8 +204,11 @@ class FlatScenes:
 
     Scene s owns corner rows [corner_begin[s], corner_begin[s] + 3 * n_faces[s])
     of position/normal/uv/texture_index, faces 3 * arange within them, and
-    texture rows [tex_begin[s], tex_begin[s] + 4 * n_objects[s]) of the 4x4
-    diffuse (RGB) and specular maps.
+    texture rows [tex_begin[s], tex_begin[s] + T * n_objects[s]) of the
+    T x T diffuse (RGB) maps, T = tex_size, and the matching rows of the
+    specular maps (spec_size, default T).  Maps smaller than T are padded
+    with zeros at the end of each axis (merge_maps) and keep their own size
+    in texture_shape.
     """
 
     position: np.ndarray
@@ -219,8 +222,10 @@ class FlatScenes:
     tex_begin: np.ndarray
     n_objects: np.ndarray
     camera_position: np.ndarray
-    tex_size: int = 4  # every object's diffuse/specular map is tex_size x tex_size
+    tex_size: int = 4  # every object's diffuse map is padded to tex_size x tex_size
     camera_target: Optional[np.ndarray] = None  # (N, 3); origin when None
+    texture_shape: Optional[np.ndarray] = None  # (objects, 2): maps' own sizes; tex_size when None
+    spec_size: Optional[int] = None  # specular maps padded to spec_size^2; tex_size when None
 
     @property
     def n_scenes(self) -> int:
@@ -467,18 +472,23 @@ def flat_subset(flat: FlatScenes, scenes: Sequence[int]) -> FlatScenes:
     (corner and texture rows gathered, offsets rebased)."""
     sel = np.asarray(scenes, np.int64)
     T = flat.tex_size
+    Ts = flat.spec_size or T
     nf = flat.n_faces[sel].astype(np.int64)
     no = flat.n_objects[sel].astype(np.int64)
-    rows = np.concatenate([np.arange(c, c + 3 * f) for c, f in zip(flat.corner_begin[sel], nf)]) if len(sel) else \
-        np.zeros(0, np.int64)
-    trows = np.concatenate([np.arange(t, t + T * o) for t, o in zip(flat.tex_begin[sel], no)]) if len(sel) else \
-        np.zeros(0, np.int64)
+    ob = np.concatenate([[0], np.cumsum(flat.n_objects.astype(np.int64))])[sel]
+    cat = lambda parts: np.concatenate(parts) if len(parts) else np.zeros(0, np.int64)  # noqa: E731
+    rows = cat([np.arange(c, c + 3 * f) for c, f in zip(flat.corner_begin[sel], nf)])
+    trows = cat([np.arange(b * T, (b + o) * T) for b, o in zip(ob, no)])
+    srows = cat([np.arange(b * Ts, (b + o) * Ts) for b, o in zip(ob, no)])
+    objs = cat([np.arange(b, b + o) for b, o in zip(ob, no)])
     corner_begin = np.concatenate([[0], np.cumsum(3 * nf)[:-1]]).astype(np.int64)
     tex_begin = np.concatenate([[0], np.cumsum(T * no)[:-1]]).astype(np.int64)
     target = None if flat.camera_target is None else flat.camera_target[sel]
+    shapes = None if flat.texture_shape is None else np.asarray(flat.texture_shape)[objs]
     return FlatScenes(flat.position[rows], flat.normal[rows], flat.uv[rows], flat.texture_index[rows],
-                      flat.texture[trows], flat.specular_map[trows], corner_begin, flat.n_faces[sel].copy(),
-                      tex_begin, flat.n_objects[sel].copy(), flat.camera_position[sel].copy(), T, target)
+                      flat.texture[trows], flat.specular_map[srows], corner_begin, flat.n_faces[sel].copy(),
+                      tex_begin, flat.n_objects[sel].copy(), flat.camera_position[sel].copy(), T, target, shapes,
+                      flat.spec_size)
 
 
 def brax_like_instances(n_scenes: int, seed: int = BASE_SEED + 1):
@@ -522,3 +532,49 @@ def brax_like_instances(n_scenes: int, seed: int = BASE_SEED + 1):
     azim = np.deg2rad(rng.uniform(0, 360, n_scenes))
     cam = 6.0 * np.stack([np.cos(elev) * np.cos(azim), np.cos(elev) * np.sin(azim), np.sin(elev)], 1)
     return InstancedScenes(library, mesh, scene_begin, transforms, scale, diffuse, specular, cam.astype(F32))
+
+
+def ant_like_batched(n_frames: int, seed: int = BASE_SEED + 7):
+    """A stand-in for the reference's pickled Brax Ant batches, in their
+    format (see brax.load_batched_inputs): 18 objects per frame -- a box
+    ground of 12 triangles with a 100x100 checker texture and 17 capsules of
+    192 triangles with 1x1 maps (3,276 triangles) -- each array with a
+    leading frame axis; objects move between frames, meshes do not; camera
+    960x540, hfov 58, vfov 32.625, circling the moving target."""
+    from .renderer import CameraParameters
+    from .shapes.capsule import create_capsule
+
+    rng = np.random.Generator(np.random.PCG64(seed))
+    F = n_frames
+    check = ((np.indices((100, 100)).sum(0) // 10) % 2).astype(F32)
+    tex = np.stack([0.25 + 0.5 * check, 0.3 + 0.4 * check, 0.35 + 0.3 * check], -1).astype(F32)
+    ground = create_cube(np.array((1000.0, 1000.0, 1e-4), F32), np.array((1000.0, 1000.0), F32) / 100.0, tex,
+                         np.full((1, 1), 2.0, F32))
+    caps = [create_capsule(F32(r), F32(h), 2, np.array([[[0.4, 0.33, 0.26]]], F32), np.full((1, 1), 2.0, F32))
+            for r, h in zip(rng.uniform(0.06, 0.12, 17), rng.uniform(0.1, 0.25, 17))]
+    models = [ground] + caps
+
+    def batched(a):
+        return np.broadcast_to(np.asarray(a), (F,) + np.asarray(a).shape).copy()
+
+    centre = np.cumsum(rng.normal(0, 0.05, (F, 3)), axis=0).astype(F32)
+    centre[:, 2] = 0.0
+    objects = []
+    for k, m in enumerate(models):
+        model = Model(*(batched(x) for x in m))
+        T = np.tile(np.identity(4, F32), (F, 1, 1))
+        if k > 0:
+            q = rng.normal(size=(F, 4))
+            q /= np.linalg.norm(q, axis=1, keepdims=True)
+            T[:, :3, :3] = _quat_matrices(q)
+            T[:, :3, 3] = centre + rng.normal(0, 0.35, (F, 3)).astype(F32) * np.array((1, 1, 0.3), F32)
+            T[:, 2, 3] = np.abs(T[:, 2, 3]) + 0.2
+        objects.append(ModelObject(model=model, local_scaling=batched(np.ones(3, F32)), transform=T,
+                                   double_sided=np.zeros(F, bool)))
+    ang = np.linspace(0, np.pi / 2, F) + rng.uniform(0, 2 * np.pi)
+    pos = centre + np.stack([3.7 * np.cos(ang), 3.7 * np.sin(ang), np.full(F, 1.9)], 1).astype(F32)
+    camera = CameraParameters(viewWidth=np.full(F, 960, np.int32), viewHeight=np.full(F, 540, np.int32),
+                              viewDepth=np.ones(F, F32), near=np.full(F, 0.01, F32), far=np.full(F, 1000.0, F32),
+                              hfov=np.full(F, 58.0, F32), vfov=np.full(F, 32.625, F32), position=pos.astype(F32),
+                              target=centre, up=batched(np.array((0, 0, 1), F32)))
+    return objects, camera, centre.copy()
