@@ -505,7 +505,8 @@ def run_ours(args, rank, world, local):
         "config": dict({
             "workload": wl.desc,
             "form": form + (" (CUDA graph replay)" if form == "tiled" else ""),
-            "tiled_config": {name: [c.tile_w, c.tile_h, int(c.bin_capacity)] for name, r, p in prof["passes"]
+            "tiled_config": {name: [c.tile_w, c.tile_h, int(c.bin_capacity), int(c.small_area)]
+                             for name, r, p in prof["passes"]
                              for c in [r.configs.get(p)] if c is not None},
             "l2": ("inputs larger than L2 (input pools %.2f GB)" % (in_bytes / 1e9)) if not flush else
                   ("L2 flushed between timed steps (a %d MB buffer written; input pools %.1f MB)"

@@ -176,6 +176,11 @@ typedef struct RastTiledConfig {
   int32_t tile_w;          /* tile width along x (buffer axis 0): 8, 16 or 32 */
   int32_t tile_h;          /* tile height along y (buffer axis 1): 8, 16 or 32 */
   uint64_t bin_capacity;   /* total (tile, primitive) bin entries reserved in the workspace */
+  int32_t small_area;      /* 0, or 1..32: faces whose conservative pixel rectangle has at most this
+                              many pixels are rasterised by the setup kernel (64-bit atomicMin of the
+                              packed key per pixel) instead of being binned; ignored while near ties
+                              are counted */
+  int32_t reserved;
 } RastTiledConfig;
 
 /* Workspace bytes rast_render_tiled needs for `batch` under `cfg` (NULL = defaults). */

@@ -130,7 +130,8 @@ class RastProfile(ctypes.Structure):
 
 
 class RastTiledConfig(ctypes.Structure):
-    _fields_ = [("tile_w", c_int32), ("tile_h", c_int32), ("bin_capacity", c_uint64)]
+    _fields_ = [("tile_w", c_int32), ("tile_h", c_int32), ("bin_capacity", c_uint64), ("small_area", c_int32),
+                ("reserved", c_int32)]
 
 
 class RastTiledStats(ctypes.Structure):

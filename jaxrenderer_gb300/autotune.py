@@ -1,7 +1,9 @@
-"""Autotuner of the tiled form: tile shape and bin capacity per workload.
+"""Autotuner of the tiled form: tile shape, small-face path and bin
+capacity per workload.
 
-For a pass (one RastBatch) the candidates 8x8, 16x8, 16x16, 32x8 and 8x32
-(pixels along x by y) are each timed on the batch itself; the fastest wins.
+For a pass (one RastBatch) the tile shapes 8x8, 16x8, 16x16, 32x8 and 8x32
+(pixels along x by y), each with the setup kernel's small-face
+rasterisation off and on, are timed on the batch itself; the fastest wins.
 The bin capacity is then set to 1.25x the bin entries that shape requested.
 Results are cached in a JSON file keyed by (width, height, faces-per-job
 bucket, shader mask, device name, SM count), so a workload class is tuned
@@ -22,6 +24,7 @@ import torch
 from . import _lib
 
 SHAPES = ((8, 8), (16, 8), (16, 16), (32, 8), (8, 32))
+SMALL_AREAS = (0, 32)  # small-face rasterisation in the setup kernel: off, or rectangles up to 32 pixels
 _LOCK = threading.Lock()
 
 
@@ -56,7 +59,7 @@ def workload_key(jobs: np.ndarray, device: torch.device) -> str:
     f = float(jobs["n_faces"].mean())
     bucket = 2 ** int(round(math.log2(max(f, 1.0))))
     mask = int(np.bitwise_or.reduce(1 << jobs["shader"].astype(np.int64)))
-    return f"{w}x{h}|f~{bucket}|jobs~{2 ** int(round(math.log2(max(len(jobs), 1))))}|mask{mask}|{props.name}|sm{props.multi_processor_count}"
+    return f"v2|{w}x{h}|f~{bucket}|jobs~{2 ** int(round(math.log2(max(len(jobs), 1))))}|mask{mask}|{props.name}|sm{props.multi_processor_count}"
 
 
 def _time(runner, name, b, cfg, reps=3) -> float:
@@ -86,20 +89,22 @@ def tiled_config_for(runner, name: str, b, jobs: np.ndarray) -> "_lib.RastTiledC
         cache = _load()
         hit = cache.get(key)
     if hit is not None:
-        return _lib.RastTiledConfig(int(hit["tile_w"]), int(hit["tile_h"]), int(hit["bin_capacity"]))
+        return _lib.RastTiledConfig(int(hit["tile_w"]), int(hit["tile_h"]), int(hit["bin_capacity"]),
+                                    int(hit.get("small_area", 0)))
     best = None
     for tw, th in SHAPES:
-        cfg = _lib.RastTiledConfig(tw, th, 0)
-        ms, entries = _time(runner, name, b, cfg)
-        if best is None or ms < best[0]:
-            best = (ms, tw, th, entries)
-    ms, tw, th, entries = best
+        for small in SMALL_AREAS:
+            cfg = _lib.RastTiledConfig(tw, th, 0, small)
+            ms, entries = _time(runner, name, b, cfg)
+            if best is None or ms < best[0]:
+                best = (ms, tw, th, entries, small)
+    ms, tw, th, entries, small = best
     cap = int(entries * 1.25) + 4096
     with _LOCK:
         cache = _load()
-        cache[key] = {"tile_w": tw, "tile_h": th, "bin_capacity": cap, "ms": ms}
+        cache[key] = {"tile_w": tw, "tile_h": th, "bin_capacity": cap, "small_area": small, "ms": ms}
         _store(cache)
-    return _lib.RastTiledConfig(tw, th, cap)
+    return _lib.RastTiledConfig(tw, th, cap, small)
 
 
-__all__ = ["tiled_config_for", "workload_key", "cache_path", "SHAPES"]
+__all__ = ["tiled_config_for", "workload_key", "cache_path", "SHAPES", "SMALL_AREAS"]

@@ -28,6 +28,7 @@ namespace tiled {
 constexpr int kSetupThreads = 256;
 constexpr int kScanBlock = 1024;       // elements per scan block (256 threads x 4)
 constexpr int kRasterWarps = 4;        // warps per CTA of the raster kernel
+constexpr int kTileChunk = 1;          // tiles a raster warp takes per atomic
 constexpr int kStage = 32;             // bin entries staged per warp round
 constexpr uint32_t kOverflow = 0x80000000u;
 
@@ -47,6 +48,16 @@ __host__ __device__ inline int ceil_div(int a, int b) { return (a + b - 1) / b; 
 // S -> E a stage passes on the crossing point S + t (E - S),
 // t = d_S / (d_S - d_E), when the edge crosses its line, then E when
 // d_E >= 0; the closing edge (last -> first) is passed at the end.
+// Crossing parameter t = d0 / (d0 - d1) of an edge whose ends lie on
+// opposite sides (so d0 - d1 != 0).  The fast quotient (2 ulp) moves the
+// crossing point by far less than the pixel the box is widened by; outside
+// the range where it is accurate the IEEE quotient is used.
+__device__ __forceinline__ float clip_t(float d0, float d1) {
+  const float den = d0 - d1;
+  const float a = fabsf(den);
+  return (a > 1e-30f && a < 1e30f) ? __fdividef(d0, den) : d0 / den;
+}
+
 struct ClipBox {
   float mnx, mxx, mny, mxy;
   int n;
@@ -70,7 +81,7 @@ __device__ __forceinline__ void clip_push2(ClipStage& s, ClipBox& box, float x, 
   const float d = s.a * x + s.b * y + s.c;
   if (s.any) {
     if ((s.sd >= 0.0f) != (d >= 0.0f)) {
-      const float t = s.sd / (s.sd - d);  // no cancellation: opposite signs
+      const float t = clip_t(s.sd, d);
       clip_sink(box, s.sx + t * (x - s.sx), s.sy + t * (y - s.sy));
     }
     if (d >= 0.0f) clip_sink(box, x, y);
@@ -84,7 +95,7 @@ __device__ __forceinline__ void clip_push1(ClipStage& s, ClipStage& s2, ClipBox&
   const float d = s.a * x + s.b * y + s.c;
   if (s.any) {
     if ((s.sd >= 0.0f) != (d >= 0.0f)) {
-      const float t = s.sd / (s.sd - d);
+      const float t = clip_t(s.sd, d);
       clip_push2(s2, box, s.sx + t * (x - s.sx), s.sy + t * (y - s.sy));
     }
     if (d >= 0.0f) clip_push2(s2, box, x, y);
@@ -99,7 +110,7 @@ __device__ __forceinline__ void clip_push0(ClipStage& s, ClipStage& s1, ClipStag
   const float d = s.a * x + s.b * y + s.c;
   if (s.any) {
     if ((s.sd >= 0.0f) != (d >= 0.0f)) {
-      const float t = s.sd / (s.sd - d);
+      const float t = clip_t(s.sd, d);
       clip_push1(s1, s2, box, s.sx + t * (x - s.sx), s.sy + t * (y - s.sy));
     }
     if (d >= 0.0f) clip_push1(s1, s2, box, x, y);
@@ -115,26 +126,45 @@ __device__ __forceinline__ void clip_push0(ClipStage& s, ClipStage& s1, ClipStag
 // every side, in NDC) against c_k >= -eps_k, where eps_k is 64x the rounding
 // bound of the three-operation evaluation of c_k, then widening the bounding
 // box by one pixel.  Returns false when no pixel can be covered.
-__device__ __forceinline__ bool coverage_bbox(const float* inv, const RastJob& J, int* i0, int* i1,
-                                              int* j0, int* j1) {
+// The job's screen rectangle one pixel wider on every side, in NDC (pixels
+// -1 and W), computed once per block.
+struct ScreenRect {
+  float xl, xh, yl, yh, X, Y;
+  bool ok;  // finite, non-degenerate viewport
+};
+
+__device__ __forceinline__ ScreenRect screen_rect(const RastJob& J) {
+  ScreenRect r{};
+  const float sx = J.viewport[0], ox = J.viewport[3];
+  const float sy = J.viewport[5], oy = J.viewport[7];
+  r.ok = (sx != 0.0f) && (sy != 0.0f) && isfinite(sx) && isfinite(sy);
+  const float xa = (-1.0f - ox) / sx, xb = (static_cast<float>(J.width) - ox) / sx;
+  const float ya = (-1.0f - oy) / sy, yb = (static_cast<float>(J.height) - oy) / sy;
+  r.xl = fminf(xa, xb);
+  r.xh = fmaxf(xa, xb);
+  r.yl = fminf(ya, yb);
+  r.yh = fmaxf(ya, yb);
+  r.X = fmaxf(fabsf(r.xl), fabsf(r.xh));
+  r.Y = fmaxf(fabsf(r.yl), fabsf(r.yh));
+  return r;
+}
+
+__device__ __forceinline__ bool coverage_bbox(const float* inv, const RastJob& J, const ScreenRect& R, int* i0,
+                                              int* i1, int* j0, int* j1) {
   const int W = J.width, H = J.height;
   const float sx = J.viewport[0], ox = J.viewport[3];
   const float sy = J.viewport[5], oy = J.viewport[7];
   bool finite = true;
 #pragma unroll
   for (int k = 0; k < 9; ++k) finite = finite && isfinite(inv[k]);
-  if (!finite || !(sx != 0.0f) || !(sy != 0.0f) || !isfinite(sx) || !isfinite(sy)) {
+  if (!finite || !R.ok) {
     *i0 = 0;
     *i1 = W - 1;
     *j0 = 0;
     *j1 = H - 1;
     return true;  // cannot bound: every pixel of the job
   }
-  // NDC of pixels -1 and W (one pixel outside the screen on each side)
-  const float xa = (-1.0f - ox) / sx, xb = (static_cast<float>(W) - ox) / sx;
-  const float ya = (-1.0f - oy) / sy, yb = (static_cast<float>(H) - oy) / sy;
-  const float xl = fminf(xa, xb), xh = fmaxf(xa, xb), yl = fminf(ya, yb), yh = fmaxf(ya, yb);
-  const float X = fmaxf(fabsf(xl), fabsf(xh)), Y = fmaxf(fabsf(yl), fabsf(yh));
+  const float xl = R.xl, xh = R.xh, yl = R.yl, yh = R.yh, X = R.X, Y = R.Y;
   // edge k: a_k x + b_k y + (c_k + eps_k), kept in scalars (no arrays: the
   // clip stages below capture them)
   bool small = true;  // |c_k| < 1e37 on the rectangle: no overflow below
@@ -246,86 +276,164 @@ __device__ __forceinline__ void warp_tiles(int tx0, int ty0, int tx1, int ty1, i
   }
 }
 
-// Phase 1, one thread per face: clip positions, determinant, keep/front
-// flags and inverse -> setup record.  Candidates (kept, front-facing) are
-// queued in shared memory; phase 2, one thread per queued candidate:
-// conservative coverage rectangle -> bbox, then the warp adds the tile counts
-// with one atomic per distinct tile per round (lanes hitting the same tile
-// are merged with __match_any_sync).
+// Phase 1, one thread per face: clip positions, determinant and keep/front
+// flags (written for every face).  Candidates (kept, front-facing) and face
+// 0 (the chooser's fallback, whose record is read even when it is not a
+// candidate) are queued in shared memory with their [x, y, w] clip rows and
+// depths.  Phase 2, one thread per queued face, so culled faces leave no idle
+// lanes: the LU inverse -> setup record, and for candidates a conservative
+// coverage rectangle.  Rectangles of at most kSmallArea pixels (when near
+// ties are not counted) go to a second queue; the others are binned: the
+// warp adds their tile counts with one atomic per distinct tile per round
+// (lanes hitting the same tile merged with __match_any_sync).  Phase 3, one
+// warp per queued small face, one lane per pixel of its rectangle: the
+// raster kernel's edge tests and depth, folded into the per-pixel minimum of
+// the packed (depth | id) keys with a 64-bit atomicMin.
 // Grid: one block per kSetupThreads faces of a job (face block map).
+constexpr int kRecordOnly = static_cast<int>(0x80000000u);  // queued for its record, not binned
+constexpr int kSmallArea = 32;                               // largest small rectangle: one pixel per lane
+constexpr int kTableMax = 1024;                              // pixel -> NDC tables kept in shared memory
+
+template <bool kSmall>
 __global__ void __launch_bounds__(kSetupThreads)
 setup_bin_kernel(RastBatch B, Geometry G, const int2* __restrict__ fmap, float4* __restrict__ setup,
-                 ushort4* __restrict__ bbox, uint32_t* __restrict__ counts) {
+                 ushort4* __restrict__ bbox, uint32_t* __restrict__ counts, unsigned long long* __restrict__ keys,
+                 int small_area) {
   __shared__ RastJob sJ;
-  __shared__ float s_inv[9][kSetupThreads];
+  __shared__ float s_m[12][kSetupThreads];
   __shared__ int s_face[kSetupThreads];
-  __shared__ int s_qn;
+  constexpr int kQ = kSmall ? kSetupThreads : 1;  // small-path arrays only where used
+  constexpr int kT = kSmall ? kTableMax : 1;
+  __shared__ float s_small[12][kQ];  // inverse (9) and clip depths (3) of small faces
+  __shared__ int s_sface[kQ];
+  __shared__ int s_srect[kQ][2];     // i0 | i1 << 16, j0 | j1 << 16
+  __shared__ float s_xs[kT], s_ys[kT];
+  __shared__ int s_qn, s_sn;
+  __shared__ ScreenRect s_rect;
   const int2 blk = fmap[blockIdx.x];
   if (blk.x < 0) return;
   const int jid = blk.x;
   const int nf = __ldg(&B.jobs[jid].n_faces);
   load_job_to_shared(B.jobs + jid, &sJ);
-  if (threadIdx.x == 0) s_qn = 0;
+  if (threadIdx.x == 0) s_qn = s_sn = 0;
   __syncthreads();
   const RastJob& J = sJ;
+  const float sx = J.viewport[0], ox = J.viewport[3], sy = J.viewport[5], oy = J.viewport[7];
+  const bool tables = kSmall && J.width <= kTableMax && J.height <= kTableMax;
+  if (tables) {  // the same quotients the raster kernel computes per pixel
+    for (int i = threadIdx.x; i < J.width; i += kSetupThreads) s_xs[i] = (static_cast<float>(i) - ox) / sx;
+    for (int j = threadIdx.x; j < J.height; j += kSetupThreads) s_ys[j] = (static_cast<float>(j) - oy) / sy;
+  }
+  if (threadIdx.x == 0) s_rect = screen_rect(J);  // read after the queue's barrier
   const int f = blk.y + static_cast<int>(threadIdx.x);
-  bool cand = false;
-  float inv[9];
+  bool queued = false, cand = false;
+  float m[12];
   if (f < nf) {
     const int64_t row = J.setup_begin + f;
     float4 c[3];
     face_clip(J, B.pools, f, c);
-    float det;
-    int flags;
-    setup_from_clip(c, inv, &det, &flags);
-    float4* out = setup + row * 4;
-    cand = (flags & kCandidate) == kCandidate;
-    // the inverse is read only for candidates (raster) and for face 0 (the
-    // chooser's fallback); the flags of every face are kept
-    if (cand || f == 0) {
-      out[0] = make_float4(inv[0], inv[1], inv[2], inv[3]);
-      out[1] = make_float4(inv[4], inv[5], inv[6], inv[7]);
-      out[2] = make_float4(inv[8], c[0].z, c[1].z, c[2].z);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      m[3 * k + 0] = c[k].x;
+      m[3 * k + 1] = c[k].y;
+      m[3 * k + 2] = c[k].w;
+      m[9 + k] = c[k].z;
     }
-    out[3] = make_float4(det, __int_as_float(flags), 0.0f, 0.0f);
+    const float det = det3(m);
+    int flags = 0;
+    if (fabsf(det) > 1e-6f) flags |= kKeep;
+    if (det >= 0.0f) flags |= kFront;
+    setup[row * 4 + 3] = make_float4(det, __int_as_float(flags), 0.0f, 0.0f);
+    cand = (flags & kCandidate) == kCandidate;
+    queued = cand || f == 0;
     if (!cand) bbox[row] = make_ushort4(1, 1, 0, 0);  // empty: lo > hi
   }
-  const unsigned m = __ballot_sync(0xffffffffu, cand);
+  const unsigned qm = __ballot_sync(0xffffffffu, queued);
   int base = 0;
-  if ((threadIdx.x & 31) == 0 && m) base = atomicAdd(&s_qn, __popc(m));
+  if ((threadIdx.x & 31) == 0 && qm) base = atomicAdd(&s_qn, __popc(qm));
   base = __shfl_sync(0xffffffffu, base, 0);
-  if (cand) {
-    const int q = base + __popc(m & lanemask_lt());
-    s_face[q] = f;
+  if (queued) {
+    const int q = base + __popc(qm & lanemask_lt());
+    s_face[q] = cand ? f : (f | kRecordOnly);
 #pragma unroll
-    for (int k = 0; k < 9; ++k) s_inv[k][q] = inv[k];
+    for (int k = 0; k < 12; ++k) s_m[k][q] = m[k];
   }
   __syncthreads();
   const int qn = s_qn;
-  if (static_cast<int>(threadIdx.x & ~31u) >= qn) return;  // the whole warp is past the queue
   const int q = threadIdx.x;
-  int tx0 = 1, ty0 = 1, tx1 = 0, ty1 = 0;
-  if (q < qn) {
-    const int fq = s_face[q];
+  if (static_cast<int>(threadIdx.x & ~31u) < qn) {  // warps holding queued faces
+    int tx0 = 1, ty0 = 1, tx1 = 0, ty1 = 0;
+    bool small = false;
+    int fq = 0, i0 = 0, i1 = 0, j0 = 0, j1 = 0;
     float iv[9];
+    if (q < qn) {
+      const int entry = s_face[q];
+      fq = entry & ~kRecordOnly;
+      float mq[9];
 #pragma unroll
-    for (int k = 0; k < 9; ++k) iv[k] = s_inv[k][q];
-    int i0, i1, j0, j1;
-    ushort4 bb = make_ushort4(1, 1, 0, 0);
-    if (coverage_bbox(iv, J, &i0, &i1, &j0, &j1)) {
-      tx0 = i0 / G.tw;
-      tx1 = i1 / G.tw;
-      ty0 = j0 / G.th;
-      ty1 = j1 / G.th;
-      bb = make_ushort4(tx0, ty0, tx1, ty1);
+      for (int k = 0; k < 9; ++k) mq[k] = s_m[k][q];
+      inv3(mq, iv);
+      float4* out = setup + (J.setup_begin + fq) * 4;
+      out[0] = make_float4(iv[0], iv[1], iv[2], iv[3]);
+      out[1] = make_float4(iv[4], iv[5], iv[6], iv[7]);
+      out[2] = make_float4(iv[8], s_m[9][q], s_m[10][q], s_m[11][q]);
+      if (!(entry & kRecordOnly)) {
+        ushort4 bb = make_ushort4(1, 1, 0, 0);
+        if (coverage_bbox(iv, J, s_rect, &i0, &i1, &j0, &j1)) {
+          if (kSmall && (i1 - i0 + 1) * (j1 - j0 + 1) <= small_area) {
+            small = true;  // rasterised in phase 3, not binned
+          } else {
+            tx0 = i0 / G.tw;
+            tx1 = i1 / G.tw;
+            ty0 = j0 / G.th;
+            ty1 = j1 / G.th;
+            bb = make_ushort4(tx0, ty0, tx1, ty1);
+          }
+        }
+        bbox[J.setup_begin + fq] = bb;
+      }
     }
-    bbox[J.setup_begin + fq] = bb;
+    const unsigned sm = kSmall ? __ballot_sync(0xffffffffu, small) : 0u;
+    int sbase = 0;
+    if ((threadIdx.x & 31) == 0 && sm) sbase = atomicAdd(&s_sn, __popc(sm));
+    if (kSmall) sbase = __shfl_sync(0xffffffffu, sbase, 0);
+    if (kSmall && small) {
+      const int e = sbase + __popc(sm & lanemask_lt());
+      s_sface[e] = fq;
+#pragma unroll
+      for (int k = 0; k < 9; ++k) s_small[k][e] = iv[k];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) s_small[9 + k][e] = s_m[9 + k][q];
+      s_srect[e][0] = i0 | (i1 << 16);
+      s_srect[e][1] = j0 | (j1 << 16);
+    }
+    uint32_t* cnt = counts + static_cast<int64_t>(jid) * G.tiles_per_job;
+    warp_tiles(tx0, ty0, tx1, ty1, G.tiles_x, [&](int, int tile, bool valid) {
+      const unsigned peers = __match_any_sync(0xffffffffu, valid ? tile : -1);
+      if (valid && __popc(peers & lanemask_lt()) == 0) atomicAdd(cnt + tile, static_cast<unsigned>(__popc(peers)));
+    });
   }
-  uint32_t* cnt = counts + static_cast<int64_t>(jid) * G.tiles_per_job;
-  warp_tiles(tx0, ty0, tx1, ty1, G.tiles_x, [&](int, int tile, bool valid) {
-    const unsigned peers = __match_any_sync(0xffffffffu, valid ? tile : -1);
-    if (valid && __popc(peers & lanemask_lt()) == 0) atomicAdd(cnt + tile, static_cast<unsigned>(__popc(peers)));
-  });
+  if (!kSmall) return;  // no small path: nothing below (no barrier follows)
+  __syncthreads();
+  const int sn = s_sn;
+  const int lane = threadIdx.x & 31;
+  const float vp22 = J.viewport[10], vp23 = J.viewport[11];
+  for (int e = threadIdx.x >> 5; e < sn; e += kSetupThreads / 32) {
+    const int ri = s_srect[e][0], rj = s_srect[e][1];
+    const int a0 = ri & 0xffff, b0 = rj & 0xffff;
+    const int bw = (ri >> 16) - a0 + 1, bh = (rj >> 16) - b0 + 1;
+    if (lane >= bw * bh) continue;
+    const int i = a0 + lane % bw, j = b0 + lane / bw;
+    const float x = tables ? s_xs[i] : (static_cast<float>(i) - ox) / sx;
+    const float y = tables ? s_ys[j] : (static_cast<float>(j) - oy) / sy;
+    const float c0 = (x * s_small[0][e] + y * s_small[3][e]) + s_small[6][e];
+    const float c1 = (x * s_small[1][e] + y * s_small[4][e]) + s_small[7][e];
+    const float c2 = (x * s_small[2][e] + y * s_small[5][e]) + s_small[8][e];
+    if (all_nonneg(c0, c1, c2)) {
+      const float z = ((c0 * s_small[9][e] + c1 * s_small[10][e]) + c2 * s_small[11][e]) * vp22 + vp23;
+      atomicMin(keys + J.pixel_begin + static_cast<int64_t>(i) * J.height + j, pack_key(z, s_sface[e]));
+    }
+  }
 }
 
 // Block-local exclusive scan of counts -> offsets, block sums out.
@@ -436,12 +544,13 @@ scatter_kernel(RastBatch B, Geometry G, const int2* __restrict__ fmap, const ush
 // slice of shared memory (one record per lane), then every lane tests its
 // pixels against the 32 staged setups.  Tiles whose bin overflowed scan
 // every primitive of the job instead.
-template <int TW, int TH>
+template <int TW, int TH, bool kKeys>
 __global__ void __launch_bounds__(32 * kRasterWarps)
 raster_kernel(RastBatch B, Geometry G, const float4* __restrict__ setup,
               const uint32_t* __restrict__ counts, const uint32_t* __restrict__ offsets,
               const int32_t* __restrict__ bins, int32_t* __restrict__ winner,
-              unsigned int* __restrict__ work, int64_t n_tiles, unsigned char* __restrict__ visible) {
+              unsigned int* __restrict__ work, int64_t n_tiles, unsigned char* __restrict__ visible,
+              const unsigned long long* __restrict__ keys) {
   constexpr int PPL = TW * TH / 32;
   __shared__ float4 s_rec[kRasterWarps][kStage][3];
   __shared__ int s_id[kRasterWarps][kStage];
@@ -449,10 +558,17 @@ raster_kernel(RastBatch B, Geometry G, const float4* __restrict__ setup,
   float4 (*rec)[3] = s_rec[warp];
   int* ids = s_id[warp];
   unsigned long long tie_count = 0;
+  unsigned int chunk = 0;
+  int taken = kTileChunk;  // tiles of the current chunk already processed
   while (true) {
-    unsigned int t = 0;
-    if (lane == 0) t = atomicAdd(work, 1u);
-    t = __shfl_sync(0xffffffffu, t, 0);
+    // tiles are taken kTileChunk at a time: one atomic on the shared
+    // counter per chunk instead of per tile
+    if (taken == kTileChunk) {
+      if (lane == 0) chunk = atomicAdd(work, static_cast<unsigned>(kTileChunk));
+      chunk = __shfl_sync(0xffffffffu, chunk, 0);
+      taken = 0;
+    }
+    const unsigned int t = chunk + taken++;
     if (t >= n_tiles) break;
     const int jid = static_cast<int>(t / G.tiles_per_job);
     const int local = static_cast<int>(t % G.tiles_per_job);
@@ -471,10 +587,13 @@ raster_kernel(RastBatch B, Geometry G, const float4* __restrict__ setup,
     float x[PPL], best_z[PPL];
     unsigned long long best[PPL];
     uint32_t second[PPL];
+    unsigned z_known = 0;  // bit q: best_z[q] holds the depth of best[q] (set by this kernel's tests)
 #pragma unroll
     for (int q = 0; q < PPL; ++q) {
-      x[q] = (static_cast<float>(tx * TW + q * LPC + lane / TH) - ox) / sx;
-      best[q] = kEmptyKey;
+      const int pi = tx * TW + q * LPC + lane / TH;
+      x[q] = (static_cast<float>(pi) - ox) / sx;
+      // the minimum over the faces the setup kernel rasterised itself
+      best[q] = (kKeys && pi < W && pj < H) ? keys[J.pixel_begin + static_cast<int64_t>(pi) * H + pj] : kEmptyKey;
       best_z[q] = 0.0f;
       second[q] = 0xffffffffu;
     }
@@ -528,6 +647,7 @@ raster_kernel(RastBatch B, Geometry G, const float4* __restrict__ setup,
                 second[q] = min(second[q], static_cast<uint32_t>(best[q] >> 32));
                 best[q] = key;
                 best_z[q] = z;
+                z_known |= 1u << q;
               } else {
                 second[q] = min(second[q], static_cast<uint32_t>(key >> 32));
               }
@@ -560,6 +680,16 @@ raster_kernel(RastBatch B, Geometry G, const float4* __restrict__ setup,
         bool keep = found;
         float z = best_z[q];
         int prim = found ? static_cast<int>(best[q] & 0xffffffffu) : 0;
+        if (kKeys && found && !(z_known & (1u << q))) {
+          // the winner came from the setup kernel's own rasterisation: its
+          // depth again, with the same operations
+          const float4* r = jrec + static_cast<int64_t>(prim) * 4;
+          const float4 a = __ldg(r), b = __ldg(r + 1), cz = __ldg(r + 2);
+          const float c0 = (x[q] * a.x + y * a.w) + b.z;
+          const float c1 = (x[q] * a.y + y * b.x) + b.w;
+          const float c2 = (x[q] * a.z + y * b.y) + cz.x;
+          z = ((c0 * cz.y + c1 * cz.z) + c2 * cz.w) * vp22 + vp23;
+        }
         if (!found && J.n_faces > 0) {
           const float4 a = __ldg(jrec), b = __ldg(jrec + 1), cz = __ldg(jrec + 2), d = __ldg(jrec + 3);
           const float c0 = (x[q] * a.x + y * a.w) + b.z;
@@ -625,7 +755,7 @@ face_varyings_kernel(RastBatch B, const int2* __restrict__ fmap, const unsigned 
 // Deferred shading: one thread per pixel of every job, reading the winner's
 // corner varyings computed once per visible face.
 // Grid: (ceil(max pixels per job / 256), n_jobs).
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 4)  // 4 blocks per SM: 64 registers
 tiled_shade_kernel(RastBatch B, const float4* __restrict__ setup, const int32_t* __restrict__ winner,
                    bool depth_resolved, const float* __restrict__ fvar, int vstride) {
   __shared__ RastJob sJ;
@@ -658,15 +788,16 @@ inline uint64_t default_bin_capacity(const RastBatch& b) {
 
 struct Layout {
   size_t setup_off, bbox_off, counts_off, offsets_off, cursors_off, bsums_off, bins_off, winner_off,
-      vis_off, fvar_off, fmap_off, fstart_off, misc_off, total;
+      vis_off, fvar_off, fmap_off, fstart_off, keys_off, misc_off, total;
   unsigned fmap_blocks;
+  bool small_path;  // setup kernel rasterises small faces (not when near ties are counted)
   int vstride;
   int64_t n_tiles, n_scan_blocks;
   uint64_t bin_capacity;
   Geometry G;
 };
 
-static Layout layout(const RastBatch& b, TileShape ts, uint64_t bin_capacity) {
+static Layout layout(const RastBatch& b, TileShape ts, uint64_t bin_capacity, int small_area) {
   Layout L{};
   L.G.tw = ts.tw;
   L.G.th = ts.th;
@@ -700,14 +831,45 @@ static Layout layout(const RastBatch& b, TileShape ts, uint64_t bin_capacity) {
   L.fmap_blocks = block_map_capacity(b.total_setup, b.n_jobs, kSetupThreads);
   L.fmap_off = take(static_cast<size_t>(L.fmap_blocks) * sizeof(int2));
   L.fstart_off = take(block_start_bytes(b.n_jobs));
+  L.small_path = b.near_ties == nullptr && small_area > 0;
+  L.keys_off = take(L.small_path ? static_cast<size_t>(b.total_pixels) * sizeof(unsigned long long) : 0);
   L.misc_off = take(256);
   L.total = off;
   return L;
 }
 
+// The small-face threshold of a config (0 = off), clamped to one warp's lanes.
+static int small_area_of(const RastTiledConfig* cfg) {
+  if (!cfg || cfg->small_area <= 0) return 0;
+  return std::min(cfg->small_area, kSmallArea);
+}
+
 static bool valid_shape(TileShape t) {
   return (t.tw == 8 && t.th == 8) || (t.tw == 16 && t.th == 16) || (t.tw == 32 && t.th == 8) ||
          (t.tw == 8 && t.th == 32) || (t.tw == 16 && t.th == 8);
+}
+
+template <bool kKeys>
+static void launch_raster(TileShape ts, unsigned grid, cudaStream_t s, const RastBatch& b, const Layout& L,
+                          const float4* setup, const uint32_t* counts, const uint32_t* offsets, const int32_t* bins,
+                          int32_t* winner, unsigned int* misc, unsigned char* vis,
+                          const unsigned long long* keys) {
+  const unsigned block = 32 * kRasterWarps;
+  if (ts.tw == 8 && ts.th == 8)
+    raster_kernel<8, 8, kKeys><<<grid, block, 0, s>>>(b, L.G, setup, counts, offsets, bins, winner, misc, L.n_tiles,
+                                                      vis, keys);
+  else if (ts.tw == 16 && ts.th == 16)
+    raster_kernel<16, 16, kKeys><<<grid, block, 0, s>>>(b, L.G, setup, counts, offsets, bins, winner, misc,
+                                                        L.n_tiles, vis, keys);
+  else if (ts.tw == 32 && ts.th == 8)
+    raster_kernel<32, 8, kKeys><<<grid, block, 0, s>>>(b, L.G, setup, counts, offsets, bins, winner, misc,
+                                                       L.n_tiles, vis, keys);
+  else if (ts.tw == 8 && ts.th == 32)
+    raster_kernel<8, 32, kKeys><<<grid, block, 0, s>>>(b, L.G, setup, counts, offsets, bins, winner, misc,
+                                                       L.n_tiles, vis, keys);
+  else
+    raster_kernel<16, 8, kKeys><<<grid, block, 0, s>>>(b, L.G, setup, counts, offsets, bins, winner, misc,
+                                                       L.n_tiles, vis, keys);
 }
 
 static int render(const RastBatch* batch, const RastTiledConfig* cfg, void* workspace,
@@ -718,7 +880,8 @@ static int render(const RastBatch* batch, const RastTiledConfig* cfg, void* work
   TileShape ts{cfg ? cfg->tile_w : 8, cfg ? cfg->tile_h : 8};
   if (!valid_shape(ts)) return RAST_ERR_INVALID_ARGUMENT;
   const uint64_t cap = cfg && cfg->bin_capacity > 0 ? cfg->bin_capacity : default_bin_capacity(b);
-  const Layout L = layout(b, ts, cap);
+  const int small_area = small_area_of(cfg);
+  const Layout L = layout(b, ts, cap, small_area);
   if (workspace_bytes < L.total) return RAST_ERR_WORKSPACE_TOO_SMALL;
   if (L.total > 0 && (workspace == nullptr || (reinterpret_cast<uintptr_t>(workspace) & 255)))
     return RAST_ERR_INVALID_ARGUMENT;
@@ -739,6 +902,13 @@ static int render(const RastBatch* batch, const RastTiledConfig* cfg, void* work
   // counts and cursors are adjacent: one memset clears both, plus the counters
   if (cudaMemsetAsync(counts, 0, L.offsets_off - L.counts_off, s) != cudaSuccess) return RAST_ERR_CUDA;
   if (cudaMemsetAsync(misc, 0, 256, s) != cudaSuccess) return RAST_ERR_CUDA;
+  unsigned long long* keys = nullptr;
+  if (L.small_path && b.total_pixels > 0 && b.total_setup > 0) {
+    keys = reinterpret_cast<unsigned long long*>(ws + L.keys_off);
+    if (cudaMemsetAsync(keys, 0xff, static_cast<size_t>(b.total_pixels) * sizeof(unsigned long long), s) !=
+        cudaSuccess)  // every key starts as kEmptyKey
+      return RAST_ERR_CUDA;
+  }
   unsigned char* vis = L.vstride > 0 ? reinterpret_cast<unsigned char*>(ws + L.vis_off) : nullptr;
   float* fvar = L.vstride > 0 ? reinterpret_cast<float*>(ws + L.fvar_off) : nullptr;
   if (vis && b.total_setup > 0 && cudaMemsetAsync(vis, 0, static_cast<size_t>(b.total_setup), s) != cudaSuccess)
@@ -751,7 +921,10 @@ static int render(const RastBatch* batch, const RastTiledConfig* cfg, void* work
       return RAST_ERR_CUDA;
     prof.mark("block_map_kernel");
     const unsigned grid = L.fmap_blocks;
-    setup_bin_kernel<<<grid, kSetupThreads, 0, s>>>(b, L.G, fmap, setup, bbox, counts);
+    if (keys)
+      setup_bin_kernel<true><<<grid, kSetupThreads, 0, s>>>(b, L.G, fmap, setup, bbox, counts, keys, small_area);
+    else
+      setup_bin_kernel<false><<<grid, kSetupThreads, 0, s>>>(b, L.G, fmap, setup, bbox, counts, nullptr, 0);
     prof.mark("setup_bin_kernel");
     scan_local_kernel<<<static_cast<unsigned>(L.n_scan_blocks), 256, 0, s>>>(counts, offsets, bsums, L.n_tiles);
     scan_apply_kernel<<<static_cast<unsigned>(L.n_scan_blocks), 256, 0, s>>>(counts, offsets, bsums, L.n_tiles,
@@ -766,16 +939,10 @@ static int render(const RastBatch* batch, const RastTiledConfig* cfg, void* work
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (b.total_setup > 0) {
       const unsigned grid = static_cast<unsigned>(std::max(sms, 1) * 8);
-      if (ts.tw == 8 && ts.th == 8)
-        raster_kernel<8, 8><<<grid, 32 * kRasterWarps, 0, s>>>(b, L.G, setup, counts, offsets, bins, winner, misc, L.n_tiles, vis);
-      else if (ts.tw == 16 && ts.th == 16)
-        raster_kernel<16, 16><<<grid, 32 * kRasterWarps, 0, s>>>(b, L.G, setup, counts, offsets, bins, winner, misc, L.n_tiles, vis);
-      else if (ts.tw == 32 && ts.th == 8)
-        raster_kernel<32, 8><<<grid, 32 * kRasterWarps, 0, s>>>(b, L.G, setup, counts, offsets, bins, winner, misc, L.n_tiles, vis);
-      else if (ts.tw == 8 && ts.th == 32)
-        raster_kernel<8, 32><<<grid, 32 * kRasterWarps, 0, s>>>(b, L.G, setup, counts, offsets, bins, winner, misc, L.n_tiles, vis);
+      if (keys)
+        launch_raster<true>(ts, grid, s, b, L, setup, counts, offsets, bins, winner, misc, vis, keys);
       else
-        raster_kernel<16, 8><<<grid, 32 * kRasterWarps, 0, s>>>(b, L.G, setup, counts, offsets, bins, winner, misc, L.n_tiles, vis);
+        launch_raster<false>(ts, grid, s, b, L, setup, counts, offsets, bins, winner, misc, vis, nullptr);
     } else {
       if (cudaMemsetAsync(winner, 0xff, static_cast<size_t>(b.total_pixels) * 4, s) != cudaSuccess)
         return RAST_ERR_CUDA;
@@ -808,7 +975,7 @@ extern "C" size_t rast_tiled_workspace_bytes(const RastBatch* batch, const RastT
   if (!batch) return 0;
   tiled::TileShape ts{cfg ? cfg->tile_w : 8, cfg ? cfg->tile_h : 8};
   const uint64_t cap = cfg && cfg->bin_capacity > 0 ? cfg->bin_capacity : tiled::default_bin_capacity(*batch);
-  return tiled::layout(*batch, ts, cap).total;
+  return tiled::layout(*batch, ts, cap, tiled::small_area_of(cfg)).total;
 }
 
 extern "C" int rast_tiled_stats(const RastBatch* batch, const RastTiledConfig* cfg, const void* workspace,
@@ -816,7 +983,7 @@ extern "C" int rast_tiled_stats(const RastBatch* batch, const RastTiledConfig* c
   if (!batch || !workspace || !out) return RAST_ERR_INVALID_ARGUMENT;
   tiled::TileShape ts{cfg ? cfg->tile_w : 8, cfg ? cfg->tile_h : 8};
   const uint64_t cap = cfg && cfg->bin_capacity > 0 ? cfg->bin_capacity : tiled::default_bin_capacity(*batch);
-  const tiled::Layout L = tiled::layout(*batch, ts, cap);
+  const tiled::Layout L = tiled::layout(*batch, ts, cap, tiled::small_area_of(cfg));
   unsigned int misc[4] = {0, 0, 0, 0};
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   if (cudaMemcpyAsync(misc, static_cast<const char*>(workspace) + L.misc_off, sizeof(misc),

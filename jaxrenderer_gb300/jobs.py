@@ -318,12 +318,12 @@ def render_plain(packed: PackedBatch, stream: Optional[torch.cuda.Stream] = None
 
 
 def render_tiled(packed: PackedBatch, tile=(8, 8), bin_capacity: int = 0,
-                 stream: Optional[torch.cuda.Stream] = None) -> "_lib.RastTiledStats":
+                 stream: Optional[torch.cuda.Stream] = None, small_area: int = 0) -> "_lib.RastTiledStats":
     """Run the tiled form on a packed batch; returns its bin statistics
     (reading them synchronises the stream)."""
     lib = _lib.load()
     b = packed.batch
-    cfg = _lib.RastTiledConfig(int(tile[0]), int(tile[1]), int(bin_capacity))
+    cfg = _lib.RastTiledConfig(int(tile[0]), int(tile[1]), int(bin_capacity), int(small_area))
     nbytes = lib.rast_tiled_workspace_bytes(ctypes.byref(b), ctypes.byref(cfg))
     dev = packed.zbuffer.device
     ws = torch.empty(max(int(nbytes), 256), dtype=torch.uint8, device=dev)

@@ -17,9 +17,9 @@ F32 = np.float32
 SHAPES = [(8, 8), (16, 8), (16, 16), (32, 8), (8, 32)]
 
 
-def _tiled_job(spec, z0, c0, device, tile=(8, 8), cap=0, ties=False):
+def _tiled_job(spec, z0, c0, device, tile=(8, 8), cap=0, ties=False, small=0):
     packed = pack([spec], [z0], [c0], device, count_ties=ties)
-    stats = render_tiled(packed, tile=tile, bin_capacity=cap)
+    stats = render_tiled(packed, tile=tile, bin_capacity=cap, small_area=small)
     z, c, p = unpack(packed, [spec])[0]
     return z, c, p, packed.near_ties, stats
 
@@ -33,6 +33,17 @@ def test_tiled_random_scene_parity(cuda_device, shader):
     assert_parity(z, c, p, ref, f"tiled shader {shader}")
     assert int(ties.item()) == ref["near_ties"]
     assert stats.overflow == 0
+
+
+@pytest.mark.parametrize("shader", scenes.ALL_SHADERS)
+def test_small_face_path_parity(cuda_device, shader):
+    # small faces rasterised by the setup kernel (atomicMin of packed keys)
+    # and large ones binned, in one render: identical results
+    spec = scenes.random_job(shader, seed=720 + shader, W=61, H=47, F=400, spread=2.5)
+    z0, c0 = scenes.initial_buffers(spec)
+    for tile in ((8, 8), (16, 16)):
+        z, c, p, _, stats = _tiled_job(spec, z0, c0, cuda_device, tile=tile, small=32)
+        assert_parity(z, c, p, oracle.render(spec, z0, c0), f"small path shader {shader} tile {tile}")
 
 
 @pytest.mark.parametrize("tile", SHAPES)
@@ -74,11 +85,11 @@ def _copy(out):
     return {k: getattr(out, k).clone() for k in keys}
 
 
-@pytest.mark.parametrize("tile", [(8, 8), (16, 16), (32, 8)])
-def test_tiled_batch_equals_plain_batch(cuda_device, brax_batch, tile):
+@pytest.mark.parametrize("tile,small", [((8, 8), 0), ((16, 16), 0), ((32, 8), 0), ((8, 8), 32), ((16, 8), 32)])
+def test_tiled_batch_equals_plain_batch(cuda_device, brax_batch, tile, small):
     flat, sb = brax_batch
     plain = _copy(jb.BatchRunner(sb, form="plain").run())
-    cfg = _lib.RastTiledConfig(tile[0], tile[1], 0)
+    cfg = _lib.RastTiledConfig(tile[0], tile[1], 0, small)
     runner = jb.BatchRunner(sb, form="tiled", tiled_config=cfg)
     tiled = _copy(runner.run())
     torch.cuda.synchronize()

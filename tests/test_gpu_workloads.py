@@ -28,15 +28,16 @@ def overdraw(cuda_device):
     z0 = np.ones((spec.width, spec.height), F32)
     c0 = np.ones((spec.width, spec.height, 3), F32)
     out = {}
-    for form in ("plain", "tiled"):
-        packed = pack([spec], [z0], [c0], cuda_device, count_ties=True)
+    for form in ("plain", "tiled", "tiled_small"):
+        packed = pack([spec], [z0], [c0], cuda_device, count_ties=form != "tiled_small")
         if form == "plain":
             render_plain(packed)
         else:
-            stats = render_tiled(packed, tile=(8, 8))
+            stats = render_tiled(packed, tile=(8, 8), small_area=32 if form == "tiled_small" else 0)
             assert stats.overflow == 0
         z, c, p = unpack(packed, [spec])[0]
-        out[form] = (z.clone(), c.clone(), p.clone(), int(packed.near_ties.item()))
+        ties = int(packed.near_ties.item()) if packed.near_ties is not None else None
+        out[form] = (z.clone(), c.clone(), p.clone(), ties)
     return spec, z0, c0, out
 
 
@@ -48,6 +49,10 @@ def test_overdraw_scene_tiled_equals_plain(overdraw):
     assert torch.equal(cp.view(torch.int32), ct.view(torch.int32))
     assert tp == tt
     assert (pp >= 0).float().mean() > 0.5  # the spheres cover most of the frame
+    zs, cs, ps, _ = out["tiled_small"]  # small faces rasterised by the setup kernel
+    assert torch.equal(pp, ps)
+    assert torch.equal(zp.view(torch.int32), zs.view(torch.int32))
+    assert torch.equal(cp.view(torch.int32), cs.view(torch.int32))
 
 
 def band(spec: JobSpec, i0: int, w: int) -> JobSpec:
