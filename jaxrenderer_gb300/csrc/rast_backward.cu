@@ -423,7 +423,8 @@ __device__ __forceinline__ void fragment_bwd(const RastJob& J, const RastPools& 
       tg.sidx = sidx;
       tg.gs = gspec * spec * logf(rz);
     }
-    const float dspec_drz = (sexp == 0.0f) ? 0.0f : sexp * powf(rz, sexp - 1.0f);
+    // s x^(s-1) = s x^s / x for x > 0 (no second pow); at x = 0 the pow form
+    const float dspec_drz = (sexp == 0.0f) ? 0.0f : (rz > 0.0f ? sexp * (spec / rz) : sexp * powf(rz, sexp - 1.0f));
     const float grn[3] = {0.0f, 0.0f, gspec * dspec_drz * dmax0(rn[2])};
     float gr[3];
     normalise3_bwd(rn, rnorm, grn, gr);
@@ -449,7 +450,7 @@ __device__ __forceinline__ void fragment_bwd(const RastJob& J, const RastPools& 
 }
 
 template <int SH>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, 3)  // 3 blocks per SM: 80 registers
 pixel_kernel(RastBatch B, Work w, const float* __restrict__ grad_canvas, const float* __restrict__ grad_zbuffer,
              RastGradPools G) {
   __shared__ RastJob sJ;
