@@ -243,31 +243,55 @@ corner_kernel(RastMergeBatch B, const float* __restrict__ mpos, const int* __res
   const RastInstance& F = B.instances[I.scene_first];
   const int64_t vbase = F.vert_row, nbase = F.norm_row, ubase = F.uv_row;
   const int64_t corners = 3 * static_cast<int64_t>(mesh.n_faces);
-  for (int64_t c = lane; c < corners; c += 32) {
-    const int64_t src = mesh.face_begin * 3 + c;  // faces are (rows, 3): corner c of the mesh
-    const int64_t corner = I.corner_begin + c;
-    const int vi = wrap_clamp(I.vert_offset + __ldg(B.mesh_faces + src), I.scene_verts);
-    const float* p = mpos + (vbase + vi) * 3;
-    B.position[corner * 3 + 0] = p[0];
-    B.position[corner * 3 + 1] = p[1];
-    B.position[corner * 3 + 2] = p[2];
-    if (B.normal) {
-      const int ni = wrap_clamp(I.norm_offset + __ldg(B.mesh_faces_norm + src), I.scene_norms);
-      const float* q = mnrm + (nbase + ni) * 3;
-      B.normal[corner * 3 + 0] = q[0];
-      B.normal[corner * 3 + 1] = q[1];
-      B.normal[corner * 3 + 2] = q[2];
-    }
-    if (B.uv || B.texture_index) {
-      const int fu = __ldg(B.mesh_faces_uv + src);
-      if (B.uv) {
-        const int ui = wrap_clamp(I.uv_offset + fu, I.scene_uvs);
-        B.uv[corner * 2 + 0] = muv[(ubase + ui) * 2 + 0];
-        B.uv[corner * 2 + 1] = muv[(ubase + ui) * 2 + 1];
+  const int64_t fsrc = mesh.face_begin * 3;  // faces are (rows, 3): corner c of the mesh is fsrc + c
+  float* __restrict__ out_pos = B.position;
+  float* __restrict__ out_nrm = B.normal;
+  float* __restrict__ out_uv = B.uv;
+  int* __restrict__ out_tix = B.texture_index;
+  constexpr int kU = 2;  // corners per lane per round: their gathers are in flight together
+  for (int64_t base = 0; base < corners; base += 32 * kU) {
+    float pv[kU][3], nv[kU][3], uv[kU][2];
+    int tix[kU];
+#pragma unroll
+    for (int u = 0; u < kU; ++u) {
+      const int64_t c = base + u * 32 + lane;
+      if (c >= corners) continue;
+      const int vi = wrap_clamp(I.vert_offset + __ldg(B.mesh_faces + fsrc + c), I.scene_verts);
+#pragma unroll
+      for (int k = 0; k < 3; ++k) pv[u][k] = mpos[(vbase + vi) * 3 + k];
+      if (out_nrm) {
+        const int ni = wrap_clamp(I.norm_offset + __ldg(B.mesh_faces_norm + fsrc + c), I.scene_norms);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) nv[u][k] = mnrm[(nbase + ni) * 3 + k];
       }
-      // texture_index[faces_uv]: the per-vertex object index gathered with
-      // merged uv indices (renderer.py:287-289)
-      if (B.texture_index) B.texture_index[corner] = mobj[vbase + wrap_clamp(I.uv_offset + fu, I.scene_verts)];
+      if (out_uv || out_tix) {
+        const int fu = __ldg(B.mesh_faces_uv + fsrc + c);
+        if (out_uv) {
+          const int ui = wrap_clamp(I.uv_offset + fu, I.scene_uvs);
+          uv[u][0] = muv[(ubase + ui) * 2 + 0];
+          uv[u][1] = muv[(ubase + ui) * 2 + 1];
+        }
+        // texture_index[faces_uv]: the per-vertex object index gathered
+        // with merged uv indices (renderer.py:287-289)
+        if (out_tix) tix[u] = mobj[vbase + wrap_clamp(I.uv_offset + fu, I.scene_verts)];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < kU; ++u) {
+      const int64_t c = base + u * 32 + lane;
+      if (c >= corners) continue;
+      const int64_t corner = I.corner_begin + c;
+#pragma unroll
+      for (int k = 0; k < 3; ++k) out_pos[corner * 3 + k] = pv[u][k];
+      if (out_nrm) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) out_nrm[corner * 3 + k] = nv[u][k];
+      }
+      if (out_uv) {
+        out_uv[corner * 2 + 0] = uv[u][0];
+        out_uv[corner * 2 + 1] = uv[u][1];
+      }
+      if (out_tix) out_tix[corner] = tix[u];
     }
   }
 }
