@@ -544,7 +544,7 @@ scatter_kernel(RastBatch B, Geometry G, const int2* __restrict__ fmap, const ush
 // slice of shared memory (one record per lane), then every lane tests its
 // pixels against the 32 staged setups.  Tiles whose bin overflowed scan
 // every primitive of the job instead.
-template <int TW, int TH, bool kKeys>
+template <int TW, int TH, bool kKeys, bool kTies>
 __global__ void __launch_bounds__(32 * kRasterWarps)
 raster_kernel(RastBatch B, Geometry G, const float4* __restrict__ setup,
               const uint32_t* __restrict__ counts, const uint32_t* __restrict__ offsets,
@@ -644,11 +644,11 @@ raster_kernel(RastBatch B, Geometry G, const float4* __restrict__ setup,
               const float z = ((c0 * cz.y + c1 * cz.z) + c2 * cz.w) * vp22 + vp23;
               const unsigned long long key = pack_key(z, id);
               if (key < best[q]) {
-                second[q] = min(second[q], static_cast<uint32_t>(best[q] >> 32));
+                if (kTies) second[q] = min(second[q], static_cast<uint32_t>(best[q] >> 32));
                 best[q] = key;
                 best_z[q] = z;
                 z_known |= 1u << q;
-              } else {
+              } else if (kTies) {
                 second[q] = min(second[q], static_cast<uint32_t>(key >> 32));
               }
             }
@@ -665,7 +665,7 @@ raster_kernel(RastBatch B, Geometry G, const float4* __restrict__ setup,
         const uint32_t o1 = static_cast<uint32_t>(best[q] >> 32);
         const bool found = !(best[q] == kEmptyKey || o1 == kInfOrder);
         const int64_t pix = J.pixel_begin + static_cast<int64_t>(pi) * H + pj;
-        if (is_near_tie(best[q], second[q])) ++tie_count;
+        if (kTies && is_near_tie(best[q], second[q])) ++tie_count;
         if (!depth_only) {
           const int32_t w = found ? static_cast<int32_t>(best[q] & 0xffffffffu) : -1;
           winner[pix] = w;
@@ -707,7 +707,7 @@ raster_kernel(RastBatch B, Geometry G, const float4* __restrict__ setup,
       }
     }
   }
-  if (B.near_ties) {
+  if (kTies) {
     for (int o = 16; o > 0; o >>= 1) tie_count += __shfl_xor_sync(0xffffffffu, tie_count, o);
     if (lane == 0 && tie_count) atomicAdd(B.near_ties, tie_count);
   }
@@ -849,26 +849,26 @@ static bool valid_shape(TileShape t) {
          (t.tw == 8 && t.th == 32) || (t.tw == 16 && t.th == 8);
 }
 
-template <bool kKeys>
+template <bool kKeys, bool kTies>
 static void launch_raster(TileShape ts, unsigned grid, cudaStream_t s, const RastBatch& b, const Layout& L,
                           const float4* setup, const uint32_t* counts, const uint32_t* offsets, const int32_t* bins,
                           int32_t* winner, unsigned int* misc, unsigned char* vis,
                           const unsigned long long* keys) {
   const unsigned block = 32 * kRasterWarps;
   if (ts.tw == 8 && ts.th == 8)
-    raster_kernel<8, 8, kKeys><<<grid, block, 0, s>>>(b, L.G, setup, counts, offsets, bins, winner, misc, L.n_tiles,
+    raster_kernel<8, 8, kKeys, kTies><<<grid, block, 0, s>>>(b, L.G, setup, counts, offsets, bins, winner, misc, L.n_tiles,
                                                       vis, keys);
   else if (ts.tw == 16 && ts.th == 16)
-    raster_kernel<16, 16, kKeys><<<grid, block, 0, s>>>(b, L.G, setup, counts, offsets, bins, winner, misc,
+    raster_kernel<16, 16, kKeys, kTies><<<grid, block, 0, s>>>(b, L.G, setup, counts, offsets, bins, winner, misc,
                                                         L.n_tiles, vis, keys);
   else if (ts.tw == 32 && ts.th == 8)
-    raster_kernel<32, 8, kKeys><<<grid, block, 0, s>>>(b, L.G, setup, counts, offsets, bins, winner, misc,
+    raster_kernel<32, 8, kKeys, kTies><<<grid, block, 0, s>>>(b, L.G, setup, counts, offsets, bins, winner, misc,
                                                        L.n_tiles, vis, keys);
   else if (ts.tw == 8 && ts.th == 32)
-    raster_kernel<8, 32, kKeys><<<grid, block, 0, s>>>(b, L.G, setup, counts, offsets, bins, winner, misc,
+    raster_kernel<8, 32, kKeys, kTies><<<grid, block, 0, s>>>(b, L.G, setup, counts, offsets, bins, winner, misc,
                                                        L.n_tiles, vis, keys);
   else
-    raster_kernel<16, 8, kKeys><<<grid, block, 0, s>>>(b, L.G, setup, counts, offsets, bins, winner, misc,
+    raster_kernel<16, 8, kKeys, kTies><<<grid, block, 0, s>>>(b, L.G, setup, counts, offsets, bins, winner, misc,
                                                        L.n_tiles, vis, keys);
 }
 
@@ -939,10 +939,13 @@ static int render(const RastBatch* batch, const RastTiledConfig* cfg, void* work
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (b.total_setup > 0) {
       const unsigned grid = static_cast<unsigned>(std::max(sms, 1) * 8);
+      // the key path exists only when ties are not counted
       if (keys)
-        launch_raster<true>(ts, grid, s, b, L, setup, counts, offsets, bins, winner, misc, vis, keys);
+        launch_raster<true, false>(ts, grid, s, b, L, setup, counts, offsets, bins, winner, misc, vis, keys);
+      else if (b.near_ties)
+        launch_raster<false, true>(ts, grid, s, b, L, setup, counts, offsets, bins, winner, misc, vis, nullptr);
       else
-        launch_raster<false>(ts, grid, s, b, L, setup, counts, offsets, bins, winner, misc, vis, nullptr);
+        launch_raster<false, false>(ts, grid, s, b, L, setup, counts, offsets, bins, winner, misc, vis, nullptr);
     } else {
       if (cudaMemsetAsync(winner, 0xff, static_cast<size_t>(b.total_pixels) * 4, s) != cudaSuccess)
         return RAST_ERR_CUDA;
