@@ -266,6 +266,7 @@ typedef struct RastGradPools {
   float* texture;       /* like RastPools.texture: d/d diffuse texels */
   float* specular_map;  /* like RastPools.specular_map: d/d specular exponents */
   float* job_params;    /* (n_jobs, RAST_NPARAM) per-job camera/light gradients */
+  float* normal_map;    /* like RastPools.normal_map: d/d normal-map texels (phong_darboux) */
 } RastGradPools;
 
 /* Workspace rast_backward needs for `batch` (256-byte aligned base). */
@@ -276,7 +277,7 @@ size_t rast_backward_workspace_bytes(const RastBatch* batch);
  * pixel (fragment and interpolation backward, accumulating dL/d inverse and
  * dL/d varyings), then per face (inverse and clip transform backward) and
  * per vertex (vertex shader backward).  uv gets no gradient (nearest texel:
- * floor).  Not available for PHONG_DARBOUX (RAST_ERR_UNSUPPORTED).
+ * floor).
  * grad_canvas (pixels, 3) and grad_zbuffer (pixels) may each be NULL. */
 int rast_backward(const RastBatch* batch, const float* grad_canvas, const float* grad_zbuffer,
                   const RastGradPools* grads, void* workspace, size_t workspace_bytes, void* stream);

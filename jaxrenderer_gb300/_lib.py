@@ -153,7 +153,7 @@ NPARAM = 56
 
 class RastGradPools(ctypes.Structure):
     _fields_ = [("position", c_void_p), ("normal", c_void_p), ("colour", c_void_p), ("texture", c_void_p),
-                ("specular_map", c_void_p), ("job_params", c_void_p)]
+                ("specular_map", c_void_p), ("job_params", c_void_p), ("normal_map", c_void_p)]
 
 
 # Exported symbols and their prototypes: (name, restype, argtypes).

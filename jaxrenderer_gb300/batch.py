@@ -442,7 +442,8 @@ class BatchRunner:
         """Zeroed gradient arrays matching the batch's pools (for backward(out=...))."""
         dev = self.sb.device
         P = self.pools
-        g = {k: torch.zeros_like(P[k]) for k in ("position", "normal", "colour", "texture", "specular_map") if k in P}
+        g = {k: torch.zeros_like(P[k]) for k in ("position", "normal", "colour", "texture", "specular_map",
+                                                 "normal_map") if k in P}
         g["job_params"] = torch.zeros((self.sb.n_scenes, _lib.NPARAM), dtype=torch.float32, device=dev)
         return g
 

@@ -73,6 +73,18 @@ __device__ __forceinline__ void add_texel_grad(float* g, int64_t base, int ch, c
 // segment's sum.  Every lane of the warp must call these.
 constexpr unsigned kFull = 0xffffffffu;
 
+// Template values of the shader-specialised kernels: a shader id, kAnyShader
+// (any mix, dispatch on each job's shader) or kReflectionShaders (jobs of
+// phong_reflection and phong_reflection_shadow only).  may<SH>(x): code for
+// shader x is needed.
+constexpr int kAnyShader = -1;
+constexpr int kReflectionShaders = -2;
+template <int SH>
+__host__ __device__ constexpr bool may(int x) {
+  return SH == x || SH == kAnyShader ||
+         (SH == kReflectionShaders && (x == RAST_SHADER_PHONG_REFLECTION || x == RAST_SHADER_PHONG_REFLECTION_SHADOW));
+}
+
 struct Seg {
   int start;    // first lane of this lane's segment
   bool tail;    // last lane of its segment (and active)
@@ -125,7 +137,10 @@ __host__ __device__ constexpr unsigned long long pixel_bits(int sh) {
 __host__ __device__ constexpr unsigned long long vertex_bits(int sh) {
   return (sh == RAST_SHADER_GOURAUD || sh == RAST_SHADER_GOURAUD_TEXTURE) ? range_bits(RAST_GRAD_LIGHT_DIRECTION, 6)
        : sh == RAST_SHADER_DEPTH ? 0ull
-       : sh < 0 ? range_bits(RAST_GRAD_WORLD_TO_EYE_NORM, 16) | range_bits(RAST_GRAD_LIGHT_DIRECTION, 6)
+       : sh == kReflectionShaders ? range_bits(RAST_GRAD_WORLD_TO_EYE_NORM, 16)
+       : sh < 0 ? range_bits(RAST_GRAD_WORLD_TO_EYE_NORM, 16) | range_bits(RAST_GRAD_LIGHT_DIRECTION, 6) |
+                  range_bits(RAST_GRAD_WORLD_TO_CLIP, 16)
+       : sh == RAST_SHADER_PHONG_DARBOUX ? range_bits(RAST_GRAD_WORLD_TO_EYE_NORM, 16) | range_bits(RAST_GRAD_WORLD_TO_CLIP, 16)
        : range_bits(RAST_GRAD_WORLD_TO_EYE_NORM, 16);
 }
 constexpr unsigned long long kClipBits = range_bits(RAST_GRAD_WORLD_TO_CLIP, 16);
@@ -171,8 +186,10 @@ struct Work {
   float* facc;          // per face: dL/dm (9), dL/dz_clip (3)
   unsigned char* vvis;  // per vertex (vout rows): corner of a shown face
   float* vvar;          // per vertex: varyings (vstride)
-  float* vacc;          // per vertex: dL/d(eye normal or colour varying) (3)
+  float* vacc;          // per vertex: dL/d(eye normal or colour varying) (3), then dL/d of the
+                        // phong_darboux NDC triangle (9) when that shader is in the batch
   int vstride;
+  int vacc_stride;      // 3, or 12 with phong_darboux
   const int2* fmap;     // face block map (kThreads faces per block)
   const int2* vmap;     // vertex block map
   unsigned* starts;     // per-job block starts of both maps (2 x (n_jobs + 1))
@@ -259,9 +276,7 @@ __global__ void __launch_bounds__(kThreads) vertex_prep_kernel(RastBatch B, Work
     for (int k = 0; k < kMaxVarying; ++k)
       if (k < nv) w.vvar[row * w.vstride + k] = var[k];
   }
-  w.vacc[row * 3 + 0] = 0.0f;
-  w.vacc[row * 3 + 1] = 0.0f;
-  w.vacc[row * 3 + 2] = 0.0f;
+  for (int k = 0; k < w.vacc_stride; ++k) w.vacc[row * w.vacc_stride + k] = 0.0f;
 }
 
 // Reverse mode of the fragment of shader `sh` at one pixel.  In: the three
@@ -277,20 +292,23 @@ struct TexGrad {
   float gt[3] = {0.0f, 0.0f, 0.0f};
   int64_t sidx = -1;
   float gs = 0.0f;
+  int64_t nb = -1;  // normal-map texel (phong_darboux)
+  float gn[3] = {0.0f, 0.0f, 0.0f};
 };
 
 template <int SH>
 __device__ __forceinline__ void fragment_bwd(const RastJob& J, const RastPools& P, const RastGradPools& G,
                                              const float* r0, const float* r1, const float* r2, const float* b,
-                                             const float* gcv, float* g_interp, ParamGrad& pg, TexGrad& tg) {
+                                             const float* gcv, float* g_interp, ParamGrad& pg, TexGrad& tg,
+                                             float* gtri) {
   const int sh = SH >= 0 ? SH : J.shader;
   g_interp[0] = g_interp[1] = g_interp[2] = 0.0f;
-  if (sh == RAST_SHADER_GOURAUD) {
+  if (may<SH>(RAST_SHADER_GOURAUD) && sh == RAST_SHADER_GOURAUD) {
 #pragma unroll
     for (int q = 0; q < 3; ++q) g_interp[q] = gcv[q];
     return;
   }
-  if (sh == RAST_SHADER_GOURAUD_TEXTURE) {
+  if (may<SH>(RAST_SHADER_GOURAUD_TEXTURE) && sh == RAST_SHADER_GOURAUD_TEXTURE) {
     const float u = interp1(b, r0[kVUvG], r1[kVUvG], r2[kVUvG]);
     const float v = interp1(b, r0[kVUvG + 1], r1[kVUvG + 1], r2[kVUvG + 1]);
     const int ui = pymod(f2i(floorf(u)), J.tex_w), wi = pymod(f2i(floorf(v)), J.tex_h);
@@ -305,7 +323,7 @@ __device__ __forceinline__ void fragment_bwd(const RastJob& J, const RastPools& 
     texel_index(J, ui, wi, &tg.tb, &tg.ch);
     return;
   }
-  if (sh == RAST_SHADER_DEPTH || sh == RAST_SHADER_PHONG_DARBOUX) return;
+  if (sh == RAST_SHADER_DEPTH || sh == RAST_SHADER_GOURAUD || sh == RAST_SHADER_GOURAUD_TEXTURE) return;
   // phong family: n = normalise(sum_k b_k ne_k)
   float nrm[3], n[3];
 #pragma unroll
@@ -313,7 +331,114 @@ __device__ __forceinline__ void fragment_bwd(const RastJob& J, const RastPools& 
   const float nrmn = norm3(nrm);
   normalise3(nrm, n);
   float gn[3] = {0.0f, 0.0f, 0.0f};
-  if (sh == RAST_SHADER_PHONG) {
+  if (may<SH>(RAST_SHADER_PHONG_DARBOUX) && sh == RAST_SHADER_PHONG_DARBOUX) {
+    // phong_darboux.py:212-293: a Darboux frame from vertex 0's NDC and uv
+    // triangles and the interpolated normal, the normal map in that frame,
+    // then PhongTextureShader's lighting with the perturbed normal
+    const float u = interp1(b, r0[kVUv], r1[kVUv], r2[kVUv]);
+    const float v = interp1(b, r0[kVUv + 1], r1[kVUv + 1], r2[kVUv + 1]);
+    const int ui = pymod(f2i(floorf(u)), J.tex_w), wi = pymod(f2i(floorf(v)), J.tex_h);
+    const float* t = r0 + kVTri;
+    const float* tu = r0 + kVTriUv;
+    float A[9], AI[9];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      A[c] = t[3 + c] - t[c];
+      A[3 + c] = t[6 + c] - t[c];
+      A[6 + c] = n[c];
+    }
+    inv3(A, AI);
+    const float bi[3] = {tu[2] - tu[0], tu[4] - tu[0], 0.0f};
+    const float bj[3] = {tu[3] - tu[1], tu[5] - tu[1], 0.0f};
+    float vi[3], vj[3], ni[3], nj[3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+      vi[r] = dot3(AI + 3 * r, bi);
+      vj[r] = dot3(AI + 3 * r, bj);
+    }
+    const float vin = norm3(vi), vjn = norm3(vj);
+    normalise3(vi, ni);
+    normalise3(vj, nj);
+    float nm[3], bn[3], n2[3], tc[3], l[3], lc[3];
+    texel3(P.normal_map + J.normal_map_begin, J.nm_w, J.nm_h, 3, ui, wi, nm);
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+      const float row[3] = {ni[r], nj[r], n[r]};
+      bn[r] = dot3(row, nm);
+    }
+    const float bnn = norm3(bn);
+    normalise3(bn, n2);
+    texel3(P.texture + J.texture_begin, J.tex_w, J.tex_h, J.tex_c, ui, wi, tc);
+    const float ln = norm3(J.light_direction);
+    normalise3(J.light_direction, l);
+    const float d = dot3(n2, l);
+    bool nonneg = true;
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      lc[q] = J.light_colour[q] * d;
+      nonneg = nonneg && lc[q] >= 0.0f;
+    }
+    if (!nonneg) return;
+    texel_index(J, ui, wi, &tg.tb, &tg.ch);
+    float gd = 0.0f;
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      tg.gt[q] = gcv[q] * lc[q];
+      const float glc = gcv[q] * tc[q];
+      pg.v[RAST_GRAD_LIGHT_COLOUR + q] += glc * d;
+      gd += glc * J.light_colour[q];
+    }
+    float gn2[3], gl[3], gL[3], gbn[3];
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      gn2[q] = gd * l[q];
+      gl[q] = gd * n2[q];
+    }
+    normalise3_bwd(l, ln, gl, gL);
+#pragma unroll
+    for (int q = 0; q < 3; ++q) pg.v[RAST_GRAD_LIGHT_DIRECTION + q] += gL[q];
+    normalise3_bwd(n2, bnn, gn2, gbn);
+    // bn[r] = ni[r] nm0 + nj[r] nm1 + n[r] nm2
+    float gni[3], gnj[3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+      gni[r] = gbn[r] * nm[0];
+      gnj[r] = gbn[r] * nm[1];
+      gn[r] += gbn[r] * nm[2];
+    }
+    const int nu = gather_clamp(ui, J.nm_w), nv = gather_clamp(wi, J.nm_h);
+    tg.nb = J.normal_map_begin + (static_cast<int64_t>(nu) * J.nm_h + nv) * 3;
+    tg.gn[0] = (gbn[0] * ni[0] + gbn[1] * ni[1]) + gbn[2] * ni[2];
+    tg.gn[1] = (gbn[0] * nj[0] + gbn[1] * nj[1]) + gbn[2] * nj[2];
+    tg.gn[2] = (gbn[0] * n[0] + gbn[1] * n[1]) + gbn[2] * n[2];
+    float gvi[3], gvj[3];
+    normalise3_bwd(ni, vin, gni, gvi);
+    normalise3_bwd(nj, vjn, gnj, gvj);
+    // v = AI b  ->  dL/dAI = gv b^T;  AI = inv(A)  ->  dL/dA = -AI^T dL/dAI AI^T
+    float gAI[9], tmp[9], gA[9];
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) gAI[3 * r + k] = gvi[r] * bi[k] + gvj[r] * bj[k];
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+      for (int k = 0; k < 3; ++k)
+        tmp[3 * r + k] = (gAI[3 * r + 0] * AI[3 * k + 0] + gAI[3 * r + 1] * AI[3 * k + 1]) + gAI[3 * r + 2] * AI[3 * k + 2];
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+      for (int k = 0; k < 3; ++k)
+        gA[3 * r + k] = -((AI[0 * 3 + r] * tmp[0 * 3 + k] + AI[1 * 3 + r] * tmp[1 * 3 + k]) + AI[2 * 3 + r] * tmp[2 * 3 + k]);
+    // rows of A: t1 - t0, t2 - t0, n
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      gtri[c] = -(gA[c] + gA[3 + c]);
+      gtri[3 + c] = gA[c];
+      gtri[6 + c] = gA[3 + c];
+      gn[c] += gA[6 + c];
+    }
+  } else if (may<SH>(RAST_SHADER_PHONG) && sh == RAST_SHADER_PHONG) {
     // colour = all(lc >= 0) ? tex * lc : 0,  lc = light_colour * (n . l)
     const float u = interp1(b, r0[kVUv], r1[kVUv], r2[kVUv]);
     const float v = interp1(b, r0[kVUv + 1], r1[kVUv + 1], r2[kVUv + 1]);
@@ -449,8 +574,17 @@ __device__ __forceinline__ void fragment_bwd(const RastJob& J, const RastPools& 
   normalise3_bwd(n, nrmn, gn, g_interp);
 }
 
+// Single-reflection-shader variants fit 80 registers (3 blocks per SM); the
+// others keep 128 (2 blocks) rather than spill.
 template <int SH>
-__global__ void __launch_bounds__(kThreads, 3)  // 3 blocks per SM: 80 registers
+__host__ __device__ constexpr int pixel_min_blocks() {
+  return (SH == RAST_SHADER_PHONG_REFLECTION || SH == RAST_SHADER_PHONG_REFLECTION_SHADOW ||
+          SH == RAST_SHADER_PHONG || SH == RAST_SHADER_GOURAUD || SH == RAST_SHADER_GOURAUD_TEXTURE ||
+          SH == RAST_SHADER_DEPTH) ? 3 : 2;
+}
+
+template <int SH>
+__global__ void __launch_bounds__(kThreads, pixel_min_blocks<SH>())
 pixel_kernel(RastBatch B, Work w, const float* __restrict__ grad_canvas, const float* __restrict__ grad_zbuffer,
              RastGradPools G) {
   __shared__ RastJob sJ;
@@ -480,6 +614,10 @@ pixel_kernel(RastBatch B, Work w, const float* __restrict__ grad_canvas, const f
   for (int k = 0; k < 9; ++k) vval[k] = 0.0f;
   int64_t vrows[3] = {0, 0, 0};
   TexGrad tg;
+  constexpr bool kDarboux = may<SH>(RAST_SHADER_PHONG_DARBOUX);
+  float tval[9];  // dL/d vertex 0's NDC triangle (phong_darboux's Darboux frame)
+#pragma unroll
+  for (int k = 0; k < 9; ++k) tval[k] = 0.0f;
   if (p >= 0) {
     int i, j;
     pixel_of(local, npx, J.height, &i, &j);
@@ -529,7 +667,7 @@ pixel_kernel(RastBatch B, Work w, const float* __restrict__ grad_canvas, const f
         }
       }
       float gi[3];
-      fragment_bwd<SH>(J, P, G, r0, r1, r2, b, gcv, gi, pg, tg);
+      fragment_bwd<SH>(J, P, G, r0, r1, r2, b, gcv, gi, pg, tg, tval);
       if (gi[0] != 0.0f || gi[1] != 0.0f || gi[2] != 0.0f) {
         // interpolated = sum_k b_k v_k over the carried varying (offset 0 in
         // both families: eye normal or colour)
@@ -575,8 +713,22 @@ pixel_kernel(RastBatch B, Work w, const float* __restrict__ grad_canvas, const f
 #pragma unroll
     for (int k = 0; k < 9; ++k) {
       const float v = seg_sum(vval[k], sf);
-      if (sf.tail && v != 0.0f) atomicAdd(w.vacc + vrows[k / 3] * 3 + (k % 3), v);
+      if (sf.tail && v != 0.0f) atomicAdd(w.vacc + vrows[k / 3] * w.vacc_stride + (k % 3), v);
     }
+    if (kDarboux && w.vacc_stride > 3) {
+#pragma unroll
+      for (int k = 0; k < 9; ++k) {
+        const float v = seg_sum(tval[k], sf);
+        if (sf.tail && v != 0.0f) atomicAdd(w.vacc + vrows[0] * w.vacc_stride + 3 + k, v);
+      }
+    }
+  }
+  if (kDarboux && G.normal_map) {
+    const Seg sn = segment(tg.nb, tg.nb >= 0);
+    float g3[3];
+#pragma unroll
+    for (int q = 0; q < 3; ++q) g3[q] = seg_sum(tg.gn[q], sn);
+    if (sn.tail) add_texel_grad(G.normal_map, tg.nb, 3, g3);
   }
   if (G.texture) {
     const Seg st = segment(tg.tb, tg.tb >= 0);
@@ -675,14 +827,15 @@ __global__ void __launch_bounds__(kThreads) vertex_post_kernel(RastBatch B, Work
   const int sh = SH >= 0 ? SH : J.shader;
   const int v0 = blk.y + static_cast<int>(threadIdx.x);
   const int n = block_queue(v0 < nvt && w.vvis[J.vout_begin + v0], v0, s_q, &s_n);
-  const bool active = static_cast<int>(threadIdx.x) < n && sh != RAST_SHADER_DEPTH && sh != RAST_SHADER_PHONG_DARBOUX;
+  const bool active = static_cast<int>(threadIdx.x) < n && sh != RAST_SHADER_DEPTH;
   const int v = active ? s_q[threadIdx.x] : 0;
   ParamGrad pg;
 #pragma unroll
   for (int k = 0; k < RAST_NPARAM; ++k) pg.v[k] = 0.0f;
   const int64_t row = J.vout_begin + v;
   if (active) {
-    const float g[3] = {w.vacc[row * 3 + 0], w.vacc[row * 3 + 1], w.vacc[row * 3 + 2]};
+    const float* acc = w.vacc + row * w.vacc_stride;
+    const float g[3] = {acc[0], acc[1], acc[2]};
     const int64_t vrow = J.vert_begin + v;
     float N[3];
     load3(P.normal, vrow, N);
@@ -742,6 +895,44 @@ __global__ void __launch_bounds__(kThreads) vertex_post_kernel(RastBatch B, Work
 #pragma unroll
       for (int q = 0; q < 3; ++q) atomicAdd(G.normal + vrow * 3 + q, gN[q]);
     }
+    if (sh == RAST_SHADER_PHONG_DARBOUX) {
+      // the NDC triangle this vertex carried: to_cartesian(world_to_clip [p_k, 1])
+      // of its Darboux face's corners (phong_darboux.py:144-148)
+      const float* gt = acc + 3;
+      const int fid = gather_clamp(P.id_to_face[vrow], J.n_darboux_faces);
+      const int32_t* f = P.darboux_faces + (J.darboux_face_begin + fid) * 3;
+#pragma unroll 1
+      for (int k = 0; k < 3; ++k) {
+        const int64_t rk = J.vert_begin + gather_clamp(f[k], J.n_verts);
+        float pk[3], tc[4], gclip[4];
+        load3(P.position, rk, pk);
+        to_clip(J.world_to_clip, pk[0], pk[1], pk[2], tc);
+        if (tc[3] == 0.0f) {
+          gclip[0] = gt[3 * k + 0];
+          gclip[1] = gt[3 * k + 1];
+          gclip[2] = gt[3 * k + 2];
+          gclip[3] = 0.0f;
+        } else {
+          const float iw = 1.0f / tc[3];
+#pragma unroll
+          for (int c = 0; c < 3; ++c) gclip[c] = gt[3 * k + c] * iw;
+          gclip[3] = -((gclip[0] * tc[0] + gclip[1] * tc[1]) + gclip[2] * tc[2]) * iw;
+        }
+        const float ph[4] = {pk[0], pk[1], pk[2], 1.0f};
+#pragma unroll
+        for (int r = 0; r < 4; ++r)
+#pragma unroll
+          for (int q = 0; q < 4; ++q) pg.v[RAST_GRAD_WORLD_TO_CLIP + 4 * r + q] += gclip[r] * ph[q];
+        if (G.position) {
+#pragma unroll
+          for (int q = 0; q < 3; ++q) {
+            const float g = ((gclip[0] * J.world_to_clip[q] + gclip[1] * J.world_to_clip[4 + q]) +
+                             gclip[2] * J.world_to_clip[8 + q]) + gclip[3] * J.world_to_clip[12 + q];
+            atomicAdd(G.position + rk * 3 + q, g);
+          }
+        }
+      }
+    }
   }
   reduce_params<vertex_bits(SH)>(pg, G.job_params, active, blk.x);
 }
@@ -750,6 +941,7 @@ __global__ void __launch_bounds__(kThreads) vertex_post_kernel(RastBatch B, Work
 
 struct Layout {
   size_t fvis_off, frec_off, facc_off, vvis_off, vvar_off, vacc_off, fmap_off, vmap_off, start_off, total;
+  int vacc_stride;
   int vstride;
   unsigned fblocks, vblocks;
 };
@@ -772,7 +964,8 @@ static Layout layout(const RastBatch& b) {
   L.facc_off = take(F * 12 * sizeof(float));
   L.vvis_off = take(V);
   L.vvar_off = take(V * vstride * sizeof(float));
-  L.vacc_off = take(V * 3 * sizeof(float));
+  L.vacc_stride = (b.shader_mask & (1 << RAST_SHADER_PHONG_DARBOUX)) ? 12 : 3;
+  L.vacc_off = take(V * L.vacc_stride * sizeof(float));
   L.fblocks = block_map_capacity(b.total_setup, b.n_jobs, kThreads);
   L.vblocks = block_map_capacity(b.total_vout, b.n_jobs, kThreads);
   L.fmap_off = take(static_cast<size_t>(L.fblocks) * sizeof(int2));
@@ -807,7 +1000,6 @@ static int run(const RastBatch* batch, const float* grad_canvas, const float* gr
   int st = check_batch(batch);
   if (st != RAST_OK) return st;
   if (!grads || !batch->pools.prim_id) return RAST_ERR_INVALID_ARGUMENT;
-  if (batch->shader_mask & (1 << RAST_SHADER_PHONG_DARBOUX)) return RAST_ERR_UNSUPPORTED;
   const RastBatch& b = *batch;
   const Layout L = layout(b);
   if (workspace_bytes < L.total) return RAST_ERR_WORKSPACE_TOO_SMALL;
@@ -819,6 +1011,7 @@ static int run(const RastBatch* batch, const float* grad_canvas, const float* gr
   Work w{reinterpret_cast<unsigned char*>(ws + L.fvis_off), reinterpret_cast<float4*>(ws + L.frec_off),
          reinterpret_cast<float*>(ws + L.facc_off), reinterpret_cast<unsigned char*>(ws + L.vvis_off),
          reinterpret_cast<float*>(ws + L.vvar_off), reinterpret_cast<float*>(ws + L.vacc_off), L.vstride,
+         L.vacc_stride,
          reinterpret_cast<const int2*>(ws + L.fmap_off), reinterpret_cast<const int2*>(ws + L.vmap_off),
          reinterpret_cast<unsigned*>(ws + L.start_off)};
   Profiler prof(profile, s);
@@ -835,8 +1028,12 @@ static int run(const RastBatch* batch, const float* grad_canvas, const float* gr
     launch_all<RAST_SHADER_PHONG_REFLECTION>(b, w, L, grad_canvas, grad_zbuffer, *grads, s, prof);
   else if (only(RAST_SHADER_PHONG_REFLECTION_SHADOW))
     launch_all<RAST_SHADER_PHONG_REFLECTION_SHADOW>(b, w, L, grad_canvas, grad_zbuffer, *grads, s, prof);
+  else if (only(RAST_SHADER_PHONG_DARBOUX))
+    launch_all<RAST_SHADER_PHONG_DARBOUX>(b, w, L, grad_canvas, grad_zbuffer, *grads, s, prof);
+  else if (mask == ((1 << RAST_SHADER_PHONG_REFLECTION) | (1 << RAST_SHADER_PHONG_REFLECTION_SHADOW)))
+    launch_all<kReflectionShaders>(b, w, L, grad_canvas, grad_zbuffer, *grads, s, prof);
   else
-    launch_all<-1>(b, w, L, grad_canvas, grad_zbuffer, *grads, s, prof);
+    launch_all<kAnyShader>(b, w, L, grad_canvas, grad_zbuffer, *grads, s, prof);
   if (cudaGetLastError() != cudaSuccess) return RAST_ERR_CUDA;
   return prof.finish();
 }

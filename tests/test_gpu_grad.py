@@ -212,3 +212,101 @@ def test_depth_sum_gradient_wrt_world_to_clip(cuda_device):
             continue  # visibility changed: not differentiable here
         g_fd = (lp - lm) / (2 * EPS)
         assert abs(g[r, q] - g_fd) <= 2e-3 * max(abs(g_fd), 1e-1) + 1e-3, (r, q, g[r, q], g_fd)
+
+
+def _darboux_job():
+    from tests.scenes import random_job
+
+    spec = random_job(_lib.SHADER_PHONG_DARBOUX, seed=51, W=40, H=36, F=30, spread=1.0)
+    spec.light_colour = np.ones(3, F32)
+    spec.light_direction = np.array((0.2, -0.3, 0.93), F32)
+    return spec
+
+
+def _as64(spec):
+    import copy
+
+    s = copy.copy(spec)
+    for name in ("position", "normal", "uv", "texture", "normal_map", "light_direction", "light_colour",
+                 "viewport", "world_to_clip", "world_to_eye_norm"):
+        setattr(s, name, np.asarray(getattr(spec, name), np.float64))
+    return s
+
+
+def test_phong_darboux_gradients_vs_fd64(cuda_device):
+    """phong_darboux: gradients through the Darboux frame (vertex 0's NDC and
+    uv triangles, the per-fragment 3x3 inverse), the normal map, the lighting
+    and the interpolated normal, to positions, normals, normal-map and
+    diffuse texels and the light direction."""
+    spec = _darboux_job()
+    Wd, Hd = spec.width, spec.height
+    base = oracle.render(_as64(spec), np.ones((Wd, Hd)), np.ones((Wd, Hd, 3)), dtype=np.float64)
+    assert (base["prim_id"] >= 0).sum() > 50
+    target = base["canvas"] * 0.7 + 0.1
+    sb = jb.scene_batch_from_specs([spec], cuda_device)
+    db = DifferentiableBatch(sb, form="tiled", tiled_config=_lib.RastTiledConfig(8, 8, 0))
+    leaves = {
+        "position": torch.tensor(spec.position, requires_grad=True),
+        "normal": torch.tensor(spec.normal, requires_grad=True),
+        "texture": torch.tensor(spec.texture.reshape(-1), requires_grad=True),
+        "normal_map": torch.tensor(spec.normal_map.reshape(-1), requires_grad=True),
+        "light_direction": torch.tensor(spec.light_direction[None], requires_grad=True),
+    }
+
+    def fd(name, flat_index, mutate):
+        p, m = _as64(spec), _as64(spec)
+        mutate(p, flat_index, EPS)
+        mutate(m, flat_index, -EPS)
+        op = oracle.render(p, np.ones((Wd, Hd)), np.ones((Wd, Hd, 3)), dtype=np.float64)
+        om = oracle.render(m, np.ones((Wd, Hd)), np.ones((Wd, Hd, 3)), dtype=np.float64)
+        mask = ((op["prim_id"] == base["prim_id"]) & (om["prim_id"] == base["prim_id"]) &
+                (base["prim_id"] >= 0)).astype(np.float64)
+        lp = float((mask[..., None] * (op["canvas"] - target) ** 2).sum())
+        lm = float((mask[..., None] * (om["canvas"] - target) ** 2).sum())
+        return (lp - lm) / (2 * EPS), mask
+
+    def bump(field):
+        def mutate(s, k, e):
+            a = np.array(getattr(s, field), np.float64, copy=True)
+            a.reshape(-1)[k] += e
+            setattr(s, field, a)
+        return mutate
+
+    rng = np.random.Generator(np.random.PCG64(11))
+    visible = np.unique(base["prim_id"][base["prim_id"] >= 0])
+    verts = np.unique(spec.faces[rng.choice(visible, 3)].reshape(-1))[:4]
+    cases = [("light_direction", k) for k in range(3)]
+    cases += [("position", 3 * v + q) for v in verts for q in (0, 1)]
+    cases += [("normal", 3 * v + q) for v in verts[:2] for q in range(3)]
+    for name, k in cases:
+        g_fd, mask = fd(name, k, bump(name))
+        for t in leaves.values():
+            t.grad = None
+        canvas, _ = db.render(**{n: t.to(cuda_device) for n, t in leaves.items()})
+        m = torch.tensor(mask, dtype=torch.float32, device=cuda_device)[None, ..., None]
+        tg = torch.tensor(target, dtype=torch.float32, device=cuda_device)[None]
+        (m * (canvas - tg) ** 2).sum().backward()
+        g_an = float(leaves[name].grad.reshape(-1)[k])
+        assert abs(g_an - g_fd) <= 3e-3 * max(abs(g_fd), 1e-2) + 2e-4, (name, k, g_an, g_fd)
+    # texels of the normal map and of the diffuse texture that pixels sample
+    mask = (base["prim_id"] >= 0).astype(np.float64)
+    for t in leaves.values():
+        t.grad = None
+    canvas, _ = db.render(**{n: t.to(cuda_device) for n, t in leaves.items()})
+    m = torch.tensor(mask, dtype=torch.float32, device=cuda_device)[None, ..., None]
+    tg = torch.tensor(target, dtype=torch.float32, device=cuda_device)[None]
+    (m * (canvas - tg) ** 2).sum().backward()
+    for name, field in (("normal_map", "normal_map"), ("texture", "texture")):
+        g = leaves[name].grad.numpy()
+        used = np.argsort(-np.abs(g))[:4]
+        assert np.abs(g[used]).min() > 0
+        for k in used:
+            def loss(e):
+                s = _as64(spec)
+                a = np.array(getattr(s, field), np.float64, copy=True)
+                a.reshape(-1)[k] += e
+                setattr(s, field, a)
+                out = oracle.render(s, np.ones((Wd, Hd)), np.ones((Wd, Hd, 3)), dtype=np.float64)
+                return float((mask[..., None] * (out["canvas"] - target) ** 2).sum())
+            g_fd = (loss(EPS) - loss(-EPS)) / (2 * EPS)
+            assert abs(g[k] - g_fd) <= 3e-3 * max(abs(g_fd), 1e-2) + 2e-4, (name, k, g[k], g_fd)
