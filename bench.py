@@ -792,6 +792,14 @@ def kernel_bytes(kname, info, visible):
     return table.get(kname, 0.0)
 
 
+# DRAM bytes per face of the setup kernel measured by ncu (dram__bytes_read.sum +
+# dram__bytes_write.sum) on the 256-scene brax-like case
+# (profiles/ncu_forward_tiled_brax84x256.md: 119.06 MB and 121.98 MB for
+# 1,470,504 faces, binning only / with the small-face path); its traffic
+# grows with the faces processed, so a full launch's is this times its faces.
+NCU_SETUP_BYTES_PER_FACE = {0: 80.96, 1: 82.95}
+
+
 def roofline(prof, visible):
     """HBM roofline of the dominant kernel: algorithmic bytes per launch /
     average launch duration (CUDA events inside the library)."""
@@ -823,6 +831,14 @@ def roofline(prof, visible):
         v = summ[name]
         gbs = b / (v["avg_ms"] / 1e3) / 1e9 if v["avg_ms"] > 0 else None
         per_kernel[name] = {"bytes": b, "GB/s": gbs, "frac": gbs / peak if gbs is not None else None}
+    traffic, traffic_note = None, None
+    r_dom, p_dom, k_dom = prof["where"][dom]
+    if k_dom == "setup_bin_kernel":
+        cfg = r_dom.configs.get(p_dom)
+        small = 1 if (cfg is not None and int(cfg.small_area) > 0) else 0
+        traffic = NCU_SETUP_BYTES_PER_FACE[small] * info["F"]
+        traffic_note = ("ncu DRAM bytes per face of this kernel on the 256-scene case, times this launch's "
+                        f"{int(info['F'])} faces")
     out = {
         "bound": "hbm",
         "kernel": dom,
@@ -831,7 +847,8 @@ def roofline(prof, visible):
         "peak_source": kind,
         "unit": "GB/s",
         "frac": achieved / peak,
-        "traffic": None,
+        "traffic": traffic,
+        "traffic_note": traffic_note,
         "algorithmic_bytes_per_launch": alg,
         "avg_launch_ms": ms,
         "per_kernel": per_kernel,
