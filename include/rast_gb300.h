@@ -173,8 +173,8 @@ int rast_render_plain_profiled(const RastBatch* batch, void* workspace, size_t w
 /* Tiled form parameters (chosen by the autotuner).  Zero fields take the
  * defaults: 8x8 tiles, bin capacity of 4 entries per face. */
 typedef struct RastTiledConfig {
-  int32_t tile_w;          /* tile width along x (buffer axis 0): 8, 16 or 32 */
-  int32_t tile_h;          /* tile height along y (buffer axis 1): 8, 16 or 32 */
+  int32_t tile_w;          /* tile (w, h) pixels along x (buffer axis 0) and y (axis 1): */
+  int32_t tile_h;          /* 8x8, 16x8, 16x16, 32x8, 8x32, 8x4 or 4x8 */
   uint64_t bin_capacity;   /* total (tile, primitive) bin entries reserved in the workspace */
   int32_t small_area;      /* 0, or 1..32: faces whose conservative pixel rectangle has at most this
                               many pixels are rasterised by the setup kernel (64-bit atomicMin of the

@@ -1,8 +1,8 @@
 """Autotuner of the tiled form: tile shape, small-face path and bin
 capacity per workload.
 
-For a pass (one RastBatch) the tile shapes 8x8, 16x8, 16x16, 32x8 and 8x32
-(pixels along x by y), each with the setup kernel's small-face
+For a pass (one RastBatch) the tile shapes 8x8, 16x8, 16x16, 32x8, 8x32,
+8x4 and 4x8 (pixels along x by y), each with the setup kernel's small-face
 rasterisation off and on, are timed on the batch itself; the fastest wins.
 The bin capacity is then set to 1.25x the bin entries that shape requested.
 Results are cached in a JSON file keyed by (width, height, faces-per-job
@@ -23,7 +23,7 @@ import torch
 
 from . import _lib
 
-SHAPES = ((8, 8), (16, 8), (16, 16), (32, 8), (8, 32))
+SHAPES = ((8, 8), (16, 8), (16, 16), (32, 8), (8, 32), (8, 4), (4, 8))
 SMALL_AREAS = (0, 32)  # small-face rasterisation in the setup kernel: off, or rectangles up to 32 pixels
 _LOCK = threading.Lock()
 
@@ -59,7 +59,7 @@ def workload_key(jobs: np.ndarray, device: torch.device) -> str:
     f = float(jobs["n_faces"].mean())
     bucket = 2 ** int(round(math.log2(max(f, 1.0))))
     mask = int(np.bitwise_or.reduce(1 << jobs["shader"].astype(np.int64)))
-    return f"v2|{w}x{h}|f~{bucket}|jobs~{2 ** int(round(math.log2(max(len(jobs), 1))))}|mask{mask}|{props.name}|sm{props.multi_processor_count}"
+    return f"v3|{w}x{h}|f~{bucket}|jobs~{2 ** int(round(math.log2(max(len(jobs), 1))))}|mask{mask}|{props.name}|sm{props.multi_processor_count}"
 
 
 def _time(runner, name, b, cfg, reps=3) -> float:

@@ -846,7 +846,8 @@ static int small_area_of(const RastTiledConfig* cfg) {
 
 static bool valid_shape(TileShape t) {
   return (t.tw == 8 && t.th == 8) || (t.tw == 16 && t.th == 16) || (t.tw == 32 && t.th == 8) ||
-         (t.tw == 8 && t.th == 32) || (t.tw == 16 && t.th == 8);
+         (t.tw == 8 && t.th == 32) || (t.tw == 16 && t.th == 8) || (t.tw == 8 && t.th == 4) ||
+         (t.tw == 4 && t.th == 8);
 }
 
 template <bool kKeys, bool kTies>
@@ -867,6 +868,12 @@ static void launch_raster(TileShape ts, unsigned grid, cudaStream_t s, const Ras
   else if (ts.tw == 8 && ts.th == 32)
     raster_kernel<8, 32, kKeys, kTies><<<grid, block, 0, s>>>(b, L.G, setup, counts, offsets, bins, winner, misc,
                                                        L.n_tiles, vis, keys);
+  else if (ts.tw == 8 && ts.th == 4)
+    raster_kernel<8, 4, kKeys, kTies><<<grid, block, 0, s>>>(b, L.G, setup, counts, offsets, bins, winner, misc,
+                                                      L.n_tiles, vis, keys);
+  else if (ts.tw == 4 && ts.th == 8)
+    raster_kernel<4, 8, kKeys, kTies><<<grid, block, 0, s>>>(b, L.G, setup, counts, offsets, bins, winner, misc,
+                                                      L.n_tiles, vis, keys);
   else
     raster_kernel<16, 8, kKeys, kTies><<<grid, block, 0, s>>>(b, L.G, setup, counts, offsets, bins, winner, misc,
                                                        L.n_tiles, vis, keys);

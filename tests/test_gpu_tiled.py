@@ -14,7 +14,7 @@ from tests.test_gpu_plain import assert_parity
 
 pytestmark = pytest.mark.gpu
 F32 = np.float32
-SHAPES = [(8, 8), (16, 8), (16, 16), (32, 8), (8, 32)]
+SHAPES = [(8, 8), (16, 8), (16, 16), (32, 8), (8, 32), (8, 4), (4, 8)]
 
 
 def _tiled_job(spec, z0, c0, device, tile=(8, 8), cap=0, ties=False, small=0):
@@ -85,7 +85,8 @@ def _copy(out):
     return {k: getattr(out, k).clone() for k in keys}
 
 
-@pytest.mark.parametrize("tile,small", [((8, 8), 0), ((16, 16), 0), ((32, 8), 0), ((8, 8), 32), ((16, 8), 32)])
+@pytest.mark.parametrize("tile,small", [((8, 8), 0), ((16, 16), 0), ((32, 8), 0), ((8, 4), 0), ((4, 8), 0),
+                                        ((8, 8), 32), ((16, 8), 32), ((8, 4), 32)])
 def test_tiled_batch_equals_plain_batch(cuda_device, brax_batch, tile, small):
     flat, sb = brax_batch
     plain = _copy(jb.BatchRunner(sb, form="plain").run())
