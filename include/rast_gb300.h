@@ -102,11 +102,45 @@ typedef struct RastJob {
   float ambient[3], diffuse[3], specular[3];
   float shadow_strength[3];  /* Shadow.strength */
   int32_t flags;             /* RAST_JOB_* bits */
-  int32_t reserved[2];
+  int32_t layers;            /* primitive_chooser hook: 0 = the default chooser (nearest
+                                candidate, shader.py:207-251); 1..RAST_MAX_LAYERS = the
+                                layered chooser (that many nearest candidates) */
+  int32_t mixer;             /* mix hook (RastMixer); RAST_MIX_NEAREST is the default mix */
+  float opacity;             /* RAST_MIX_OVER: opacity of every face (without
+                                RAST_JOB_FACE_ALPHA) */
+  float background[3];       /* RAST_MIX_OVER: colour seen through the last layer */
+  int32_t reserved;
 } RastJob;
 
 /* RastJob.flags */
 #define RAST_JOB_APPLY_DEPTH_OFFSET 1  /* zbuffer += depth_offset on every pixel after the pass */
+#define RAST_JOB_FACE_ALPHA 2          /* RAST_MIX_OVER reads per-face opacity from
+                                          RastPools.face_alpha[face_begin + face] */
+
+/* Compiled primitive_chooser / mix hooks (the override points of
+ * shader.py:159-251 and :339-396) for multi-candidate transparency.
+ *
+ * Layered chooser (RastJob.layers = L >= 1): the L candidates (kept,
+ * inside, front-facing, depth below +inf) nearest to the camera, in
+ * ascending (depth, primitive id) order; slots past the last candidate are
+ * not kept.  Each kept slot runs interpolation and the fragment shader.
+ *
+ * Mixers, over the slots in that order:
+ *  RAST_MIX_NEAREST  the first slot the fragment shader keeps (the default
+ *                    mix: argmin of depth over kept fragments);
+ *  RAST_MIX_OVER     front-to-back "over" compositing: T = 1, C = 0; for
+ *                    every kept slot s with opacity a: w = T * a,
+ *                    C = C + w * colour_s, T = T * (1 - a); the pixel gets
+ *                    C + T * background, the depth of the first kept slot,
+ *                    and that slot's primitive id.
+ * A pixel with no kept slot is left unchanged (merge_buffers keep = False).
+ * The DEPTH shader takes the default chooser only.  The backward entry
+ * point rejects layered jobs (RAST_ERR_UNSUPPORTED). */
+#define RAST_MAX_LAYERS 4
+typedef enum RastMixer {
+  RAST_MIX_NEAREST = 0,
+  RAST_MIX_OVER = 1
+} RastMixer;
 
 /* Flat input/output arrays shared by all jobs of a batch (device). */
 typedef struct RastPools {
@@ -126,6 +160,8 @@ typedef struct RastPools {
   float* zbuffer;              /* (pixels)     in/out */
   float* canvas;               /* (pixels, 3)  in/out; unused by DEPTH */
   int32_t* prim_id;            /* (pixels)     out, optional (NULL): primitive written or -1 */
+  const float* face_alpha;     /* (faces)      opacity per face, read by RAST_MIX_OVER jobs
+                                  with RAST_JOB_FACE_ALPHA; optional (NULL) otherwise */
 } RastPools;
 
 typedef struct RastBatch {
@@ -142,6 +178,9 @@ typedef struct RastBatch {
   RastPools pools;
   unsigned long long* near_ties; /* optional device counter (NULL): pixels whose two best
                                     candidate depths are <= 1 ulp apart, accumulated */
+  int32_t max_layers;    /* max over jobs of RastJob.layers (0 .. RAST_MAX_LAYERS); a job's
+                            layers beyond it are clamped to it */
+  int32_t reserved;
 } RastBatch;
 
 /* Workspace the caller must pass to rast_render_plain, in bytes, 256-byte

@@ -11,9 +11,10 @@ reached through the C ABI in include/rast_gb300.h.
 from typing import Dict as DictT
 from typing import List, NamedTuple, ParamSpec, Sequence, Tuple, Type, TypeAlias
 
-from . import shaders
+from . import hooks, shaders
 from .batch import SceneBatch, render_batch
 from .geometry import Camera, normalise, quaternion, quaternion_mul, rotation_matrix
+from .hooks import LayeredChooser, NearestMixer, OverMixer
 from .model import Model, ModelObject, batch_models, merge_objects
 from .pipeline import render, render_with_ids
 from .renderer import CameraParameters, LightParameters, Renderer, ShadowParameters
@@ -58,6 +59,7 @@ __all__ = [
     "JaxFloating",
     "JaxInteger",
     "jit",
+    "LayeredChooser",
     "LightParameters",
     "LightSource",
     "List",
@@ -65,7 +67,9 @@ __all__ = [
     "Model",
     "ModelObject",
     "NamedTuple",
+    "NearestMixer",
     "normalise",
+    "OverMixer",
     "ParamSpec",
     "quaternion_mul",
     "quaternion",

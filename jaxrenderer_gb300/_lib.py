@@ -21,6 +21,11 @@ SHADER_PHONG_REFLECTION = 5
 SHADER_PHONG_REFLECTION_SHADOW = 6
 
 JOB_APPLY_DEPTH_OFFSET = 1
+JOB_FACE_ALPHA = 2
+
+MAX_LAYERS = 4
+MIX_NEAREST = 0
+MIX_OVER = 1
 
 STATUS_NAMES = {
     0: "RAST_OK",
@@ -83,7 +88,11 @@ class RastJob(ctypes.Structure):
         ("specular", F3),
         ("shadow_strength", F3),
         ("flags", c_int32),
-        ("reserved", c_int32 * 2),
+        ("layers", c_int32),
+        ("mixer", c_int32),
+        ("opacity", c_float),
+        ("background", F3),
+        ("reserved", c_int32),
     ]
 
 
@@ -105,6 +114,7 @@ class RastPools(ctypes.Structure):
         ("zbuffer", c_void_p),
         ("canvas", c_void_p),
         ("prim_id", c_void_p),
+        ("face_alpha", c_void_p),
     ]
 
 
@@ -122,6 +132,8 @@ class RastBatch(ctypes.Structure):
         ("total_pixels", c_int64),
         ("pools", RastPools),
         ("near_ties", c_void_p),
+        ("max_layers", c_int32),
+        ("reserved", c_int32),
     ]
 
 

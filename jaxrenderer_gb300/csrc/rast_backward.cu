@@ -1000,6 +1000,7 @@ static int run(const RastBatch* batch, const float* grad_canvas, const float* gr
   int st = check_batch(batch);
   if (st != RAST_OK) return st;
   if (!grads || !batch->pools.prim_id) return RAST_ERR_INVALID_ARGUMENT;
+  if (batch->max_layers > 0) return RAST_ERR_UNSUPPORTED;  // layered chooser: forward only
   const RastBatch& b = *batch;
   const Layout L = layout(b);
   if (workspace_bytes < L.total) return RAST_ERR_WORKSPACE_TOO_SMALL;

@@ -42,5 +42,11 @@ extern "C" int rast_validate_job(const RastJob* j) {
     return RAST_ERR_INVALID_ARGUMENT;
   if (sh == RAST_SHADER_PHONG_REFLECTION_SHADOW && (j->shadow_w < 0 || j->shadow_h < 0))
     return RAST_ERR_INVALID_ARGUMENT;
+  // chooser / mix hooks: the layered chooser takes 1..RAST_MAX_LAYERS slots,
+  // not for the DEPTH shader; the mixer is one of RastMixer
+  if (j->layers < 0 || j->layers > RAST_MAX_LAYERS) return RAST_ERR_INVALID_ARGUMENT;
+  if (j->layers > 0 && sh == RAST_SHADER_DEPTH) return RAST_ERR_INVALID_ARGUMENT;
+  if (j->mixer != RAST_MIX_NEAREST && j->mixer != RAST_MIX_OVER) return RAST_ERR_INVALID_ARGUMENT;
+  if (j->mixer == RAST_MIX_OVER && j->layers == 0) return RAST_ERR_INVALID_ARGUMENT;
   return RAST_OK;
 }

@@ -227,19 +227,19 @@ struct PixelResult {
   int prim;
 };
 
-// One pixel after the scan: `w` is the winning candidate (-1: none, or its
-// depth was +inf).  Reproduces the default chooser's fallback to primitive 0
-// (shader.py:215-217), then Shader.interpolate / fragment / mix
-// (pipeline.py:283-359) for the chosen primitive.
-__device__ __forceinline__ void resolve_pixel(const RastJob& J, const RastPools& P,
-                                              const float4* rec_base, int i, int j, int w,
-                                              const VaryingSource& src, PixelResult* r) {
-  r->keep = false;
-  r->prim = -1;
-  r->z = 0.0f;
-  r->colour[0] = r->colour[1] = r->colour[2] = 0.0f;
-  if (J.n_faces <= 0) return;
-  const int p = w < 0 ? 0 : w;
+// Interpolation and fragment shader of primitive p at pixel (i, j)
+// (pipeline.py:283-326): clip coefficients, chooser keep (keep & inside),
+// depth, perspective-correct barycentrics, the corner varyings from `src`,
+// then the job's fragment shader.
+struct Fragment {
+  bool chooser_keep;  // keep & inside (the chooser's keeps slice)
+  bool keep;          // the fragment shader's keep
+  float z;
+  float colour[3];
+};
+
+__device__ __forceinline__ void shade_primitive(const RastJob& J, const RastPools& P, const float4* rec_base,
+                                                int i, int j, int p, const VaryingSource& src, Fragment* f) {
   const float4* rec = rec_base + static_cast<int64_t>(p) * 4;
   const float4 a = rec[0], b = rec[1], cz = rec[2], d = rec[3];
   const float x = (static_cast<float>(i) - J.viewport[3]) / J.viewport[0];
@@ -248,10 +248,10 @@ __device__ __forceinline__ void resolve_pixel(const RastJob& J, const RastPools&
                       (x * a.z + y * b.y) + cz.x};
   const bool in_tri = c[0] >= 0.0f && c[1] >= 0.0f && c[2] >= 0.0f;
   const int flags = __float_as_int(d.y);
-  const bool chooser_keep = (flags & kKeep) && in_tri;
+  f->chooser_keep = (flags & kKeep) && in_tri;
   const bool front = (flags & kFront) != 0;
   const float w_rcp = (c[0] + c[1]) + c[2];
-  const float z = ((c[0] * cz.y + c[1] * cz.z) + c[2] * cz.w) * J.viewport[10] + J.viewport[11];
+  f->z = ((c[0] * cz.y + c[1] * cz.z) + c[2] * cz.w) * J.viewport[10] + J.viewport[11];
   const float bary[3] = {c[0] / w_rcp, c[1] / w_rcp, c[2] / w_rcp};
   const int32_t* face = P.faces + (J.face_begin + p) * 3;
   const int nv = varying_count(J.shader);
@@ -287,10 +287,88 @@ __device__ __forceinline__ void resolve_pixel(const RastJob& J, const RastPools&
       vertex_shader<false>(J, P, i2, clip, v2);
     }
   }
-  const bool frag_keep = fragment_shader(J, P, v0, v1, v2, bary, front, r->colour);
-  r->keep = chooser_keep && frag_keep;
-  r->z = z;
+  f->colour[0] = f->colour[1] = f->colour[2] = 0.0f;
+  f->keep = fragment_shader(J, P, v0, v1, v2, bary, front, f->colour);
+}
+
+// One pixel after the scan: `w` is the winning candidate (-1: none, or its
+// depth was +inf).  Reproduces the default chooser's fallback to primitive 0
+// (shader.py:215-217), then Shader.interpolate / fragment / mix
+// (pipeline.py:283-359) for the chosen primitive.
+__device__ __forceinline__ void resolve_pixel(const RastJob& J, const RastPools& P,
+                                              const float4* rec_base, int i, int j, int w,
+                                              const VaryingSource& src, PixelResult* r) {
+  r->keep = false;
+  r->prim = -1;
+  r->z = 0.0f;
+  r->colour[0] = r->colour[1] = r->colour[2] = 0.0f;
+  if (J.n_faces <= 0) return;
+  const int p = w < 0 ? 0 : w;
+  Fragment f;
+  shade_primitive(J, P, rec_base, i, j, p, src, &f);
+  r->keep = f.chooser_keep && f.keep;
+  r->z = f.z;
   r->prim = r->keep ? p : -1;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) r->colour[k] = f.colour[k];
+}
+
+// Chooser slots of job J: 0 = the default chooser, else the layered
+// chooser's slot count (clamped to the batch's max_layers).
+__device__ __forceinline__ int job_layers(const RastJob& J, int max_layers) {
+  return J.layers <= 0 ? 0 : min(J.layers, max_layers);
+}
+
+// One pixel of a layered job (RastJob.layers = L >= 1): slots
+// w[0 .. L-1] (stride `wstride`) hold the nearest candidates in ascending
+// (depth, id) order, -1 past the last.  Every slot runs interpolation +
+// fragment; the job's mixer combines the kept ones (RastMixer).
+__device__ __forceinline__ void resolve_layers(const RastJob& J, const RastPools& P, const float4* rec_base,
+                                               int i, int j, const int32_t* w, int64_t wstride, int L,
+                                               const VaryingSource& src, PixelResult* r) {
+  r->keep = false;
+  r->prim = -1;
+  r->z = 0.0f;
+  r->colour[0] = r->colour[1] = r->colour[2] = 0.0f;
+  const bool over = J.mixer == RAST_MIX_OVER;
+  const bool per_face = (J.flags & RAST_JOB_FACE_ALPHA) && P.face_alpha;
+  float T = 1.0f, C[3] = {0.0f, 0.0f, 0.0f};
+  for (int s = 0; s < L; ++s) {
+    const int p = w[s * wstride];
+    if (p < 0) break;
+    Fragment f;
+    shade_primitive(J, P, rec_base, i, j, p, src, &f);
+    if (!(f.chooser_keep && f.keep)) continue;
+    if (!r->keep) {
+      r->keep = true;
+      r->z = f.z;
+      r->prim = p;
+      if (!over) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) r->colour[k] = f.colour[k];
+        return;
+      }
+    }
+    const float alpha = per_face ? __ldg(P.face_alpha + J.face_begin + p) : J.opacity;
+    const float wgt = T * alpha;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) C[k] = C[k] + wgt * f.colour[k];
+    T = T * (1.0f - alpha);
+  }
+  if (r->keep && over) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) r->colour[k] = C[k] + T * J.background[k];
+  }
+}
+
+// Keeps best[0 .. L-1] the L smallest keys seen, ascending: `key` goes in
+// at its rank and the larger ones move down one slot.
+template <int L>
+__device__ __forceinline__ void insert_key(unsigned long long (&best)[L], unsigned long long key) {
+#pragma unroll
+  for (int s = L - 1; s > 0; --s)
+    if (key < best[s]) best[s] = key < best[s - 1] ? best[s - 1] : key;
+  if (key < best[0]) best[0] = key;
 }
 
 // merge_buffers (pipeline.py:401-440): overwrite where kept, no depth test;
@@ -349,6 +427,7 @@ inline int check_batch(const RastBatch* b) {
   if (b->max_width < 0 || b->max_height < 0 || b->max_faces < 0 || b->max_verts < 0)
     return RAST_ERR_INVALID_ARGUMENT;
   if ((b->shader_mask & ~0x7f) != 0) return RAST_ERR_INVALID_ARGUMENT;
+  if (b->max_layers < 0 || b->max_layers > RAST_MAX_LAYERS) return RAST_ERR_INVALID_ARGUMENT;
   if (b->total_pixels > 0 && !b->pools.zbuffer) return RAST_ERR_INVALID_ARGUMENT;
   if (b->total_setup > 0 && (!b->pools.faces || !b->pools.position)) return RAST_ERR_INVALID_ARGUMENT;
   if (b->total_vout > 0 && !b->pools.position) return RAST_ERR_INVALID_ARGUMENT;

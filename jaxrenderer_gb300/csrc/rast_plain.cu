@@ -61,7 +61,11 @@ setup_kernel(RastBatch B, const float4* __restrict__ clip, float4* __restrict__ 
 }
 
 // One CTA = one 16x16 pixel tile of one job; every primitive of the job is
-// staged through shared memory in chunks and tested by every pixel.
+// staged through shared memory in chunks and tested by every pixel.  Each
+// pixel keeps the kL smallest packed keys (kL = 1: the default chooser's
+// argmin; kL = RAST_MAX_LAYERS when the batch has layered jobs, whose slots
+// are the layered chooser's); slot s goes to winner[s * total_pixels + pix].
+template <int kL>
 __global__ void __launch_bounds__(kScanThreads)
 scan_kernel(RastBatch B, const float4* __restrict__ setup, int32_t* __restrict__ winner) {
   __shared__ float4 s_rec[kScanChunk * 3];
@@ -78,7 +82,9 @@ scan_kernel(RastBatch B, const float4* __restrict__ setup, int32_t* __restrict__
   const float x = (static_cast<float>(i) - J.viewport[3]) / J.viewport[0];
   const float y = (static_cast<float>(j) - J.viewport[7]) / J.viewport[5];
   const float vp22 = J.viewport[10], vp23 = J.viewport[11];
-  unsigned long long best = kEmptyKey;
+  unsigned long long best[kL];
+#pragma unroll
+  for (int l = 0; l < kL; ++l) best[l] = kEmptyKey;
   uint32_t second = 0xffffffffu;
   const float4* rec = setup + J.setup_begin * 4;
   for (int base = 0; base < F; base += kScanChunk) {
@@ -101,12 +107,12 @@ scan_kernel(RastBatch B, const float4* __restrict__ setup, int32_t* __restrict__
           const float z = ((c0 * cz.y + c1 * cz.z) + c2 * cz.w) * vp22 + vp23;
           const unsigned long long key = pack_key(z, base + p);
           const uint32_t o = static_cast<uint32_t>(key >> 32);
-          if (key < best) {
-            second = min(second, static_cast<uint32_t>(best >> 32));
-            best = key;
+          if (key < best[0]) {
+            second = min(second, static_cast<uint32_t>(best[0] >> 32));
           } else {
             second = min(second, o);
           }
+          insert_key<kL>(best, key);
         }
       }
     }
@@ -114,14 +120,21 @@ scan_kernel(RastBatch B, const float4* __restrict__ setup, int32_t* __restrict__
   }
   const bool valid = i < W && j < H;
   if (valid) {
-    const uint32_t o1 = static_cast<uint32_t>(best >> 32);
-    winner[J.pixel_begin + static_cast<int64_t>(i) * H + j] =
-        (best == kEmptyKey || o1 == kInfOrder) ? -1 : static_cast<int32_t>(best & 0xffffffffu);
+    const int64_t pix = J.pixel_begin + static_cast<int64_t>(i) * H + j;
+#pragma unroll
+    for (int l = 0; l < kL; ++l) {
+      const uint32_t o = static_cast<uint32_t>(best[l] >> 32);
+      winner[l * B.total_pixels + pix] =
+          (best[l] == kEmptyKey || o == kInfOrder) ? -1 : static_cast<int32_t>(best[l] & 0xffffffffu);
+    }
   }
-  if (B.near_ties) count_near_tie(B.near_ties, valid && is_near_tie(best, second));
+  if (B.near_ties) count_near_tie(B.near_ties, valid && is_near_tie(best[0], second));
 }
 
-// One thread per pixel: the chosen primitive's fragment, mixed and merged.
+// One thread per pixel: the chosen primitive's fragment, mixed and merged
+// (kLayered: the batch has layered jobs, whose pixels shade and mix every
+// slot).
+template <bool kLayered>
 __global__ void __launch_bounds__(kScanThreads)
 shade_kernel(RastBatch B, const float4* __restrict__ setup, const float* __restrict__ var,
              int vstride, const int32_t* __restrict__ winner) {
@@ -139,8 +152,12 @@ shade_kernel(RastBatch B, const float4* __restrict__ setup, const float* __restr
   if (i >= W || j >= H) return;
   const int64_t pix = J.pixel_begin + static_cast<int64_t>(i) * H + j;
   PixelResult r;
-  resolve_pixel(J, B.pools, setup + J.setup_begin * 4, i, j, winner[pix],
-                VaryingSource{var, vstride, J.vout_begin}, &r);
+  const VaryingSource src{var, vstride, J.vout_begin};
+  const int L = kLayered ? job_layers(J, B.max_layers) : 0;
+  if (kLayered && L > 0)
+    resolve_layers(J, B.pools, setup + J.setup_begin * 4, i, j, winner + pix, B.total_pixels, L, src, &r);
+  else
+    resolve_pixel(J, B.pools, setup + J.setup_begin * 4, i, j, winner[pix], src, &r);
   store_pixel(J, B.pools, pix, r);
 }
 
@@ -165,7 +182,9 @@ static PlainLayout plain_layout(const RastBatch& b) {
   L.setup_off = off;
   off = align256(off + static_cast<size_t>(b.total_setup) * 4 * sizeof(float4));
   L.winner_off = off;
-  off = align256(off + static_cast<size_t>(b.total_pixels) * sizeof(int32_t));
+  // one slot per pixel, or RAST_MAX_LAYERS (every slot scan_kernel writes) with layered jobs
+  const size_t slots = b.max_layers > 0 ? RAST_MAX_LAYERS : 1;
+  off = align256(off + static_cast<size_t>(b.total_pixels) * slots * sizeof(int32_t));
   L.total = off;
   return L;
 }
@@ -210,9 +229,15 @@ static int render_plain(const RastBatch* batch, void* workspace, size_t workspac
     const int tiles = ((b.max_width + kTile - 1) / kTile) * ((b.max_height + kTile - 1) / kTile);
     const dim3 grid(static_cast<unsigned>(tiles), static_cast<unsigned>(b.n_jobs));
     const dim3 block(kTile, kTile);
-    scan_kernel<<<grid, block, 0, s>>>(b, setup, winner);
+    if (b.max_layers > 0)
+      scan_kernel<RAST_MAX_LAYERS><<<grid, block, 0, s>>>(b, setup, winner);
+    else
+      scan_kernel<1><<<grid, block, 0, s>>>(b, setup, winner);
     prof.mark("scan_kernel");
-    shade_kernel<<<grid, block, 0, s>>>(b, setup, var, L.vstride, winner);
+    if (b.max_layers > 0)
+      shade_kernel<true><<<grid, block, 0, s>>>(b, setup, var, L.vstride, winner);
+    else
+      shade_kernel<false><<<grid, block, 0, s>>>(b, setup, var, L.vstride, winner);
     prof.mark("shade_kernel");
   }
   const cudaError_t e = cudaGetLastError();

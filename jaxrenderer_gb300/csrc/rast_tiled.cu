@@ -543,8 +543,10 @@ scatter_kernel(RastBatch B, Geometry G, const int2* __restrict__ fmap, const ush
 // PPL pixels of the tile.  Bin entries are staged 32 at a time in the warp's
 // slice of shared memory (one record per lane), then every lane tests its
 // pixels against the 32 staged setups.  Tiles whose bin overflowed scan
-// every primitive of the job instead.
-template <int TW, int TH, bool kKeys, bool kTies>
+// every primitive of the job instead.  Each pixel keeps its kL smallest
+// keys (kL = 1: the default chooser; kL = RAST_MAX_LAYERS for batches with
+// layered jobs), slot s written to winner[s * total_pixels + pixel].
+template <int TW, int TH, bool kKeys, bool kTies, int kL>
 __global__ void __launch_bounds__(32 * kRasterWarps)
 raster_kernel(RastBatch B, Geometry G, const float4* __restrict__ setup,
               const uint32_t* __restrict__ counts, const uint32_t* __restrict__ offsets,
@@ -585,7 +587,7 @@ raster_kernel(RastBatch B, Geometry G, const float4* __restrict__ setup,
     const int pj = ty * TH + lane % TH;
     const float y = (static_cast<float>(pj) - oy) / sy;
     float x[PPL], best_z[PPL];
-    unsigned long long best[PPL];
+    unsigned long long best[PPL][kL];
     uint32_t second[PPL];
     unsigned z_known = 0;  // bit q: best_z[q] holds the depth of best[q] (set by this kernel's tests)
 #pragma unroll
@@ -593,7 +595,9 @@ raster_kernel(RastBatch B, Geometry G, const float4* __restrict__ setup,
       const int pi = tx * TW + q * LPC + lane / TH;
       x[q] = (static_cast<float>(pi) - ox) / sx;
       // the minimum over the faces the setup kernel rasterised itself
-      best[q] = (kKeys && pi < W && pj < H) ? keys[J.pixel_begin + static_cast<int64_t>(pi) * H + pj] : kEmptyKey;
+      best[q][0] = (kKeys && pi < W && pj < H) ? keys[J.pixel_begin + static_cast<int64_t>(pi) * H + pj] : kEmptyKey;
+#pragma unroll
+      for (int l = 1; l < kL; ++l) best[q][l] = kEmptyKey;
       best_z[q] = 0.0f;
       second[q] = 0xffffffffu;
     }
@@ -643,14 +647,14 @@ raster_kernel(RastBatch B, Geometry G, const float4* __restrict__ setup,
             if (id >= 0) {
               const float z = ((c0 * cz.y + c1 * cz.z) + c2 * cz.w) * vp22 + vp23;
               const unsigned long long key = pack_key(z, id);
-              if (key < best[q]) {
-                if (kTies) second[q] = min(second[q], static_cast<uint32_t>(best[q] >> 32));
-                best[q] = key;
+              if (key < best[q][0]) {
+                if (kTies) second[q] = min(second[q], static_cast<uint32_t>(best[q][0] >> 32));
                 best_z[q] = z;
                 z_known |= 1u << q;
               } else if (kTies) {
                 second[q] = min(second[q], static_cast<uint32_t>(key >> 32));
               }
+              insert_key<kL>(best[q], key);
             }
           }
         }
@@ -658,20 +662,29 @@ raster_kernel(RastBatch B, Geometry G, const float4* __restrict__ setup,
       __syncwarp();
     }
     const bool depth_only = J.shader == RAST_SHADER_DEPTH;
+    const int layers = kL > 1 ? job_layers(J, B.max_layers) : 0;
 #pragma unroll
     for (int q = 0; q < PPL; ++q) {
       const int pi = tx * TW + q * LPC + lane / TH;
       if (pi < W && pj < H) {
-        const uint32_t o1 = static_cast<uint32_t>(best[q] >> 32);
-        const bool found = !(best[q] == kEmptyKey || o1 == kInfOrder);
+        const uint32_t o1 = static_cast<uint32_t>(best[q][0] >> 32);
+        const bool found = !(best[q][0] == kEmptyKey || o1 == kInfOrder);
         const int64_t pix = J.pixel_begin + static_cast<int64_t>(pi) * H + pj;
-        if (kTies && is_near_tie(best[q], second[q])) ++tie_count;
+        if (kTies && is_near_tie(best[q][0], second[q])) ++tie_count;
         if (!depth_only) {
-          const int32_t w = found ? static_cast<int32_t>(best[q] & 0xffffffffu) : -1;
+          const int32_t w = found ? static_cast<int32_t>(best[q][0] & 0xffffffffu) : -1;
           winner[pix] = w;
           // faces whose varyings the shade needs: winners, and face 0 for the
-          // chooser's fallback
-          if (visible && J.n_faces > 0) visible[J.setup_begin + (w < 0 ? 0 : w)] = 1;
+          // default chooser's fallback
+          if (visible && J.n_faces > 0 && (layers == 0 || w >= 0)) visible[J.setup_begin + (w < 0 ? 0 : w)] = 1;
+#pragma unroll
+          for (int l = 1; l < kL; ++l) {
+            const uint32_t o = static_cast<uint32_t>(best[q][l] >> 32);
+            const int32_t wl = (best[q][l] == kEmptyKey || o == kInfOrder) ? -1
+                                                                          : static_cast<int32_t>(best[q][l] & 0xffffffffu);
+            winner[l * B.total_pixels + pix] = wl;
+            if (visible && wl >= 0 && l < layers) visible[J.setup_begin + wl] = 1;
+          }
           continue;
         }
         // DepthShader: the fragment keeps everything and writes the default
@@ -679,7 +692,7 @@ raster_kernel(RastBatch B, Geometry G, const float4* __restrict__ setup,
         // resolve_pixel): the winner's depth, or primitive 0's chooser fallback.
         bool keep = found;
         float z = best_z[q];
-        int prim = found ? static_cast<int>(best[q] & 0xffffffffu) : 0;
+        int prim = found ? static_cast<int>(best[q][0] & 0xffffffffu) : 0;
         if (kKeys && found && !(z_known & (1u << q))) {
           // the winner came from the setup kernel's own rasterisation: its
           // depth again, with the same operations
@@ -753,9 +766,11 @@ face_varyings_kernel(RastBatch B, const int2* __restrict__ fmap, const unsigned 
 }
 
 // Deferred shading: one thread per pixel of every job, reading the winner's
-// corner varyings computed once per visible face.
+// corner varyings computed once per visible face (kLayered: the batch has
+// layered jobs, whose pixels shade and mix every slot).
 // Grid: (ceil(max pixels per job / 256), n_jobs).
-__global__ void __launch_bounds__(256, 4)  // 4 blocks per SM: 64 registers
+template <bool kLayered>
+__global__ void __launch_bounds__(256, kLayered ? 2 : 4)  // 4 blocks per SM: 64 registers
 tiled_shade_kernel(RastBatch B, const float4* __restrict__ setup, const int32_t* __restrict__ winner,
                    bool depth_resolved, const float* __restrict__ fvar, int vstride) {
   __shared__ RastJob sJ;
@@ -773,7 +788,11 @@ tiled_shade_kernel(RastBatch B, const float4* __restrict__ setup, const int32_t*
   pixel_of(local0, npx, J.height, &i, &j);
   PixelResult r;
   VaryingSource src{nullptr, vstride, 0, fvar, J.setup_begin};
-  resolve_pixel(J, B.pools, setup + J.setup_begin * 4, i, j, winner[pix], src, &r);
+  const int L = kLayered ? job_layers(J, B.max_layers) : 0;
+  if (kLayered && L > 0)
+    resolve_layers(J, B.pools, setup + J.setup_begin * 4, i, j, winner + pix, B.total_pixels, L, src, &r);
+  else
+    resolve_pixel(J, B.pools, setup + J.setup_begin * 4, i, j, winner[pix], src, &r);
   store_pixel(J, B.pools, pix, r);
 }
 
@@ -792,6 +811,7 @@ struct Layout {
   unsigned fmap_blocks;
   bool small_path;  // setup kernel rasterises small faces (not when near ties are counted)
   int vstride;
+  int winner_layers;  // chooser slots kept per pixel: 1, or RAST_MAX_LAYERS with layered jobs
   int64_t n_tiles, n_scan_blocks;
   uint64_t bin_capacity;
   Geometry G;
@@ -820,7 +840,8 @@ static Layout layout(const RastBatch& b, TileShape ts, uint64_t bin_capacity, in
   L.offsets_off = take(static_cast<size_t>(L.n_tiles) * 4);
   L.bsums_off = take(static_cast<size_t>(L.n_scan_blocks) * 4);
   L.bins_off = take(static_cast<size_t>(bin_capacity) * 4);
-  L.winner_off = take(static_cast<size_t>(b.total_pixels) * 4);
+  L.winner_layers = b.max_layers > 0 ? RAST_MAX_LAYERS : 1;  // the raster variant writes every slot
+  L.winner_off = take(static_cast<size_t>(b.total_pixels) * 4 * L.winner_layers);
   int vstride = 0;
   for (int sh = 0; sh < 7; ++sh)
     if (b.shader_mask & (1 << sh)) vstride = std::max(vstride, varying_count(sh));
@@ -831,7 +852,7 @@ static Layout layout(const RastBatch& b, TileShape ts, uint64_t bin_capacity, in
   L.fmap_blocks = block_map_capacity(b.total_setup, b.n_jobs, kSetupThreads);
   L.fmap_off = take(static_cast<size_t>(L.fmap_blocks) * sizeof(int2));
   L.fstart_off = take(block_start_bytes(b.n_jobs));
-  L.small_path = b.near_ties == nullptr && small_area > 0;
+  L.small_path = b.near_ties == nullptr && small_area > 0 && b.max_layers == 0;
   L.keys_off = take(L.small_path ? static_cast<size_t>(b.total_pixels) * sizeof(unsigned long long) : 0);
   L.misc_off = take(256);
   L.total = off;
@@ -850,33 +871,38 @@ static bool valid_shape(TileShape t) {
          (t.tw == 4 && t.th == 8);
 }
 
-template <bool kKeys, bool kTies>
+// Shapes with a layered raster variant: at most four pixels per lane, so
+// the RAST_MAX_LAYERS keys of every pixel stay in registers.
+static bool valid_layered_shape(TileShape t) {
+  return (t.tw == 8 && t.th == 8) || (t.tw == 16 && t.th == 8) || (t.tw == 8 && t.th == 4) ||
+         (t.tw == 4 && t.th == 8);
+}
+
+template <bool kKeys, bool kTies, int kL>
 static void launch_raster(TileShape ts, unsigned grid, cudaStream_t s, const RastBatch& b, const Layout& L,
                           const float4* setup, const uint32_t* counts, const uint32_t* offsets, const int32_t* bins,
                           int32_t* winner, unsigned int* misc, unsigned char* vis,
                           const unsigned long long* keys) {
   const unsigned block = 32 * kRasterWarps;
+  auto go = [&](auto kernel) {
+    kernel<<<grid, block, 0, s>>>(b, L.G, setup, counts, offsets, bins, winner, misc, L.n_tiles, vis, keys);
+  };
   if (ts.tw == 8 && ts.th == 8)
-    raster_kernel<8, 8, kKeys, kTies><<<grid, block, 0, s>>>(b, L.G, setup, counts, offsets, bins, winner, misc, L.n_tiles,
-                                                      vis, keys);
-  else if (ts.tw == 16 && ts.th == 16)
-    raster_kernel<16, 16, kKeys, kTies><<<grid, block, 0, s>>>(b, L.G, setup, counts, offsets, bins, winner, misc,
-                                                        L.n_tiles, vis, keys);
-  else if (ts.tw == 32 && ts.th == 8)
-    raster_kernel<32, 8, kKeys, kTies><<<grid, block, 0, s>>>(b, L.G, setup, counts, offsets, bins, winner, misc,
-                                                       L.n_tiles, vis, keys);
-  else if (ts.tw == 8 && ts.th == 32)
-    raster_kernel<8, 32, kKeys, kTies><<<grid, block, 0, s>>>(b, L.G, setup, counts, offsets, bins, winner, misc,
-                                                       L.n_tiles, vis, keys);
+    go(raster_kernel<8, 8, kKeys, kTies, kL>);
   else if (ts.tw == 8 && ts.th == 4)
-    raster_kernel<8, 4, kKeys, kTies><<<grid, block, 0, s>>>(b, L.G, setup, counts, offsets, bins, winner, misc,
-                                                      L.n_tiles, vis, keys);
+    go(raster_kernel<8, 4, kKeys, kTies, kL>);
   else if (ts.tw == 4 && ts.th == 8)
-    raster_kernel<4, 8, kKeys, kTies><<<grid, block, 0, s>>>(b, L.G, setup, counts, offsets, bins, winner, misc,
-                                                      L.n_tiles, vis, keys);
-  else
-    raster_kernel<16, 8, kKeys, kTies><<<grid, block, 0, s>>>(b, L.G, setup, counts, offsets, bins, winner, misc,
-                                                       L.n_tiles, vis, keys);
+    go(raster_kernel<4, 8, kKeys, kTies, kL>);
+  else if (ts.tw == 16 && ts.th == 8)
+    go(raster_kernel<16, 8, kKeys, kTies, kL>);
+  else if constexpr (kL == 1) {  // eight pixels per lane: default chooser only
+    if (ts.tw == 16 && ts.th == 16)
+      go(raster_kernel<16, 16, kKeys, kTies, kL>);
+    else if (ts.tw == 32 && ts.th == 8)
+      go(raster_kernel<32, 8, kKeys, kTies, kL>);
+    else
+      go(raster_kernel<8, 32, kKeys, kTies, kL>);
+  }
 }
 
 static int render(const RastBatch* batch, const RastTiledConfig* cfg, void* workspace,
@@ -886,6 +912,7 @@ static int render(const RastBatch* batch, const RastTiledConfig* cfg, void* work
   const RastBatch& b = *batch;
   TileShape ts{cfg ? cfg->tile_w : 8, cfg ? cfg->tile_h : 8};
   if (!valid_shape(ts)) return RAST_ERR_INVALID_ARGUMENT;
+  if (b.max_layers > 0 && !valid_layered_shape(ts)) return RAST_ERR_UNSUPPORTED;
   const uint64_t cap = cfg && cfg->bin_capacity > 0 ? cfg->bin_capacity : default_bin_capacity(b);
   const int small_area = small_area_of(cfg);
   const Layout L = layout(b, ts, cap, small_area);
@@ -946,15 +973,22 @@ static int render(const RastBatch* batch, const RastTiledConfig* cfg, void* work
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (b.total_setup > 0) {
       const unsigned grid = static_cast<unsigned>(std::max(sms, 1) * 8);
-      // the key path exists only when ties are not counted
+      // the key path exists only when ties are not counted and no job is
+      // layered
       if (keys)
-        launch_raster<true, false>(ts, grid, s, b, L, setup, counts, offsets, bins, winner, misc, vis, keys);
+        launch_raster<true, false, 1>(ts, grid, s, b, L, setup, counts, offsets, bins, winner, misc, vis, keys);
+      else if (b.max_layers > 0 && b.near_ties)
+        launch_raster<false, true, RAST_MAX_LAYERS>(ts, grid, s, b, L, setup, counts, offsets, bins, winner, misc,
+                                                    vis, nullptr);
+      else if (b.max_layers > 0)
+        launch_raster<false, false, RAST_MAX_LAYERS>(ts, grid, s, b, L, setup, counts, offsets, bins, winner, misc,
+                                                     vis, nullptr);
       else if (b.near_ties)
-        launch_raster<false, true>(ts, grid, s, b, L, setup, counts, offsets, bins, winner, misc, vis, nullptr);
+        launch_raster<false, true, 1>(ts, grid, s, b, L, setup, counts, offsets, bins, winner, misc, vis, nullptr);
       else
-        launch_raster<false, false>(ts, grid, s, b, L, setup, counts, offsets, bins, winner, misc, vis, nullptr);
+        launch_raster<false, false, 1>(ts, grid, s, b, L, setup, counts, offsets, bins, winner, misc, vis, nullptr);
     } else {
-      if (cudaMemsetAsync(winner, 0xff, static_cast<size_t>(b.total_pixels) * 4, s) != cudaSuccess)
+      if (cudaMemsetAsync(winner, 0xff, static_cast<size_t>(b.total_pixels) * 4 * L.winner_layers, s) != cudaSuccess)
         return RAST_ERR_CUDA;
     }
     prof.mark("raster_kernel");
@@ -966,8 +1000,12 @@ static int render(const RastBatch* batch, const RastTiledConfig* cfg, void* work
         face_varyings_kernel<<<L.fmap_blocks, kFaceThreads, 0, s>>>(b, fmap, vis, fvar, L.vstride);
         prof.mark("face_varyings_kernel");
       }
-      tiled_shade_kernel<<<sgrid, 256, 0, s>>>(b, setup, winner, b.total_setup > 0, pre ? fvar : nullptr,
-                                               L.vstride);
+      if (b.max_layers > 0)
+        tiled_shade_kernel<true><<<sgrid, 256, 0, s>>>(b, setup, winner, b.total_setup > 0, pre ? fvar : nullptr,
+                                                       L.vstride);
+      else
+        tiled_shade_kernel<false><<<sgrid, 256, 0, s>>>(b, setup, winner, b.total_setup > 0, pre ? fvar : nullptr,
+                                                        L.vstride);
       prof.mark("tiled_shade_kernel");
     }
   }

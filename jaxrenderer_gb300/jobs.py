@@ -66,6 +66,13 @@ class JobSpec:
     shadow_strength: np.ndarray = field(default_factory=lambda: np.zeros(3, F32))
     depth_offset: float = 0.0
     apply_depth_offset: bool = False
+    # compiled primitive_chooser / mix hooks (rast_gb300.h, RastMixer):
+    # layers 0 = the default chooser, 1..4 = that many nearest candidates
+    layers: int = 0
+    mixer: int = 0  # _lib.MIX_NEAREST or _lib.MIX_OVER
+    opacity: float = 1.0  # MIX_OVER, every face (without face_alpha)
+    background: Any = (0.0, 0.0, 0.0)  # MIX_OVER, seen through the last layer
+    face_alpha: Any = None  # MIX_OVER, (F,) opacity per face
 
     @property
     def n_verts(self) -> int:
@@ -204,6 +211,8 @@ def pack(specs: Sequence[JobSpec], zbuffers: Sequence[Any], canvases: Sequence[A
     tex, spm, nmp, tsh, shm = (_Pool(torch.float32, 1), _Pool(torch.float32, 1), _Pool(torch.float32, 1),
                                _Pool(torch.int32, 2), _Pool(torch.float32, 1))
     zb, cv = _Pool(torch.float32, 1), _Pool(torch.float32, 3)
+    alp = _Pool(torch.float32, 1)  # row-aligned with faces
+    max_layers = 0
     vout = setup = pixels = 0
     pixel_begin = []
     mask = 0
@@ -222,6 +231,13 @@ def pack(specs: Sequence[JobSpec], zbuffers: Sequence[Any], canvases: Sequence[A
                     pool.add(np.zeros((J.vert_begin - pool.rows, pool.row), np.float32 if pool.dtype == torch.float32 else np.int32))
                 pool.add(arr)
         J.face_begin = fac.add(s.faces)
+        if s.face_alpha is not None:
+            fa = _host_or_device(s.face_alpha, np.float32).reshape(-1)
+            if int(fa.shape[0]) != F:
+                raise ValueError(f"job {k}: face_alpha has {int(fa.shape[0])} entries for {F} faces")
+            if alp.rows < J.face_begin:
+                alp.add(np.zeros(J.face_begin - alp.rows, np.float32))
+            alp.add(fa)
         if s.darboux_faces is not None:
             J.darboux_face_begin = dfc.add(s.darboux_faces)
             J.n_darboux_faces = int(s.darboux_faces.shape[0])
@@ -249,7 +265,12 @@ def pack(specs: Sequence[JobSpec], zbuffers: Sequence[Any], canvases: Sequence[A
             J.shadow_begin = shm.add(s.shadow_map)
             J.shadow_w, J.shadow_h = (int(d) for d in s.shadow_map.shape[:2])
         J.depth_offset = float(np.float32(s.depth_offset))
-        J.flags = _lib.JOB_APPLY_DEPTH_OFFSET if s.apply_depth_offset else 0
+        J.flags = (_lib.JOB_APPLY_DEPTH_OFFSET if s.apply_depth_offset else 0) | (
+            _lib.JOB_FACE_ALPHA if s.face_alpha is not None else 0)
+        J.layers, J.mixer = int(s.layers), int(s.mixer)
+        J.opacity = float(np.float32(s.opacity))
+        _lib.as_c_floats(J.background, _f3(s.background))
+        max_layers = max(max_layers, J.layers)
         for name in ("viewport", "world_to_clip", "world_to_eye_norm", "shadow_viewport", "shadow_world_to_clip"):
             _lib.as_c_floats(getattr(J, name), np.asarray(getattr(s, name), F32).reshape(-1))
         for name in ("light_direction", "light_colour", "light_dir_eye", "ambient", "diffuse", "specular", "shadow_strength"):
@@ -275,7 +296,8 @@ def pack(specs: Sequence[JobSpec], zbuffers: Sequence[Any], canvases: Sequence[A
     tensors = {name: dev(p) for name, p in (
         ("position", pos), ("normal", nrm), ("uv", uvp), ("colour", col), ("texture_index", tix),
         ("id_to_face", i2f), ("faces", fac), ("darboux_faces", dfc), ("texture", tex),
-        ("specular_map", spm), ("normal_map", nmp), ("texture_shape", tsh), ("shadow_map", shm))}
+        ("specular_map", spm), ("normal_map", nmp), ("texture_shape", tsh), ("shadow_map", shm),
+        ("face_alpha", alp))}
     zbuf = zb.tensor(device).clone()
     canvas = None
     if cv.parts:
@@ -293,6 +315,7 @@ def pack(specs: Sequence[JobSpec], zbuffers: Sequence[Any], canvases: Sequence[A
     b.max_width, b.max_height, b.max_verts, b.max_faces = maxw, maxh, maxv, maxf
     b.shader_mask = mask
     b.total_vout, b.total_setup, b.total_pixels = vout, setup, pixels
+    b.max_layers = max_layers
     P = b.pools
     for name, t in tensors.items():
         setattr(P, name, _ptr(t))

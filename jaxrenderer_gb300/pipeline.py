@@ -16,6 +16,7 @@ import torch
 
 from . import jobs as _jobs
 from .geometry import Camera
+from .hooks import apply_hooks
 from .shader import kernel_id_of
 from .types import Buffers
 
@@ -50,6 +51,7 @@ def render_with_ids(camera: Camera, shader, buffers: Buffers, face_indices, extr
     width, height = int(zbuffer.shape[0]), int(zbuffer.shape[1])
     spec = _jobs.job_from_extra(sid, camera, extra, width, height)
     spec.faces = _faces(face_indices)
+    apply_hooks(spec, shader)
     canvas = buffers.targets[0] if len(buffers.targets) > 0 else None
     z, c, p, ties = render_job(spec, zbuffer, canvas, count_ties=count_ties)
     targets = (c,) if c is not None else ()
@@ -57,7 +59,9 @@ def render_with_ids(camera: Camera, shader, buffers: Buffers, face_indices, extr
 
 
 def render(camera: Camera, shader, buffers: Buffers, face_indices, extra, loop_unroll: int = 1) -> Buffers:
-    """Render a scene with a built-in shader (pipeline.py:470-537).
+    """Render a scene with a built-in shader (pipeline.py:470-537), with the
+    default chooser / mix or the compiled hooks of `hooks` assigned to the
+    shader's `primitive_chooser` / `mix`.
 
     `loop_unroll` is accepted for API compatibility; the CUDA kernels have
     no row loop to unroll.

@@ -62,6 +62,7 @@ def _scene_struct(real):
             ("shadow_map", R), ("shadow_w", c_int), ("shadow_h", c_int),
             ("shadow_world_to_clip", R), ("shadow_viewport", R), ("shadow_strength", R3),
             ("zbuffer", R), ("canvas", R), ("prim_id", I), ("near_ties", c_longlong),
+            ("layers", c_int), ("mixer", c_int), ("opacity", real), ("background", R3), ("face_alpha", R),
         ]
 
     return Scene
@@ -168,6 +169,16 @@ def render(spec, zbuffer, canvas=None, n_threads: int = 1, dtype=np.float32):
         s.shadow_w, s.shadow_h = shm.shape[:2]
     s.shadow_world_to_clip = rp(spec.shadow_world_to_clip)
     s.shadow_viewport = rp(spec.shadow_viewport)
+    s.layers = int(getattr(spec, "layers", 0))
+    s.mixer = int(getattr(spec, "mixer", 0))
+    s.opacity = float(getattr(spec, "opacity", 1.0))
+    bg = _np(getattr(spec, "background", (0.0, 0.0, 0.0)), dtype).reshape(-1)
+    if bg.size == 1:
+        bg = np.repeat(bg, 3)
+    for k in range(3):
+        s.background[k] = float(bg[k])
+    if getattr(spec, "face_alpha", None) is not None:
+        s.face_alpha = rp(_np(spec.face_alpha, dtype).reshape(-1))
     z = np.array(_np(zbuffer, dtype), copy=True)
     s.zbuffer = z.ctypes.data_as(POINTER(real))
     c = None

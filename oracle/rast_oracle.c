@@ -85,6 +85,11 @@ typedef struct Scene {
   real* canvas;
   int* prim_id;
   long long near_ties;
+  int layers;
+  int mixer;
+  real opacity;
+  real background[3];
+  const real* face_alpha;
 } Scene;
 
 /* ---------------------------------------------------------------- basics */
@@ -518,6 +523,112 @@ static int fragment(const Scene* s, const VOut* v0, const VOut* v1, const VOut* 
 
 /* ------------------------------------------------------------- pipeline */
 
+/* Depth order of the choosers: NaN first (argmin's NaN rule), -0 == +0,
+ * then ascending; equal depths (both NaN included) are ordered by index. */
+static inline int depth_before(real za, int ia, real zb, int ib) {
+  int na = za != za, nb = zb != zb;
+  if (na || nb) return na && nb ? ia < ib : na;
+  if (za < zb) return 1;
+  if (zb < za) return 0;
+  return ia < ib;
+}
+
+/* Interpolation + fragment of primitive `p` at pixel (x, y)
+ * (pipeline.py:283-326): keeps `chooser_keep` (keep & inside), depth,
+ * colour; returns the fragment shader's keep. */
+static int shade_prim(const Scene* s, const VOut* vo, const Prim* pr, int p, real x, real y, int* chooser_keep,
+                      real* z, real* colour) {
+  const Prim* P = pr + p;
+  real c[3];
+  clip_coef(P, x, y, c);
+  real w_rcp = (c[0] + c[1]) + c[2];
+  int in_tri = c[0] >= (real)0 && c[1] >= (real)0 && c[2] >= (real)0;
+  *chooser_keep = P->keep && in_tri;
+  *z = frag_depth(P, c, s->viewport);
+  real b[3] = {c[0] / w_rcp, c[1] / w_rcp, c[2] / w_rcp};
+  const int* face = s->faces + 3 * p;
+  colour[0] = colour[1] = colour[2] = 0;
+  return fragment(s, vo + face[0], vo + face[1], vo + face[2], b, P->front, colour);
+}
+
+/* Layered chooser and its mixers: the compiled primitive_chooser / mix
+ * hooks at the override points shader.py:159-251 and :339-396.  The chooser
+ * keeps the L nearest candidates (keep & inside & front, depth not +inf) in
+ * depth_before order; slots past the last candidate are not kept.  Every
+ * kept slot is interpolated and shaded (pipeline.py:337-342).  Mixer 0 takes
+ * the first slot the fragment shader keeps (the default mix's argmin over
+ * kept depths, shader.py:374-396); mixer 1 composites the kept slots front to
+ * back: w = T * a, C = C + w * colour, T = T * (1 - a), then
+ * C + T * background.  Depth and primitive id are the first kept slot's. */
+#define OR_MAX_LAYERS 4
+static int layered_pixel(const Scene* s, const VOut* vo, const Prim* pr, int i, int j, real x, real y) {
+  const real* vp = s->viewport;
+  const int H = s->height, F = s->n_faces;
+  const int L = s->layers > OR_MAX_LAYERS ? OR_MAX_LAYERS : s->layers;
+  real sz[OR_MAX_LAYERS];
+  int si[OR_MAX_LAYERS];
+  int n = 0;
+  uint32_t ord1 = 0xFFFFFFFFu, ord2 = 0xFFFFFFFFu; /* two best candidate depths */
+  for (int p = 0; p < F; ++p) {
+    const Prim* P = pr + p;
+    real c[3];
+    clip_coef(P, x, y, c);
+    int in_tri = c[0] >= (real)0 && c[1] >= (real)0 && c[2] >= (real)0;
+    if (!(P->keep && in_tri && P->front)) continue;
+    real z = frag_depth(P, c, vp);
+    uint32_t o = depth_order(z);
+    if (o < ord1) {
+      ord2 = ord1;
+      ord1 = o;
+    } else if (o < ord2) {
+      ord2 = o;
+    }
+    if (z == (real)INFINITY) continue;
+    int pos = n;
+    while (pos > 0 && depth_before(z, p, sz[pos - 1], si[pos - 1])) --pos;
+    if (pos >= L) continue;
+    int last = n < L ? n : L - 1;
+    for (int k = last; k > pos; --k) {
+      sz[k] = sz[k - 1];
+      si[k] = si[k - 1];
+    }
+    sz[pos] = z;
+    si[pos] = p;
+    if (n < L) ++n;
+  }
+  int keep = 0, prim = -1;
+  real depth = 0, out[3] = {0, 0, 0}, C[3] = {0, 0, 0}, T = 1;
+  for (int k = 0; k < n; ++k) {
+    int ck;
+    real z, col[3];
+    int fk = shade_prim(s, vo, pr, si[k], x, y, &ck, &z, col);
+    if (!(ck && fk)) continue;
+    if (!keep) {
+      keep = 1;
+      prim = si[k];
+      depth = z;
+      if (s->mixer == 0) {
+        for (int ch = 0; ch < 3; ++ch) out[ch] = col[ch];
+        break;
+      }
+    }
+    real a = s->face_alpha ? s->face_alpha[si[k]] : s->opacity;
+    real w = T * a;
+    for (int ch = 0; ch < 3; ++ch) C[ch] = C[ch] + w * col[ch];
+    T = T * ((real)1 - a);
+  }
+  if (keep && s->mixer == 1)
+    for (int ch = 0; ch < 3; ++ch) out[ch] = C[ch] + T * s->background[ch];
+  size_t pix = (size_t)i * H + j;
+  if (keep) {
+    s->zbuffer[pix] = depth;
+    if (s->canvas)
+      for (int ch = 0; ch < 3; ++ch) s->canvas[pix * 3 + ch] = out[ch];
+  }
+  if (s->prim_id) s->prim_id[pix] = prim;
+  return ord2 != 0xFFFFFFFFu && ord2 - ord1 <= 1u && ord1 != depth_order((real)INFINITY);
+}
+
 /* pipeline.render (pipeline.py:470-537) + _postprocessing (:127-459). */
 static int render(Scene* s) {
   if (s->n_faces <= 0 || s->width <= 0 || s->height <= 0) {
@@ -544,6 +655,10 @@ static int render(Scene* s) {
     real x = ((real)i - vp[3]) / vp[0];
     for (int j = 0; j < H; ++j) {
       real y = ((real)j - vp[7]) / vp[5];
+      if (s->layers > 0) {
+        ties += layered_pixel(s, vo, pr, i, j, x, y);
+        continue;
+      }
       /* per-primitive preprocess + default primitive_chooser
        * (shader.py:207-217): argmin over where(keep & in & front, z, inf),
        * first index on ties, NaN first. */

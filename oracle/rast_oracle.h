@@ -72,6 +72,12 @@ typedef struct OrSceneF32 {
   float* canvas;                 /* (W,H,3) in/out, NULL for depth */
   int* prim_id;                  /* (W,H) out: written primitive or -1; may be NULL */
   long long near_ties;           /* out: pixels whose two best depths are <= 1 ulp apart */
+  /* compiled chooser / mix hooks (RastJob.layers / mixer in rast_gb300.h) */
+  int layers;                    /* 0: default chooser; 1..4: layered chooser */
+  int mixer;                     /* 0: nearest kept slot; 1: front-to-back over */
+  float opacity;                 /* over: every face's opacity (face_alpha NULL) */
+  float background[3];           /* over: colour behind the last layer */
+  const float* face_alpha;       /* over: (F) per-face opacity, or NULL */
 } OrSceneF32;
 
 /* Render one scene; `scene` points at an OrSceneF32 (f32 build) or its
