@@ -51,8 +51,9 @@ METRIC = "frames/s @84x84x4096 scenes fwd and fwd+bwd, tiled-batched vs plain GP
 UNIT = "frames/s"
 L2_BYTES = 129 * 1024 * 1024
 MIXED_CLASSES = [(32, 32), (84, 84), (480, 270)]
-WORKLOADS = ("brax84", "ant84", "cube640", "overdraw960", "phong128", "mixed1024")
-DEFAULT_SCENES = {"brax84": 4096, "ant84": 200, "cube640": 1, "overdraw960": 1, "phong128": 256, "mixed1024": 1024}
+WORKLOADS = ("brax84", "ant84", "cube640", "overdraw960", "phong128", "mixed1024", "glass84")
+DEFAULT_SCENES = {"brax84": 4096, "ant84": 200, "cube640": 1, "overdraw960": 1, "phong128": 256, "mixed1024": 1024,
+                  "glass84": 4096}
 
 
 def parse():
@@ -128,6 +129,35 @@ def build_brax84(n, rank, dev):
                     chain, work, groups, merges=merges, instances=inst,
                     config={"scenes": n, "mean_faces_per_scene": float(n_faces.mean()),
                             "objects": int(inst.n_instances), "resolution": [W, H], "shadow_map": list(shadow)})
+
+
+GLASS = {"layers": 4, "opacity": 0.6, "background": (0.55, 0.7, 0.9)}
+
+
+def build_glass84(n, rank, dev):
+    """The brax-like 84x84 batch through the compiled chooser / mix hooks:
+    the 4 nearest candidates of every pixel blended front to back with
+    opacity 0.6 over a sky colour (forward only)."""
+    from jaxrenderer_gb300 import _lib, batch as jb
+
+    wl = build_brax84(n, rank, dev)
+    hooks = dict(layers=GLASS["layers"], mixer=_lib.MIX_OVER, opacity=GLASS["opacity"],
+                 background=GLASS["background"])
+    for sb in wl.groups:
+        jb.set_layers(sb, **hooks)
+    brax_chain = wl.chain
+
+    def chain(k):
+        depth, main = brax_chain(k)
+        for name, v in hooks.items():
+            setattr(main, name, v)
+        return depth, main
+
+    wl.key, wl.chain, wl.bwd = "glass84", chain, None
+    wl.desc = ("brax-like 84x84 x 4096 scenes, phong_reflection_shadow + 128x128 depth pass, layered chooser "
+               "(4 nearest candidates) + over mixer (opacity 0.6)")
+    wl.config["hooks"] = {"primitive_chooser": "LayeredChooser(4)", "mix": "OverMixer(opacity=0.6)"}
+    return wl
 
 
 def build_cube640(n, rank, dev):
@@ -253,7 +283,7 @@ def build_ant84(n, rank, dev):
 
 
 BUILDERS = {"ant84": build_ant84, "brax84": build_brax84, "cube640": build_cube640, "overdraw960": build_overdraw960,
-            "phong128": build_phong128, "mixed1024": build_mixed1024}
+            "phong128": build_phong128, "mixed1024": build_mixed1024, "glass84": build_glass84}
 
 
 # ------------------------------------------------------------ CPU baseline
@@ -758,6 +788,7 @@ def pass_info(runner, pass_name):
         "vs": max(_VARYINGS[int(s)] for s in np.unique(sh)),
         "tests": float((px * jobs["n_faces"].astype(np.int64)).sum()),
         "main": bool((sh != 0).any()),
+        "slots": 4 if int(jobs["layers"].max()) > 0 else 1,  # chooser slots written per pixel
         "E": 0.0,
         "T": 0.0,
     }
@@ -771,23 +802,25 @@ def kernel_bytes(kname, info, visible):
     """Algorithmic bytes one launch of `kname` must move: inputs read once,
     outputs written once; re-reads served by caches are not counted.
     F faces, P pixels, E bin entries, T tiles, V faces visible in the main
-    pass, vs varyings per corner."""
+    pass (the front-most kept face of a pixel: with layered choosers a lower
+    bound), vs varyings per corner, S chooser slots written per pixel."""
     F, P, E, T, vs = info["F"], info["P"], info["E"], info["T"], info["vs"]
+    S = info.get("slots", 1)
     V = float(visible) if info["main"] else 0.0
     out_px = 16 if info["main"] else 4  # zbuffer (+ canvas) written
     table = {
         # plain form
         "vertex_kernel": info["cin"] + info["corners"] * (16 + 4 * vs),
         "setup_kernel": F * (12 + 3 * 16 + 64),
-        "scan_kernel": F * 48 + P * 4,
-        "shade_kernel": P * (4 + out_px) + info["Ptex"] + V * (64 + 3 * (16 + 4 * vs)),
+        "scan_kernel": F * 48 + P * 4 * S,
+        "shade_kernel": P * (4 * S + out_px) + info["Ptex"] + V * (64 + 3 * (16 + 4 * vs)),
         # tiled form
         "setup_bin_kernel": F * (12 + 36 + 64 + 8) + E * 4,
         "scan_kernels": T * 12,
         "scatter_kernel": F * 8 + E * 12,
-        "raster_kernel": F * 48 + E * 4 + P * 4,
+        "raster_kernel": F * 48 + E * 4 + P * 4 * S,
         "face_varyings_kernel": F + V * (12 + 3 * (info["cin"] / max(info["corners"], 1)) + 3 * 4 * vs),
-        "tiled_shade_kernel": P * (4 + out_px) + info["Ptex"] + V * (64 + 3 * 4 * vs),
+        "tiled_shade_kernel": P * (4 * S + out_px) + info["Ptex"] + V * (64 + 3 * 4 * vs),
     }
     return table.get(kname, 0.0)
 

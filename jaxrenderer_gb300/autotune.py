@@ -4,6 +4,8 @@ capacity per workload.
 For a pass (one RastBatch) the tile shapes 8x8, 16x8, 16x16, 32x8, 8x32,
 8x4 and 4x8 (pixels along x by y), each with the setup kernel's small-face
 rasterisation off and on, are timed on the batch itself; the fastest wins.
+Passes with layered-chooser jobs try the four shapes that have a layered
+raster variant, without the small-face path.
 The bin capacity is then set to 1.25x the bin entries that shape requested.
 Results are cached in a JSON file keyed by (width, height, faces-per-job
 bucket, shader mask, device name, SM count), so a workload class is tuned
@@ -24,6 +26,7 @@ import torch
 from . import _lib
 
 SHAPES = ((8, 8), (16, 8), (16, 16), (32, 8), (8, 32), (8, 4), (4, 8))
+LAYERED_SHAPES = ((8, 8), (16, 8), (8, 4), (4, 8))  # shapes with a layered-chooser raster variant
 SMALL_AREAS = (0, 32)  # small-face rasterisation in the setup kernel: off, or rectangles up to 32 pixels
 _LOCK = threading.Lock()
 
@@ -59,7 +62,9 @@ def workload_key(jobs: np.ndarray, device: torch.device) -> str:
     f = float(jobs["n_faces"].mean())
     bucket = 2 ** int(round(math.log2(max(f, 1.0))))
     mask = int(np.bitwise_or.reduce(1 << jobs["shader"].astype(np.int64)))
-    return f"v3|{w}x{h}|f~{bucket}|jobs~{2 ** int(round(math.log2(max(len(jobs), 1))))}|mask{mask}|{props.name}|sm{props.multi_processor_count}"
+    layers = int(jobs["layers"].max())
+    return (f"v3|{w}x{h}|f~{bucket}|jobs~{2 ** int(round(math.log2(max(len(jobs), 1))))}|mask{mask}"
+            + (f"|layers{layers}" if layers > 0 else "") + f"|{props.name}|sm{props.multi_processor_count}")
 
 
 def _time(runner, name, b, cfg, reps=3) -> float:
@@ -92,8 +97,9 @@ def tiled_config_for(runner, name: str, b, jobs: np.ndarray) -> "_lib.RastTiledC
         return _lib.RastTiledConfig(int(hit["tile_w"]), int(hit["tile_h"]), int(hit["bin_capacity"]),
                                     int(hit.get("small_area", 0)))
     best = None
-    for tw, th in SHAPES:
-        for small in SMALL_AREAS:
+    layered = int(jobs["layers"].max()) > 0  # no small-face path and fewer shapes
+    for tw, th in LAYERED_SHAPES if layered else SHAPES:
+        for small in (0,) if layered else SMALL_AREAS:
             cfg = _lib.RastTiledConfig(tw, th, 0, small)
             ms, entries = _time(runner, name, b, cfg)
             if best is None or ms < best[0]:
@@ -107,4 +113,4 @@ def tiled_config_for(runner, name: str, b, jobs: np.ndarray) -> "_lib.RastTiledC
     return _lib.RastTiledConfig(tw, th, cap, small)
 
 
-__all__ = ["tiled_config_for", "workload_key", "cache_path", "SHAPES", "SMALL_AREAS"]
+__all__ = ["tiled_config_for", "workload_key", "cache_path", "SHAPES", "LAYERED_SHAPES", "SMALL_AREAS"]

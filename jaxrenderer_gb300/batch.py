@@ -257,6 +257,26 @@ def scene_batch_from_instances(inst, width: int = 84, height: int = 84,
     return sb, merge
 
 
+def set_layers(sb: SceneBatch, layers: int, mixer: int = _lib.MIX_NEAREST, opacity=1.0,
+               background=(0.0, 0.0, 0.0)) -> None:
+    """Main-pass primitive_chooser / mix hooks of every scene of `sb`
+    (rast_gb300.h, RastMixer): the `layers` nearest candidates per pixel,
+    blended by `mixer` with `opacity` (one value, or one per scene) over
+    `background`.  Takes effect for runners created afterwards; the depth
+    pass keeps the default chooser."""
+    if not 0 <= int(layers) <= _lib.MAX_LAYERS:
+        raise ValueError(f"layers must be 0..{_lib.MAX_LAYERS}")
+    if mixer not in (_lib.MIX_NEAREST, _lib.MIX_OVER) or (mixer == _lib.MIX_OVER and layers == 0):
+        raise ValueError("mixer must be MIX_NEAREST, or MIX_OVER with layers >= 1")
+    t = sb.main_jobs
+    if layers > 0 and np.any(t["shader"] == _lib.SHADER_DEPTH):
+        raise ValueError("the DEPTH shader takes the default chooser only")
+    t["layers"] = int(layers)
+    t["mixer"] = int(mixer)
+    t["opacity"] = np.broadcast_to(np.asarray(opacity, F32), (len(t),))
+    t["background"] = np.broadcast_to(np.asarray(background, F32), (3,))
+
+
 def scene_batch_from_specs(specs, device=None) -> SceneBatch:
     """A SceneBatch of N independent single-pass jobs (same size and shader,
     no shadow pass) from JobSpecs, e.g. N differentiable scenes."""
@@ -299,6 +319,8 @@ def scene_job_specs(flat, tables, s: int):
     main.texture_offset = T
     for k in ("light_direction", "light_colour", "light_dir_eye", "ambient", "diffuse", "specular"):
         setattr(main, k, np.asarray(m[k], F32))
+    main.layers, main.mixer = int(m["layers"]), int(m["mixer"])
+    main.opacity, main.background = float(m["opacity"]), np.asarray(m["background"], F32)
     depth = None
     index = getattr(tables, "shadow_index", None)
     srow = s if index is None else int(index[s])
@@ -330,6 +352,7 @@ def _rast_batch(jobs: np.ndarray, pools: Dict[str, torch.Tensor], zbuffer: torch
     b.total_vout = int(jobs["n_verts"].astype(np.int64).sum())
     b.total_setup = int(jobs["n_faces"].astype(np.int64).sum())
     b.total_pixels = int((jobs["width"].astype(np.int64) * jobs["height"]).sum())
+    b.max_layers = max(int(jobs["layers"].max()), 0)
     P = b.pools
     for name, t in pools.items():
         setattr(P, name, t.data_ptr())
@@ -612,5 +635,6 @@ def render_batch(sb: SceneBatch, form: str = "plain", want_prim_id: bool = True)
 
 
 __all__ = ["SceneBatch", "SceneTables", "scene_batch_tables", "scene_batch_from_flat", "scene_batch_from_specs",
+           "set_layers",
            "scene_job_specs", "MultiRunner", "mixed_scene_batches", "scene_batch_from_instances",
            "flat_pools", "render_batch", "BatchRunner", "BatchOutputs", "job_table"]

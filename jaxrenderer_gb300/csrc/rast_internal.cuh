@@ -227,8 +227,8 @@ struct PixelResult {
   int prim;
 };
 
-// Interpolation and fragment shader of primitive p at pixel (i, j)
-// (pipeline.py:283-326): clip coefficients, chooser keep (keep & inside),
+// Interpolation and fragment shader of primitive p at the pixel whose NDC
+// coordinates are (x, y) (pipeline.py:283-326): clip coefficients, chooser keep (keep & inside),
 // depth, perspective-correct barycentrics, the corner varyings from `src`,
 // then the job's fragment shader.
 struct Fragment {
@@ -238,12 +238,16 @@ struct Fragment {
   float colour[3];
 };
 
+// Without xy_given, (x, y) is computed here from the pixel (i, j).
 __device__ __forceinline__ void shade_primitive(const RastJob& J, const RastPools& P, const float4* rec_base,
-                                                int i, int j, int p, const VaryingSource& src, Fragment* f) {
+                                                int i, int j, float x, float y, int p, const VaryingSource& src,
+                                                Fragment* f, bool xy_given) {
   const float4* rec = rec_base + static_cast<int64_t>(p) * 4;
   const float4 a = rec[0], b = rec[1], cz = rec[2], d = rec[3];
-  const float x = (static_cast<float>(i) - J.viewport[3]) / J.viewport[0];
-  const float y = (static_cast<float>(j) - J.viewport[7]) / J.viewport[5];
+  if (!xy_given) {
+    x = (static_cast<float>(i) - J.viewport[3]) / J.viewport[0];
+    y = (static_cast<float>(j) - J.viewport[7]) / J.viewport[5];
+  }
   const float c[3] = {(x * a.x + y * a.w) + b.z, (x * a.y + y * b.x) + b.w,
                       (x * a.z + y * b.y) + cz.x};
   const bool in_tri = c[0] >= 0.0f && c[1] >= 0.0f && c[2] >= 0.0f;
@@ -305,7 +309,7 @@ __device__ __forceinline__ void resolve_pixel(const RastJob& J, const RastPools&
   if (J.n_faces <= 0) return;
   const int p = w < 0 ? 0 : w;
   Fragment f;
-  shade_primitive(J, P, rec_base, i, j, p, src, &f);
+  shade_primitive(J, P, rec_base, i, j, 0.0f, 0.0f, p, src, &f, false);
   r->keep = f.chooser_keep && f.keep;
   r->z = f.z;
   r->prim = r->keep ? p : -1;
@@ -321,23 +325,34 @@ __device__ __forceinline__ int job_layers(const RastJob& J, int max_layers) {
 
 // One pixel of a layered job (RastJob.layers = L >= 1): slots
 // w[0 .. L-1] (stride `wstride`) hold the nearest candidates in ascending
-// (depth, id) order, -1 past the last.  Every slot runs interpolation +
-// fragment; the job's mixer combines the kept ones (RastMixer).
+// (depth, id) order, -1 past the last.  Every slot from `first` on runs
+// interpolation + fragment; the job's mixer combines the kept ones
+// (RastMixer).  first > 0 continues a nearest-mixer pixel whose earlier
+// slots were all discarded.
 __device__ __forceinline__ void resolve_layers(const RastJob& J, const RastPools& P, const float4* rec_base,
                                                int i, int j, const int32_t* w, int64_t wstride, int L,
-                                               const VaryingSource& src, PixelResult* r) {
+                                               const VaryingSource& src, PixelResult* r, int first = 0) {
   r->keep = false;
   r->prim = -1;
   r->z = 0.0f;
   r->colour[0] = r->colour[1] = r->colour[2] = 0.0f;
   const bool over = J.mixer == RAST_MIX_OVER;
   const bool per_face = (J.flags & RAST_JOB_FACE_ALPHA) && P.face_alpha;
+  const float x = (static_cast<float>(i) - J.viewport[3]) / J.viewport[0];
+  const float y = (static_cast<float>(j) - J.viewport[7]) / J.viewport[5];
+  // the slots, loaded up front and shifted down one per step (no indexed
+  // register array)
+  int w0 = first < 1 ? w[0] : -1, w1 = L > 1 && first < 2 ? w[wstride] : -1;
+  int w2 = L > 2 && first < 3 ? w[2 * wstride] : -1, w3 = L > 3 && first < 4 ? w[3 * wstride] : -1;
+  static_assert(RAST_MAX_LAYERS == 4, "slot registers w0..w3");
+  for (int s = 0; s < first; ++s) w0 = w1, w1 = w2, w2 = w3, w3 = -1;
   float T = 1.0f, C[3] = {0.0f, 0.0f, 0.0f};
-  for (int s = 0; s < L; ++s) {
-    const int p = w[s * wstride];
+  for (int s = first; s < L; ++s) {
+    const int p = w0;
+    w0 = w1, w1 = w2, w2 = w3, w3 = -1;
     if (p < 0) break;
     Fragment f;
-    shade_primitive(J, P, rec_base, i, j, p, src, &f);
+    shade_primitive(J, P, rec_base, i, j, x, y, p, src, &f, true);
     if (!(f.chooser_keep && f.keep)) continue;
     if (!r->keep) {
       r->keep = true;
@@ -358,6 +373,99 @@ __device__ __forceinline__ void resolve_layers(const RastJob& J, const RastPools
   if (r->keep && over) {
 #pragma unroll
     for (int k = 0; k < 3; ++k) r->colour[k] = C[k] + T * J.background[k];
+  }
+}
+
+// Fragments of one warp's pixels under the layered chooser: at most
+// RAST_MAX_LAYERS per pixel.
+constexpr int kWarpFrags = 32 * RAST_MAX_LAYERS;
+
+// Shared-memory staging of one warp's fragments for resolve_over_warp.
+struct WarpFrags {
+  float colour[3][kWarpFrags];
+  float z[kWarpFrags];
+  unsigned char keep[kWarpFrags];
+};
+
+// RAST_MIX_OVER pixels of one warp, all 32 lanes calling (inactive lanes
+// own no pixel): the warp's (pixel, slot) fragments are numbered in lane
+// order, 32 of them shaded per round with one fragment per lane (so pixels
+// with fewer layers leave no lane idle while others shade), staged in `wf`,
+// then every lane mixes its own pixel's fragments in slot order.  Same
+// operations and order as resolve_layers.
+__device__ __forceinline__ void resolve_over_warp(const RastJob& J, const RastPools& P, const float4* rec_base,
+                                                  bool active, int i, int j, const int32_t* w, int64_t wstride,
+                                                  int L, const VaryingSource& src, WarpFrags& wf,
+                                                  PixelResult* r) {
+  const int lane = threadIdx.x & 31;
+  r->keep = false;
+  r->prim = -1;
+  r->z = 0.0f;
+  r->colour[0] = r->colour[1] = r->colour[2] = 0.0f;
+  static_assert(RAST_MAX_LAYERS == 4, "slot registers w0..w3");
+  int w0 = -1, w1 = -1, w2 = -1, w3 = -1, n = 0;
+  float x = 0.0f, y = 0.0f;
+  if (active) {
+    x = (static_cast<float>(i) - J.viewport[3]) / J.viewport[0];
+    y = (static_cast<float>(j) - J.viewport[7]) / J.viewport[5];
+    w0 = w[0];
+    if (L > 1) w1 = w[wstride];
+    if (L > 2) w2 = w[2 * wstride];
+    if (L > 3) w3 = w[3 * wstride];
+    n = w0 < 0 ? 0 : w1 < 0 ? 1 : w2 < 0 ? 2 : w3 < 0 ? 3 : 4;  // leading filled slots
+  }
+  int incl = n;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const int v = __shfl_up_sync(0xffffffffu, incl, d);
+    if (lane >= d) incl += v;
+  }
+  const int excl = incl - n;
+  const int total = __shfl_sync(0xffffffffu, incl, 31);  // <= kWarpFrags
+  for (int base = 0; base < total; base += 32) {
+    const int k = base + lane;
+    int owner = 0;  // the lane whose fragments [excl, incl) hold k
+#pragma unroll
+    for (int step = 16; step > 0; step >>= 1) {
+      const int v = __shfl_sync(0xffffffffu, incl, owner + step - 1);
+      if (v <= k) owner += step;
+    }
+    const int slot = k - __shfl_sync(0xffffffffu, excl, owner);
+    const int a0 = __shfl_sync(0xffffffffu, w0, owner), a1 = __shfl_sync(0xffffffffu, w1, owner);
+    const int a2 = __shfl_sync(0xffffffffu, w2, owner), a3 = __shfl_sync(0xffffffffu, w3, owner);
+    const float ox = __shfl_sync(0xffffffffu, x, owner), oy = __shfl_sync(0xffffffffu, y, owner);
+    if (k < total) {
+      const int p = slot == 0 ? a0 : slot == 1 ? a1 : slot == 2 ? a2 : a3;
+      Fragment f;
+      shade_primitive(J, P, rec_base, 0, 0, ox, oy, p, src, &f, true);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) wf.colour[c][k] = f.colour[c];
+      wf.z[k] = f.z;
+      wf.keep[k] = f.chooser_keep && f.keep;
+    }
+  }
+  __syncwarp();
+  const bool per_face = (J.flags & RAST_JOB_FACE_ALPHA) && P.face_alpha;
+  float T = 1.0f, C[3] = {0.0f, 0.0f, 0.0f};
+  for (int s = 0; s < n; ++s) {
+    const int k = excl + s;
+    const int p = w0;
+    w0 = w1, w1 = w2, w2 = w3, w3 = -1;
+    if (!wf.keep[k]) continue;
+    if (!r->keep) {
+      r->keep = true;
+      r->z = wf.z[k];
+      r->prim = p;
+    }
+    const float alpha = per_face ? __ldg(P.face_alpha + J.face_begin + p) : J.opacity;
+    const float wgt = T * alpha;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) C[c] = C[c] + wgt * wf.colour[c][k];
+    T = T * (1.0f - alpha);
+  }
+  if (r->keep) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) r->colour[c] = C[c] + T * J.background[c];
   }
 }
 

@@ -766,14 +766,18 @@ face_varyings_kernel(RastBatch B, const int2* __restrict__ fmap, const unsigned 
 }
 
 // Deferred shading: one thread per pixel of every job, reading the winner's
-// corner varyings computed once per visible face (kLayered: the batch has
-// layered jobs, whose pixels shade and mix every slot).
+// corner varyings computed once per visible face.  kLayered: the batch has
+// layered jobs.  Their nearest-mixer pixels shade slot 0 with the default
+// path's code and look at later slots only when its fragment is discarded;
+// their "over" pixels spread the warp's fragments over its lanes
+// (resolve_over_warp).
 // Grid: (ceil(max pixels per job / 256), n_jobs).
 template <bool kLayered>
-__global__ void __launch_bounds__(256, kLayered ? 2 : 4)  // 4 blocks per SM: 64 registers
+__global__ void __launch_bounds__(256, kLayered ? 3 : 4)  // 64 registers (85 layered)
 tiled_shade_kernel(RastBatch B, const float4* __restrict__ setup, const int32_t* __restrict__ winner,
                    bool depth_resolved, const float* __restrict__ fvar, int vstride) {
   __shared__ RastJob sJ;
+  __shared__ WarpFrags s_frags[kLayered ? 8 : 1];  // per warp, layered "over" jobs
   const int jid = blockIdx.y;
   const int64_t npx = static_cast<int64_t>(__ldg(&B.jobs[jid].width)) * __ldg(&B.jobs[jid].height);
   if (static_cast<int64_t>(blockIdx.x) * 256 >= npx) return;
@@ -782,17 +786,35 @@ tiled_shade_kernel(RastBatch B, const float4* __restrict__ setup, const int32_t*
   __syncthreads();
   const RastJob& J = sJ;
   const int64_t local0 = static_cast<int64_t>(blockIdx.x) * 256 + threadIdx.x;
-  if (local0 >= npx) return;
   const int64_t pix = J.pixel_begin + local0;
+  const VaryingSource src{nullptr, vstride, 0, fvar, J.setup_begin};
+  const float4* rec = setup + J.setup_begin * 4;
+  const int L = kLayered ? job_layers(J, B.max_layers) : 0;
+  if (kLayered && L > 0 && J.mixer == RAST_MIX_OVER) {  // every lane of the warp takes part
+    const bool active = local0 < npx;
+    int i = 0, j = 0;
+    if (active) pixel_of(local0, npx, J.height, &i, &j);
+    PixelResult r;
+    resolve_over_warp(J, B.pools, rec, active, i, j, winner + (active ? pix : 0), B.total_pixels, L, src,
+                      s_frags[threadIdx.x >> 5], &r);
+    if (active) store_pixel(J, B.pools, pix, r);
+    return;
+  }
+  if (local0 >= npx) return;
   int i, j;
   pixel_of(local0, npx, J.height, &i, &j);
   PixelResult r;
-  VaryingSource src{nullptr, vstride, 0, fvar, J.setup_begin};
-  const int L = kLayered ? job_layers(J, B.max_layers) : 0;
-  if (kLayered && L > 0)
-    resolve_layers(J, B.pools, setup + J.setup_begin * 4, i, j, winner + pix, B.total_pixels, L, src, &r);
-  else
-    resolve_pixel(J, B.pools, setup + J.setup_begin * 4, i, j, winner[pix], src, &r);
+  const int w0 = winner[pix];
+  if (kLayered && L > 0 && w0 < 0) {  // no candidate: the layered chooser keeps nothing
+    r.keep = false;
+    r.prim = -1;
+    r.z = 0.0f;
+    store_pixel(J, B.pools, pix, r);
+    return;
+  }
+  resolve_pixel(J, B.pools, rec, i, j, w0, src, &r);  // the winner, or the layered chooser's slot 0
+  if (kLayered && L > 1 && !r.keep)  // slot 0 discarded by its fragment shader: the next kept slot
+    resolve_layers(J, B.pools, rec, i, j, winner + pix, B.total_pixels, L, src, &r, 1);
   store_pixel(J, B.pools, pix, r);
 }
 
@@ -1000,12 +1022,11 @@ static int render(const RastBatch* batch, const RastTiledConfig* cfg, void* work
         face_varyings_kernel<<<L.fmap_blocks, kFaceThreads, 0, s>>>(b, fmap, vis, fvar, L.vstride);
         prof.mark("face_varyings_kernel");
       }
+      const float* fv = pre ? fvar : nullptr;
       if (b.max_layers > 0)
-        tiled_shade_kernel<true><<<sgrid, 256, 0, s>>>(b, setup, winner, b.total_setup > 0, pre ? fvar : nullptr,
-                                                       L.vstride);
+        tiled_shade_kernel<true><<<sgrid, 256, 0, s>>>(b, setup, winner, b.total_setup > 0, fv, L.vstride);
       else
-        tiled_shade_kernel<false><<<sgrid, 256, 0, s>>>(b, setup, winner, b.total_setup > 0, pre ? fvar : nullptr,
-                                                        L.vstride);
+        tiled_shade_kernel<false><<<sgrid, 256, 0, s>>>(b, setup, winner, b.total_setup > 0, fv, L.vstride);
       prof.mark("tiled_shade_kernel");
     }
   }
