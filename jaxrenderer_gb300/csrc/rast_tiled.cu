@@ -539,6 +539,20 @@ scatter_kernel(RastBatch B, Geometry G, const int2* __restrict__ fmap, const ush
   });
 }
 
+// True when edge function (x ea + y eb) + ec is negative at every pixel of
+// the tile [xa, xb] x [ya, yb] (NDC of its first and last pixel centres)
+// whatever the rounding of the per-pixel evaluation: its maximum over the
+// rectangle, max(xa ea, xb ea) + max(ya eb, yb eb) + ec, plus a margin of
+// 16 u (X |ea| + Y |eb| + |ec|) (X, Y: the largest |x|, |y| of the tile;
+// u = 2^-24; the per-pixel and the bound's own rounding are each below
+// 3.1 u times that sum) is below zero.  NaN anywhere gives false.
+__device__ __forceinline__ bool edge_misses_tile(float ea, float eb, float ec, float xa, float xb, float ya, float yb,
+                                                 float X, float Y) {
+  const float bound = (fmaxf(xa * ea, xb * ea) + fmaxf(ya * eb, yb * eb)) + ec;
+  const float margin = 16.0f * 5.9604645e-08f * ((X * fabsf(ea) + Y * fabsf(eb)) + fabsf(ec)) + 1e-30f;
+  return bound + margin < 0.0f;
+}
+
 // Persistent warps: each takes one tile (of any job) at a time.  Lane l owns
 // PPL pixels of the tile.  Bin entries are staged 32 at a time in the warp's
 // slice of shared memory (one record per lane), then every lane tests its
@@ -586,6 +600,13 @@ raster_kernel(RastBatch B, Geometry G, const float4* __restrict__ setup,
     constexpr int LPC = 32 / TH;
     const int pj = ty * TH + lane % TH;
     const float y = (static_cast<float>(pj) - oy) / sy;
+    // NDC of the tile's first and last pixel (inside the job) for the
+    // per-entry rejection test: the same quotients the pixels compute
+    const float xa = (static_cast<float>(tx * TW) - ox) / sx;
+    const float xb = (static_cast<float>(min(tx * TW + TW - 1, W - 1)) - ox) / sx;
+    const float ya = (static_cast<float>(ty * TH) - oy) / sy;
+    const float yb = (static_cast<float>(min(ty * TH + TH - 1, H - 1)) - oy) / sy;
+    const float XM = fmaxf(fabsf(xa), fabsf(xb)), YM = fmaxf(fabsf(ya), fabsf(yb));
     float x[PPL], best_z[PPL];
     unsigned long long best[PPL][kL];
     uint32_t second[PPL];
@@ -624,12 +645,22 @@ raster_kernel(RastBatch B, Geometry G, const float4* __restrict__ setup,
     int nid = -1;
     if (lane < n) fetch(lane, n0, n1, n2, nid);
     for (int base = 0; base < n; base += kStage) {
-      const int m = min(kStage, n - base);
-      if (lane < m) {
-        rec[lane][0] = n0;
-        rec[lane][1] = n1;
-        rec[lane][2] = n2;
-        ids[lane] = nid;
+      // entries whose triangle misses every pixel of the tile (one edge
+      // negative over the whole tile) are dropped; the rest are staged
+      // compacted
+      bool take = lane < min(kStage, n - base) && nid >= 0;
+      if (take)
+        take = !(edge_misses_tile(n0.x, n0.w, n1.z, xa, xb, ya, yb, XM, YM) ||
+                 edge_misses_tile(n0.y, n1.x, n1.w, xa, xb, ya, yb, XM, YM) ||
+                 edge_misses_tile(n0.z, n1.y, n2.x, xa, xb, ya, yb, XM, YM));
+      const unsigned keep = __ballot_sync(0xffffffffu, take);
+      const int m = __popc(keep);
+      if (take) {
+        const int slot = __popc(keep & lanemask_lt());
+        rec[slot][0] = n0;
+        rec[slot][1] = n1;
+        rec[slot][2] = n2;
+        ids[slot] = nid;
       }
       __syncwarp();
       // prefetch the next chunk while this one is tested
@@ -642,20 +673,17 @@ raster_kernel(RastBatch B, Geometry G, const float4* __restrict__ setup,
           const float c0 = (x[q] * a.x + y0) + b.z;
           const float c1 = (x[q] * a.y + y1) + b.w;
           const float c2 = (x[q] * a.z + y2) + cz.x;
-          if (all_nonneg(c0, c1, c2)) {
-            const int id = ids[e];
-            if (id >= 0) {
-              const float z = ((c0 * cz.y + c1 * cz.z) + c2 * cz.w) * vp22 + vp23;
-              const unsigned long long key = pack_key(z, id);
-              if (key < best[q][0]) {
-                if (kTies) second[q] = min(second[q], static_cast<uint32_t>(best[q][0] >> 32));
-                best_z[q] = z;
-                z_known |= 1u << q;
-              } else if (kTies) {
-                second[q] = min(second[q], static_cast<uint32_t>(key >> 32));
-              }
-              insert_key<kL>(best[q], key);
+          if (all_nonneg(c0, c1, c2)) {  // staged entries are candidates (id >= 0)
+            const float z = ((c0 * cz.y + c1 * cz.z) + c2 * cz.w) * vp22 + vp23;
+            const unsigned long long key = pack_key(z, ids[e]);
+            if (key < best[q][0]) {
+              if (kTies) second[q] = min(second[q], static_cast<uint32_t>(best[q][0] >> 32));
+              best_z[q] = z;
+              z_known |= 1u << q;
+            } else if (kTies) {
+              second[q] = min(second[q], static_cast<uint32_t>(key >> 32));
             }
+            insert_key<kL>(best[q], key);
           }
         }
       }
