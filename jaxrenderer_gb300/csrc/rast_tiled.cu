@@ -125,7 +125,11 @@ __device__ __forceinline__ void clip_push0(ClipStage& s, ClipStage& s1, ClipStag
 // >= 0.  Computed by clipping the job's screen rectangle (one pixel wider on
 // every side, in NDC) against c_k >= -eps_k, where eps_k is 64x the rounding
 // bound of the three-operation evaluation of c_k, then widening the bounding
-// box by one pixel.  Returns false when no pixel can be covered.
+// box by one pixel.  When those three half-planes bound a triangle whose
+// corners are known to a quarter pixel, the clipping is skipped: the
+// corners' box, clamped to the screen, contains the clipped box (equals it
+// for a triangle inside the rectangle).  Returns false when no pixel can be
+// covered.
 // The job's screen rectangle one pixel wider on every side, in NDC (pixels
 // -1 and W), computed once per block.
 struct ScreenRect {
@@ -147,6 +151,41 @@ __device__ __forceinline__ ScreenRect screen_rect(const RastJob& J) {
   r.X = fmaxf(fabsf(r.xl), fabsf(r.xh));
   r.Y = fmaxf(fabsf(r.yl), fabsf(r.yh));
   return r;
+}
+
+// Corner of the widened half-planes i and j: the solution of
+// a_i x + b_i y + c_i = 0 = a_j x + b_j y + c_j by Cramer's rule, with a
+// bound on its rounding error: N and D each carry at most 2u times the sum
+// of their products' magnitudes, the quotient 2u relative (u = 2^-24); the
+// bound below doubles both.  False when the corner's error could exceed a
+// quarter pixel (scales psx, psy: pixels per NDC unit) or D's sign is not
+// certain.  *d returns D = cross((a_i, b_i), (a_j, b_j)).
+__device__ __forceinline__ bool widened_corner(float ai, float bi, float ci, float aj, float bj, float cj, float psx,
+                                               float psy, float* x, float* y, float* d) {
+  constexpr float u4 = 4.0f * 5.9604645e-08f;
+  const float D = ai * bj - aj * bi;
+  const float eD = fabsf(ai * bj) + fabsf(aj * bi);
+  const float r = 1.0f / D;
+  *x = (bi * cj - bj * ci) * r;
+  *y = (aj * ci - ai * cj) * r;
+  *d = D;
+  const float ex = u4 * ((fabsf(bi * cj) + fabsf(bj * ci) + fabsf(*x) * eD) * fabsf(r) + fabsf(*x));
+  const float ey = u4 * ((fabsf(aj * ci) + fabsf(ai * cj) + fabsf(*y) * eD) * fabsf(r) + fabsf(*y));
+  // written so that NaN or inf anywhere fails
+  return fabsf(D) > 2.0f * u4 * eD && ex * psx < 0.25f && ey * psy < 0.25f;
+}
+
+// The region where all three widened edge functions are >= 0 is a bounded
+// triangle (or empty) when the edge normals (a_k, b_k) wind around the
+// origin: D01, D12, D20 of one strict sign.  Then it is the convex hull of
+// the three corners (tx, ty), each within a quarter pixel.
+__device__ __forceinline__ bool widened_triangle(float a0, float b0, float c0, float a1, float b1, float c1, float a2,
+                                                 float b2, float c2, float psx, float psy, float* tx, float* ty) {
+  float d01, d12, d20;
+  const bool ok = widened_corner(a0, b0, c0, a1, b1, c1, psx, psy, tx + 0, ty + 0, &d01) &
+                  widened_corner(a1, b1, c1, a2, b2, c2, psx, psy, tx + 1, ty + 1, &d12) &
+                  widened_corner(a2, b2, c2, a0, b0, c0, psx, psy, tx + 2, ty + 2, &d20);
+  return ok && ((d01 > 0.0f && d12 > 0.0f && d20 > 0.0f) || (d01 < 0.0f && d12 < 0.0f && d20 < 0.0f));
 }
 
 __device__ __forceinline__ bool coverage_bbox(const float* inv, const RastJob& J, const ScreenRect& R, int* i0,
@@ -183,19 +222,31 @@ __device__ __forceinline__ bool coverage_bbox(const float* inv, const RastJob& J
     *j1 = H - 1;
     return true;  // edge functions too large to evaluate safely: every pixel
   }
-  ClipStage s0{a0, b0, c0, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, false};
-  ClipStage s1{a1, b1, c1, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, false};
-  ClipStage s2{a2, b2, c2, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, false};
-  ClipBox box{kInf, -kInf, kInf, -kInf, 0};
+  float mnx, mxx, mny, mxy;
+  float tx[3], ty[3];
+  const float psx = fabsf(sx), psy = fabsf(sy);
+  if (widened_triangle(a0, b0, c0, a1, b1, c1, a2, b2, c2, psx, psy, tx, ty)) {
+    // the region lies in the triangle tx, ty: its corners' box (clamped to
+    // the screen below) contains the clipped box, and equals it when the
+    // triangle is inside the rectangle
+    mnx = fminf(tx[0], fminf(tx[1], tx[2]));
+    mxx = fmaxf(tx[0], fmaxf(tx[1], tx[2]));
+    mny = fminf(ty[0], fminf(ty[1], ty[2]));
+    mxy = fmaxf(ty[0], fmaxf(ty[1], ty[2]));
+  } else {
+    ClipStage s0{a0, b0, c0, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, false};
+    ClipStage s1{a1, b1, c1, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, false};
+    ClipStage s2{a2, b2, c2, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, false};
+    ClipBox box{kInf, -kInf, kInf, -kInf, 0};
 #pragma unroll 1
-  for (int k = 0; k < 4; ++k) clip_push0(s0, s1, s2, box, (k == 1 || k == 2) ? xh : xl, k >= 2 ? yh : yl);
-  // closing edges, stage by stage: re-sending a stage's first vertex closes it
-  clip_push0(s0, s1, s2, box, s0.fx, s0.fy);
-  if (s1.any) clip_push1(s1, s2, box, s1.fx, s1.fy);
-  if (s2.any) clip_push2(s2, box, s2.fx, s2.fy);
-  const int n_out = box.n;
-  const float mnx = box.mnx, mxx = box.mxx, mny = box.mny, mxy = box.mxy;
-  if (n_out == 0) return false;
+    for (int k = 0; k < 4; ++k) clip_push0(s0, s1, s2, box, (k == 1 || k == 2) ? xh : xl, k >= 2 ? yh : yl);
+    // closing edges, stage by stage: re-sending a stage's first vertex closes it
+    clip_push0(s0, s1, s2, box, s0.fx, s0.fy);
+    if (s1.any) clip_push1(s1, s2, box, s1.fx, s1.fy);
+    if (s2.any) clip_push2(s2, box, s2.fx, s2.fy);
+    if (box.n == 0) return false;
+    mnx = box.mnx, mxx = box.mxx, mny = box.mny, mxy = box.mxy;
+  }
   // NDC -> pixel index: i = x * sx + ox (monotone in x with the sign of sx)
   const float pa = mnx * sx + ox, pb = mxx * sx + ox;
   const float qa = mny * sy + oy, qb = mxy * sy + oy;
