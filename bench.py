@@ -825,12 +825,20 @@ def kernel_bytes(kname, info, visible):
     return table.get(kname, 0.0)
 
 
-# DRAM bytes per face of the setup kernel measured by ncu (dram__bytes_read.sum +
-# dram__bytes_write.sum) on the 256-scene brax-like case
-# (profiles/ncu_forward_tiled_brax84x256.md: 119.06 MB and 121.98 MB for
-# 1,470,504 faces, binning only / with the small-face path); its traffic
-# grows with the faces processed, so a full launch's is this times its faces.
-NCU_SETUP_BYTES_PER_FACE = {0: 80.96, 1: 82.95}
+# DRAM bytes per unit of work of the forward kernels measured by ncu
+# (dram__bytes_read.sum + dram__bytes_write.sum) on the 256-scene brax-like
+# case (profiles/ncu_forward_tiled_brax84x256.md: 1,470,504 faces per pass,
+# 1,806,336 main-pass pixels): setup_bin 119.6 MB, scatter 12.4 MB,
+# face_varyings 43.6 MB per pass, tiled_shade 70.8 MB.  Their traffic grows
+# with the faces (F) or pixels (P) processed, so a full launch's is this
+# times its units.  The raster kernel's depends on the tile shape the
+# autotuner picks for a batch size and is not scaled.
+NCU_BYTES_PER_UNIT = {
+    "setup_bin_kernel": ("F", 81.3),
+    "scatter_kernel": ("F", 8.4),
+    "face_varyings_kernel": ("F", 29.6),
+    "tiled_shade_kernel": ("P", 39.2),
+}
 
 
 def roofline(prof, visible):
@@ -866,12 +874,14 @@ def roofline(prof, visible):
         per_kernel[name] = {"bytes": b, "GB/s": gbs, "frac": gbs / peak if gbs is not None else None}
     traffic, traffic_note = None, None
     r_dom, p_dom, k_dom = prof["where"][dom]
-    if k_dom == "setup_bin_kernel":
-        cfg = r_dom.configs.get(p_dom)
-        small = 1 if (cfg is not None and int(cfg.small_area) > 0) else 0
-        traffic = NCU_SETUP_BYTES_PER_FACE[small] * info["F"]
-        traffic_note = ("ncu DRAM bytes per face of this kernel on the 256-scene case, times this launch's "
-                        f"{int(info['F'])} faces")
+    cfg = r_dom.configs.get(p_dom)
+    small = cfg is not None and int(cfg.small_area) > 0
+    if k_dom in NCU_BYTES_PER_UNIT and not small and info["slots"] == 1:
+        unit, per = NCU_BYTES_PER_UNIT[k_dom]
+        traffic = per * info[unit]
+        traffic_note = (f"ncu DRAM bytes per {'face' if unit == 'F' else 'pixel'} of this kernel on the 256-scene "
+                        f"brax-like case, times this launch's {int(info[unit])} "
+                        f"{'faces' if unit == 'F' else 'pixels'}")
     out = {
         "bound": "hbm",
         "kernel": dom,
