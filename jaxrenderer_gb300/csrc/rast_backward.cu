@@ -35,6 +35,12 @@ namespace rast {
 namespace bwd {
 
 constexpr int kThreads = 256;
+// Rows (faces or vertices) per block of the per-face and per-vertex kernels:
+// few rows of a block are visible, so each block scans kRowsPerThread rows
+// per thread and works through the queued ones, paying its job load, queue
+// and parameter reduction once per kRows rows.
+constexpr int kRowsPerThread = 32;
+constexpr int kRows = kThreads * kRowsPerThread;
 
 // y = v / |v|;  dv = (dy - y (y . dy)) / |v|
 __device__ __forceinline__ void normalise3_bwd(const float* y, float norm, const float* dy, float* dv) {
@@ -190,7 +196,7 @@ struct Work {
                         // phong_darboux NDC triangle (9) when that shader is in the batch
   int vstride;
   int vacc_stride;      // 3, or 12 with phong_darboux
-  const int2* fmap;     // face block map (kThreads faces per block)
+  const int2* fmap;     // face block map (kRows faces per block)
   const int2* vmap;     // vertex block map
   unsigned* starts;     // per-job block starts of both maps (2 x (n_jobs + 1))
 };
@@ -209,23 +215,9 @@ __global__ void __launch_bounds__(kThreads) mark_kernel(RastBatch B, Work w) {
   if (p >= 0) w.fvis[J.setup_begin + p] = 1;
 }
 
-// The per-face and per-corner kernels queue the block's visible faces (or
-// flagged corners) in shared memory first, so only they occupy lanes.
-__global__ void __launch_bounds__(kThreads) face_prep_kernel(RastBatch B, Work w) {
-  __shared__ RastJob sJ;
-  __shared__ int s_q[kThreads];
-  __shared__ int s_n;
-  const int2 blk = w.fmap[blockIdx.x];
-  if (blk.x < 0) return;
-  const int nf = __ldg(&B.jobs[blk.x].n_faces);
-  load_job_to_shared(B.jobs + blk.x, &sJ);
-  if (threadIdx.x == 0) s_n = 0;
-  __syncthreads();
-  const RastJob& J = sJ;
-  const int f0 = blk.y + static_cast<int>(threadIdx.x);
-  const int n = block_queue(f0 < nf && w.fvis[J.setup_begin + f0], f0, s_q, &s_n);
-  if (static_cast<int>(threadIdx.x) >= n) return;
-  const int f = s_q[threadIdx.x];
+// Per visible face: clip rows of its corners, their 3x3 inverse (the forward
+// set-up's operations), accumulators zeroed, corner vertices flagged.
+__device__ __forceinline__ void face_prep(const RastBatch& B, const Work& w, const RastJob& J, int f) {
   const int64_t row = J.setup_begin + f;
   const int32_t* face = B.pools.faces + (J.face_begin + f) * 3;
   float M[9], zc[3];
@@ -252,21 +244,8 @@ __global__ void __launch_bounds__(kThreads) face_prep_kernel(RastBatch B, Work w
   for (int k = 0; k < 12; ++k) a[k] = 0.0f;
 }
 
-__global__ void __launch_bounds__(kThreads) vertex_prep_kernel(RastBatch B, Work w) {
-  __shared__ RastJob sJ;
-  __shared__ int s_q[kThreads];
-  __shared__ int s_n;
-  const int2 blk = w.vmap[blockIdx.x];
-  if (blk.x < 0) return;
-  const int nvt = __ldg(&B.jobs[blk.x].n_verts);
-  load_job_to_shared(B.jobs + blk.x, &sJ);
-  if (threadIdx.x == 0) s_n = 0;
-  __syncthreads();
-  const RastJob& J = sJ;
-  const int v0 = blk.y + static_cast<int>(threadIdx.x);
-  const int n = block_queue(v0 < nvt && w.vvis[J.vout_begin + v0], v0, s_q, &s_n);
-  if (static_cast<int>(threadIdx.x) >= n) return;
-  const int v = s_q[threadIdx.x];
+// Per flagged vertex: the vertex shader's varyings, accumulators zeroed.
+__device__ __forceinline__ void vertex_prep(const RastBatch& B, const Work& w, const RastJob& J, int v) {
   const int64_t row = J.vout_begin + v;
   const int nv = varying_count(J.shader);
   if (nv > 0) {
@@ -277,6 +256,41 @@ __global__ void __launch_bounds__(kThreads) vertex_prep_kernel(RastBatch B, Work
       if (k < nv) w.vvar[row * w.vstride + k] = var[k];
   }
   for (int k = 0; k < w.vacc_stride; ++k) w.vacc[row * w.vacc_stride + k] = 0.0f;
+}
+
+// The per-face and per-corner kernels cover kRows rows per block: the
+// block's visible faces (or flagged corners) are queued in shared memory
+// first, so only they occupy lanes.
+__global__ void __launch_bounds__(kThreads) face_prep_kernel(RastBatch B, Work w) {
+  __shared__ RastJob sJ;
+  __shared__ int s_q[kRows];
+  __shared__ int s_n;
+  const int2 blk = w.fmap[blockIdx.x];
+  if (blk.x < 0) return;
+  const int nf = __ldg(&B.jobs[blk.x].n_faces);
+  load_job_to_shared(B.jobs + blk.x, &sJ);
+  if (threadIdx.x == 0) s_n = 0;
+  __syncthreads();
+  const RastJob& J = sJ;
+  const int n = block_queue_rows<kRowsPerThread, kThreads>(
+      [&](int r) { return blk.y + r < nf && w.fvis[J.setup_begin + blk.y + r]; }, s_q, &s_n);
+  for (int t = threadIdx.x; t < n; t += kThreads) face_prep(B, w, J, blk.y + s_q[t]);
+}
+
+__global__ void __launch_bounds__(kThreads) vertex_prep_kernel(RastBatch B, Work w) {
+  __shared__ RastJob sJ;
+  __shared__ int s_q[kRows];
+  __shared__ int s_n;
+  const int2 blk = w.vmap[blockIdx.x];
+  if (blk.x < 0) return;
+  const int nvt = __ldg(&B.jobs[blk.x].n_verts);
+  load_job_to_shared(B.jobs + blk.x, &sJ);
+  if (threadIdx.x == 0) s_n = 0;
+  __syncthreads();
+  const RastJob& J = sJ;
+  const int n = block_queue_rows<kRowsPerThread, kThreads>(
+      [&](int r) { return blk.y + r < nvt && w.vvis[J.vout_begin + blk.y + r]; }, s_q, &s_n);
+  for (int t = threadIdx.x; t < n; t += kThreads) vertex_prep(B, w, J, blk.y + s_q[t]);
 }
 
 // Reverse mode of the fragment of shader `sh` at one pixel.  In: the three
@@ -746,10 +760,53 @@ pixel_kernel(RastBatch B, Work w, const float* __restrict__ grad_canvas, const f
 }
 
 // dL/dM = -m^T (dL/dm) m^T for the [x, y, w] rows of the clip positions,
-// then clip_k = A [p_k, 1]: dL/dA (per scene) and dL/dp_k (atomics).
+// then clip_k = A [p_k, 1]: dL/dA (per scene, into pg) and dL/dp_k (atomics).
+__device__ __forceinline__ void face_post(const RastBatch& B, const Work& w, const RastJob& J,
+                                          const RastGradPools& G, int f, ParamGrad& pg) {
+  const int64_t row = J.setup_begin + f;
+  const float4* fr = w.frec + row * 3;
+  const float4 a = fr[0], bb = fr[1], cz = fr[2];
+  const float m[9] = {a.x, a.y, a.z, a.w, bb.x, bb.y, bb.z, bb.w, cz.x};
+  const float* acc = w.facc + row * 12;
+  float gm[9], t[9], gM[9];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) gm[k] = acc[k];
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+      t[3 * r + k] = (gm[3 * r + 0] * m[3 * k + 0] + gm[3 * r + 1] * m[3 * k + 1]) + gm[3 * r + 2] * m[3 * k + 2];
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+      gM[3 * r + k] = -((m[0 * 3 + r] * t[0 * 3 + k] + m[1 * 3 + r] * t[1 * 3 + k]) + m[2 * 3 + r] * t[2 * 3 + k]);
+  const int32_t* face = B.pools.faces + (J.face_begin + f) * 3;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const float gclip[4] = {gM[3 * k + 0], gM[3 * k + 1], acc[9 + k], gM[3 * k + 2]};
+    const int v = gather_clamp(face[k], J.n_verts);
+    float p[3];
+    load3(B.pools.position, J.vert_begin + v, p);
+    const float ph[4] = {p[0], p[1], p[2], 1.0f};
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) pg.v[RAST_GRAD_WORLD_TO_CLIP + 4 * r + q] += gclip[r] * ph[q];
+    if (G.position) {
+#pragma unroll
+      for (int q = 0; q < 3; ++q) {
+        const float g = ((gclip[0] * J.world_to_clip[q] + gclip[1] * J.world_to_clip[4 + q]) +
+                         gclip[2] * J.world_to_clip[8 + q]) + gclip[3] * J.world_to_clip[12 + q];
+        atomicAdd(G.position + (J.vert_begin + v) * 3 + q, g);
+      }
+    }
+  }
+}
+
 __global__ void __launch_bounds__(kThreads) face_post_kernel(RastBatch B, Work w, RastGradPools G) {
   __shared__ RastJob sJ;
-  __shared__ int s_q[kThreads];
+  __shared__ int s_q[kRows];
   __shared__ int s_n;
   const int2 blk = w.fmap[blockIdx.x];
   if (blk.x < 0) return;
@@ -758,82 +815,24 @@ __global__ void __launch_bounds__(kThreads) face_post_kernel(RastBatch B, Work w
   if (threadIdx.x == 0) s_n = 0;
   __syncthreads();
   const RastJob& J = sJ;
-  const int f0 = blk.y + static_cast<int>(threadIdx.x);
-  const int n = block_queue(f0 < nf && w.fvis[J.setup_begin + f0], f0, s_q, &s_n);
-  const bool active = static_cast<int>(threadIdx.x) < n;
-  const int f = active ? s_q[threadIdx.x] : 0;
+  const int n = block_queue_rows<kRowsPerThread, kThreads>(
+      [&](int r) { return blk.y + r < nf && w.fvis[J.setup_begin + blk.y + r]; }, s_q, &s_n);
   ParamGrad pg;
 #pragma unroll
   for (int k = 0; k < 16; ++k) pg.v[RAST_GRAD_WORLD_TO_CLIP + k] = 0.0f;
-  const int64_t row = J.setup_begin + f;
-  if (active) {
-    const float4* fr = w.frec + row * 3;
-    const float4 a = fr[0], bb = fr[1], cz = fr[2];
-    const float m[9] = {a.x, a.y, a.z, a.w, bb.x, bb.y, bb.z, bb.w, cz.x};
-    const float* acc = w.facc + row * 12;
-    float gm[9], t[9], gM[9];
-#pragma unroll
-    for (int k = 0; k < 9; ++k) gm[k] = acc[k];
-#pragma unroll
-    for (int r = 0; r < 3; ++r)
-#pragma unroll
-      for (int k = 0; k < 3; ++k)
-        t[3 * r + k] = (gm[3 * r + 0] * m[3 * k + 0] + gm[3 * r + 1] * m[3 * k + 1]) + gm[3 * r + 2] * m[3 * k + 2];
-#pragma unroll
-    for (int r = 0; r < 3; ++r)
-#pragma unroll
-      for (int k = 0; k < 3; ++k)
-        gM[3 * r + k] = -((m[0 * 3 + r] * t[0 * 3 + k] + m[1 * 3 + r] * t[1 * 3 + k]) + m[2 * 3 + r] * t[2 * 3 + k]);
-    const int32_t* face = B.pools.faces + (J.face_begin + f) * 3;
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-      const float gclip[4] = {gM[3 * k + 0], gM[3 * k + 1], acc[9 + k], gM[3 * k + 2]};
-      const int v = gather_clamp(face[k], J.n_verts);
-      float p[3];
-      load3(B.pools.position, J.vert_begin + v, p);
-      const float ph[4] = {p[0], p[1], p[2], 1.0f};
-#pragma unroll
-      for (int r = 0; r < 4; ++r)
-#pragma unroll
-        for (int q = 0; q < 4; ++q) pg.v[RAST_GRAD_WORLD_TO_CLIP + 4 * r + q] += gclip[r] * ph[q];
-      if (G.position) {
-#pragma unroll
-        for (int q = 0; q < 3; ++q) {
-          const float g = ((gclip[0] * J.world_to_clip[q] + gclip[1] * J.world_to_clip[4 + q]) +
-                           gclip[2] * J.world_to_clip[8 + q]) + gclip[3] * J.world_to_clip[12 + q];
-          atomicAdd(G.position + (J.vert_begin + v) * 3 + q, g);
-        }
-      }
-    }
-  }
-  reduce_params<kClipBits>(pg, G.job_params, active, blk.x);
+  for (int t = threadIdx.x; t < n; t += kThreads) face_post(B, w, J, G, blk.y + s_q[t], pg);
+  reduce_params<kClipBits>(pg, G.job_params, static_cast<int>(threadIdx.x) < n, blk.x);
 }
 
 // Reverse mode of the vertex shader: Gouraud lighting or the eye-space
 // normal transform, from the vertex's accumulated dL/d(varying).
 template <int SH>
-__global__ void __launch_bounds__(kThreads) vertex_post_kernel(RastBatch B, Work w, RastGradPools G) {
-  __shared__ RastJob sJ;
-  __shared__ int s_q[kThreads];
-  __shared__ int s_n;
-  const int2 blk = w.vmap[blockIdx.x];
-  if (blk.x < 0) return;
-  const int nvt = __ldg(&B.jobs[blk.x].n_verts);
-  load_job_to_shared(B.jobs + blk.x, &sJ);
-  if (threadIdx.x == 0) s_n = 0;
-  __syncthreads();
-  const RastJob& J = sJ;
+__device__ __forceinline__ void vertex_post(const RastBatch& B, const Work& w, const RastJob& J,
+                                            const RastGradPools& G, int v, ParamGrad& pg) {
   const RastPools& P = B.pools;
   const int sh = SH >= 0 ? SH : J.shader;
-  const int v0 = blk.y + static_cast<int>(threadIdx.x);
-  const int n = block_queue(v0 < nvt && w.vvis[J.vout_begin + v0], v0, s_q, &s_n);
-  const bool active = static_cast<int>(threadIdx.x) < n && sh != RAST_SHADER_DEPTH;
-  const int v = active ? s_q[threadIdx.x] : 0;
-  ParamGrad pg;
-#pragma unroll
-  for (int k = 0; k < RAST_NPARAM; ++k) pg.v[k] = 0.0f;
   const int64_t row = J.vout_begin + v;
-  if (active) {
+  {
     const float* acc = w.vacc + row * w.vacc_stride;
     const float g[3] = {acc[0], acc[1], acc[2]};
     const int64_t vrow = J.vert_begin + v;
@@ -934,7 +933,28 @@ __global__ void __launch_bounds__(kThreads) vertex_post_kernel(RastBatch B, Work
       }
     }
   }
-  reduce_params<vertex_bits(SH)>(pg, G.job_params, active, blk.x);
+}
+
+template <int SH>
+__global__ void __launch_bounds__(kThreads) vertex_post_kernel(RastBatch B, Work w, RastGradPools G) {
+  __shared__ RastJob sJ;
+  __shared__ int s_q[kRows];
+  __shared__ int s_n;
+  const int2 blk = w.vmap[blockIdx.x];
+  if (blk.x < 0) return;
+  const int nvt = __ldg(&B.jobs[blk.x].n_verts);
+  load_job_to_shared(B.jobs + blk.x, &sJ);
+  if (threadIdx.x == 0) s_n = 0;
+  __syncthreads();
+  const RastJob& J = sJ;
+  const int sh = SH >= 0 ? SH : J.shader;
+  const int n = sh == RAST_SHADER_DEPTH ? 0 : block_queue_rows<kRowsPerThread, kThreads>(
+      [&](int r) { return blk.y + r < nvt && w.vvis[J.vout_begin + blk.y + r]; }, s_q, &s_n);
+  ParamGrad pg;
+#pragma unroll
+  for (int k = 0; k < RAST_NPARAM; ++k) pg.v[k] = 0.0f;
+  for (int t = threadIdx.x; t < n; t += kThreads) vertex_post<SH>(B, w, J, G, blk.y + s_q[t], pg);
+  reduce_params<vertex_bits(SH)>(pg, G.job_params, static_cast<int>(threadIdx.x) < n, blk.x);
 }
 
 // ------------------------------------------------------------------ layout
@@ -966,8 +986,8 @@ static Layout layout(const RastBatch& b) {
   L.vvar_off = take(V * vstride * sizeof(float));
   L.vacc_stride = (b.shader_mask & (1 << RAST_SHADER_PHONG_DARBOUX)) ? 12 : 3;
   L.vacc_off = take(V * L.vacc_stride * sizeof(float));
-  L.fblocks = block_map_capacity(b.total_setup, b.n_jobs, kThreads);
-  L.vblocks = block_map_capacity(b.total_vout, b.n_jobs, kThreads);
+  L.fblocks = block_map_capacity(b.total_setup, b.n_jobs, kRows);
+  L.vblocks = block_map_capacity(b.total_vout, b.n_jobs, kRows);
   L.fmap_off = take(static_cast<size_t>(L.fblocks) * sizeof(int2));
   L.vmap_off = take(static_cast<size_t>(L.vblocks) * sizeof(int2));
   L.start_off = take(2 * block_start_bytes(b.n_jobs));
@@ -981,17 +1001,20 @@ static void launch_all(const RastBatch& b, const Work& w, const Layout& L, const
   const int64_t max_px = static_cast<int64_t>(b.max_width) * b.max_height;
   const dim3 pgrid(static_cast<unsigned>((max_px + kThreads - 1) / kThreads), static_cast<unsigned>(b.n_jobs));
   const unsigned fgrid = L.fblocks, vgrid = L.vblocks;
-  build_block_map(b, kMapFaces, kThreads, const_cast<int2*>(w.fmap), w.starts, s);
-  build_block_map(b, kMapVertices, kThreads, const_cast<int2*>(w.vmap), w.starts + b.n_jobs + 1, s);
+  build_block_map(b, kMapFaces, kRows, const_cast<int2*>(w.fmap), w.starts, s);
+  build_block_map(b, kMapVertices, kRows, const_cast<int2*>(w.vmap), w.starts + b.n_jobs + 1, s);
   mark_kernel<<<pgrid, kThreads, 0, s>>>(b, w);
+  prof.mark("backward_mark_kernels");
   face_prep_kernel<<<fgrid, kThreads, 0, s>>>(b, w);
+  prof.mark("backward_face_prep_kernel");
   vertex_prep_kernel<<<vgrid, kThreads, 0, s>>>(b, w);
-  prof.mark("backward_prep_kernels");
+  prof.mark("backward_vertex_prep_kernel");
   pixel_kernel<SH><<<pgrid, kThreads, 0, s>>>(b, w, gc, gz, G);
   prof.mark("backward_pixel_kernel");
   face_post_kernel<<<fgrid, kThreads, 0, s>>>(b, w, G);
+  prof.mark("backward_face_post_kernel");
   vertex_post_kernel<SH><<<vgrid, kThreads, 0, s>>>(b, w, G);
-  prof.mark("backward_post_kernels");
+  prof.mark("backward_vertex_post_kernel");
 }
 
 static int run(const RastBatch* batch, const float* grad_canvas, const float* grad_zbuffer,

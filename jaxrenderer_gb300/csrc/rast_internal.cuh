@@ -109,6 +109,26 @@ __device__ __forceinline__ int block_queue(bool flag, int idx, int* s_q, int* s_
   return *s_n;
 }
 
+// block_queue over kR rows per thread: row r = threadIdx.x + k * kBlock
+// (k < kR) is offered when flag(r); the offered rows land in s_q (order
+// unspecified, room for kR * kBlock) and the count is returned.  *s_n must be
+// zero and visible to the block on entry; every thread must call.
+template <int kR, int kBlock, class Flag>
+__device__ __forceinline__ int block_queue_rows(Flag flag, int* s_q, int* s_n) {
+#pragma unroll
+  for (int k = 0; k < kR; ++k) {
+    const int r = static_cast<int>(threadIdx.x) + k * kBlock;
+    const bool f = flag(r);
+    const unsigned m = __ballot_sync(0xffffffffu, f);
+    int base = 0;
+    if ((threadIdx.x & 31) == 0 && m) base = atomicAdd(s_n, __popc(m));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (f) s_q[base + __popc(m & lanemask_lt())] = r;
+  }
+  __syncthreads();
+  return *s_n;
+}
+
 // ---- block maps: grids over the faces (or vertices) of every job with no
 // empty blocks.  Entry b of the map is (job, first item of the block) for
 // the b-th block of the concatenated per-job block ranges, (-1, 0) past the

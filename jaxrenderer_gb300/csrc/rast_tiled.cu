@@ -807,19 +807,22 @@ raster_kernel(RastBatch B, Geometry G, const float4* __restrict__ setup,
 
 // Vertex varyings of the three corners of every face some pixel needs
 // (marked by the raster kernel), stored per face: the shade then reads them
-// instead of re-running the vertex shader per pixel.  The block queues its
-// visible faces in shared memory, then one thread per (visible face, corner)
-// runs the vertex shader, so faces nobody sees leave no idle lanes.
-// Grid: one block per kFaceThreads faces of a job (face block map).
+// instead of re-running the vertex shader per pixel.  A block covers
+// kVaryRows faces of one job (its own block map): it queues the visible ones
+// in shared memory, then one thread per (visible face, corner) runs the
+// vertex shader, so faces nobody sees leave no idle lanes and the block's
+// job load and queue are paid once per kVaryRows faces.
 constexpr int kFaceThreads = kSetupThreads;
+constexpr int kVaryRowsPerThread = 16;
+constexpr int kVaryRows = kFaceThreads * kVaryRowsPerThread;
 
 __global__ void __launch_bounds__(kFaceThreads)
-face_varyings_kernel(RastBatch B, const int2* __restrict__ fmap, const unsigned char* __restrict__ visible,
+face_varyings_kernel(RastBatch B, const int2* __restrict__ vmap, const unsigned char* __restrict__ visible,
                      float* __restrict__ fvar, int vstride) {
   __shared__ RastJob sJ;
-  __shared__ int s_face[kFaceThreads];
+  __shared__ int s_face[kVaryRows];
   __shared__ int s_n;
-  const int2 blk = fmap[blockIdx.x];
+  const int2 blk = vmap[blockIdx.x];
   if (blk.x < 0) return;
   const int jid = blk.x;
   const int nf = __ldg(&B.jobs[jid].n_faces);
@@ -828,12 +831,12 @@ face_varyings_kernel(RastBatch B, const int2* __restrict__ fmap, const unsigned 
   if (threadIdx.x == 0) s_n = 0;
   __syncthreads();
   const RastJob& J = sJ;
-  const int f = blk.y + static_cast<int>(threadIdx.x);
-  const int pairs = 3 * block_queue(f < nf && visible[J.setup_begin + f], f, s_face, &s_n);
+  const int pairs = 3 * block_queue_rows<kVaryRowsPerThread, kFaceThreads>(
+                            [&](int r) { return blk.y + r < nf && visible[J.setup_begin + blk.y + r]; }, s_face, &s_n);
   const int nv = varying_count(J.shader);
   for (int t = threadIdx.x; t < pairs; t += kFaceThreads) {
     const int q = t / 3, k = t - 3 * q;
-    const int fq = s_face[q];
+    const int fq = blk.y + s_face[q];
     const int32_t* face = B.pools.faces + (J.face_begin + fq) * 3;
     float var[kMaxVarying], clip[4];
     vertex_shader<false>(J, B.pools, gather_clamp(__ldg(face + k), J.n_verts), clip, var);
@@ -908,8 +911,8 @@ inline uint64_t default_bin_capacity(const RastBatch& b) {
 
 struct Layout {
   size_t setup_off, bbox_off, counts_off, offsets_off, cursors_off, bsums_off, bins_off, winner_off,
-      vis_off, fvar_off, fmap_off, fstart_off, keys_off, misc_off, total;
-  unsigned fmap_blocks;
+      vis_off, fvar_off, fmap_off, fstart_off, vmap_off, vstart_off, keys_off, misc_off, total;
+  unsigned fmap_blocks, vmap_blocks;  // face block maps: setup/scatter, face varyings
   bool small_path;  // setup kernel rasterises small faces (not when near ties are counted)
   int vstride;
   int winner_layers;  // chooser slots kept per pixel: 1, or RAST_MAX_LAYERS with layered jobs
@@ -953,6 +956,9 @@ static Layout layout(const RastBatch& b, TileShape ts, uint64_t bin_capacity, in
   L.fmap_blocks = block_map_capacity(b.total_setup, b.n_jobs, kSetupThreads);
   L.fmap_off = take(static_cast<size_t>(L.fmap_blocks) * sizeof(int2));
   L.fstart_off = take(block_start_bytes(b.n_jobs));
+  L.vmap_blocks = shading ? block_map_capacity(b.total_setup, b.n_jobs, kVaryRows) : 0;
+  L.vmap_off = take(static_cast<size_t>(L.vmap_blocks) * sizeof(int2));
+  L.vstart_off = take(shading ? block_start_bytes(b.n_jobs) : 0);
   L.small_path = b.near_ties == nullptr && small_area > 0 && b.max_layers == 0;
   L.keys_off = take(L.small_path ? static_cast<size_t>(b.total_pixels) * sizeof(unsigned long long) : 0);
   L.misc_off = take(256);
@@ -1098,7 +1104,11 @@ static int render(const RastBatch* batch, const RastTiledConfig* cfg, void* work
     if (b.shader_mask != (1 << RAST_SHADER_DEPTH) || b.total_setup == 0) {
       const bool pre = fvar != nullptr && b.total_setup > 0;
       if (pre) {
-        face_varyings_kernel<<<L.fmap_blocks, kFaceThreads, 0, s>>>(b, fmap, vis, fvar, L.vstride);
+        int2* vmap = reinterpret_cast<int2*>(ws + L.vmap_off);
+        if (build_block_map(b, kMapFaces, kVaryRows, vmap, reinterpret_cast<unsigned*>(ws + L.vstart_off), s) !=
+            cudaSuccess)
+          return RAST_ERR_CUDA;
+        face_varyings_kernel<<<L.vmap_blocks, kFaceThreads, 0, s>>>(b, vmap, vis, fvar, L.vstride);
         prof.mark("face_varyings_kernel");
       }
       const float* fv = pre ? fvar : nullptr;
