@@ -124,3 +124,83 @@ def test_graph_replay_matches_eager(cuda_device, brax_batch):
     torch.cuda.synchronize()
     assert torch.equal(eager["canvas"].view(torch.int32), replayed.canvas.view(torch.int32))
     assert torch.equal(eager["prim_id"], replayed.prim_id)
+
+
+def adversarial_job(shader, seed, W=72, H=56):
+    """Faces made to stress the conservative coverage rectangle: slivers
+    (nearly parallel edges), sub-pixel triangles at pixel centres, corners
+    exactly on pixel coordinates, huge triangles reaching far off screen,
+    faces crossing w = 0 or with a corner at tiny w, needles across the
+    frame, and repeated vertices.  world_to_clip maps (x, y, z) to
+    (x, y, z, z) so each corner's w is its z."""
+    rng = np.random.Generator(np.random.PCG64(synthetic.BASE_SEED + seed))
+    vp = jr.Camera.viewport_matrix(np.zeros(2, np.int32), np.array((W, H)), 1.0).astype(F32)
+    w2c = np.array([[1, 0, 0, 0], [0, 1, 0, 0], [0, 0, 1, 0], [0, 0, 1, 0]], F32)
+    # NDC of pixel (i, j) as the kernels compute it: x = (i - vp[0, 3]) / vp[0, 0]
+    def ndc(i, j):
+        return F32((F32(i) - vp[0, 3]) / vp[0, 0]), F32((F32(j) - vp[1, 3]) / vp[1, 1])
+
+    tris = []
+    for _ in range(60):  # slivers: a long edge and a third corner a hair off it
+        p = rng.uniform(-1.2, 1.2, 2)
+        d = rng.normal(size=2)
+        d /= np.linalg.norm(d)
+        n = np.array([-d[1], d[0]])
+        L = rng.uniform(0.3, 2.5)
+        eps = 10.0 ** rng.uniform(-7, -2)
+        tris.append([p, p + L * d, p + rng.uniform(0.1, 0.9) * L * d + eps * n])
+    for _ in range(60):  # sub-pixel triangles around pixel centres
+        cx, cy = ndc(rng.integers(0, W), rng.integers(0, H))
+        s = 10.0 ** rng.uniform(-5, -1.5)
+        tris.append([np.array((cx, cy)) + s * rng.normal(size=2) for _ in range(3)])
+    for _ in range(40):  # corners exactly on pixel coordinates
+        tris.append([np.array(ndc(rng.integers(-2, W + 2), rng.integers(-2, H + 2))) for _ in range(3)])
+    for _ in range(20):  # huge triangles
+        tris.append([rng.uniform(-1e3, 1e3, 2) for _ in range(3)])
+    for _ in range(20):  # needles across the frame
+        a = rng.uniform(-1.5, 1.5, 2)
+        b = -a + rng.normal(scale=0.01, size=2)
+        tris.append([a, b, b + rng.normal(scale=1e-4, size=2)])
+    for _ in range(10):  # a repeated corner (det 0: never kept)
+        a, b = rng.uniform(-1, 1, 2), rng.uniform(-1, 1, 2)
+        tris.append([a, a, b])
+    verts, faces = [], []
+    for k, t in enumerate(tris):
+        z = rng.uniform(0.5, 3.0, 3)
+        if k % 7 == 3:  # one corner behind the eye: the face crosses w = 0
+            z[rng.integers(0, 3)] = -rng.uniform(0.05, 2.0)
+        if k % 11 == 5:  # a corner at tiny positive w: huge projected coordinates
+            z[rng.integers(0, 3)] = 10.0 ** rng.uniform(-6, -3)
+        for q in range(3):
+            verts.append((t[q][0] * z[q], t[q][1] * z[q], z[q]))  # NDC (x, y) at w = z
+        faces.append((3 * k, 3 * k + 1, 3 * k + 2))
+    verts = np.asarray(verts, F32)
+    faces = np.asarray(faces, np.int32)
+    rng.shuffle(faces)
+    spec = jr.jobs.JobSpec(shader=shader, width=W, height=H, viewport=vp, world_to_clip=w2c,
+                           world_to_eye_norm=np.identity(4, dtype=F32), position=verts, faces=faces)
+    if shader == _lib.SHADER_GOURAUD:
+        spec.normal = scenes.unit(rng, verts.shape[0])
+        spec.colour = rng.uniform(0.0, 1.0, (verts.shape[0], 3)).astype(F32)
+        spec.light_direction = np.array((0.3, 0.4, -0.8), F32)
+    return spec
+
+
+@pytest.mark.parametrize("shader", [_lib.SHADER_DEPTH, _lib.SHADER_GOURAUD])
+def test_adversarial_faces_tiled_equals_plain_and_oracle(cuda_device, shader):
+    spec = adversarial_job(shader, seed=900 + shader)
+    z0, c0 = scenes.initial_buffers(spec)
+    ref = oracle.render(spec, z0, c0)
+    assert (ref["prim_id"] >= 0).sum() > 100
+    packed = pack([spec], [z0], [c0], cuda_device, count_ties=True)
+    render_plain(packed)
+    zp, cp, pp = (None if t is None else t.clone() for t in unpack(packed, [spec])[0])
+    assert_parity(zp, cp, pp, ref, f"plain adversarial shader {shader}")
+    for tile in SHAPES:
+        for small in (0, 32):
+            z, c, p, _, stats = _tiled_job(spec, z0, c0, cuda_device, tile=tile, small=small)
+            assert stats.overflow == 0
+            assert torch.equal(p, pp), (tile, small)
+            assert torch.equal(z.view(torch.int32), zp.view(torch.int32)), (tile, small)
+            if c is not None:
+                assert torch.equal(c.view(torch.int32), cp.view(torch.int32)), (tile, small)
