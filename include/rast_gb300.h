@@ -37,7 +37,7 @@
 extern "C" {
 #endif
 
-#define RAST_ABI_VERSION 1
+#define RAST_ABI_VERSION 2  /* 2: chooser / mix hook fields (RastJob.layers ..., RastPools.face_alpha, RastBatch.max_layers) */
 
 /* Built-in shader classes (renderer/shaders/*.py), one kernel path each. */
 typedef enum RastShader {

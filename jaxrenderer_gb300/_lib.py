@@ -20,6 +20,8 @@ SHADER_PHONG_DARBOUX = 4
 SHADER_PHONG_REFLECTION = 5
 SHADER_PHONG_REFLECTION_SHADOW = 6
 
+ABI_VERSION = 2  # RAST_ABI_VERSION of the header these structures mirror
+
 JOB_APPLY_DEPTH_OFFSET = 1
 JOB_FACE_ALPHA = 2
 
@@ -247,7 +249,7 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         fn = getattr(lib, name)
         fn.restype = res
         fn.argtypes = args
-    if lib.rast_abi_version() != 1:
+    if lib.rast_abi_version() != ABI_VERSION:
         raise RuntimeError("librast_gb300.so ABI version mismatch")
     _LIB = lib
     return lib
