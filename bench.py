@@ -137,7 +137,7 @@ GLASS = {"layers": 4, "opacity": 0.6, "background": (0.55, 0.7, 0.9)}
 def build_glass84(n, rank, dev):
     """The brax-like 84x84 batch through the compiled chooser / mix hooks:
     the 4 nearest candidates of every pixel blended front to back with
-    opacity 0.6 over a sky colour (forward only)."""
+    opacity 0.6 over a sky colour (timed forward only)."""
     from jaxrenderer_gb300 import _lib, batch as jb
 
     wl = build_brax84(n, rank, dev)

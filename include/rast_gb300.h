@@ -134,8 +134,11 @@ typedef struct RastJob {
  *                    C + T * background, the depth of the first kept slot,
  *                    and that slot's primitive id.
  * A pixel with no kept slot is left unchanged (merge_buffers keep = False).
- * The DEPTH shader takes the default chooser only.  The backward entry
- * point rejects layered jobs (RAST_ERR_UNSUPPORTED). */
+ * The DEPTH shader takes the default chooser only.  Differentiation: the
+ * nearest mixer's gradient flows through the primitive each pixel shows
+ * (prim_id); the over mixer's through every kept slot, weighted by its w,
+ * and to the background (RAST_GRAD_BACKGROUND), with the slots the forward
+ * saved in RastPools.layer_prim.  Opacities get no gradient. */
 #define RAST_MAX_LAYERS 4
 typedef enum RastMixer {
   RAST_MIX_NEAREST = 0,
@@ -162,6 +165,10 @@ typedef struct RastPools {
   int32_t* prim_id;            /* (pixels)     out, optional (NULL): primitive written or -1 */
   const float* face_alpha;     /* (faces)      opacity per face, read by RAST_MIX_OVER jobs
                                   with RAST_JOB_FACE_ALPHA; optional (NULL) otherwise */
+  int32_t* layer_prim;         /* (RAST_MAX_LAYERS, pixels) out, optional (NULL): the layered
+                                  chooser's slots of layered jobs' pixels, slot-major (slot s
+                                  of pixel p at s * total_pixels + p), -1 past the last;
+                                  rast_backward reads it for batches with layered jobs */
 } RastPools;
 
 typedef struct RastBatch {
@@ -296,6 +303,7 @@ int rast_tiled_stats(const RastBatch* batch, const RastTiledConfig* cfg, const v
 #define RAST_GRAD_DIFFUSE 44            /* 3 */
 #define RAST_GRAD_SPECULAR 47           /* 3 */
 #define RAST_GRAD_SHADOW_STRENGTH 50    /* 3: d/d Shadow.strength */
+#define RAST_GRAD_BACKGROUND 53         /* 3: d/d RastJob.background (RAST_MIX_OVER jobs) */
 #define RAST_NPARAM 56                  /* per-job stride of job_params */
 
 typedef struct RastGradPools {

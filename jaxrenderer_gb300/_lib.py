@@ -117,6 +117,7 @@ class RastPools(ctypes.Structure):
         ("canvas", c_void_p),
         ("prim_id", c_void_p),
         ("face_alpha", c_void_p),
+        ("layer_prim", c_void_p),
     ]
 
 
@@ -162,6 +163,7 @@ GRAD_AMBIENT = 41
 GRAD_DIFFUSE = 44
 GRAD_SPECULAR = 47
 GRAD_SHADOW_STRENGTH = 50
+GRAD_BACKGROUND = 53
 NPARAM = 56
 
 

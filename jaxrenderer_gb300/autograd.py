@@ -34,6 +34,7 @@ PARAM_COLUMNS = {
     "diffuse": (_lib.GRAD_DIFFUSE, 3),
     "specular": (_lib.GRAD_SPECULAR, 3),
     "shadow_strength": (_lib.GRAD_SHADOW_STRENGTH, 3),
+    "background": (_lib.GRAD_BACKGROUND, 3),
 }
 POOL_PARAMS = ("position", "normal", "texture", "specular_map", "normal_map")
 JOB_OFFSETS = {name: getattr(_lib.RastJob, name).offset // 4 for name in PARAM_COLUMNS}

@@ -411,6 +411,11 @@ class BatchRunner:
             self.shadow_batch = None
             pools = sb.pools
         self.main_batch = _rast_batch(sb.main_jobs, pools, self.zbuffer, self.canvas, self.prim_id, self.ties, self.keep)
+        # layered jobs: the chooser's slots, saved for the backward (RastPools.layer_prim)
+        self.layer_prim = None
+        if self.main_batch.max_layers > 0:
+            self.layer_prim = torch.empty((_lib.MAX_LAYERS, n * W * H), dtype=torch.int32, device=dev)
+            self.main_batch.pools.layer_prim = self.layer_prim.data_ptr()
         self.main_jobs_dev = self.keep[-1][2]  # device copy of the main job table (uint8)
         self.pools = pools
         self.configs = {}

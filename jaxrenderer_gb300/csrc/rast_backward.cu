@@ -133,12 +133,13 @@ __host__ __device__ constexpr unsigned long long range_bits(int lo, int n) {
 
 // Per-scene parameters each kernel can touch (bit k = RAST_GRAD index k).
 __host__ __device__ constexpr unsigned long long pixel_bits(int sh) {
-  return (sh == RAST_SHADER_GOURAUD || sh == RAST_SHADER_GOURAUD_TEXTURE) ? 0ull
-       : sh == RAST_SHADER_PHONG ? range_bits(RAST_GRAD_LIGHT_DIRECTION, 6)
-       : (sh == RAST_SHADER_PHONG_REFLECTION || sh == RAST_SHADER_PHONG_REFLECTION_SHADOW)
-           ? range_bits(RAST_GRAD_LIGHT_COLOUR, 18)
-       : sh == RAST_SHADER_DEPTH ? 0ull
-       : range_bits(RAST_GRAD_LIGHT_DIRECTION, 21);
+  return sh == RAST_SHADER_DEPTH ? 0ull
+       : range_bits(RAST_GRAD_BACKGROUND, 3) |  // the over mixer's background
+         ((sh == RAST_SHADER_GOURAUD || sh == RAST_SHADER_GOURAUD_TEXTURE) ? 0ull
+          : sh == RAST_SHADER_PHONG ? range_bits(RAST_GRAD_LIGHT_DIRECTION, 6)
+          : (sh == RAST_SHADER_PHONG_REFLECTION || sh == RAST_SHADER_PHONG_REFLECTION_SHADOW)
+              ? range_bits(RAST_GRAD_LIGHT_COLOUR, 18)
+          : range_bits(RAST_GRAD_LIGHT_DIRECTION, 21));
 }
 __host__ __device__ constexpr unsigned long long vertex_bits(int sh) {
   return (sh == RAST_SHADER_GOURAUD || sh == RAST_SHADER_GOURAUD_TEXTURE) ? range_bits(RAST_GRAD_LIGHT_DIRECTION, 6)
@@ -211,7 +212,16 @@ __global__ void __launch_bounds__(kThreads) mark_kernel(RastBatch B, Work w) {
   const int64_t npx = static_cast<int64_t>(J.width) * J.height;
   const int64_t local = static_cast<int64_t>(blockIdx.x) * kThreads + threadIdx.x;
   if (local >= npx || J.n_faces <= 0) return;
-  const int p = B.pools.prim_id[J.pixel_begin + local];
+  const int64_t pix = J.pixel_begin + local;
+  const int layers = job_layers(J, B.max_layers);
+  if (layers > 0 && J.mixer == RAST_MIX_OVER && B.pools.layer_prim) {  // every slot the over mixer may blend
+    for (int s = 0; s < layers; ++s) {
+      const int p = B.pools.layer_prim[s * B.total_pixels + pix];
+      if (p >= 0) w.fvis[J.setup_begin + p] = 1;
+    }
+    return;
+  }
+  const int p = B.pools.prim_id[pix];
   if (p >= 0) w.fvis[J.setup_begin + p] = 1;
 }
 
@@ -564,7 +574,10 @@ __device__ __forceinline__ void fragment_bwd(const RastJob& J, const RastPools& 
     }
     // s x^(s-1) = s x^s / x for x > 0 (no second pow); at x = 0 the pow form
     const float dspec_drz = (sexp == 0.0f) ? 0.0f : (rz > 0.0f ? sexp * (spec / rz) : sexp * powf(rz, sexp - 1.0f));
-    const float grn[3] = {0.0f, 0.0f, gspec * dspec_drz * dmax0(rn[2])};
+    // through max(rn_z, 0): zero below the kink, without forming 0 * inf
+    // (pow's slope at 0 is infinite for exponents below 1)
+    const float dmz = dmax0(rn[2]);
+    const float grn[3] = {0.0f, 0.0f, dmz == 0.0f ? 0.0f : gspec * dspec_drz * dmz};
     float gr[3];
     normalise3_bwd(rn, rnorm, grn, gr);
     float gd = gdif * dmax0(d);
@@ -597,7 +610,9 @@ __host__ __device__ constexpr int pixel_min_blocks() {
           SH == RAST_SHADER_DEPTH) ? 3 : 2;
 }
 
-template <int SH>
+// kLayers: the batch has layered jobs (their over-mixed pixels take one pass
+// per slot); without, the pass loop is compiled away.
+template <int SH, bool kLayers>
 __global__ void __launch_bounds__(kThreads, pixel_min_blocks<SH>())
 pixel_kernel(RastBatch B, Work w, const float* __restrict__ grad_canvas, const float* __restrict__ grad_zbuffer,
              RastGradPools G) {
@@ -612,151 +627,197 @@ pixel_kernel(RastBatch B, Work w, const float* __restrict__ grad_canvas, const f
   ParamGrad pg;
 #pragma unroll
   for (int k = 0; k < RAST_NPARAM; ++k) pg.v[k] = 0.0f;
-  int p = -1;
-  int64_t pix = 0;
-  if (local < npx && J.n_faces > 0) {
-    pix = J.pixel_begin + local;
-    p = P.prim_id[pix];
-  }
-  // per-pixel contributions, added with warp-aggregated atomics below
-  int64_t frow = -1;
-  float fval[12];
-  float vval[9];
+  const bool in_job = local < npx && J.n_faces > 0;
+  const int64_t pix = in_job ? J.pixel_begin + local : 0;
+  // The over mixer's pixels take one pass per chooser slot (the slots the
+  // forward saved), each kept slot's colour weighted by w = T a of the
+  // compositing; every other pixel takes one pass for the primitive it
+  // shows.  The pass count is uniform over the block (one job per block).
+  const int layers = kLayers ? job_layers(J, B.max_layers) : 0;
+  const bool over = kLayers && layers > 0 && J.mixer == RAST_MIX_OVER && P.layer_prim;
+  const int passes = over ? layers : 1;
+  const bool per_face_alpha = (J.flags & RAST_JOB_FACE_ALPHA) && P.face_alpha;
+  // the pixel's output gradients: loaded once up front for layered batches
+  // (every pass reads them), at the pass otherwise
+  float gz_px = 0.0f, gcv_px[3] = {0.0f, 0.0f, 0.0f};
+  auto load_grads = [&]() {
+    gz_px = (in_job && grad_zbuffer) ? grad_zbuffer[pix] : 0.0f;
 #pragma unroll
-  for (int k = 0; k < 12; ++k) fval[k] = 0.0f;
-#pragma unroll
-  for (int k = 0; k < 9; ++k) vval[k] = 0.0f;
-  int64_t vrows[3] = {0, 0, 0};
-  TexGrad tg;
+    for (int q = 0; q < 3; ++q) gcv_px[q] = (in_job && grad_canvas) ? grad_canvas[pix * 3 + q] : 0.0f;
+  };
+  if (kLayers) load_grads();
+  float transmit = 1.0f;  // the over mixer's T
+  bool shown = false;     // a slot of this pixel was kept
   constexpr bool kDarboux = may<SH>(RAST_SHADER_PHONG_DARBOUX);
-  float tval[9];  // dL/d vertex 0's NDC triangle (phong_darboux's Darboux frame)
+  for (int pass = 0; pass < passes; ++pass) {
+    int p = -1;
+    if (in_job) p = over ? P.layer_prim[pass * B.total_pixels + pix] : P.prim_id[pix];
+    // per-pixel contributions, added with warp-aggregated atomics below
+    int64_t frow = -1;
+    float fval[12];
+    float vval[9];
 #pragma unroll
-  for (int k = 0; k < 9; ++k) tval[k] = 0.0f;
-  if (p >= 0) {
-    int i, j;
-    pixel_of(local, npx, J.height, &i, &j);
-    const float x = (static_cast<float>(i) - J.viewport[3]) / J.viewport[0];
-    const float y = (static_cast<float>(j) - J.viewport[7]) / J.viewport[5];
-    const int64_t row = J.setup_begin + p;
-    const float4* fr = w.frec + row * 3;
-    const float4 a = fr[0], bb = fr[1], cz = fr[2];
-    const float m[9] = {a.x, a.y, a.z, a.w, bb.x, bb.y, bb.z, bb.w, cz.x};
-    const float zc[3] = {cz.y, cz.z, cz.w};
-    {
-      // corner vertex rows: the same for every pixel of the face (the key of
-      // the aggregated vertex accumulation)
-      const int32_t* face = P.faces + (J.face_begin + p) * 3;
+    for (int k = 0; k < 12; ++k) fval[k] = 0.0f;
 #pragma unroll
-      for (int k = 0; k < 3; ++k) vrows[k] = J.vout_begin + gather_clamp(__ldg(face + k), J.n_verts);
-    }
-    float c[3];
+    for (int k = 0; k < 9; ++k) vval[k] = 0.0f;
+    int64_t vrows[3] = {0, 0, 0};
+    TexGrad tg;
+    float tval[9];  // dL/d vertex 0's NDC triangle (phong_darboux's Darboux frame)
 #pragma unroll
-    for (int k = 0; k < 3; ++k) c[k] = (x * m[k] + y * m[3 + k]) + m[6 + k];
-    const float wr = (c[0] + c[1]) + c[2];
-    const float b[3] = {c[0] / wr, c[1] / wr, c[2] / wr};
-    float gc[3] = {0.0f, 0.0f, 0.0f};
-    float gzc[3] = {0.0f, 0.0f, 0.0f};
-    // ---- depth output: z = (sum c_k z_k) * vp22 + vp23
-    const float gz = grad_zbuffer ? grad_zbuffer[pix] : 0.0f;
-    if (gz != 0.0f) {
+    for (int k = 0; k < 9; ++k) tval[k] = 0.0f;
+    if (p >= 0) {
+      int i, j;
+      pixel_of(local, npx, J.height, &i, &j);
+      const float x = (static_cast<float>(i) - J.viewport[3]) / J.viewport[0];
+      const float y = (static_cast<float>(j) - J.viewport[7]) / J.viewport[5];
+      const int64_t row = J.setup_begin + p;
+      const float4* fr = w.frec + row * 3;
+      const float4 a = fr[0], bb = fr[1], cz = fr[2];
+      const float m[9] = {a.x, a.y, a.z, a.w, bb.x, bb.y, bb.z, bb.w, cz.x};
+      const float zc[3] = {cz.y, cz.z, cz.w};
+      {
+        // corner vertex rows: the same for every pixel of the face (the key of
+        // the aggregated vertex accumulation)
+        const int32_t* face = P.faces + (J.face_begin + p) * 3;
 #pragma unroll
-      for (int k = 0; k < 3; ++k) {
-        gc[k] += gz * J.viewport[10] * zc[k];
-        gzc[k] += gz * J.viewport[10] * c[k];
+        for (int k = 0; k < 3; ++k) vrows[k] = J.vout_begin + gather_clamp(__ldg(face + k), J.n_verts);
       }
-    }
-    const float gcv[3] = {grad_canvas ? grad_canvas[pix * 3 + 0] : 0.0f,
-                          grad_canvas ? grad_canvas[pix * 3 + 1] : 0.0f,
-                          grad_canvas ? grad_canvas[pix * 3 + 2] : 0.0f};
-    if (sh != RAST_SHADER_DEPTH && (gcv[0] != 0.0f || gcv[1] != 0.0f || gcv[2] != 0.0f)) {
-      const int64_t* vr = vrows;
+      float c[3];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) c[k] = (x * m[k] + y * m[3 + k]) + m[6 + k];
+      const float wr = (c[0] + c[1]) + c[2];
+      const float b[3] = {c[0] / wr, c[1] / wr, c[2] / wr};
+      if (!kLayers) load_grads();
       float r0[kMaxVarying], r1[kMaxVarying], r2[kMaxVarying];
-      const int nv = varying_count(sh);
+      const int nv = sh != RAST_SHADER_DEPTH ? varying_count(sh) : 0;
+      bool loaded = false;
+      auto load_rows = [&]() {
 #pragma unroll
-      for (int k = 0; k < kMaxVarying; ++k) {
-        if (k < nv) {
-          r0[k] = w.vvar[vr[0] * w.vstride + k];
-          r1[k] = w.vvar[vr[1] * w.vstride + k];
-          r2[k] = w.vvar[vr[2] * w.vstride + k];
+        for (int k = 0; k < kMaxVarying; ++k) {
+          if (k < nv) {
+            r0[k] = w.vvar[vrows[0] * w.vstride + k];
+            r1[k] = w.vvar[vrows[1] * w.vstride + k];
+            r2[k] = w.vvar[vrows[2] * w.vstride + k];
+          }
+        }
+        loaded = true;
+      };
+      float wgt = 1.0f, gz = gz_px;
+      bool keep = true;
+      if (over) {
+        // the slot counts only when its fragment shader keeps it (the
+        // Gouraud shaders drop negative interpolated colours)
+        if (sh == RAST_SHADER_GOURAUD || sh == RAST_SHADER_GOURAUD_TEXTURE) {
+          load_rows();
+#pragma unroll
+          for (int q = 0; q < 3; ++q) keep = keep && interp1(b, r0[kVColour + q], r1[kVColour + q], r2[kVColour + q]) >= 0.0f;
+        }
+        if (keep) {
+          const float alpha = per_face_alpha ? __ldg(P.face_alpha + J.face_begin + p) : J.opacity;
+          wgt = transmit * alpha;
+          transmit = transmit * (1.0f - alpha);
+          gz = shown ? 0.0f : gz_px;  // the depth written is the first kept slot's
+          shown = true;
         }
       }
-      float gi[3];
-      fragment_bwd<SH>(J, P, G, r0, r1, r2, b, gcv, gi, pg, tg, tval);
-      if (gi[0] != 0.0f || gi[1] != 0.0f || gi[2] != 0.0f) {
-        // interpolated = sum_k b_k v_k over the carried varying (offset 0 in
-        // both families: eye normal or colour)
-        float gb[3];
-        gb[0] = (gi[0] * r0[0] + gi[1] * r0[1]) + gi[2] * r0[2];
-        gb[1] = (gi[0] * r1[0] + gi[1] * r1[1]) + gi[2] * r1[2];
-        gb[2] = (gi[0] * r2[0] + gi[1] * r2[1]) + gi[2] * r2[2];
+      if (keep) {
+        float gc[3] = {0.0f, 0.0f, 0.0f};
+        float gzc[3] = {0.0f, 0.0f, 0.0f};
+        // ---- depth output: z = (sum c_k z_k) * vp22 + vp23
+        if (gz != 0.0f) {
 #pragma unroll
-        for (int k = 0; k < 3; ++k) {
-          vval[3 * k + 0] = b[k] * gi[0];
-          vval[3 * k + 1] = b[k] * gi[1];
-          vval[3 * k + 2] = b[k] * gi[2];
+          for (int k = 0; k < 3; ++k) {
+            gc[k] += gz * J.viewport[10] * zc[k];
+            gzc[k] += gz * J.viewport[10] * c[k];
+          }
         }
-        // b = c / sum(c)
-        const float s = (gb[0] * b[0] + gb[1] * b[1]) + gb[2] * b[2];
-        const float rw = __frcp_rn(wr);
+        const float gcv[3] = {wgt * gcv_px[0], wgt * gcv_px[1], wgt * gcv_px[2]};
+        if (sh != RAST_SHADER_DEPTH && (gcv[0] != 0.0f || gcv[1] != 0.0f || gcv[2] != 0.0f)) {
+          if (!loaded) load_rows();
+          float gi[3];
+          fragment_bwd<SH>(J, P, G, r0, r1, r2, b, gcv, gi, pg, tg, tval);
+          if (gi[0] != 0.0f || gi[1] != 0.0f || gi[2] != 0.0f) {
+            // interpolated = sum_k b_k v_k over the carried varying (offset 0 in
+            // both families: eye normal or colour)
+            float gb[3];
+            gb[0] = (gi[0] * r0[0] + gi[1] * r0[1]) + gi[2] * r0[2];
+            gb[1] = (gi[0] * r1[0] + gi[1] * r1[1]) + gi[2] * r1[2];
+            gb[2] = (gi[0] * r2[0] + gi[1] * r2[1]) + gi[2] * r2[2];
 #pragma unroll
-        for (int k = 0; k < 3; ++k) gc[k] += (gb[k] - s) * rw;
+            for (int k = 0; k < 3; ++k) {
+              vval[3 * k + 0] = b[k] * gi[0];
+              vval[3 * k + 1] = b[k] * gi[1];
+              vval[3 * k + 2] = b[k] * gi[2];
+            }
+            // b = c / sum(c)
+            const float s = (gb[0] * b[0] + gb[1] * b[1]) + gb[2] * b[2];
+            const float rw = __frcp_rn(wr);
+#pragma unroll
+            for (int k = 0; k < 3; ++k) gc[k] += (gb[k] - s) * rw;
+          }
+        }
+        // ---- c_k = x m[k] + y m[3+k] + m[6+k]: dL/dm, dL/dz_clip per face
+        frow = row;
+        const float xy1[3] = {x, y, 1.0f};
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+#pragma unroll
+          for (int k = 0; k < 3; ++k) fval[3 * r + k] = xy1[r] * gc[k];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) fval[9 + k] = gzc[k];
       }
     }
-    // ---- c_k = x m[k] + y m[3+k] + m[6+k]: dL/dm, dL/dz_clip per face
-    frow = row;
-    const float xy1[3] = {x, y, 1.0f};
+    // ---- warp-aggregated accumulation (pixels of a warp run along a column,
+    // so neighbours usually share the face and the texel)
+    {
+      const Seg sf = segment(frow, frow >= 0);
+      float* facc = w.facc + (frow >= 0 ? frow : 0) * 12;
+      const int nf = grad_zbuffer ? 12 : 9;  // dL/dz_clip only with a depth gradient
 #pragma unroll
-    for (int r = 0; r < 3; ++r)
-#pragma unroll
-      for (int k = 0; k < 3; ++k) fval[3 * r + k] = xy1[r] * gc[k];
-#pragma unroll
-    for (int k = 0; k < 3; ++k) fval[9 + k] = gzc[k];
-  }
-  // ---- warp-aggregated accumulation (pixels of a warp run along a column,
-  // so neighbours usually share the face and the texel)
-  {
-    const Seg sf = segment(frow, frow >= 0);
-    float* facc = w.facc + (frow >= 0 ? frow : 0) * 12;
-    const int nf = grad_zbuffer ? 12 : 9;  // dL/dz_clip only with a depth gradient
-#pragma unroll
-    for (int k = 0; k < 12; ++k) {
-      if (k >= nf) break;
-      const float v = seg_sum(fval[k], sf);
-      if (sf.tail && v != 0.0f) atomicAdd(facc + k, v);
-    }
-#pragma unroll
-    for (int k = 0; k < 9; ++k) {
-      const float v = seg_sum(vval[k], sf);
-      if (sf.tail && v != 0.0f) atomicAdd(w.vacc + vrows[k / 3] * w.vacc_stride + (k % 3), v);
-    }
-    if (kDarboux && w.vacc_stride > 3) {
+      for (int k = 0; k < 12; ++k) {
+        if (k >= nf) break;
+        const float v = seg_sum(fval[k], sf);
+        if (sf.tail && v != 0.0f) atomicAdd(facc + k, v);
+      }
 #pragma unroll
       for (int k = 0; k < 9; ++k) {
-        const float v = seg_sum(tval[k], sf);
-        if (sf.tail && v != 0.0f) atomicAdd(w.vacc + vrows[0] * w.vacc_stride + 3 + k, v);
+        const float v = seg_sum(vval[k], sf);
+        if (sf.tail && v != 0.0f) atomicAdd(w.vacc + vrows[k / 3] * w.vacc_stride + (k % 3), v);
+      }
+      if (kDarboux && w.vacc_stride > 3) {
+#pragma unroll
+        for (int k = 0; k < 9; ++k) {
+          const float v = seg_sum(tval[k], sf);
+          if (sf.tail && v != 0.0f) atomicAdd(w.vacc + vrows[0] * w.vacc_stride + 3 + k, v);
+        }
       }
     }
-  }
-  if (kDarboux && G.normal_map) {
-    const Seg sn = segment(tg.nb, tg.nb >= 0);
-    float g3[3];
+    if (kDarboux && G.normal_map) {
+      const Seg sn = segment(tg.nb, tg.nb >= 0);
+      float g3[3];
 #pragma unroll
-    for (int q = 0; q < 3; ++q) g3[q] = seg_sum(tg.gn[q], sn);
-    if (sn.tail) add_texel_grad(G.normal_map, tg.nb, 3, g3);
-  }
-  if (G.texture) {
-    const Seg st = segment(tg.tb, tg.tb >= 0);
-    float g3[3];
+      for (int q = 0; q < 3; ++q) g3[q] = seg_sum(tg.gn[q], sn);
+      if (sn.tail) add_texel_grad(G.normal_map, tg.nb, 3, g3);
+    }
+    if (G.texture) {
+      const Seg st = segment(tg.tb, tg.tb >= 0);
+      float g3[3];
 #pragma unroll
-    for (int q = 0; q < 3; ++q) g3[q] = seg_sum(tg.gt[q], st);
-    if (st.tail) add_texel_grad(G.texture, tg.tb, tg.ch, g3);
+      for (int q = 0; q < 3; ++q) g3[q] = seg_sum(tg.gt[q], st);
+      if (st.tail) add_texel_grad(G.texture, tg.tb, tg.ch, g3);
+    }
+    if (G.specular_map) {
+      const Seg ss = segment(tg.sidx, tg.sidx >= 0);
+      const float v = seg_sum(tg.gs, ss);
+      if (ss.tail && v != 0.0f) atomicAdd(G.specular_map + tg.sidx, v);
+    }
   }
-  if (G.specular_map) {
-    const Seg ss = segment(tg.sidx, tg.sidx >= 0);
-    const float v = seg_sum(tg.gs, ss);
-    if (ss.tail && v != 0.0f) atomicAdd(G.specular_map + tg.sidx, v);
+  // over: the background is seen through what the kept slots let pass
+  if (over && shown) {
+#pragma unroll
+    for (int q = 0; q < 3; ++q) pg.v[RAST_GRAD_BACKGROUND + q] += gcv_px[q] * transmit;
   }
-  reduce_params<pixel_bits(SH)>(pg, G.job_params, p >= 0, blockIdx.y);
+  reduce_params<pixel_bits(SH)>(pg, G.job_params, in_job && (over ? shown : P.prim_id[pix] >= 0), blockIdx.y);
 }
 
 // dL/dM = -m^T (dL/dm) m^T for the [x, y, w] rows of the clip positions,
@@ -1009,7 +1070,10 @@ static void launch_all(const RastBatch& b, const Work& w, const Layout& L, const
   prof.mark("backward_face_prep_kernel");
   vertex_prep_kernel<<<vgrid, kThreads, 0, s>>>(b, w);
   prof.mark("backward_vertex_prep_kernel");
-  pixel_kernel<SH><<<pgrid, kThreads, 0, s>>>(b, w, gc, gz, G);
+  if (b.max_layers > 0)
+    pixel_kernel<SH, true><<<pgrid, kThreads, 0, s>>>(b, w, gc, gz, G);
+  else
+    pixel_kernel<SH, false><<<pgrid, kThreads, 0, s>>>(b, w, gc, gz, G);
   prof.mark("backward_pixel_kernel");
   face_post_kernel<<<fgrid, kThreads, 0, s>>>(b, w, G);
   prof.mark("backward_face_post_kernel");
@@ -1023,7 +1087,8 @@ static int run(const RastBatch* batch, const float* grad_canvas, const float* gr
   int st = check_batch(batch);
   if (st != RAST_OK) return st;
   if (!grads || !batch->pools.prim_id) return RAST_ERR_INVALID_ARGUMENT;
-  if (batch->max_layers > 0) return RAST_ERR_UNSUPPORTED;  // layered chooser: forward only
+  // the over mixer's gradient needs the slots the forward saved
+  if (batch->max_layers > 0 && !batch->pools.layer_prim) return RAST_ERR_INVALID_ARGUMENT;
   const RastBatch& b = *batch;
   const Layout L = layout(b);
   if (workspace_bytes < L.total) return RAST_ERR_WORKSPACE_TOO_SMALL;

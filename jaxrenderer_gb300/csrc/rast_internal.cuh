@@ -489,6 +489,16 @@ __device__ __forceinline__ void resolve_over_warp(const RastJob& J, const RastPo
   }
 }
 
+// The forward's record of a layered pixel's slots for the backward
+// (RastPools.layer_prim, slot-major): slots 0 .. L-1 from the winner planes,
+// -1 past them.
+__device__ __forceinline__ void save_layers(const RastPools& P, const int32_t* w, int64_t wstride, int64_t pix,
+                                            int L) {
+  if (!P.layer_prim) return;
+#pragma unroll
+  for (int s = 0; s < RAST_MAX_LAYERS; ++s) P.layer_prim[s * wstride + pix] = s < L ? w[s * wstride] : -1;
+}
+
 // Keeps best[0 .. L-1] the L smallest keys seen, ascending: `key` goes in
 // at its rank and the larger ones move down one slot.
 template <int L>

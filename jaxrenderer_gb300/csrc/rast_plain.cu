@@ -154,10 +154,12 @@ shade_kernel(RastBatch B, const float4* __restrict__ setup, const float* __restr
   PixelResult r;
   const VaryingSource src{var, vstride, J.vout_begin};
   const int L = kLayered ? job_layers(J, B.max_layers) : 0;
-  if (kLayered && L > 0)
+  if (kLayered && L > 0) {
     resolve_layers(J, B.pools, setup + J.setup_begin * 4, i, j, winner + pix, B.total_pixels, L, src, &r);
-  else
+    save_layers(B.pools, winner + pix, B.total_pixels, pix, L);
+  } else {
     resolve_pixel(J, B.pools, setup + J.setup_begin * 4, i, j, winner[pix], src, &r);
+  }
   store_pixel(J, B.pools, pix, r);
 }
 

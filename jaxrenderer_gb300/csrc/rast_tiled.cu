@@ -879,7 +879,10 @@ tiled_shade_kernel(RastBatch B, const float4* __restrict__ setup, const int32_t*
     PixelResult r;
     resolve_over_warp(J, B.pools, rec, active, i, j, winner + (active ? pix : 0), B.total_pixels, L, src,
                       s_frags[threadIdx.x >> 5], &r);
-    if (active) store_pixel(J, B.pools, pix, r);
+    if (active) {
+      store_pixel(J, B.pools, pix, r);
+      save_layers(B.pools, winner + pix, B.total_pixels, pix, L);
+    }
     return;
   }
   if (local0 >= npx) return;
@@ -887,6 +890,7 @@ tiled_shade_kernel(RastBatch B, const float4* __restrict__ setup, const int32_t*
   pixel_of(local0, npx, J.height, &i, &j);
   PixelResult r;
   const int w0 = winner[pix];
+  if (kLayered && L > 0) save_layers(B.pools, winner + pix, B.total_pixels, pix, L);
   if (kLayered && L > 0 && w0 < 0) {  // no candidate: the layered chooser keeps nothing
     r.keep = false;
     r.prim = -1;

@@ -25,8 +25,9 @@ objects assigned in place of those methods, each selecting a kernel path:
   primitive id of the first kept slot.  `opacity` is one number for every
   face or an array with one entry per face of `face_indices`.
 
-A pixel with no kept slot keeps its buffer values.  The layered chooser is
-forward only: the backward entry point rejects it.
+A pixel with no kept slot keeps its buffer values.  Gradients: the nearest
+mixer's through the primitive each pixel shows; the over mixer's through
+every kept slot (weight w) and to the background; opacities get none.
 """
 from __future__ import annotations
 

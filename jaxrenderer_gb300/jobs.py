@@ -196,6 +196,7 @@ class PackedBatch:
     pixel_begin: List[int]
     pools: dict = None  # name -> device tensor (RastPools inputs)
     jobs: object = None  # ctypes array of RastJob (host copy)
+    layer_prim: Optional[torch.Tensor] = None  # (MAX_LAYERS, pixels) slots of layered jobs
 
 
 def pack(specs: Sequence[JobSpec], zbuffers: Sequence[Any], canvases: Sequence[Any], device,
@@ -305,6 +306,8 @@ def pack(specs: Sequence[JobSpec], zbuffers: Sequence[Any], canvases: Sequence[A
             cv.add(np.zeros((pixels - cv.rows, 3), np.float32))
         canvas = cv.tensor(device).clone()
     prim = torch.empty(pixels, dtype=torch.int32, device=device) if want_prim_id else None
+    # layered jobs: the chooser's slots, saved for the backward
+    layer_prim = torch.empty((_lib.MAX_LAYERS, pixels), dtype=torch.int32, device=device) if max_layers > 0 else None
     ties = torch.zeros(1, dtype=torch.int64, device=device) if count_ties else None
     jobs_dev = torch.frombuffer(bytearray(bytes(jobs)), dtype=torch.uint8).to(device)
     keep.append(jobs_dev)
@@ -322,9 +325,10 @@ def pack(specs: Sequence[JobSpec], zbuffers: Sequence[Any], canvases: Sequence[A
     P.zbuffer = _ptr(zbuf)
     P.canvas = _ptr(canvas)
     P.prim_id = _ptr(prim)
+    P.layer_prim = _ptr(layer_prim)
     b.near_ties = _ptr(ties)
     return PackedBatch(b, keep, zbuf, canvas, prim, ties, pixel_begin,
-                       {k: v for k, v in tensors.items() if v is not None}, jobs)
+                       {k: v for k, v in tensors.items() if v is not None}, jobs, layer_prim)
 
 
 def render_plain(packed: PackedBatch, stream: Optional[torch.cuda.Stream] = None) -> None:

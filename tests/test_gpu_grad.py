@@ -310,3 +310,22 @@ def test_phong_darboux_gradients_vs_fd64(cuda_device):
                 return float((mask[..., None] * (out["canvas"] - target) ** 2).sum())
             g_fd = (loss(EPS) - loss(-EPS)) / (2 * EPS)
             assert abs(g[k] - g_fd) <= 3e-3 * max(abs(g_fd), 1e-2) + 2e-4, (name, k, g[k], g_fd)
+
+
+def test_specular_exponents_below_one_give_finite_gradients(cuda_device):
+    # pow's slope at 0 is infinite for exponents below 1; where the clamp
+    # max(r_z, 0) is below its kink the gradient through it is exactly 0
+    from tests.scenes import random_job
+
+    spec = random_job(_lib.SHADER_PHONG_REFLECTION, seed=44, W=40, H=40, F=60, spread=1.2)
+    spec.specular_map = np.full_like(spec.specular_map, 0.6)
+    sb = jb.scene_batch_from_specs([spec], cuda_device)
+    db = DifferentiableBatch(sb, form="tiled", tiled_config=_lib.RastTiledConfig(8, 8, 0))
+    leaves = {"light_dir_eye": torch.tensor(spec.light_dir_eye[None], requires_grad=True),
+              "position": torch.tensor(spec.position, requires_grad=True),
+              "specular_map": torch.tensor(spec.specular_map.reshape(-1), requires_grad=True)}
+    canvas, _ = db.render(**{k: v.to(cuda_device) for k, v in leaves.items()})
+    (canvas ** 2).sum().backward()
+    for k, v in leaves.items():
+        assert torch.isfinite(v.grad).all(), k
+    assert leaves["light_dir_eye"].grad.abs().sum() > 0

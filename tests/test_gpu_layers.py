@@ -112,10 +112,11 @@ def test_tile_shape_without_layered_variant_is_refused(cuda_device):
         render_tiled(packed, tile=(16, 16))
 
 
-def test_backward_refuses_layered_batches(cuda_device):
-    spec = layered_job(_lib.SHADER_PHONG, 11, 2, _lib.MIX_NEAREST)
+def test_backward_needs_the_saved_slots(cuda_device):
+    spec = layered_job(_lib.SHADER_PHONG, 11, 2, _lib.MIX_OVER)
     z0, c0 = scenes.initial_buffers(spec)
     packed = pack([spec], [z0], [c0], cuda_device)
+    assert packed.layer_prim is not None
     render_plain(packed)
     lib = _lib.load()
     b = packed.batch
@@ -123,9 +124,20 @@ def test_backward_refuses_layered_batches(cuda_device):
     ws = torch.empty(max(n, 256), dtype=torch.uint8, device=cuda_device)
     gc = torch.zeros_like(packed.canvas)
     grads = _lib.RastGradPools()
-    st = lib.rast_backward(ctypes.byref(b), gc.data_ptr(), None, ctypes.byref(grads), ws.data_ptr(), n,
-                           torch.cuda.current_stream(cuda_device).cuda_stream)
-    assert _lib.STATUS_NAMES[st] == "RAST_ERR_UNSUPPORTED"
+    s = torch.cuda.current_stream(cuda_device).cuda_stream
+    saved = b.pools.layer_prim
+    b.pools.layer_prim = None
+    st = lib.rast_backward(ctypes.byref(b), gc.data_ptr(), None, ctypes.byref(grads), ws.data_ptr(), n, s)
+    assert _lib.STATUS_NAMES[st] == "RAST_ERR_INVALID_ARGUMENT"
+    b.pools.layer_prim = saved
+    st = lib.rast_backward(ctypes.byref(b), gc.data_ptr(), None, ctypes.byref(grads), ws.data_ptr(), n, s)
+    assert st == 0
+    # the saved slots: slot 0 is the nearest candidate; the shown primitive is
+    # the first kept slot (phong keeps every candidate)
+    lp = packed.layer_prim.reshape(_lib.MAX_LAYERS, -1)
+    pid = packed.prim_id.reshape(-1)
+    assert torch.equal(lp[0], pid)
+    assert (lp[2:] == -1).all()  # layers = 2
 
 
 def test_scene_batch_layers_tiled_equals_plain_and_oracle(cuda_device):
@@ -155,3 +167,115 @@ def test_scene_batch_layers_tiled_equals_plain_and_oracle(cuda_device):
         mspec.shadow_map = dref["zbuffer"]
         ref = oracle.render(mspec, np.ones((84, 84), F32), np.ones((84, 84, 3), F32))
         assert_parity(got["zbuffer"][s], got["canvas"][s], got["prim_id"][s], ref, f"layered scene {s}")
+
+
+def _over_job():
+    spec = layered_job(_lib.SHADER_PHONG_REFLECTION, 61, 3, _lib.MIX_OVER, "per_face", F=50)
+    spec.background = (0.3, 0.5, 0.7)
+    return spec
+
+
+def _spec64(spec):
+    import copy
+
+    s = copy.copy(spec)
+    for name in ("position", "normal", "uv", "texture", "specular_map", "viewport", "world_to_clip",
+                 "world_to_eye_norm", "light_dir_eye", "ambient", "diffuse", "specular", "light_colour"):
+        setattr(s, name, np.asarray(getattr(spec, name), np.float64))
+    s.background = np.asarray(spec.background, np.float64)
+    s.face_alpha = np.asarray(spec.face_alpha, np.float64)
+    return s
+
+
+def test_over_mixer_gradients_vs_fd64(cuda_device):
+    """The over mixer's backward (one pass per kept slot, weighted by its
+    w = T a, and the background seen through T) against central differences
+    of the FP64 oracle: texels, light and material terms, the background,
+    and positions of faces shown in some slot (pixels whose slots change
+    under the perturbation are masked out on both sides)."""
+    from jaxrenderer_gb300 import batch as jb
+    from jaxrenderer_gb300.autograd import DifferentiableBatch
+
+    eps = 1e-3
+    spec = _over_job()
+    Wd, Hd = spec.width, spec.height
+    z1, c1 = np.ones((Wd, Hd)), np.ones((Wd, Hd, 3))
+    base = oracle.render(_spec64(spec), z1, c1, dtype=np.float64)
+    assert (base["prim_id"] >= 0).sum() > 100
+    target = base["canvas"] * 0.6 + 0.1
+    sb = jb.scene_batch_from_specs([spec], cuda_device)
+    db = DifferentiableBatch(sb, form="tiled", tiled_config=_lib.RastTiledConfig(8, 8, 0))
+    names = ["ambient", "diffuse", "specular", "light_dir_eye", "background"]
+    leaves = {k: torch.tensor(np.asarray(getattr(spec, k), F32)[None], requires_grad=True) for k in names}
+    leaves["texture"] = torch.tensor(spec.texture.reshape(-1), requires_grad=True)
+    leaves["position"] = torch.tensor(spec.position, requires_grad=True)
+    canvas, _ = db.render(**{k: v.to(cuda_device) for k, v in leaves.items()})
+    layers0 = db.runner.layer_prim.clone()
+    tgt = torch.tensor(target, dtype=torch.float32, device=cuda_device)[None]
+    ((canvas - tgt) ** 2).sum().backward()
+
+    def loss(s, mask=None):
+        out = oracle.render(s, z1, c1, dtype=np.float64)
+        d = (out["canvas"] - target) ** 2
+        return float((d if mask is None else mask[..., None] * d).sum())
+
+    # smooth parameters: no visibility change
+    for name in names:
+        for c in range(3):
+            sp, sm = _spec64(spec), _spec64(spec)
+            getattr(sp, name)[c] += eps
+            getattr(sm, name)[c] -= eps
+            g_fd = (loss(sp) - loss(sm)) / (2 * eps)
+            g_an = float(leaves[name].grad[0, c])
+            assert abs(g_an - g_fd) <= 2e-3 * max(abs(g_fd), 1e-1) + 1e-3, (name, c, g_an, g_fd)
+    gt = leaves["texture"].grad.numpy().reshape(spec.texture.shape)
+    used = np.argwhere(np.abs(gt).sum(-1) > 0)[:6]
+    assert len(used) >= 3
+    for (u, v) in used:
+        for ch in range(3):
+            sp, sm = _spec64(spec), _spec64(spec)
+            sp.texture[u, v, ch] += eps
+            sm.texture[u, v, ch] -= eps
+            g_fd = (loss(sp) - loss(sm)) / (2 * eps)
+            assert abs(gt[u, v, ch] - g_fd) <= 1e-3 * max(abs(g_fd), 1e-2) + 1e-5, (u, v, ch, gt[u, v, ch], g_fd)
+    # positions: flat texture and specular maps (no texel jumps as corners
+    # move) and slot-stable pixels only, judged by the GPU's saved slots
+    gp = leaves["position"].grad.numpy()
+    assert np.abs(gp).sum() > 0
+    spec.texture = np.full_like(spec.texture, 0.8)
+    spec.specular_map = np.full_like(spec.specular_map, 3.0)
+    base = oracle.render(_spec64(spec), z1, c1, dtype=np.float64)
+    target = base["canvas"] * 0.6 + 0.1
+    tgt = torch.tensor(target, dtype=torch.float32, device=cuda_device)[None]
+    db = DifferentiableBatch(jb.scene_batch_from_specs([spec], cuda_device), form="tiled",
+                             tiled_config=_lib.RastTiledConfig(8, 8, 0))
+    db.render()
+    layers0 = db.runner.layer_prim.clone()
+    rng = np.random.Generator(np.random.PCG64(3))
+    shown = np.unique(layers0[layers0 >= 0].cpu().numpy())
+    checked = 0
+    for f in rng.choice(shown, size=min(6, len(shown)), replace=False):
+        v = int(spec.faces[f][rng.integers(0, 3)])
+        for q in (0, 1):
+            pos_p, pos_m = spec.position.copy(), spec.position.copy()
+            pos_p[v, q] += F32(eps)
+            pos_m[v, q] -= F32(eps)
+            stable = np.ones((Wd, Hd), bool)
+            for pos in (pos_p, pos_m):
+                db.render(position=torch.tensor(pos).to(cuda_device))
+                lp = db.runner.layer_prim.reshape(_lib.MAX_LAYERS, Wd, Hd)
+                stable &= (lp == layers0.reshape(_lib.MAX_LAYERS, Wd, Hd)).all(0).cpu().numpy()
+            mask = stable.astype(np.float64)
+            sp, sm = _spec64(spec), _spec64(spec)
+            sp.position[v, q] += eps
+            sm.position[v, q] -= eps
+            g_fd = (loss(sp, mask) - loss(sm, mask)) / (2 * eps)
+            # the analytic side with the same mask
+            leaf = torch.tensor(spec.position, requires_grad=True)
+            cv, _ = db.render(position=leaf.to(cuda_device))
+            m = torch.tensor(mask, dtype=torch.float32, device=cuda_device)[None, ..., None]
+            (m * (cv - tgt) ** 2).sum().backward()
+            g_an = float(leaf.grad[v, q])
+            assert abs(g_an - g_fd) <= 3e-3 * max(abs(g_fd), 1e-1) + 1e-3, (v, q, g_an, g_fd)
+            checked += 1
+    assert checked >= 6
