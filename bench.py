@@ -102,6 +102,7 @@ class Workload:
     notebook: bool = False  # step = device merge + render + uint8 display epilogue, as the notebooks time it
     published: Optional[float] = None  # the reference's published frames/s for this configuration
     display: object = None  # uint8 display images of the notebook step
+    pipeline: Optional[Callable[[], object]] = None  # builds a batch.InstancedPipeline (instanced workloads)
 
 
 def _pass_work(spec) -> float:
@@ -128,7 +129,9 @@ def build_brax84(n, rank, dev):
     return Workload("brax84", "brax-like 84x84 x 4096 scenes, phong_reflection_shadow + 128x128 depth pass", n,
                     chain, work, groups, merges=merges, instances=inst,
                     config={"scenes": n, "mean_faces_per_scene": float(n_faces.mean()),
-                            "objects": int(inst.n_instances), "resolution": [W, H], "shadow_map": list(shadow)})
+                            "objects": int(inst.n_instances), "resolution": [W, H], "shadow_map": list(shadow)},
+                    pipeline=lambda prepare=None: jb.InstancedPipeline(inst, W, H, shadow_size=shadow, device=dev,
+                                                                       prepare=prepare))
 
 
 GLASS = {"layers": 4, "opacity": 0.6, "background": (0.55, 0.7, 0.9)}
@@ -154,6 +157,8 @@ def build_glass84(n, rank, dev):
         return depth, main
 
     wl.key, wl.chain, wl.bwd = "glass84", chain, None
+    brax_pipeline = wl.pipeline
+    wl.pipeline = lambda prepare=None: brax_pipeline(prepare=lambda sb: jb.set_layers(sb, **hooks))
     wl.desc = ("brax-like 84x84 x 4096 scenes, phong_reflection_shadow + 128x128 depth pass, layered chooser "
                "(4 nearest candidates) + over mixer (opacity 0.6)")
     wl.config["hooks"] = {"primitive_chooser": "LayeredChooser(4)", "mix": "OverMixer(opacity=0.6)"}
@@ -971,24 +976,48 @@ def measure_e2e(wl: Workload, mr, step, args, dev, stream, world):
         copied[k] = ev
 
     steps = max(1, min(args.steps, 5))
-    e2e_step()
-    torch.cuda.synchronize(dev)
     start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    start.record(stream)
-    for _ in range(steps):
-        e2e_step()
-    for ev in copied:  # the last copies end inside the timed region
-        if ev is not None:
+    if wl.pipeline is not None and not wl.notebook:
+        # instanced serving through batch.InstancedPipeline: frame k + 1's
+        # transform copy and device merge overlap frame k's render, frame k's
+        # canvases go to pinned host memory while frame k + 1 renders
+        del staging
+        torch.cuda.empty_cache()
+        pipe = wl.pipeline()
+        results = [pipe.canvas(0)]
+        for _ in range(2):  # warm-up frames (both sets)
+            pipe.frame(tr, sc, out=outs[0][0])
+        pipe.synchronize()
+        start.record(stream)
+        pipe.start_after(start)
+        for k in range(steps):
+            pipe.frame(tr, sc, out=outs[k % 2][0])
+        for ev in pipe.pending():  # the last copies end inside the timed region
             stream.wait_event(ev)
-    stop.record(stream)
-    torch.cuda.synchronize(dev)
+        stop.record(stream)
+        torch.cuda.synchronize(dev)
+        del pipe
+    else:
+        e2e_step()
+        torch.cuda.synchronize(dev)
+        start.record(stream)
+        for _ in range(steps):
+            e2e_step()
+        for ev in copied:  # the last copies end inside the timed region
+            if ev is not None:
+                stream.wait_event(ev)
+        stop.record(stream)
+        torch.cuda.synchronize(dev)
     ms = start.elapsed_time(stop) / steps
     out = {"value": world * wl.frames / (ms / 1e3), "unit": UNIT, "ms_per_step": ms,
            "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h), "steps": steps,
            "inputs": ("object transforms + local scalings; per-corner pools rebuilt on the device "
                       "(rast_merge_objects)") if wl.merges else "per-corner input pools",
            "outputs": "uint8 display images" if wl.notebook else "float32 canvases",
-           "pipelined": "device->host copy of step k on a copy stream overlapping step k+1"}
+           "pipelined": ("batch.InstancedPipeline: step k+1's transform copy and device merge on a merge stream "
+                         "and step k's device->host copy on a copy stream, both overlapping the renders "
+                         "(double-buffered pools and canvases)") if (wl.pipeline is not None and not wl.notebook)
+                        else "device->host copy of step k on a copy stream overlapping step k+1"}
     if wl.merges:
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         a.record(stream)

@@ -606,6 +606,105 @@ class MultiRunner:
         return [r.backward(g, stream=stream, out=o) for r, g, o in zip(self.runners, grad_canvases, outs)]
 
 
+class InstancedPipeline:
+    """Serving loop for instanced scenes (meshes resident, transforms per
+    frame), double-buffered: two SceneBatches share the tables but own their
+    per-corner pools, canvases and captured render graphs, so frame k + 1's
+    host -> device transform copy and device merge (rast_merge_objects) run
+    on a merge stream while frame k renders, and frame k's canvases go to host
+    memory on a copy stream while frame k + 1 renders.
+
+        pipe = InstancedPipeline(instances, 84, 84, shadow_size=(128, 128))
+        for k, (tr, sc) in enumerate(frames):        # pinned host tensors
+            pipe.frame(tr, sc, out=host_canvases[k % 2])
+        pipe.synchronize()
+
+    `frame()` only enqueues work: host inputs must stay unchanged, and a
+    host buffer passed as `out` is complete, once `done_event()` of that
+    frame has been reached.  Arguments after `inst` are those of
+    scene_batch_from_instances, plus the runner's form and tiled config and
+    `prepare`, called on each SceneBatch before its runner is built (e.g.
+    set_layers)."""
+
+    def __init__(self, inst, width: int = 84, height: int = 84, light: LightParameters = LightParameters(),
+                 shadow_param: Optional[ShadowParameters] = ShadowParameters(), shadow_size=(128, 128),
+                 device=None, camera_params: Optional[CameraParameters] = None,
+                 shadow_mask: Optional[np.ndarray] = None, shadow_viewport: str = "map", form: str = "tiled",
+                 tiled_config=None, prepare=None):
+        self.device = device if device is not None else torch.device("cuda", torch.cuda.current_device())
+        self.sets = []
+        for _ in range(2):
+            sb, merge = scene_batch_from_instances(inst, width, height, light, shadow_param, shadow_size,
+                                                   self.device, camera_params, shadow_mask, shadow_viewport)
+            if prepare is not None:
+                prepare(sb)
+            runner = BatchRunner(sb, form=form, want_prim_id=False, tiled_config=tiled_config)
+            if form == "tiled":
+                runner.capture()
+            self.sets.append((sb, merge, runner))
+        # the render stream takes precedence: the merge fills the SM
+        # resources the render's kernels leave free
+        self.merge_stream = torch.cuda.Stream(self.device, priority=0)
+        self.render_stream = torch.cuda.Stream(self.device, priority=-1)
+        self.copy_stream = torch.cuda.Stream(self.device)
+        self._rendered = [None, None]  # set b's pools / canvas are in use until these
+        self._copied = [None, None]
+        self.k = 0
+
+    def canvas(self, b: int) -> torch.Tensor:
+        return self.sets[b][2].canvas
+
+    def start_after(self, event: torch.cuda.Event) -> None:
+        """Make the pipeline's streams wait for `event` (e.g. a timing start)."""
+        for s in (self.merge_stream, self.render_stream, self.copy_stream):
+            s.wait_event(event)
+
+    def frame(self, transforms, local_scaling, out: Optional[torch.Tensor] = None) -> torch.Tensor:
+        """Enqueue one frame: transforms (I, 4, 4) and local scalings (I, 3)
+        (host or device), merged and rendered into set k % 2; with `out`
+        (a pinned host tensor of the canvas shape) the canvases are copied
+        there.  Returns the set's device canvases."""
+        b = self.k % 2
+        self.k += 1
+        sb, merge, runner = self.sets[b]
+        if self._rendered[b] is not None:  # frame k - 2 read these pools
+            self.merge_stream.wait_event(self._rendered[b])
+        merge.merge(transforms, local_scaling, self.merge_stream)
+        merged = torch.cuda.Event()
+        merged.record(self.merge_stream)
+        self.render_stream.wait_event(merged)
+        if self._copied[b] is not None:  # frame k - 2's canvases left for the host
+            self.render_stream.wait_event(self._copied[b])
+        if runner.graph is not None:
+            with torch.cuda.stream(self.render_stream):
+                runner.graph.replay()
+        else:
+            runner.run(self.render_stream)
+        rendered = torch.cuda.Event()
+        rendered.record(self.render_stream)
+        self._rendered[b] = rendered
+        copied = rendered
+        if out is not None:
+            self.copy_stream.wait_event(rendered)
+            with torch.cuda.stream(self.copy_stream):
+                out.copy_(runner.canvas, non_blocking=True)
+            copied = torch.cuda.Event()
+            copied.record(self.copy_stream)
+        self._copied[b] = copied
+        return runner.canvas
+
+    def done_event(self) -> Optional[torch.cuda.Event]:
+        """The last enqueued frame's end (its host copy when it had one)."""
+        return self._copied[(self.k - 1) % 2] if self.k else None
+
+    def pending(self) -> List[torch.cuda.Event]:
+        return [e for e in self._copied if e is not None]
+
+    def synchronize(self) -> None:
+        for e in self.pending():
+            e.synchronize()
+
+
 def mixed_scene_batches(flat, resolutions: np.ndarray, classes: Sequence[Tuple[int, int]],
                         shadow_mask: Optional[np.ndarray] = None, light: LightParameters = LightParameters(),
                         shadow_param: Optional[ShadowParameters] = ShadowParameters(), device=None,
@@ -640,6 +739,6 @@ def render_batch(sb: SceneBatch, form: str = "plain", want_prim_id: bool = True)
 
 
 __all__ = ["SceneBatch", "SceneTables", "scene_batch_tables", "scene_batch_from_flat", "scene_batch_from_specs",
-           "set_layers",
+           "set_layers", "InstancedPipeline",
            "scene_job_specs", "MultiRunner", "mixed_scene_batches", "scene_batch_from_instances",
            "flat_pools", "render_batch", "BatchRunner", "BatchOutputs", "job_table"]
