@@ -16,7 +16,7 @@ render.
 """
 from __future__ import annotations
 
-from typing import Dict, Optional, Sequence, Tuple
+from typing import Tuple
 
 import numpy as np
 import torch

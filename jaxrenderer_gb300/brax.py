@@ -20,7 +20,7 @@ import io
 import pickle
 import zipfile
 from dataclasses import dataclass
-from typing import List, Tuple, Union
+from typing import List, Union
 
 import numpy as np
 

@@ -11,7 +11,7 @@ finite-difference gradient checks.
 from __future__ import annotations
 
 import enum
-from typing import NamedTuple, Optional, Sequence, Tuple, Union
+from typing import NamedTuple
 
 import numpy as np
 

@@ -8,7 +8,7 @@ reference's operation order.
 """
 from __future__ import annotations
 
-from typing import Any, List, NamedTuple, Optional, Sequence, Tuple
+from typing import Any, List, NamedTuple, Sequence, Tuple
 
 import numpy as np
 

@@ -9,7 +9,6 @@ reference's functional API returns new arrays.
 """
 from __future__ import annotations
 
-from typing import Optional, Tuple
 
 import numpy as np
 import torch

@@ -7,7 +7,7 @@ passes are CUDA kernels.
 """
 from __future__ import annotations
 
-from typing import Any, NamedTuple, Optional, Sequence, Tuple, Union
+from typing import Any, NamedTuple, Optional, Sequence, Union
 
 import numpy as np
 import torch

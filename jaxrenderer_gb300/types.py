@@ -7,7 +7,7 @@ on the GPU.
 """
 from __future__ import annotations
 
-from typing import Any, Generic, NamedTuple, Tuple, TypeVar
+from typing import Any, NamedTuple, Tuple, TypeVar
 
 import numpy as np
 
