@@ -14,7 +14,7 @@ import torch
 
 from .geometry import Camera, _arr, normalise
 from .model import MergedModel, ModelObject, merge_objects
-from .pipeline import default_device, render, render_with_ids
+from .pipeline import default_device, render_with_ids
 from .shaders.phong_reflection import PhongReflectionTextureExtraInput, PhongReflectionTextureShader
 from .shaders.phong_reflection_shadow import (
     PhongReflectionShadowTextureExtraInput,
