@@ -204,3 +204,37 @@ def test_adversarial_faces_tiled_equals_plain_and_oracle(cuda_device, shader):
             assert torch.equal(z.view(torch.int32), zp.view(torch.int32)), (tile, small)
             if c is not None:
                 assert torch.equal(c.view(torch.int32), cp.view(torch.int32)), (tile, small)
+
+
+def test_ragged_edge_case_batch(cuda_device):
+    """One tiled batch of awkward jobs: no faces, a 1x1 and a 1-row canvas, a
+    single face, reversed windings, an odd non-square canvas, a layered
+    "over" job: every job equals the plain form and the oracle, for several
+    tile shapes."""
+    specs = []
+    s = scenes.random_job(_lib.SHADER_GOURAUD, seed=950, W=20, H=20, F=30)
+    s.faces = np.zeros((0, 3), np.int32)
+    specs.append(s)
+    specs.append(scenes.random_job(_lib.SHADER_PHONG, seed=951, W=1, H=1, F=40, spread=0.3))
+    specs.append(scenes.random_job(_lib.SHADER_DEPTH, seed=952, W=37, H=1, F=40, spread=0.8))
+    one = scenes.random_job(_lib.SHADER_GOURAUD_TEXTURE, seed=953, W=16, H=12, F=5, spread=0.8)
+    one.faces = one.faces[:1]
+    specs.append(one)
+    flipped = scenes.random_job(_lib.SHADER_GOURAUD, seed=954, W=24, H=24, F=30, spread=0.8)
+    flipped.faces = np.ascontiguousarray(flipped.faces[:, ::-1])  # every winding reversed
+    specs.append(flipped)
+    specs.append(scenes.random_job(_lib.SHADER_PHONG_REFLECTION, seed=955, W=7, H=93, F=80, spread=1.0))
+    over = scenes.random_job(_lib.SHADER_PHONG_REFLECTION, seed=956, W=30, H=22, F=60, spread=0.9)
+    over.layers, over.mixer, over.opacity = 3, _lib.MIX_OVER, 0.5
+    specs.append(over)
+    bufs = [scenes.initial_buffers(s) for s in specs]
+    refs = [oracle.render(s, *b) for s, b in zip(specs, bufs)]
+    assert (refs[0]["prim_id"] == -1).all() and (refs[5]["prim_id"] >= 0).any()
+    for form, tile in (("plain", None), ("tiled", (8, 8)), ("tiled", (4, 8)), ("tiled", (16, 8))):
+        packed = pack(specs, [b[0] for b in bufs], [b[1] for b in bufs], cuda_device)
+        if form == "plain":
+            render_plain(packed)
+        else:
+            assert render_tiled(packed, tile=tile).overflow == 0
+        for k, (s, out) in enumerate(zip(specs, unpack(packed, specs))):
+            assert_parity(*out, refs[k], f"{form} {tile} job {k}")
