@@ -481,21 +481,21 @@ def run_ours(args, rank, world, local):
 
         dist.init_process_group("nccl")
     _lib.load()
-    form = "tiled" if args.form == "auto" else args.form
     wl = BUILDERS[args.workload](args.scenes, rank, dev)
     stream = torch.cuda.current_stream(dev)
+    form, form_times = args.form, None
+    if args.form == "auto":
+        form, form_times = choose_form(wl, dev)
     in_bytes = input_bytes(wl.groups)
     flush = in_bytes < 2 * L2_BYTES
     timed = Timer(dev, stream, world, flush)
 
     mr = jb.MultiRunner(wl.groups, form=form, want_prim_id=False)
     if wl.notebook:
-        step, wl.display = notebook_step(wl, mr, dev, capture=form == "tiled")
-    elif form == "tiled":
+        step, wl.display = notebook_step(wl, mr, dev, capture=True)
+    else:
         mr.capture()
         step = mr.replay
-    else:
-        step = lambda: mr.run(stream)  # noqa: E731
     with ClockSampler(local) as clk:  # sampled over the warm-up and the timed steps
         time.sleep(0.2)
         for _ in range(args.warmup):
@@ -506,11 +506,15 @@ def run_ours(args, rank, world, local):
     visible = count_visible(mr)
 
     comparison = {}
-    if form == "tiled" and not args.no_plain:
+    if not args.no_plain:  # the plain form as the reference's method runs: eager, one pass per call
         plain = jb.MultiRunner(wl.groups, form="plain", want_prim_id=False)
         pms = timed(lambda: plain.run(stream), max(1, min(args.steps, 3)), 1)
-        comparison = {"plain_fwd": world * wl.frames / (pms / 1e3), "plain_ms_per_step": pms,
-                      "tiled_over_plain": pms / ms_per_step}
+        comparison = {"plain_fwd": world * wl.frames / (pms / 1e3), "plain_ms_per_step": pms}
+        if form == "tiled":
+            comparison["tiled_over_plain"] = pms / ms_per_step
+        else:  # small workload: the graph-replayed plain form was the faster
+            comparison["tiled_graph_ms_per_step"] = form_times["tiled"]
+            comparison["tiled_fwd"] = world * wl.frames / (form_times["tiled"] / 1e3)
         del plain
         torch.cuda.empty_cache()
 
@@ -539,7 +543,10 @@ def run_ours(args, rank, world, local):
                 "inputs-only pickles)",
         "config": dict({
             "workload": wl.desc,
-            "form": form + (" (CUDA graph replay)" if form == "tiled" else ""),
+            "form": form + " (CUDA graph replay)" + (
+                "" if form_times is None else
+                ", the faster of the two forms on this workload (" +
+                ", ".join(f"{k} {v:.3f} ms" for k, v in form_times.items()) + " per step)"),
             "tiled_config": {name: [c.tile_w, c.tile_h, int(c.bin_capacity), int(c.small_area)]
                              for name, r, p in prof["passes"]
                              for c in [r.configs.get(p)] if c is not None},
@@ -563,6 +570,35 @@ def run_ours(args, rank, world, local):
         print(json.dumps(out), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def choose_form(wl: Workload, dev):
+    """The form `value` is timed with: tiled for large workloads; for small
+    ones (under 1e9 pixel-triangle pairs, where the tiled form's fixed
+    launch costs can dominate) the faster of both forms' graph replays.
+    Both give identical results.  Returns (form, {form: ms per replay} or
+    None)."""
+    import torch
+
+    from jaxrenderer_gb300 import batch as jb
+
+    if wl.notebook or float(wl.work.sum()) >= 1e9:
+        return "tiled", None
+    times = {}
+    for f in ("tiled", "plain"):
+        mr = jb.MultiRunner(wl.groups, form=f, want_prim_id=False)
+        mr.capture()
+        for _ in range(3):
+            mr.replay()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(10):
+            mr.replay()
+        e1.record()
+        torch.cuda.synchronize(dev)
+        times[f] = e0.elapsed_time(e1) / 10
+        del mr
+    return min(times, key=times.get), times
 
 
 def notebook_step(wl: Workload, mr, dev, capture: bool):
