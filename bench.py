@@ -527,6 +527,7 @@ def run_ours(args, rank, world, local):
         e2e = measure_e2e(wl, mr, step, args, dev, stream, world)
 
     kernels_per_step = prof["launches_per_step"]
+    clocks = clk.summary()
     out = {
         "metric": METRIC,
         "value": value,
@@ -557,10 +558,10 @@ def run_ours(args, rank, world, local):
         }, **wl.config),
         "fwd_comparison": comparison,
         "fwd_bwd": fwd_bwd,
-        "roofline": roofline(prof, visible),
+        "roofline": roofline(prof, visible, clocks),
         "kernels": prof["summary"],
         "gpu_launches": kernels_per_step * args.steps,
-        "clocks": clk.summary(),
+        "clocks": clocks,
     }
     if e2e is not None:
         out["e2e"] = e2e
@@ -881,10 +882,44 @@ NCU_BYTES_PER_UNIT = {
     "tiled_shade_kernel": ("P", 39.2),
 }
 
+# Warp instructions executed per unit of work (ncu smsp__inst_executed.sum,
+# same capture): setup_bin 70.9 M for both passes' faces, scatter 18.5 M,
+# face_varyings 12.2 M for the main pass's 735,252 faces, tiled_shade 52.4 M.
+# These kernels are bound by instruction issue, not DRAM: achieved warp
+# instructions per second over the SMs' issue rate (4 schedulers per SM, one
+# warp instruction per clock each) is the ceiling they approach.
+NCU_WARP_INSTR_PER_UNIT = {
+    "setup_bin_kernel": ("F", 48.2),
+    "scatter_kernel": ("F", 12.6),
+    "face_varyings_kernel": ("F", 16.6),
+    "tiled_shade_kernel": ("P", 29.0),
+}
 
-def roofline(prof, visible):
+
+def issue_roofline(kname, info, ms, clocks):
+    """Issue-slot ceiling of a launch of `kname`: ncu's warp instructions per
+    unit times the launch's units, per second of the live launch time, over
+    SMs x 4 schedulers x the median SM clock sampled during the run."""
+    import torch
+
+    if kname not in NCU_WARP_INSTR_PER_UNIT or ms <= 0:
+        return None
+    mhz = (clocks or {}).get("sm_mhz") or (clocks or {}).get("sm_max_mhz")
+    if not mhz:
+        return None
+    unit, per = NCU_WARP_INSTR_PER_UNIT[kname]
+    sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    peak = sms * 4 * float(mhz) * 1e6
+    achieved = per * info[unit] / (ms / 1e3)
+    return {"achieved": achieved, "peak": peak, "unit": "warp instructions/s", "frac": achieved / peak,
+            "note": f"ncu warp instructions per {'face' if unit == 'F' else 'pixel'} on the 256-scene "
+                    f"brax-like case x this launch's units; peak {sms} SMs x 4 schedulers x {float(mhz):.0f} MHz"}
+
+
+def roofline(prof, visible, clocks=None):
     """HBM roofline of the dominant kernel: algorithmic bytes per launch /
-    average launch duration (CUDA events inside the library)."""
+    average launch duration (CUDA events inside the library); with the
+    issue-slot figure beside it where ncu's instruction counts apply."""
     peak, kind = measured_peaks()
     summ = prof["summary"]
     infos = {}
@@ -937,6 +972,10 @@ def roofline(prof, visible):
         "avg_launch_ms": ms,
         "per_kernel": per_kernel,
     }
+    if not small and info["slots"] == 1:
+        issue = issue_roofline(k_dom, info, ms, clocks)
+        if issue is not None:
+            out["issue"] = issue
     kname = prof["where"][dom][2]
     if kname in ("scan_kernel", "raster_kernel"):
         tests = info["tests"] if kname == "scan_kernel" else None
