@@ -42,11 +42,12 @@ constexpr int kThreads = 256;
 constexpr int kRowsPerThread = 32;
 constexpr int kRows = kThreads * kRowsPerThread;
 
-// y = v / |v|;  dv = (dy - y (y . dy)) / |v|
+// y = v / |v|;  dv = (dy - y (y . dy)) / |v|  (one division, three products)
 __device__ __forceinline__ void normalise3_bwd(const float* y, float norm, const float* dy, float* dv) {
   const float s = (y[0] * dy[0] + y[1] * dy[1]) + y[2] * dy[2];
+  const float r = 1.0f / norm;
 #pragma unroll
-  for (int k = 0; k < 3; ++k) dv[k] = (dy[k] - y[k] * s) / norm;
+  for (int k = 0; k < 3; ++k) dv[k] = (dy[k] - y[k] * s) * r;
 }
 
 __device__ __forceinline__ float norm3(const float* v) {
@@ -92,7 +93,7 @@ __host__ __device__ constexpr bool may(int x) {
 }
 
 struct Seg {
-  int start;    // first lane of this lane's segment
+  int rel;      // this lane's offset from the first lane of its segment
   bool tail;    // last lane of its segment (and active)
   int levels;   // shuffle levels that cover the longest segment of the warp
 };
@@ -107,24 +108,30 @@ __device__ __forceinline__ Seg segment(long long key, bool active) {
   const unsigned heads = __ballot_sync(kFull, head);
   const unsigned upto = heads & (0xffffffffu >> (31 - lane));
   Seg s;
-  s.start = 31 - __clz(upto);
+  s.rel = lane - (31 - __clz(upto));
   s.tail = tail && active;
-  const unsigned len = tail ? static_cast<unsigned>(lane - s.start + 1) : 0u;
+  const unsigned len = tail ? static_cast<unsigned>(s.rel + 1) : 0u;
   const unsigned longest = __reduce_max_sync(kFull, len);
-  s.levels = 0;
-  while ((1u << s.levels) < longest) ++s.levels;
+  s.levels = longest <= 1u ? 0 : 32 - __clz(longest - 1u);  // ceil(log2(longest))
   return s;
 }
 
-// Inclusive segmented sum up to this lane (the tail lane holds the total).
-__device__ __forceinline__ float seg_sum(float v, const Seg& s) {
-  const int lane = threadIdx.x & 31;
-  for (int l = 0; l < s.levels; ++l) {
+// Inclusive segmented sums of N values up to this lane (the tail lane holds
+// the totals), in place.  Levels outside, values inside: the level test and
+// the lane's predicate are paid once per level, not once per value.
+template <int N>
+__device__ __forceinline__ void seg_sums(float* v, const Seg& s) {
+#pragma unroll
+  for (int l = 0; l < 5; ++l) {
+    if (l >= s.levels) break;  // uniform over the warp
     const int d = 1 << l;
-    const float o = __shfl_up_sync(kFull, v, d);
-    if (lane - d >= s.start) v += o;
+    const bool take = s.rel >= d;
+#pragma unroll
+    for (int k = 0; k < N; ++k) {
+      const float o = __shfl_up_sync(kFull, v[k], d);
+      if (take) v[k] += o;
+    }
   }
-  return v;
 }
 
 __host__ __device__ constexpr unsigned long long range_bits(int lo, int n) {
@@ -156,13 +163,22 @@ struct ParamGrad {
   float v[RAST_NPARAM];
 };
 
+struct NoPost {
+  static constexpr bool kActive = false;
+  __device__ void operator()(float*) const {}
+};
+
 // Block reduction of the parameters in BITS, added to this block's scene.
 // Every thread of the block must call it.
 // `active`: this thread contributed; warps without a contributing thread
-// skip their shuffles and add zeros.
-template <unsigned long long BITS>
-__device__ __forceinline__ void reduce_params(const ParamGrad& pg, float* job_params, bool active, int job) {
+// skip their shuffles and add zeros.  `post` (when Post::kActive) maps the
+// block's totals, on one thread, before they are added: the linear maps
+// every pixel's contribution would go through are applied once per block.
+template <unsigned long long BITS, class Post = NoPost>
+__device__ __forceinline__ void reduce_params(const ParamGrad& pg, float* job_params, bool active, int job,
+                                              const Post& post = Post()) {
   __shared__ float s_red[kThreads / 32][RAST_NPARAM];
+  __shared__ float s_tot[Post::kActive ? RAST_NPARAM : 1];
   if (BITS == 0ull || !job_params) return;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const bool warp_active = __any_sync(0xffffffffu, active);
@@ -178,13 +194,47 @@ __device__ __forceinline__ void reduce_params(const ParamGrad& pg, float* job_pa
     if (lane == 0) s_red[warp][k] = v;
   }
   __syncthreads();
-  if (threadIdx.x < RAST_NPARAM && ((BITS >> threadIdx.x) & 1ull)) {
-    float v = 0.0f;
+  const bool mine = threadIdx.x < RAST_NPARAM && ((BITS >> threadIdx.x) & 1ull);
+  float v = 0.0f;
+  if (mine) {
 #pragma unroll
     for (int w = 0; w < kThreads / 32; ++w) v += s_red[w][threadIdx.x];
-    if (v != 0.0f) atomicAdd(job_params + static_cast<int64_t>(job) * RAST_NPARAM + threadIdx.x, v);
   }
+  if (Post::kActive) {
+    if (threadIdx.x < RAST_NPARAM) s_tot[threadIdx.x] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) post(s_tot);
+    __syncthreads();
+    if (mine) v = s_tot[threadIdx.x];
+  }
+  if (mine && v != 0.0f) atomicAdd(job_params + static_cast<int64_t>(job) * RAST_NPARAM + threadIdx.x, v);
 }
+
+// The scene's light directions normalised once per block (the same
+// operations as the fragment shaders'), with their norms.
+struct LightUnit {
+  float dir[3], dir_n;  // light_direction (phong, phong_darboux)
+  float eye[3], eye_n;  // light_dir_eye (phong_reflection[_shadow])
+};
+
+// Pixels add dL/d(normalised light) to the scene's light-direction slots;
+// the block's total goes through normalise's reverse mode once (it is
+// linear in the incoming gradient).
+struct LightPost {
+  static constexpr bool kActive = true;
+  const LightUnit* lu;
+  int shader;
+  __device__ void operator()(float* tot) const {
+    const bool eye = shader == RAST_SHADER_PHONG_REFLECTION || shader == RAST_SHADER_PHONG_REFLECTION_SHADOW;
+    if (!eye && shader != RAST_SHADER_PHONG && shader != RAST_SHADER_PHONG_DARBOUX) return;
+    const int base = eye ? RAST_GRAD_LIGHT_DIR_EYE : RAST_GRAD_LIGHT_DIRECTION;
+    const float g[3] = {tot[base], tot[base + 1], tot[base + 2]};
+    float d[3];
+    normalise3_bwd(eye ? lu->eye : lu->dir, eye ? lu->eye_n : lu->dir_n, g, d);
+#pragma unroll
+    for (int q = 0; q < 3; ++q) tot[base + q] = d[q];
+  }
+};
 
 // Workspace views (see layout()).
 struct Work {
@@ -324,7 +374,7 @@ template <int SH>
 __device__ __forceinline__ void fragment_bwd(const RastJob& J, const RastPools& P, const RastGradPools& G,
                                              const float* r0, const float* r1, const float* r2, const float* b,
                                              const float* gcv, float* g_interp, ParamGrad& pg, TexGrad& tg,
-                                             float* gtri) {
+                                             float* gtri, const LightUnit& lu) {
   const int sh = SH >= 0 ? SH : J.shader;
   g_interp[0] = g_interp[1] = g_interp[2] = 0.0f;
   if (may<SH>(RAST_SHADER_GOURAUD) && sh == RAST_SHADER_GOURAUD) {
@@ -393,8 +443,7 @@ __device__ __forceinline__ void fragment_bwd(const RastJob& J, const RastPools& 
     const float bnn = norm3(bn);
     normalise3(bn, n2);
     texel3(P.texture + J.texture_begin, J.tex_w, J.tex_h, J.tex_c, ui, wi, tc);
-    const float ln = norm3(J.light_direction);
-    normalise3(J.light_direction, l);
+    l[0] = lu.dir[0], l[1] = lu.dir[1], l[2] = lu.dir[2];
     const float d = dot3(n2, l);
     bool nonneg = true;
 #pragma unroll
@@ -412,15 +461,14 @@ __device__ __forceinline__ void fragment_bwd(const RastJob& J, const RastPools& 
       pg.v[RAST_GRAD_LIGHT_COLOUR + q] += glc * d;
       gd += glc * J.light_colour[q];
     }
-    float gn2[3], gl[3], gL[3], gbn[3];
+    float gn2[3], gl[3], gbn[3];
 #pragma unroll
     for (int q = 0; q < 3; ++q) {
       gn2[q] = gd * l[q];
       gl[q] = gd * n2[q];
     }
-    normalise3_bwd(l, ln, gl, gL);
 #pragma unroll
-    for (int q = 0; q < 3; ++q) pg.v[RAST_GRAD_LIGHT_DIRECTION + q] += gL[q];
+    for (int q = 0; q < 3; ++q) pg.v[RAST_GRAD_LIGHT_DIRECTION + q] += gl[q];  // normalise's reverse: per block
     normalise3_bwd(n2, bnn, gn2, gbn);
     // bn[r] = ni[r] nm0 + nj[r] nm1 + n[r] nm2
     float gni[3], gnj[3];
@@ -469,8 +517,7 @@ __device__ __forceinline__ void fragment_bwd(const RastJob& J, const RastPools& 
     const int ui = pymod(f2i(floorf(u)), J.tex_w), wi = pymod(f2i(floorf(v)), J.tex_h);
     float tc[3], l[3];
     texel3(P.texture + J.texture_begin, J.tex_w, J.tex_h, J.tex_c, ui, wi, tc);
-    const float ln = norm3(J.light_direction);
-    normalise3(J.light_direction, l);
+    l[0] = lu.dir[0], l[1] = lu.dir[1], l[2] = lu.dir[2];
     const float d = dot3(n, l);
     bool nonneg = true;
     float lc[3];
@@ -489,15 +536,14 @@ __device__ __forceinline__ void fragment_bwd(const RastJob& J, const RastPools& 
       pg.v[RAST_GRAD_LIGHT_COLOUR + q] += glc * d;
       gd += glc * J.light_colour[q];
     }
-    float gl[3], gL[3];
+    float gl[3];
 #pragma unroll
     for (int q = 0; q < 3; ++q) {
       gn[q] = gd * l[q];
       gl[q] = gd * n[q];
     }
-    normalise3_bwd(l, ln, gl, gL);
 #pragma unroll
-    for (int q = 0; q < 3; ++q) pg.v[RAST_GRAD_LIGHT_DIRECTION + q] += gL[q];
+    for (int q = 0; q < 3; ++q) pg.v[RAST_GRAD_LIGHT_DIRECTION + q] += gl[q];  // normalise's reverse: per block
   } else {
     // phong_reflection[_shadow] (phong_reflection.py:158-235)
     const bool shadowed = sh == RAST_SHADER_PHONG_REFLECTION_SHADOW;
@@ -537,8 +583,7 @@ __device__ __forceinline__ void fragment_bwd(const RastJob& J, const RastPools& 
     const int ui = f2i(floorf(uvr[0])), wi = f2i(floorf(uvr[1]));
     float tc[3], l[3];
     texel3(P.texture + J.texture_begin, J.tex_w, J.tex_h, J.tex_c, ui, wi, tc);
-    const float ln = norm3(J.light_dir_eye);
-    normalise3(J.light_dir_eye, l);
+    l[0] = lu.eye[0], l[1] = lu.eye[1], l[2] = lu.eye[2];
     const float d = dot3(n, l);
     const float dif = max0(d);
     float r[3], rn[3];
@@ -593,10 +638,8 @@ __device__ __forceinline__ void fragment_bwd(const RastJob& J, const RastPools& 
       gn[q] += gd * l[q];
       gl[q] += gd * n[q];
     }
-    float gLe[3];
-    normalise3_bwd(l, ln, gl, gLe);
 #pragma unroll
-    for (int q = 0; q < 3; ++q) pg.v[RAST_GRAD_LIGHT_DIR_EYE + q] += gLe[q];
+    for (int q = 0; q < 3; ++q) pg.v[RAST_GRAD_LIGHT_DIR_EYE + q] += gl[q];  // normalise's reverse: per block
   }
   normalise3_bwd(n, nrmn, gn, g_interp);
 }
@@ -617,7 +660,15 @@ __global__ void __launch_bounds__(kThreads, pixel_min_blocks<SH>())
 pixel_kernel(RastBatch B, Work w, const float* __restrict__ grad_canvas, const float* __restrict__ grad_zbuffer,
              RastGradPools G) {
   __shared__ RastJob sJ;
+  __shared__ LightUnit sL;
   load_job_to_shared(B.jobs + blockIdx.y, &sJ);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    sL.dir_n = norm3(sJ.light_direction);
+    normalise3(sJ.light_direction, sL.dir);
+    sL.eye_n = norm3(sJ.light_dir_eye);
+    normalise3(sJ.light_dir_eye, sL.eye);
+  }
   __syncthreads();
   const RastJob& J = sJ;
   const RastPools& P = B.pools;
@@ -735,7 +786,7 @@ pixel_kernel(RastBatch B, Work w, const float* __restrict__ grad_canvas, const f
         if (sh != RAST_SHADER_DEPTH && (gcv[0] != 0.0f || gcv[1] != 0.0f || gcv[2] != 0.0f)) {
           if (!loaded) load_rows();
           float gi[3];
-          fragment_bwd<SH>(J, P, G, r0, r1, r2, b, gcv, gi, pg, tg, tval);
+          fragment_bwd<SH>(J, P, G, r0, r1, r2, b, gcv, gi, pg, tg, tval, sL);
           if (gi[0] != 0.0f || gi[1] != 0.0f || gi[2] != 0.0f) {
             // interpolated = sum_k b_k v_k over the carried varying (offset 0 in
             // both families: eye normal or colour)
@@ -773,43 +824,42 @@ pixel_kernel(RastBatch B, Work w, const float* __restrict__ grad_canvas, const f
       const Seg sf = segment(frow, frow >= 0);
       float* facc = w.facc + (frow >= 0 ? frow : 0) * 12;
       const int nf = grad_zbuffer ? 12 : 9;  // dL/dz_clip only with a depth gradient
+      if (grad_zbuffer)
+        seg_sums<12>(fval, sf);
+      else
+        seg_sums<9>(fval, sf);
+      seg_sums<9>(vval, sf);
+      if (sf.tail) {
 #pragma unroll
-      for (int k = 0; k < 12; ++k) {
-        if (k >= nf) break;
-        const float v = seg_sum(fval[k], sf);
-        if (sf.tail && v != 0.0f) atomicAdd(facc + k, v);
-      }
+        for (int k = 0; k < 12; ++k)
+          if (k < nf && fval[k] != 0.0f) atomicAdd(facc + k, fval[k]);
 #pragma unroll
-      for (int k = 0; k < 9; ++k) {
-        const float v = seg_sum(vval[k], sf);
-        if (sf.tail && v != 0.0f) atomicAdd(w.vacc + vrows[k / 3] * w.vacc_stride + (k % 3), v);
+        for (int k = 0; k < 9; ++k)
+          if (vval[k] != 0.0f) atomicAdd(w.vacc + vrows[k / 3] * w.vacc_stride + (k % 3), vval[k]);
       }
       if (kDarboux && w.vacc_stride > 3) {
+        seg_sums<9>(tval, sf);
+        if (sf.tail) {
 #pragma unroll
-        for (int k = 0; k < 9; ++k) {
-          const float v = seg_sum(tval[k], sf);
-          if (sf.tail && v != 0.0f) atomicAdd(w.vacc + vrows[0] * w.vacc_stride + 3 + k, v);
+          for (int k = 0; k < 9; ++k)
+            if (tval[k] != 0.0f) atomicAdd(w.vacc + vrows[0] * w.vacc_stride + 3 + k, tval[k]);
         }
       }
     }
     if (kDarboux && G.normal_map) {
       const Seg sn = segment(tg.nb, tg.nb >= 0);
-      float g3[3];
-#pragma unroll
-      for (int q = 0; q < 3; ++q) g3[q] = seg_sum(tg.gn[q], sn);
-      if (sn.tail) add_texel_grad(G.normal_map, tg.nb, 3, g3);
+      seg_sums<3>(tg.gn, sn);
+      if (sn.tail) add_texel_grad(G.normal_map, tg.nb, 3, tg.gn);
     }
     if (G.texture) {
       const Seg st = segment(tg.tb, tg.tb >= 0);
-      float g3[3];
-#pragma unroll
-      for (int q = 0; q < 3; ++q) g3[q] = seg_sum(tg.gt[q], st);
-      if (st.tail) add_texel_grad(G.texture, tg.tb, tg.ch, g3);
+      seg_sums<3>(tg.gt, st);
+      if (st.tail) add_texel_grad(G.texture, tg.tb, tg.ch, tg.gt);
     }
     if (G.specular_map) {
       const Seg ss = segment(tg.sidx, tg.sidx >= 0);
-      const float v = seg_sum(tg.gs, ss);
-      if (ss.tail && v != 0.0f) atomicAdd(G.specular_map + tg.sidx, v);
+      seg_sums<1>(&tg.gs, ss);
+      if (ss.tail && tg.gs != 0.0f) atomicAdd(G.specular_map + tg.sidx, tg.gs);
     }
   }
   // over: the background is seen through what the kept slots let pass
@@ -817,7 +867,8 @@ pixel_kernel(RastBatch B, Work w, const float* __restrict__ grad_canvas, const f
 #pragma unroll
     for (int q = 0; q < 3; ++q) pg.v[RAST_GRAD_BACKGROUND + q] += gcv_px[q] * transmit;
   }
-  reduce_params<pixel_bits(SH)>(pg, G.job_params, in_job && (over ? shown : P.prim_id[pix] >= 0), blockIdx.y);
+  reduce_params<pixel_bits(SH)>(pg, G.job_params, in_job && (over ? shown : P.prim_id[pix] >= 0), blockIdx.y,
+                                LightPost{&sL, sh});
 }
 
 // dL/dM = -m^T (dL/dm) m^T for the [x, y, w] rows of the clip positions,
