@@ -174,24 +174,56 @@ struct NoPost {
 // skip their shuffles and add zeros.  `post` (when Post::kActive) maps the
 // block's totals, on one thread, before they are added: the linear maps
 // every pixel's contribution would go through are applied once per block.
-template <unsigned long long BITS, class Post = NoPost>
+// kTransposed (kernels that reduce once per thread and pixel): the span
+// [kLo, kLo + kSpan) of BITS, up to 32 parameters, is summed by a transpose
+// through shared memory (each lane stores its values, lane n adds parameter
+// kLo + n's 32 values) instead of one shuffle tree per parameter.  Rows of
+// 36 floats: the 128-bit row reads of 8 lanes hit distinct banks.
+template <unsigned long long BITS, bool kTransposed = false, class Post = NoPost>
 __device__ __forceinline__ void reduce_params(const ParamGrad& pg, float* job_params, bool active, int job,
                                               const Post& post = Post()) {
+  constexpr int kLo = BITS ? __builtin_ctzll(BITS) : 0;
+  constexpr int kSpan = BITS ? 64 - __builtin_clzll(BITS) - kLo : 0;
+  constexpr bool kTranspose = kTransposed && kSpan > 0 && kSpan <= 32;
   __shared__ float s_red[kThreads / 32][RAST_NPARAM];
+  __shared__ float4 s_col[kTranspose ? kThreads / 32 : 1][kTranspose ? kSpan : 1][9];
   __shared__ float s_tot[Post::kActive ? RAST_NPARAM : 1];
   if (BITS == 0ull || !job_params) return;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const bool warp_active = __any_sync(0xffffffffu, active);
-#pragma unroll
-  for (int k = 0; k < RAST_NPARAM; ++k) {
-    if (!((BITS >> k) & 1ull)) continue;
-    float v = 0.0f;
+  if (kTranspose) {
     if (warp_active) {
-      v = pg.v[k];
+      float* col = reinterpret_cast<float*>(s_col[warp]);
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+      for (int n = 0; n < kSpan; ++n) col[n * 36 + lane] = ((BITS >> (kLo + n)) & 1ull) ? pg.v[kLo + n] : 0.0f;
+      __syncwarp();
+      if (lane < kSpan) {
+        float a = 0.0f, b = 0.0f, c = 0.0f, d = 0.0f;
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          const float4 t = s_col[warp][lane][q];
+          a += t.x;
+          b += t.y;
+          c += t.z;
+          d += t.w;
+        }
+        s_red[warp][kLo + lane] = (a + b) + (c + d);
+      }
+    } else if (lane < kSpan) {
+      s_red[warp][kLo + lane] = 0.0f;
     }
-    if (lane == 0) s_red[warp][k] = v;
+  } else {
+#pragma unroll
+    for (int k = 0; k < RAST_NPARAM; ++k) {
+      if (!((BITS >> k) & 1ull)) continue;
+      float v = 0.0f;
+      if (warp_active) {
+        v = pg.v[k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+      }
+      if (lane == 0) s_red[warp][k] = v;
+    }
   }
   __syncthreads();
   const bool mine = threadIdx.x < RAST_NPARAM && ((BITS >> threadIdx.x) & 1ull);
@@ -867,8 +899,10 @@ pixel_kernel(RastBatch B, Work w, const float* __restrict__ grad_canvas, const f
 #pragma unroll
     for (int q = 0; q < 3; ++q) pg.v[RAST_GRAD_BACKGROUND + q] += gcv_px[q] * transmit;
   }
-  reduce_params<pixel_bits(SH)>(pg, G.job_params, in_job && (over ? shown : P.prim_id[pix] >= 0), blockIdx.y,
-                                LightPost{&sL, sh});
+  // the background has a gradient only in layered batches
+  constexpr unsigned long long kBits = pixel_bits(SH) & (kLayers ? ~0ull : ~range_bits(RAST_GRAD_BACKGROUND, 3));
+  reduce_params<kBits, true>(pg, G.job_params, in_job && (over ? shown : P.prim_id[pix] >= 0), blockIdx.y,
+                             LightPost{&sL, sh});
 }
 
 // dL/dM = -m^T (dL/dm) m^T for the [x, y, w] rows of the clip positions,
