@@ -369,7 +369,7 @@ __global__ void __launch_bounds__(kThreads) face_prep_kernel(RastBatch B, Work w
   for (int t = threadIdx.x; t < n; t += kThreads) face_prep(B, w, J, blk.y + s_q[t]);
 }
 
-__global__ void __launch_bounds__(kThreads) vertex_prep_kernel(RastBatch B, Work w) {
+__global__ void __launch_bounds__(kThreads, 3) vertex_prep_kernel(RastBatch B, Work w) {
   __shared__ RastJob sJ;
   __shared__ int s_q[kRows];
   __shared__ int s_n;
