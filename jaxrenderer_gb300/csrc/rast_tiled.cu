@@ -345,8 +345,14 @@ constexpr int kRecordOnly = static_cast<int>(0x80000000u);  // queued for its re
 constexpr int kSmallArea = 32;                               // largest small rectangle: one pixel per lane
 constexpr int kTableMax = 1024;                              // pixel -> NDC tables kept in shared memory
 
+// Six blocks per SM without the small path (40 registers): the kernel is
+// latency-bound, and more resident warps beat the spills (0.83 / 0.90 ms ->
+// 0.73 / 0.76 ms per pass on the 4096-scene brax-like batch; 5 and 8
+// blocks measured slower).  The small path's shared arrays allow fewer.
+__host__ __device__ constexpr int setup_min_blocks(bool small) { return small ? 0 : 6; }
+
 template <bool kSmall>
-__global__ void __launch_bounds__(kSetupThreads)
+__global__ void __launch_bounds__(kSetupThreads, setup_min_blocks(kSmall))
 setup_bin_kernel(RastBatch B, Geometry G, const int2* __restrict__ fmap, float4* __restrict__ setup,
                  ushort4* __restrict__ bbox, uint32_t* __restrict__ counts, unsigned long long* __restrict__ keys,
                  int small_area) {
@@ -611,8 +617,18 @@ __device__ __forceinline__ bool edge_misses_tile(float ea, float eb, float ec, f
 // every primitive of the job instead.  Each pixel keeps its kL smallest
 // keys (kL = 1: the default chooser; kL = RAST_MAX_LAYERS for batches with
 // layered jobs), slot s written to winner[s * total_pixels + pixel].
+// Ten blocks per SM (48 registers) for the shapes of at most 128 pixels
+// with the default chooser: more resident warps beat the few spills
+// (16x8: 1.02 -> 0.88 ms, 8x8: 1.03 -> 1.01 ms on the 4096-scene
+// brax-like batch; 12 and 16 blocks measured slower).  The others keep the
+// compiler's choice (0: no minimum).
+template <int TW, int TH, int kL>
+__host__ __device__ constexpr int raster_min_blocks() {
+  return (kL == 1 && TW * TH <= 128) ? 10 : 0;
+}
+
 template <int TW, int TH, bool kKeys, bool kTies, int kL>
-__global__ void __launch_bounds__(32 * kRasterWarps)
+__global__ void __launch_bounds__(32 * kRasterWarps, raster_min_blocks<TW, TH, kL>())
 raster_kernel(RastBatch B, Geometry G, const float4* __restrict__ setup,
               const uint32_t* __restrict__ counts, const uint32_t* __restrict__ offsets,
               const int32_t* __restrict__ bins, int32_t* __restrict__ winner,
@@ -854,8 +870,12 @@ face_varyings_kernel(RastBatch B, const int2* __restrict__ vmap, const unsigned 
 // their "over" pixels spread the warp's fragments over its lanes
 // (resolve_over_warp).
 // Grid: (ceil(max pixels per job / 256), n_jobs).
+// Eight blocks per SM (32 registers) for the default chooser: more resident
+// warps hide the gathers and division chains better than the spills cost
+// (1.17 -> 0.95 ms on the 4096-scene brax-like batch; 4, 5 and 6 blocks
+// measured slower).  Layered batches keep three (80 registers).
 template <bool kLayered>
-__global__ void __launch_bounds__(256, kLayered ? 3 : 4)  // 64 registers (85 layered)
+__global__ void __launch_bounds__(256, kLayered ? 3 : 8)
 tiled_shade_kernel(RastBatch B, const float4* __restrict__ setup, const int32_t* __restrict__ winner,
                    bool depth_resolved, const float* __restrict__ fvar, int vstride) {
   __shared__ RastJob sJ;
@@ -990,12 +1010,19 @@ static bool valid_layered_shape(TileShape t) {
 }
 
 template <bool kKeys, bool kTies, int kL>
-static void launch_raster(TileShape ts, unsigned grid, cudaStream_t s, const RastBatch& b, const Layout& L,
+// The raster kernel is persistent: one resident wave of blocks (SMs x the
+// blocks of this instance that fit on an SM) takes the tiles.
+static void launch_raster(TileShape ts, int sms, cudaStream_t s, const RastBatch& b, const Layout& L,
                           const float4* setup, const uint32_t* counts, const uint32_t* offsets, const int32_t* bins,
                           int32_t* winner, unsigned int* misc, unsigned char* vis,
                           const unsigned long long* keys) {
   const unsigned block = 32 * kRasterWarps;
   auto go = [&](auto kernel) {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, static_cast<int>(block), 0) != cudaSuccess ||
+        per_sm <= 0)
+      per_sm = 8;
+    const unsigned grid = static_cast<unsigned>(std::max(sms, 1) * per_sm);
     kernel<<<grid, block, 0, s>>>(b, L.G, setup, counts, offsets, bins, winner, misc, L.n_tiles, vis, keys);
   };
   if (ts.tw == 8 && ts.th == 8)
@@ -1083,21 +1110,20 @@ static int render(const RastBatch* batch, const RastTiledConfig* cfg, void* work
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (b.total_setup > 0) {
-      const unsigned grid = static_cast<unsigned>(std::max(sms, 1) * 8);
       // the key path exists only when ties are not counted and no job is
       // layered
       if (keys)
-        launch_raster<true, false, 1>(ts, grid, s, b, L, setup, counts, offsets, bins, winner, misc, vis, keys);
+        launch_raster<true, false, 1>(ts, sms, s, b, L, setup, counts, offsets, bins, winner, misc, vis, keys);
       else if (b.max_layers > 0 && b.near_ties)
-        launch_raster<false, true, RAST_MAX_LAYERS>(ts, grid, s, b, L, setup, counts, offsets, bins, winner, misc,
+        launch_raster<false, true, RAST_MAX_LAYERS>(ts, sms, s, b, L, setup, counts, offsets, bins, winner, misc,
                                                     vis, nullptr);
       else if (b.max_layers > 0)
-        launch_raster<false, false, RAST_MAX_LAYERS>(ts, grid, s, b, L, setup, counts, offsets, bins, winner, misc,
+        launch_raster<false, false, RAST_MAX_LAYERS>(ts, sms, s, b, L, setup, counts, offsets, bins, winner, misc,
                                                      vis, nullptr);
       else if (b.near_ties)
-        launch_raster<false, true, 1>(ts, grid, s, b, L, setup, counts, offsets, bins, winner, misc, vis, nullptr);
+        launch_raster<false, true, 1>(ts, sms, s, b, L, setup, counts, offsets, bins, winner, misc, vis, nullptr);
       else
-        launch_raster<false, false, 1>(ts, grid, s, b, L, setup, counts, offsets, bins, winner, misc, vis, nullptr);
+        launch_raster<false, false, 1>(ts, sms, s, b, L, setup, counts, offsets, bins, winner, misc, vis, nullptr);
     } else {
       if (cudaMemsetAsync(winner, 0xff, static_cast<size_t>(b.total_pixels) * 4 * L.winner_layers, s) != cudaSuccess)
         return RAST_ERR_CUDA;
