@@ -870,29 +870,29 @@ def kernel_bytes(kname, info, visible):
 # DRAM bytes per unit of work of the forward kernels measured by ncu
 # (dram__bytes_read.sum + dram__bytes_write.sum) on the 256-scene brax-like
 # case (profiles/ncu_forward_tiled_brax84x256.md: 1,470,504 faces per pass,
-# 1,806,336 main-pass pixels): setup_bin 119.6 MB, scatter 12.4 MB,
-# face_varyings 43.6 MB per pass, tiled_shade 70.8 MB.  Their traffic grows
-# with the faces (F) or pixels (P) processed, so a full launch's is this
-# times its units.  The raster kernel's depends on the tile shape the
-# autotuner picks for a batch size and is not scaled.
+# 1,806,336 main-pass pixels): setup_bin 136.6 MB per pass, scatter 12.4 MB,
+# face_varyings 44.1 MB, tiled_shade 108.4 MB.  Their traffic grows with the
+# faces (F) or pixels (P) processed, so a full launch's is this times its
+# units.  The raster kernel's depends on the tile shape the autotuner picks
+# for a batch size and is not scaled.
 NCU_BYTES_PER_UNIT = {
-    "setup_bin_kernel": ("F", 81.3),
+    "setup_bin_kernel": ("F", 92.9),
     "scatter_kernel": ("F", 8.4),
-    "face_varyings_kernel": ("F", 29.6),
-    "tiled_shade_kernel": ("P", 39.2),
+    "face_varyings_kernel": ("F", 30.0),
+    "tiled_shade_kernel": ("P", 60.0),
 }
 
 # Warp instructions executed per unit of work (ncu smsp__inst_executed.sum,
-# same capture): setup_bin 70.9 M for both passes' faces, scatter 18.5 M,
-# face_varyings 12.2 M for the main pass's 735,252 faces, tiled_shade 52.4 M.
-# These kernels are bound by instruction issue, not DRAM: achieved warp
+# same capture, per launch): setup_bin 34.4 / 39.0 M (shadow / main pass),
+# scatter 6.3 / 12.2 M, face_varyings 6.8 M, tiled_shade 56.4 M.  These
+# kernels are bound by instruction issue and latency, not DRAM: achieved warp
 # instructions per second over the SMs' issue rate (4 schedulers per SM, one
 # warp instruction per clock each) is the ceiling they approach.
 NCU_WARP_INSTR_PER_UNIT = {
-    "setup_bin_kernel": ("F", 48.2),
-    "scatter_kernel": ("F", 12.6),
-    "face_varyings_kernel": ("F", 16.6),
-    "tiled_shade_kernel": ("P", 29.0),
+    "setup_bin_kernel": ("F", 25.0),
+    "scatter_kernel": ("F", 6.3),
+    "face_varyings_kernel": ("F", 4.6),
+    "tiled_shade_kernel": ("P", 31.2),
 }
 
 
