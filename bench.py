@@ -896,24 +896,47 @@ NCU_WARP_INSTR_PER_UNIT = {
 }
 
 
-def issue_roofline(kname, info, ms, clocks):
+# The raster kernel's DRAM bytes and warp instructions per launch, measured by
+# ncu on the full 4096-scene brax-like batch (one-pass metrics, the launches of
+# its first render; profiles/ncu_raster_brax84x4096.md), keyed by (tile width,
+# tile height, pixels of the pass): its traffic depends on the tile shape and
+# the scenes, so it applies to that workload's launches only.
+NCU_RASTER_LAUNCH = {
+    (16, 8, 67108864): (193032704 + 230909440, 887395880),  # shadow pass, 4096 x 128x128
+    (8, 8, 28901376): (767270400 + 121109504, 1036404822),  # main pass, 4096 x 84x84
+}
+
+
+def raster_launch_counts(cfg, info):
+    """(DRAM bytes, warp instructions) of a raster launch measured on this
+    very configuration, or None."""
+    if cfg is None:
+        return None
+    return NCU_RASTER_LAUNCH.get((int(cfg.tile_w), int(cfg.tile_h), int(round(info["P"]))))
+
+
+def issue_roofline(kname, info, ms, clocks, warp_instr=None, source=None):
     """Issue-slot ceiling of a launch of `kname`: ncu's warp instructions per
-    unit times the launch's units, per second of the live launch time, over
-    SMs x 4 schedulers x the median SM clock sampled during the run."""
+    unit times the launch's units (or `warp_instr` measured for this very
+    launch), per second of the live launch time, over SMs x 4 schedulers x the
+    median SM clock sampled during the run."""
     import torch
 
-    if kname not in NCU_WARP_INSTR_PER_UNIT or ms <= 0:
+    if (warp_instr is None and kname not in NCU_WARP_INSTR_PER_UNIT) or ms <= 0:
         return None
     mhz = (clocks or {}).get("sm_mhz") or (clocks or {}).get("sm_max_mhz")
     if not mhz:
         return None
-    unit, per = NCU_WARP_INSTR_PER_UNIT[kname]
+    if warp_instr is None:
+        unit, per = NCU_WARP_INSTR_PER_UNIT[kname]
+        warp_instr = per * info[unit]
+        source = (f"ncu warp instructions per {'face' if unit == 'F' else 'pixel'} on the 256-scene "
+                  f"brax-like case x this launch's units")
     sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
     peak = sms * 4 * float(mhz) * 1e6
-    achieved = per * info[unit] / (ms / 1e3)
+    achieved = warp_instr / (ms / 1e3)
     return {"achieved": achieved, "peak": peak, "unit": "warp instructions/s", "frac": achieved / peak,
-            "note": f"ncu warp instructions per {'face' if unit == 'F' else 'pixel'} on the 256-scene "
-                    f"brax-like case x this launch's units; peak {sms} SMs x 4 schedulers x {float(mhz):.0f} MHz"}
+            "note": f"{source}; peak {sms} SMs x 4 schedulers x {float(mhz):.0f} MHz"}
 
 
 def roofline(prof, visible, clocks=None):
@@ -952,7 +975,11 @@ def roofline(prof, visible, clocks=None):
     r_dom, p_dom, k_dom = prof["where"][dom]
     cfg = r_dom.configs.get(p_dom)
     small = cfg is not None and int(cfg.small_area) > 0
-    if k_dom in NCU_BYTES_PER_UNIT and not small and info["slots"] == 1:
+    measured = raster_launch_counts(cfg, info) if k_dom == "raster_kernel" and info["slots"] == 1 else None
+    if measured is not None:
+        traffic = float(measured[0])
+        traffic_note = "ncu DRAM bytes of this launch on this workload at full size (one-pass metrics)"
+    elif k_dom in NCU_BYTES_PER_UNIT and not small and info["slots"] == 1:
         unit, per = NCU_BYTES_PER_UNIT[k_dom]
         traffic = per * info[unit]
         traffic_note = (f"ncu DRAM bytes per {'face' if unit == 'F' else 'pixel'} of this kernel on the 256-scene "
@@ -972,7 +999,10 @@ def roofline(prof, visible, clocks=None):
         "avg_launch_ms": ms,
         "per_kernel": per_kernel,
     }
-    if not small and info["slots"] == 1:
+    if measured is not None:
+        out["issue"] = issue_roofline(k_dom, info, ms, clocks, warp_instr=float(measured[1]),
+                                      source="ncu warp instructions of this launch on this workload at full size")
+    elif not small and info["slots"] == 1:
         issue = issue_roofline(k_dom, info, ms, clocks)
         if issue is not None:
             out["issue"] = issue
