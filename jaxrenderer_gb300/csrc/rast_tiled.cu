@@ -620,11 +620,12 @@ __device__ __forceinline__ bool edge_misses_tile(float ea, float eb, float ec, f
 // Ten blocks per SM (48 registers) for the shapes of at most 128 pixels
 // with the default chooser: more resident warps beat the few spills
 // (16x8: 1.02 -> 0.88 ms, 8x8: 1.03 -> 1.01 ms on the 4096-scene
-// brax-like batch; 12 and 16 blocks measured slower).  The others keep the
-// compiler's choice (0: no minimum).
+// brax-like batch; 12 and 16 blocks measured slower).  The layered
+// variants of at most 64 pixels take eight (64 registers: 1.32 -> 1.18 ms
+// with 4 layers).  The others keep the compiler's choice (0: no minimum).
 template <int TW, int TH, int kL>
 __host__ __device__ constexpr int raster_min_blocks() {
-  return (kL == 1 && TW * TH <= 128) ? 10 : 0;
+  return (kL == 1 && TW * TH <= 128) ? 10 : (TW * TH <= 64 ? 8 : 0);
 }
 
 template <int TW, int TH, bool kKeys, bool kTies, int kL>
@@ -873,9 +874,10 @@ face_varyings_kernel(RastBatch B, const int2* __restrict__ vmap, const unsigned 
 // Eight blocks per SM (32 registers) for the default chooser: more resident
 // warps hide the gathers and division chains better than the spills cost
 // (1.17 -> 0.95 ms on the 4096-scene brax-like batch; 4, 5 and 6 blocks
-// measured slower).  Layered batches keep three (80 registers).
+// measured slower).  Layered batches take four (64 registers: 2.63 -> 2.56
+// ms on the 4096-scene batch with 4 layers, from three).
 template <bool kLayered>
-__global__ void __launch_bounds__(256, kLayered ? 3 : 8)
+__global__ void __launch_bounds__(256, kLayered ? 4 : 8)
 tiled_shade_kernel(RastBatch B, const float4* __restrict__ setup, const int32_t* __restrict__ winner,
                    bool depth_resolved, const float* __restrict__ fvar, int vstride) {
   __shared__ RastJob sJ;
