@@ -25,7 +25,7 @@
 namespace rast {
 namespace tiled {
 
-constexpr int kSetupThreads = 256;
+constexpr int kSetupThreads = 128;    // faces per setup/scatter block (256: 1 % slower, 64: 7 %)
 constexpr int kScanBlock = 1024;       // elements per scan block (256 threads x 4)
 constexpr int kRasterWarps = 4;        // warps per CTA of the raster kernel
 constexpr int kTileChunk = 1;          // tiles a raster warp takes per atomic
@@ -345,11 +345,12 @@ constexpr int kRecordOnly = static_cast<int>(0x80000000u);  // queued for its re
 constexpr int kSmallArea = 32;                               // largest small rectangle: one pixel per lane
 constexpr int kTableMax = 1024;                              // pixel -> NDC tables kept in shared memory
 
-// Six blocks per SM without the small path (40 registers): the kernel is
-// latency-bound, and more resident warps beat the spills (0.83 / 0.90 ms ->
-// 0.73 / 0.76 ms per pass on the 4096-scene brax-like batch; 5 and 8
-// blocks measured slower).  The small path's shared arrays allow fewer.
-__host__ __device__ constexpr int setup_min_blocks(bool small) { return small ? 0 : 6; }
+// 1,536 resident threads per SM without the small path (40 registers): the
+// kernel is latency-bound, and more resident warps beat the spills (0.83 /
+// 0.90 ms -> 0.73 / 0.76 ms per pass on the 4096-scene brax-like batch at 6
+// blocks of 256; 1,280 and 2,048 threads measured slower; 12 blocks of 128,
+// 0.71 / 0.74 ms).  The small path's shared arrays allow fewer.
+__host__ __device__ constexpr int setup_min_blocks(bool small) { return small ? 0 : 1536 / kSetupThreads; }
 
 template <bool kSmall>
 __global__ void __launch_bounds__(kSetupThreads, setup_min_blocks(kSmall))
@@ -829,7 +830,7 @@ raster_kernel(RastBatch B, Geometry G, const float4* __restrict__ setup,
 // in shared memory, then one thread per (visible face, corner) runs the
 // vertex shader, so faces nobody sees leave no idle lanes and the block's
 // job load and queue are paid once per kVaryRows faces.
-constexpr int kFaceThreads = kSetupThreads;
+constexpr int kFaceThreads = 256;
 constexpr int kVaryRowsPerThread = 16;
 constexpr int kVaryRows = kFaceThreads * kVaryRowsPerThread;
 
