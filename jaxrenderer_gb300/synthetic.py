@@ -13,7 +13,7 @@ from typing import List, Optional, Sequence, Tuple
 
 import numpy as np
 
-from .geometry import Camera, normalise, transform_matrix_from_rotation
+from .geometry import Camera, transform_matrix_from_rotation
 from .model import Model, ModelObject
 from .shapes.cube import create_cube
 

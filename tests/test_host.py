@@ -4,7 +4,6 @@ import pytest
 
 import jaxrenderer_gb300 as jr
 from jaxrenderer_gb300 import synthetic
-from jaxrenderer_gb300.geometry import Camera
 from jaxrenderer_gb300.renderer import Renderer, gather_rows
 from jaxrenderer_gb300.utils import transpose_for_display
 

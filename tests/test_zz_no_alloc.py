@@ -13,7 +13,6 @@ collects last.
 """
 import ctypes
 
-import numpy as np
 import pytest
 import torch
 
