@@ -229,7 +229,8 @@ typedef struct RastTiledConfig {
   int32_t reserved;
 } RastTiledConfig;
 
-/* Workspace bytes rast_render_tiled needs for `batch` under `cfg` (NULL = defaults). */
+/* Workspace bytes rast_render_tiled needs for `batch` under `cfg` (NULL = defaults);
+ * 0 for a tile shape rast_render_tiled refuses. */
 size_t rast_tiled_workspace_bytes(const RastBatch* batch, const RastTiledConfig* cfg);
 
 /* Tiled form for many scenes per call.  Per face: clip positions, set-up and
@@ -261,7 +262,12 @@ int rast_render_tiled_profiled(const RastBatch* batch, const RastTiledConfig* cf
  *
  *  - The first call on a device looks up the array's device address
  *    (cudaGetSymbolAddress, with that device current) and caches it; make
- *    that first call before any stream capture on that device.
+ *    that first call before any stream capture on that device.  The cache
+ *    is tagged with the CUDA context's id: after a cudaDeviceReset the next
+ *    call looks the address up again (and is then again a first call).
+ *  - A tile shape without a kernel is refused (RAST_ERR_INVALID_ARGUMENT,
+ *    or RAST_ERR_UNSUPPORTED for a layered batch) before any size
+ *    arithmetic.
  *  - Batches whose tiled workspace (rast_tiled_workspace_bytes) exceeds
  *    RAST_STATIC_SCRATCH_BYTES are rejected with
  *    RAST_ERR_STATIC_SCRATCH_TOO_SMALL; nothing is launched.

@@ -15,6 +15,7 @@
 //                      shared memory, per-pixel packed (depth | id) minimum
 //   tiled_shade_kernel one thread per pixel: deferred shading of the winner,
 //                      vertex varyings recomputed for its three corners only
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -1012,6 +1013,15 @@ static bool valid_layered_shape(TileShape t) {
          (t.tw == 4 && t.th == 8);
 }
 
+// RAST_OK, or the status rast_render_tiled returns for a tile shape it has
+// no kernel for.  Checked before any layout arithmetic (which divides by the
+// tile's sides).
+static int check_shape(const RastBatch& b, TileShape t) {
+  if (!valid_shape(t)) return RAST_ERR_INVALID_ARGUMENT;
+  if (b.max_layers > 0 && !valid_layered_shape(t)) return RAST_ERR_UNSUPPORTED;
+  return RAST_OK;
+}
+
 template <bool kKeys, bool kTies, int kL>
 // The raster kernel is persistent: one resident wave of blocks (SMs x the
 // blocks of this instance that fit on an SM) takes the tiles.
@@ -1052,8 +1062,8 @@ static int render(const RastBatch* batch, const RastTiledConfig* cfg, void* work
   if (st != RAST_OK) return st;
   const RastBatch& b = *batch;
   TileShape ts{cfg ? cfg->tile_w : 8, cfg ? cfg->tile_h : 8};
-  if (!valid_shape(ts)) return RAST_ERR_INVALID_ARGUMENT;
-  if (b.max_layers > 0 && !valid_layered_shape(ts)) return RAST_ERR_UNSUPPORTED;
+  st = check_shape(b, ts);
+  if (st != RAST_OK) return st;
   const uint64_t cap = cfg && cfg->bin_capacity > 0 ? cfg->bin_capacity : default_bin_capacity(b);
   const int small_area = small_area_of(cfg);
   const Layout L = layout(b, ts, cap, small_area);
@@ -1165,6 +1175,7 @@ using namespace rast;
 extern "C" size_t rast_tiled_workspace_bytes(const RastBatch* batch, const RastTiledConfig* cfg) {
   if (!batch) return 0;
   tiled::TileShape ts{cfg ? cfg->tile_w : 8, cfg ? cfg->tile_h : 8};
+  if (tiled::check_shape(*batch, ts) != RAST_OK) return 0;
   const uint64_t cap = cfg && cfg->bin_capacity > 0 ? cfg->bin_capacity : tiled::default_bin_capacity(*batch);
   return tiled::layout(*batch, ts, cap, tiled::small_area_of(cfg)).total;
 }
@@ -1173,6 +1184,8 @@ extern "C" int rast_tiled_stats(const RastBatch* batch, const RastTiledConfig* c
                                 void* stream, RastTiledStats* out) {
   if (!batch || !workspace || !out) return RAST_ERR_INVALID_ARGUMENT;
   tiled::TileShape ts{cfg ? cfg->tile_w : 8, cfg ? cfg->tile_h : 8};
+  const int shape_status = tiled::check_shape(*batch, ts);
+  if (shape_status != RAST_OK) return shape_status;
   const uint64_t cap = cfg && cfg->bin_capacity > 0 ? cfg->bin_capacity : tiled::default_bin_capacity(*batch);
   const tiled::Layout L = tiled::layout(*batch, ts, cap, tiled::small_area_of(cfg));
   unsigned int misc[4] = {0, 0, 0, 0};
@@ -1209,21 +1222,67 @@ static __device__ __align__(256) unsigned char g_static_scratch[RAST_STATIC_SCRA
 
 constexpr int kMaxDevices = 64;
 std::mutex g_static_mutex;
-void* g_static_ptr[kMaxDevices] = {};
+
+// Cached device address of g_static_scratch per device, tagged with the id
+// of the CUDA context it was looked up in.  A cudaDeviceReset (or a primary
+// context reset) loads the module again at a new address in a new context;
+// the new context id then triggers a fresh lookup.
+struct StaticSlot {
+  unsigned long long ctx_id;
+  void* ptr;
+};
+StaticSlot g_static_slot[kMaxDevices] = {};
+
+// cuCtxGetCurrent / cuCtxGetId, resolved through the runtime so the library
+// needs no link against the driver library.  Null when the driver lacks
+// them: the cache is then keyed by device ordinal alone.
+using CtxGetCurrentFn = CUresult (*)(CUcontext*);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long*);
+CtxGetCurrentFn g_ctx_get_current = nullptr;
+CtxGetIdFn g_ctx_get_id = nullptr;
+bool g_ctx_fns_resolved = false;
+
+// Id of the current context (0 when it cannot be read).  Caller holds the mutex.
+unsigned long long current_ctx_id() {
+  if (!g_ctx_fns_resolved) {
+    g_ctx_fns_resolved = true;
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      g_ctx_get_current = reinterpret_cast<CtxGetCurrentFn>(f);
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      g_ctx_get_id = reinterpret_cast<CtxGetIdFn>(f);
+    (void)cudaGetLastError();
+  }
+  if (!g_ctx_get_current || !g_ctx_get_id) return 0;
+  CUcontext ctx = nullptr;
+  unsigned long long id = 0;
+  if (g_ctx_get_current(&ctx) != CUDA_SUCCESS || ctx == nullptr) return 0;
+  if (g_ctx_get_id(ctx, &id) != CUDA_SUCCESS) return 0;
+  return id;
+}
 
 // Device address of g_static_scratch on the current device (host code sees
-// only a host-side stand-in for the symbol).  Looked up once per device.
+// only a host-side stand-in for the symbol).  Looked up once per device and
+// context, with that device current.
 int static_scratch(void** out) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return RAST_ERR_CUDA;
   if (dev < 0 || dev >= kMaxDevices) return RAST_ERR_UNSUPPORTED;
   std::lock_guard<std::mutex> lock(g_static_mutex);
-  if (!g_static_ptr[dev]) {
+  StaticSlot& slot = g_static_slot[dev];
+  const unsigned long long id = current_ctx_id();
+  if (!slot.ptr || (id != 0 && id != slot.ctx_id)) {
     void* p = nullptr;
     if (cudaGetSymbolAddress(&p, g_static_scratch) != cudaSuccess || !p) return RAST_ERR_CUDA;
-    g_static_ptr[dev] = p;
+    slot.ptr = p;
+    // the lookup made the device's context current if it was not yet
+    slot.ctx_id = id != 0 ? id : current_ctx_id();
   }
-  *out = g_static_ptr[dev];
+  *out = slot.ptr;
   return RAST_OK;
 }
 
@@ -1231,6 +1290,8 @@ int static_scratch(void** out) {
 
 extern "C" int rast_render_tiled_static(const RastBatch* batch, const RastTiledConfig* cfg, void* stream) {
   int st = check_batch(batch);
+  if (st != RAST_OK) return st;
+  st = tiled::check_shape(*batch, tiled::TileShape{cfg ? cfg->tile_w : 8, cfg ? cfg->tile_h : 8});
   if (st != RAST_OK) return st;
   const size_t need = rast_tiled_workspace_bytes(batch, cfg);
   if (need > RAST_STATIC_SCRATCH_BYTES) return RAST_ERR_STATIC_SCRATCH_TOO_SMALL;

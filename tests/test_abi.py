@@ -75,3 +75,23 @@ def test_struct_layout_matches_c(tmp_path, struct):
     assert c["size"] == ctypes.sizeof(cls)
     for n in names:
         assert c[n] == getattr(cls, n).offset, n
+
+
+def test_tile_shapes_without_a_kernel_are_refused_before_any_size_arithmetic(lib):
+    """Invalid RastTiledConfig shapes return a status (no division by a zero
+    tile side); every call here returns before touching the device."""
+    b = _lib.RastBatch()
+    b.jobs = 256  # never dereferenced: the shape check comes first
+    b.n_jobs, b.max_width, b.max_height = 1, 16, 16
+    stats = _lib.RastTiledStats()
+    fake_ws = ctypes.c_void_p(256)
+    for tw, th in ((0, 0), (0, 8), (8, 0), (-8, 8), (7, 8), (64, 64)):
+        cfg = _lib.RastTiledConfig(tw, th, 0)
+        assert lib.rast_tiled_workspace_bytes(ctypes.byref(b), ctypes.byref(cfg)) == 0
+        assert lib.rast_tiled_stats(ctypes.byref(b), ctypes.byref(cfg), fake_ws, None, ctypes.byref(stats)) == 1
+        assert lib.rast_render_tiled(ctypes.byref(b), ctypes.byref(cfg), fake_ws, 1 << 20, None) == 1
+        assert lib.rast_render_tiled_static(ctypes.byref(b), ctypes.byref(cfg), None) == 1
+    b.max_layers = 2  # layered batches have kernels for 8x8, 16x8, 8x4 and 4x8 only
+    cfg = _lib.RastTiledConfig(16, 16, 0)
+    assert lib.rast_tiled_workspace_bytes(ctypes.byref(b), ctypes.byref(cfg)) == 0
+    assert lib.rast_render_tiled_static(ctypes.byref(b), ctypes.byref(cfg), None) == 4

@@ -75,3 +75,14 @@ def test_static_scratch_rejects_batches_beyond_its_size(cuda_device):
     st = lib.rast_render_tiled_static(ctypes.byref(big), ctypes.byref(cfg), torch.cuda.current_stream(cuda_device).cuda_stream)
     assert st == 8
     assert lib.rast_error_string(st) == b"batch exceeds the static scratch of rast_render_tiled_static"
+
+
+def test_static_scratch_refuses_tile_shapes_without_a_kernel(cuda_device):
+    lib = _lib.load()
+    spec = scenes.random_job(_lib.SHADER_DEPTH, seed=951)
+    z0, _ = scenes.initial_buffers(spec)
+    packed = pack([spec], [z0], [None], cuda_device)
+    stream = torch.cuda.current_stream(cuda_device).cuda_stream
+    for shape in ((0, 0), (0, 8), (5, 8)):
+        cfg = _lib.RastTiledConfig(shape[0], shape[1], 0)
+        assert lib.rast_render_tiled_static(ctypes.byref(packed.batch), ctypes.byref(cfg), stream) == 1
