@@ -36,7 +36,7 @@ PARAM_COLUMNS = {
     "shadow_strength": (_lib.GRAD_SHADOW_STRENGTH, 3),
     "background": (_lib.GRAD_BACKGROUND, 3),
 }
-POOL_PARAMS = ("position", "normal", "texture", "specular_map", "normal_map")
+POOL_PARAMS = ("position", "normal", "colour", "texture", "specular_map", "normal_map")
 JOB_OFFSETS = {name: getattr(_lib.RastJob, name).offset // 4 for name in PARAM_COLUMNS}
 
 
@@ -174,8 +174,8 @@ class DifferentiableBatch:
     def render(self, **params: torch.Tensor):
         """Render with the given tensors in place of the batch's inputs.
 
-        Pool inputs: position, normal, texture, specular_map (flat pool
-        shapes).  Per-scene inputs, (N, ...): world_to_clip (N, 4, 4),
+        Pool inputs: position, normal, colour (gouraud), texture,
+        specular_map, normal_map (flat pool shapes).  Per-scene inputs, (N, ...): world_to_clip (N, 4, 4),
         world_to_eye_norm (N, 4, 4), light_direction, light_colour,
         light_dir_eye, ambient, diffuse, specular, shadow_strength (N, 3).
         Returns (canvas (N, W, H, 3), zbuffer (N, W, H))."""

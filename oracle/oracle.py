@@ -63,6 +63,8 @@ def _scene_struct(real):
             ("shadow_world_to_clip", R), ("shadow_viewport", R), ("shadow_strength", R3),
             ("zbuffer", R), ("canvas", R), ("prim_id", I), ("near_ties", c_longlong),
             ("layers", c_int), ("mixer", c_int), ("opacity", real), ("background", R3), ("face_alpha", R),
+            ("x_begin", c_int), ("x_end", c_int), ("y_begin", c_int), ("y_end", c_int), ("branch", I),
+            ("texel", I),
         ]
 
     return Scene
@@ -98,9 +100,13 @@ def _np(x, dtype):
     return np.ascontiguousarray(np.asarray(x), dtype=dtype)
 
 
-def render(spec, zbuffer, canvas=None, n_threads: int = 1, dtype=np.float32):
+def render(spec, zbuffer, canvas=None, n_threads: int = 1, dtype=np.float32, window=None,
+           want_branch: bool = False):
     """Render one job described by `spec` (attributes as jaxrenderer_gb300's
-    JobSpec) on the CPU.  Returns dict(zbuffer, canvas, prim_id, near_ties)."""
+    JobSpec) on the CPU.  Returns dict(zbuffer, canvas, prim_id, near_ties),
+    plus `branch` (the per-pixel branch signature) and `texel` (the diffuse
+    texel row sampled, -1 where none) with `want_branch` (rast_oracle.h).  `window` = (x0, x1, y0, y1) renders only those pixels;
+    the others keep their input values (prim_id -1, branch 0)."""
     double = np.dtype(dtype) == np.float64
     real = c_double if double else c_float
     Scene = SceneF64 if double else SceneF32
@@ -187,12 +193,27 @@ def render(spec, zbuffer, canvas=None, n_threads: int = 1, dtype=np.float32):
         s.canvas = c.ctypes.data_as(POINTER(real))
     pid = np.full((s.width, s.height), -1, dtype=np.int32)
     s.prim_id = pid.ctypes.data_as(POINTER(c_int))
+    if window is not None:
+        x0, x1, y0, y1 = (int(v) for v in window)
+        if x1 <= x0 or y1 <= y0:
+            raise ValueError(f"empty window {window}")
+        s.x_begin, s.x_end, s.y_begin, s.y_end = x0, x1, y0, y1
+    branch = texel = None
+    if want_branch:
+        branch = np.zeros((s.width, s.height), dtype=np.int32)
+        s.branch = branch.ctypes.data_as(POINTER(c_int))
+        texel = np.full((s.width, s.height), -1, dtype=np.int32)
+        s.texel = texel.ctypes.data_as(POINTER(c_int))
     st = lib.or_render_f64(ctypes.byref(s)) if double else lib.or_render_f32(ctypes.byref(s))
     if st != 0:
         raise RuntimeError(f"oracle render failed: {st}")
     if getattr(spec, "apply_depth_offset", False):
         z = (z + np.asarray(spec.depth_offset, dtype=dtype)).astype(dtype)
-    return {"zbuffer": z, "canvas": c, "prim_id": pid, "near_ties": int(s.near_ties)}
+    out = {"zbuffer": z, "canvas": c, "prim_id": pid, "near_ties": int(s.near_ties)}
+    if branch is not None:
+        out["branch"] = branch
+        out["texel"] = texel
+    return out
 
 
 def inv3(m) -> np.ndarray:

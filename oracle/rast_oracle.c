@@ -90,6 +90,9 @@ typedef struct Scene {
   real opacity;
   real background[3];
   const real* face_alpha;
+  int x_begin, x_end, y_begin, y_end;
+  int* branch;
+  int* texel;
 } Scene;
 
 /* ---------------------------------------------------------------- basics */
@@ -374,8 +377,31 @@ static inline real max0(real x) { return (x != x) ? x : (x > (real)0 ? x : (real
 
 /* Fragment shader of the chosen primitive.  Returns the shader's keep
  * (AND-ed later with the chooser's keep) and writes the colour. */
+/* Branch signature of a fragment (for gradient checks): the sampled texel
+ * (u, w) before clamping and the shader's branch bits, hashed into 32 bits.
+ * Within one primitive the colour is a smooth function of the inputs
+ * wherever this signature does not change. */
+static inline int branch_sig(int u, int w, int bits) {
+  uint32_t h = ((uint32_t)u * 65599u + (uint32_t)w) * 16u + (uint32_t)bits;
+  return (int)(h & 0x7fffffffu);
+}
+
+typedef struct FragProbe {
+  int branch; /* branch_sig of the fragment */
+  int texel;  /* element row (u * tex_h + w, clamped) of the diffuse texel sampled, or -1 */
+} FragProbe;
+
+static inline int texel_row(const Scene* s, int u, int w) {
+  return gather_clamp(u, s->tex_w) * s->tex_h + gather_clamp(w, s->tex_h);
+}
+
 static int fragment(const Scene* s, const VOut* v0, const VOut* v1, const VOut* v2, const real* b,
-                    int front, real* colour) {
+                    int front, real* colour, FragProbe* probe) {
+  FragProbe dummy;
+  if (!probe) probe = &dummy;
+  int* branch = &probe->branch;
+  *branch = 0;
+  probe->texel = -1;
   real var[NVAR];
   for (int k = 0; k < NVAR; ++k) var[k] = interp1(b, v0->var[k], v1->var[k], v2->var[k]);
   switch (s->shader) {
@@ -387,6 +413,7 @@ static int fragment(const Scene* s, const VOut* v0, const VOut* v1, const VOut* 
         colour[c] = var[V_COLOUR + c];
         ok = ok && (var[V_COLOUR + c] >= (real)0);
       }
+      *branch = branch_sig(0, 0, ok);
       return ok;
     }
     case OR_SHADER_GOURAUD_TEXTURE: { /* gouraud_texture.py:292-329 */
@@ -394,11 +421,13 @@ static int fragment(const Scene* s, const VOut* v0, const VOut* v1, const VOut* 
       int w = pymod(f2i(R_FLOOR(var[V_UVG + 1])), s->tex_h);
       real tc[3];
       tex3(s->texture, s->tex_w, s->tex_h, s->tex_c, u, w, tc);
+      probe->texel = texel_row(s, u, w);
       int ok = front;
       for (int c = 0; c < 3; ++c) {
         ok = ok && (var[V_COLOUR + c] >= (real)0);
         colour[c] = tc[c] * var[V_COLOUR + c];
       }
+      *branch = branch_sig(u, w, ok);
       return ok;
     }
     case OR_SHADER_PHONG: { /* phong.py:462-516 */
@@ -406,6 +435,7 @@ static int fragment(const Scene* s, const VOut* v0, const VOut* v1, const VOut* 
       int w = pymod(f2i(R_FLOOR(var[V_UV + 1])), s->tex_h);
       real tc[3], n[3], l[3], lc[3];
       tex3(s->texture, s->tex_w, s->tex_h, s->tex_c, u, w, tc);
+      probe->texel = texel_row(s, u, w);
       normalise3(var + V_NORMAL, n);
       normalise3(s->light_direction, l);
       real d = dot3(n, l);
@@ -415,6 +445,7 @@ static int fragment(const Scene* s, const VOut* v0, const VOut* v1, const VOut* 
         nonneg = nonneg && (lc[c] >= (real)0);
       }
       for (int c = 0; c < 3; ++c) colour[c] = nonneg ? tc[c] * lc[c] : (real)0;
+      *branch = branch_sig(u, w, nonneg);
       return front;
     }
     case OR_SHADER_PHONG_DARBOUX: { /* phong_darboux.py:212-293 */
@@ -451,6 +482,7 @@ static int fragment(const Scene* s, const VOut* v0, const VOut* v1, const VOut* 
       for (int r = 0; r < 3; ++r) bn[r] = dot3(B + 3 * r, nm);
       normalise3(bn, nn);
       tex3(s->texture, s->tex_w, s->tex_h, s->tex_c, u, w, tc);
+      probe->texel = texel_row(s, u, w);
       normalise3(s->light_direction, l);
       real d = dot3(nn, l);
       int nonneg = 1;
@@ -459,12 +491,14 @@ static int fragment(const Scene* s, const VOut* v0, const VOut* v1, const VOut* 
         nonneg = nonneg && (lc[c] >= (real)0);
       }
       for (int c = 0; c < 3; ++c) colour[c] = nonneg ? tc[c] * lc[c] : (real)0;
+      *branch = branch_sig(u, w, nonneg);
       return front;
     }
     case OR_SHADER_PHONG_REFLECTION:
     case OR_SHADER_PHONG_REFLECTION_SHADOW: {
       /* phong_reflection.py:158-235, phong_reflection_shadow.py:436-529 */
       int shadowed = s->shader == OR_SHADER_PHONG_REFLECTION_SHADOW;
+      int shadow_bit = 0;
       real shadow[3] = {(real)1, (real)1, (real)1};
       if (shadowed) {
         real sc[4];
@@ -481,6 +515,7 @@ static int fragment(const Scene* s, const VOut* v0, const VOut* v1, const VOut* 
         if (px >= 0 && px < s->shadow_w && py >= 0 && py < s->shadow_h)
           depth = s->shadow_map[(size_t)px * s->shadow_h + py];
         int lit = sc[2] <= depth;
+        shadow_bit = lit ? 4 : 0;
         for (int c = 0; c < 3; ++c) shadow[c] = lit ? (real)1 : (real)1 - s->shadow_strength[c];
       }
       /* MergedModel.uv_repeat (model.py:306-339) */
@@ -499,6 +534,7 @@ static int fragment(const Scene* s, const VOut* v0, const VOut* v1, const VOut* 
       int w = f2i(R_FLOOR(uvr[1]));
       real tc[3], n[3], l[3], r[3], rn[3];
       tex3(s->texture, s->tex_w, s->tex_h, s->tex_c, u, w, tc);
+      probe->texel = texel_row(s, u, w);
       normalise3(var + V_NORMAL, n);
       normalise3(s->light_dir_eye, l);
       real d = dot3(n, l);
@@ -514,6 +550,7 @@ static int fragment(const Scene* s, const VOut* v0, const VOut* v1, const VOut* 
                           : (k * s->light_colour[c]) * tc[c];
         colour[c] = a + b;
       }
+      *branch = branch_sig(u, w, (d > (real)0) | ((rn[2] > (real)0) << 1) | shadow_bit);
       return front;
     }
     default:
@@ -548,7 +585,7 @@ static int shade_prim(const Scene* s, const VOut* vo, const Prim* pr, int p, rea
   real b[3] = {c[0] / w_rcp, c[1] / w_rcp, c[2] / w_rcp};
   const int* face = s->faces + 3 * p;
   colour[0] = colour[1] = colour[2] = 0;
-  return fragment(s, vo + face[0], vo + face[1], vo + face[2], b, P->front, colour);
+  return fragment(s, vo + face[0], vo + face[1], vo + face[2], b, P->front, colour, NULL);
 }
 
 /* Layered chooser and its mixers: the compiled primitive_chooser / mix
@@ -647,13 +684,20 @@ static int render(Scene* s) {
 
   const real* vp = s->viewport;
   const int W = s->width, H = s->height, F = s->n_faces;
+  /* optional pixel window [x_begin, x_end) x [y_begin, y_end): pixels outside
+   * it are left untouched (an end of 0 means the whole axis) */
+  const int xb = s->x_end > 0 ? (s->x_begin > 0 ? s->x_begin : 0) : 0;
+  const int xe = s->x_end > 0 ? (s->x_end < W ? s->x_end : W) : W;
+  const int yb = s->y_end > 0 ? (s->y_begin > 0 ? s->y_begin : 0) : 0;
+  const int ye = s->y_end > 0 ? (s->y_end < H ? s->y_end : H) : H;
   long long ties = 0;
   int nt = s->n_threads > 0 ? s->n_threads : 1;
   (void)nt;
+  (void)W;
 #pragma omp parallel for schedule(dynamic, 1) reduction(+ : ties) num_threads(nt)
-  for (int i = 0; i < W; ++i) {
+  for (int i = xb; i < xe; ++i) {
     real x = ((real)i - vp[3]) / vp[0];
-    for (int j = 0; j < H; ++j) {
+    for (int j = yb; j < ye; ++j) {
       real y = ((real)j - vp[7]) / vp[5];
       if (s->layers > 0) {
         ties += layered_pixel(s, vo, pr, i, j, x, y);
@@ -703,7 +747,8 @@ static int render(Scene* s) {
       real b[3] = {c[0] / w_rcp, c[1] / w_rcp, c[2] / w_rcp};
       const int* face = s->faces + 3 * best;
       real colour[3] = {0, 0, 0};
-      int frag_keep = fragment(s, vo + face[0], vo + face[1], vo + face[2], b, P->front, colour);
+      FragProbe probe = {0, -1};
+      int frag_keep = fragment(s, vo + face[0], vo + face[1], vo + face[2], b, P->front, colour, &probe);
       /* mix (shader.py:374-396) + merge_buffers (pipeline.py:401-440) */
       int keep = chooser_keep && frag_keep;
       size_t pix = (size_t)i * H + j;
@@ -713,6 +758,8 @@ static int render(Scene* s) {
           for (int ch = 0; ch < 3; ++ch) s->canvas[pix * 3 + ch] = colour[ch];
       }
       if (s->prim_id) s->prim_id[pix] = keep ? best : -1;
+      if (s->branch) s->branch[pix] = probe.branch;
+      if (s->texel) s->texel[pix] = keep ? probe.texel : -1;
     }
   }
   s->near_ties = ties;

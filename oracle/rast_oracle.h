@@ -78,6 +78,15 @@ typedef struct OrSceneF32 {
   float opacity;                 /* over: every face's opacity (face_alpha NULL) */
   float background[3];           /* over: colour behind the last layer */
   const float* face_alpha;       /* over: (F) per-face opacity, or NULL */
+  /* gradient-check helpers (zero = off) */
+  int x_begin, x_end;            /* render only pixels x_begin <= i < x_end (x_end 0: all) */
+  int y_begin, y_end;            /* and y_begin <= j < y_end (y_end 0: all) */
+  int* branch;                   /* (W,H) out, optional: branch signature of the default
+                                    chooser's fragment (sampled texel + the shader's
+                                    branch bits, hashed); the colour is smooth in the
+                                    inputs wherever neither it nor prim_id changes */
+  int* texel;                    /* (W,H) out, optional: element row u * tex_h + w of the
+                                    diffuse texel the written fragment sampled, or -1 */
 } OrSceneF32;
 
 /* Render one scene; `scene` points at an OrSceneF32 (f32 build) or its

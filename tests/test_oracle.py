@@ -148,3 +148,26 @@ def test_column_band_equals_full_frame_columns():
         np.testing.assert_array_equal(b["prim_id"], full["prim_id"][i0 : i0 + w])
         np.testing.assert_array_equal(b["zbuffer"].view(np.uint32), full["zbuffer"][i0 : i0 + w].view(np.uint32))
         np.testing.assert_array_equal(b["canvas"], full["canvas"][i0 : i0 + w])
+
+
+def test_windowed_render_equals_the_full_render_inside_the_window():
+    """The pixel window and the branch / texel probes used by the gradient
+    checks (tests/fdgrad.py) change nothing inside the window."""
+    from tests.scenes import random_job
+
+    for shader in (_lib.SHADER_PHONG, _lib.SHADER_GOURAUD_TEXTURE, _lib.SHADER_PHONG_REFLECTION):
+        spec = random_job(shader, seed=70 + shader, W=30, H=26, F=50)
+        W, H = spec.width, spec.height
+        full = oracle.render(spec, np.ones((W, H)), np.ones((W, H, 3)), dtype=np.float64, want_branch=True)
+        plain = oracle.render(spec, np.ones((W, H)), np.ones((W, H, 3)), dtype=np.float64)
+        assert np.array_equal(full["canvas"], plain["canvas"]) and np.array_equal(full["prim_id"], plain["prim_id"])
+        win = (5, 17, 3, 20)
+        part = oracle.render(spec, np.ones((W, H)), np.ones((W, H, 3)), dtype=np.float64, window=win, want_branch=True)
+        sx, sy = slice(5, 17), slice(3, 20)
+        for k in ("canvas", "zbuffer", "prim_id", "branch", "texel"):
+            assert np.array_equal(part[k][sx, sy], full[k][sx, sy]), k
+        outside = np.ones((W, H), bool)
+        outside[sx, sy] = False
+        assert (part["prim_id"][outside] == -1).all() and (part["canvas"][outside] == 1).all()
+        kept = full["prim_id"] >= 0
+        assert (full["texel"][kept] >= 0).all() and (full["texel"][~kept] == -1).all()
