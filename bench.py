@@ -103,6 +103,7 @@ class Workload:
     published: Optional[float] = None  # the reference's published frames/s for this configuration
     display: object = None  # uint8 display images of the notebook step
     pipeline: Optional[Callable[[], object]] = None  # builds a batch.InstancedPipeline (instanced workloads)
+    data: str = "synthetic (seeded stand-ins with the stated shapes)"
 
 
 def _pass_work(spec) -> float:
@@ -252,18 +253,22 @@ def build_mixed1024(n, rank, dev):
                             "shadow_scenes": int(shadow.sum()), "shadow_map": "canvas size (Renderer.render)"})
 
 
+ANT_FIXTURE = ROOT / "tests" / "golden" / "brax_ant_30.npz"
+
+
 def build_ant84(n, rank, dev):
-    """The notebooks' benchmark (84x84/A100.ipynb cells 4-7): Brax Ant
-    frames -- here the seeded stand-in synthetic.ant_like_batched in the same
-    batched format, 18 objects / 3,276 triangles per frame, 30 frames
-    repeated to the batch -- rendered into 84x84 canvases through the
-    pickled 960x540 camera with the notebook's light and per-frame shadow
-    centre, then clamped, scaled to uint8 and transposed for display."""
-    from jaxrenderer_gb300 import batch as jb, brax, synthetic
+    """The notebooks' benchmark (84x84/A100.ipynb cells 4-7) on the
+    reference's own Brax Ant frames (test_resources/pre-gen-brax/
+    inputs-30.zip, held as the pickle-free archive tests/golden/
+    brax_ant_30.npz): 18 objects / 3,276 triangles per frame, the 30 frames
+    cycled to the batch, rendered into 84x84 canvases through the pickled
+    960x540 camera with the notebook's light and per-frame shadow centre,
+    then clamped, scaled to uint8 and transposed for display."""
+    from jaxrenderer_gb300 import batch as jb, brax
 
     W = H = 84
-    objects, camera, target = synthetic.ant_like_batched(30, seed=synthetic.BASE_SEED + 7 + rank)
-    frames = [k % 30 for k in range(n)]
+    objects, camera, target = brax.load_batched_npz(ANT_FIXTURE)
+    frames = [(k + rank * n) % 30 for k in range(n)]
     bb = brax.scenes_from_batched(objects, camera, target, frames=frames)
     inst = bb.scenes
     work = inst.n_faces.astype(np.float64) * (2 * W * H)
@@ -279,9 +284,12 @@ def build_ant84(n, rank, dev):
     if dev is not None:
         sb, merge = brax.scene_batch(bb, W, H, dev)
         groups, merges = [sb], [merge]
-    return Workload("ant84", f"Brax-Ant-like 84x84 x {n} frames (18 objects, 3,276 tris; 960x540 camera), "
-                    "phong_reflection_shadow, device merge + render + uint8 display per step", n, chain, work,
+    return Workload("ant84", f"Brax Ant 84x84 x {n} frames (the reference's inputs-30.zip frames cycled; 18 objects, "
+                    "3,276 tris; 960x540 camera), phong_reflection_shadow, device merge + render + uint8 display "
+                    "per step", n, chain, work,
                     groups, merges=merges, instances=inst, notebook=True, published=888.6 if n == 200 else None,
+                    data="reference fixture (test_resources/pre-gen-brax/inputs-30.zip as tests/golden/"
+                         "brax_ant_30.npz)",
                     config={"scenes": n, "faces_per_scene": 3276, "resolution": [W, H],
                             "camera_viewport": [960, 540], "shadow_map": [W, H],
                             "published": "888.6 frames/s, A100, batch 200 (notebooks/84x84/A100.ipynb:1308)"})
@@ -540,8 +548,7 @@ def run_ours(args, rank, world, local):
         "scaling": "weak",
         "vs_baseline": (value / wl.published) if wl.published else None,
         "dtype": "f32",
-        "data": "synthetic (seeded stand-ins with the stated shapes; the reference's Brax fixtures are "
-                "inputs-only pickles)",
+        "data": wl.data,
         "config": dict({
             "workload": wl.desc,
             "form": form + " (CUDA graph replay)" + (
@@ -1172,7 +1179,7 @@ def run_reference(args, rank, world, local):
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f32",
-        "data": "synthetic (seeded stand-ins with the stated shapes)",
+        "data": wl.data,
         "config": dict({"workload": wl.desc, "sample_per_step": f"~{budget:.0f} s of consecutive scenes{crop}"},
                        **wl.config),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",

@@ -21,7 +21,7 @@ import numpy as np
 import torch
 
 from . import _lib
-from .geometry import Camera, normalise
+from .geometry import Camera, apply_vec_rows, bmatmul, normalise, view_matrices, view_matrices_inv
 from .renderer import CameraParameters, LightParameters, Renderer, ShadowParameters
 from .shadow import Shadow
 
@@ -56,16 +56,37 @@ class SceneBatch:
 
 
 def _cameras(positions: np.ndarray, params: CameraParameters, targets=None):
-    w2c, w2e, view = [], [], []
-    for k, p in enumerate(positions):
-        prm = params._replace(position=p)
-        if targets is not None:
-            prm = prm._replace(target=targets[k])
-        cam = Renderer.create_camera_from_parameters(prm)
-        w2c.append(cam.world_to_clip)
-        w2e.append(cam.world_to_eye_norm)
-        view.append(cam.view)
-    return np.stack(w2c), np.stack(w2e), np.stack(view), cam.viewport
+    """(world_to_clip, world_to_eye_norm, view) of one camera per row of
+    `positions` (targets per row or params.target), each bit for bit what
+    Renderer.create_camera_from_parameters gives for that camera, plus the
+    shared viewport."""
+    positions = np.asarray(positions, F32).reshape(-1, 3)
+    first = params._replace(position=positions[0])
+    if targets is not None:
+        first = first._replace(target=np.asarray(targets, F32).reshape(-1, 3)[0])
+    cam = Renderer.create_camera_from_parameters(first)  # projection and viewport are shared
+    centre = np.asarray(targets if targets is not None else params.target, F32)
+    up = np.asarray(params.up, F32)
+    view = view_matrices(positions, centre, up)
+    view_inv = view_matrices_inv(positions, centre, up)
+    w2c = bmatmul(cam.projection, view)
+    w2e = np.ascontiguousarray(np.swapaxes(view_inv, -1, -2))
+    return w2c, w2e, view, cam.viewport
+
+
+def _light_cameras(light_direction, viewport, centres: np.ndarray, up):
+    """Shadow.light_camera for one centre per row: (world_to_clip,
+    world_to_eye_norm), bit for bit the single-centre results."""
+    from .geometry import _arr, lu_inverse
+
+    d = _arr(light_direction, F32)
+    c = np.asarray(centres, F32).reshape(-1, 3)
+    eye = c + d * F32(10.0)
+    view = view_matrices(eye, c, _arr(up, F32))
+    ortho = Camera.orthographic_projection_matrix(-1.0, 1.0, -1.0, 1.0, -1.0, 1.0)
+    w2c = bmatmul(ortho, view)
+    w2e = np.ascontiguousarray(np.swapaxes(lu_inverse(view), -1, -2))
+    return w2c, w2e
 
 
 @dataclass
@@ -105,7 +126,7 @@ def scene_batch_tables(flat, width: int = 84, height: int = 84,
                                                hfov=58.0, vfov=58.0, target=np.zeros(3, F32))
     w2c, w2e, views, viewport = _cameras(flat.camera_position, params, getattr(flat, "camera_target", None))
     light_dir = normalise(np.asarray(light.direction, F32))
-    light_dir_eye = np.stack([Camera.apply_vec(light_dir, v) for v in views])
+    light_dir_eye = apply_vec_rows(light_dir, views)
 
     shadow = shadow_param is not None
     mask = np.ones(n, bool) if shadow_mask is None else np.asarray(shadow_mask, bool)
@@ -149,10 +170,8 @@ def scene_batch_tables(flat, width: int = 84, height: int = 84,
             Camera.viewport_matrix(np.zeros(2, np.int32), np.array((sw, sh)), 1.0)
         centre = np.asarray(shadow_param.centre, F32)
         if centre.ndim == 2:  # one shadow centre per scene
-            cams = [Shadow.light_camera(np.asarray(light.direction, F32), svp, c, shadow_param.up) for c in centre]
-            s_w2c = np.stack([c.world_to_clip for c in cams])
-            s_w2e = np.stack([c.world_to_eye_norm for c in cams])
-            scam = cams[0]
+            s_w2c, s_w2e = _light_cameras(light.direction, svp, centre, shadow_param.up)
+            scam = Shadow.light_camera(np.asarray(light.direction, F32), svp, centre[0], shadow_param.up)
         else:
             scam = Shadow.light_camera(np.asarray(light.direction, F32), svp, centre, shadow_param.up)
             s_w2c = np.broadcast_to(scam.world_to_clip, (n, 4, 4))

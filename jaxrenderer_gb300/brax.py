@@ -13,6 +13,8 @@ unpickler: only the array, ModelObject, Model and CameraParameters
 reconstructors are resolved; anything else is refused), and
 `scenes_from_batched` turns it into InstancedScenes (one scene per frame,
 the meshes shared) plus the camera / light / shadow settings above.
+`save_batched_npz` / `load_batched_npz` hold the same inputs in a
+compressed NumPy archive, which loads without unpickling.
 """
 from __future__ import annotations
 
@@ -82,6 +84,59 @@ def load_batched_inputs(source: Union[str, bytes]):
             data = fh.read()
     objects, camera, target = _Unpickler(io.BytesIO(data)).load()
     return list(objects), camera, np.asarray(target, F32)
+
+
+# ------------------------------------------------ pickle-free archive format
+
+_CAMERA_FIELDS = ("viewWidth", "viewHeight", "viewDepth", "near", "far", "hfov", "vfov", "position", "target", "up")
+
+
+def save_batched_npz(path, objects: List[ModelObject], camera: CameraParameters, target, source_sha256: str = ""):
+    """Write batched Brax inputs (the triple load_batched_inputs returns) as
+    a compressed .npz: every ModelObject array and camera field with its
+    leading frame axis, except arrays equal in every frame, which are stored
+    once (key suffix ".shared").  Unlike the pickle, loading it runs no code."""
+    n_frames = int(np.asarray(objects[0].transform).shape[0])
+    arrays = {"n_objects": np.asarray(len(objects)), "n_frames": np.asarray(n_frames),
+              "target": np.asarray(target, F32), "source_sha256": np.asarray(source_sha256)}
+
+    def put(key, value):
+        a = np.asarray(value)
+        if a.ndim >= 1 and a.shape[0] == n_frames and all(np.array_equal(a[0], a[f]) for f in range(1, n_frames)):
+            arrays[key + ".shared"] = a[0]
+        else:
+            arrays[key] = a
+
+    for i, o in enumerate(objects):
+        for field in Model._fields:
+            put(f"o{i}.model.{field}", getattr(o.model, field))
+        for field in ("local_scaling", "transform", "double_sided"):
+            put(f"o{i}.{field}", getattr(o, field))
+    for field in _CAMERA_FIELDS:
+        arrays[f"camera.{field}"] = np.asarray(getattr(camera, field))
+    np.savez_compressed(path, **arrays)
+
+
+def load_batched_npz(path):
+    """(batched ModelObjects, batched CameraParameters, batched target) from
+    an archive written by save_batched_npz; arrays stored once are broadcast
+    back to their frame axis (read-only views)."""
+    with np.load(path, allow_pickle=False) as z:
+        n_objects, n_frames = int(z["n_objects"]), int(z["n_frames"])
+
+        def get(key):
+            if key in z.files:
+                return z[key]
+            a = z[key + ".shared"]
+            return np.broadcast_to(a, (n_frames,) + a.shape)
+
+        objects = []
+        for i in range(n_objects):
+            model = Model(*(get(f"o{i}.model.{field}") for field in Model._fields))
+            objects.append(ModelObject(model=model, local_scaling=get(f"o{i}.local_scaling"),
+                                       transform=get(f"o{i}.transform"), double_sided=get(f"o{i}.double_sided")))
+        camera = CameraParameters(**{field: z[f"camera.{field}"] for field in _CAMERA_FIELDS})
+        return objects, camera, np.asarray(z["target"], F32)
 
 
 @dataclass
@@ -179,4 +234,5 @@ def scene_batch(bb: BraxBatch, width: int, height: int, device=None):
                                       bb.camera, shadow_viewport="camera")
 
 
-__all__ = ["load_batched_inputs", "scenes_from_batched", "scene_batch", "BraxBatch"]
+__all__ = ["load_batched_inputs", "save_batched_npz", "load_batched_npz", "scenes_from_batched", "scene_batch",
+           "BraxBatch"]

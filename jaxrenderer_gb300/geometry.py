@@ -209,6 +209,86 @@ def det3(m) -> np.ndarray:
     return ((((t1 + t2) + t3) - t4) - t5) - t6
 
 
+# ------------------------------------------- batched (leading axis) twins
+#
+# Per-scene set-up of many cameras at once.  Each function gives, for every
+# index of the leading axis, the bits its single-camera counterpart gives:
+# the same operations in the same order, applied elementwise.
+
+
+def normalise_rows(v) -> np.ndarray:
+    """normalise() of every 3-vector along the last axis (one norm per row,
+    sum of squares in index order)."""
+    v = _arr(v)
+    return v / np.sqrt((v[..., 0:1] * v[..., 0:1] + v[..., 1:2] * v[..., 1:2]) + v[..., 2:3] * v[..., 2:3])
+
+
+def bmatmul(a, b) -> np.ndarray:
+    """(..., n, k) @ (..., k, m) with products summed in index order."""
+    a = np.asarray(a)
+    b = np.asarray(b)
+    dt = np.result_type(a, b)
+    a = a.astype(dt, copy=False)
+    b = b.astype(dt, copy=False)
+    acc = a[..., :, 0:1] * b[..., 0:1, :]
+    for k in range(1, a.shape[-1]):
+        acc = acc + a[..., :, k : k + 1] * b[..., k : k + 1, :]
+    return acc
+
+
+def bmatvec(m, v) -> np.ndarray:
+    """out[..., i] = sum_k v[..., k] * m[..., i, k] in index order (Camera.apply
+    with one matrix per leading index)."""
+    m = np.asarray(m)
+    v = np.asarray(v)
+    dt = np.result_type(m, v)
+    acc = v[..., None, 0].astype(dt) * m[..., :, 0].astype(dt)
+    for k in range(1, v.shape[-1]):
+        acc = acc + v[..., None, k].astype(dt) * m[..., :, k].astype(dt)
+    return acc
+
+
+def _look_at_rows(eye, centre, up):
+    eye = _arr(eye)
+    centre = np.broadcast_to(_arr(centre, eye.dtype), eye.shape)
+    up = np.broadcast_to(_arr(up, eye.dtype), eye.shape)
+    forward = normalise_rows(centre - eye)
+    up = normalise_rows(up)
+    side = normalise_rows(cross(forward, up))
+    up = cross(side, forward)
+    m = np.broadcast_to(np.identity(4, dtype=eye.dtype), eye.shape[:-1] + (4, 4)).copy()
+    m[..., 0, :3] = side
+    m[..., 1, :3] = up
+    m[..., 2, :3] = -forward
+    return eye, m
+
+
+def view_matrices(eye, centre, up) -> np.ndarray:
+    """Camera.view_matrix of every row of eye (..., 3) (centre, up: one per
+    row or shared)."""
+    eye, m = _look_at_rows(eye, centre, up)
+    translation = np.broadcast_to(np.identity(4, dtype=eye.dtype), m.shape).copy()
+    translation[..., :3, 3] = -eye
+    return bmatmul(m, translation)
+
+
+def view_matrices_inv(eye, centre, up) -> np.ndarray:
+    """Camera.view_matrix_inv of every row of eye (..., 3)."""
+    eye, m = _look_at_rows(eye, centre, up)
+    translation_inv = np.broadcast_to(np.identity(4, dtype=eye.dtype), m.shape).copy()
+    translation_inv[..., :3, 3] = eye
+    return bmatmul(translation_inv, np.ascontiguousarray(np.swapaxes(m, -1, -2)))
+
+
+def apply_vec_rows(vectors, matrices) -> np.ndarray:
+    """Camera.apply_vec of one direction (or one per row) by matrices
+    (..., 4, 4), one result per matrix."""
+    v = normalise_rows(_arr(vectors))
+    h = to_homogeneous(v, np.zeros((), dtype=v.dtype))
+    h = np.broadcast_to(h, np.asarray(matrices).shape[:-2] + (4,))
+    return normalise_rows(bmatvec(matrices, h)[..., :3])
+
+
 class Camera(NamedTuple):
     """Camera matrices (geometry.py:205-278), 4x4 row-major NumPy arrays."""
 

@@ -1,19 +1,26 @@
 """Capsule mesh (renderer/shapes/capsule.py:1958-2015).
 
-A unit sphere of 12 longitude segments x 9 latitude bands (20 degrees each),
-split at the equator, the two halves pushed apart by +-half_height along the
-up axis: 192 triangles with 3 vertices each (576 vertices, no sharing), the
-reference's tessellation.  The reference takes its vertex values from a
-tabulated sphere; this one is generated, so coordinates differ in the last
-digits while counts, winding, normal directions and uv layout agree.
+The reference builds its capsule from a tabulated unit sphere (its
+capsule.py:19-1956, tinyrenderer's textured sphere): 192 triangles with
+three unshared vertices each (576 vertices, normals and uvs), the northern
+and southern halves pushed apart by +-half_height along the up axis.  The
+table is kept alike here (capsule_table.npz, written from the reference's
+literals by make_capsule_table.py) because its vertex values decide which
+pixels a capsule covers and its uvs which texels it samples: scenes built
+with create_capsule then render the reference's geometry.  The capsules of
+the reference's own Brax Ant fixture (test_resources/pre-gen-brax) are
+reproduced bit for bit by create_capsule (tests/test_host.py).
 """
 from __future__ import annotations
 
 import enum
+from pathlib import Path
 
 import numpy as np
 
 from ..model import Model
+
+_TABLE = Path(__file__).resolve().parent / "capsule_table.npz"
 
 
 class UpAxis(enum.IntEnum):
@@ -22,52 +29,25 @@ class UpAxis(enum.IntEnum):
     Z = 2
 
 
-_SEGMENTS = 12
-_BANDS = 9
+def _load_table():
+    with np.load(_TABLE, allow_pickle=False) as t:
+        return (t["verts"].astype(np.float32), t["normals"].astype(np.float32), t["uvs"].astype(np.float32),
+                t["faces"].astype(np.int32))
 
 
-def _sphere():
-    verts, norms, uvs = [], [], []
-
-    def point(band_edge: int, seg: int):
-        theta = np.pi * band_edge / _BANDS  # polar angle from +z
-        phi = 2.0 * np.pi * seg / _SEGMENTS
-        n = (np.sin(theta) * np.sin(phi), np.sin(theta) * np.cos(phi), np.cos(theta))
-        uv = (seg / _SEGMENTS, 1.0 - band_edge / _BANDS)
-        return n, uv
-
-    def tri(*pts):
-        for b, s in pts:
-            n, uv = point(b, s)
-            verts.append(n)
-            norms.append(n)
-            uvs.append(uv)
-
-    for b in range(_BANDS):
-        for s in range(_SEGMENTS):
-            a00, a01, a10, a11 = (b, s), (b, s + 1), (b + 1, s), (b + 1, s + 1)
-            # counter-clockwise seen from outside
-            if b == 0:  # north cap: one triangle per segment
-                tri(a00, a11, a10)
-            elif b == _BANDS - 1:  # south cap
-                tri(a00, a01, a10)
-            else:
-                tri(a00, a11, a10)
-                tri(a00, a01, a11)
-    v = np.asarray(verts, dtype=np.float32)
-    return v, np.asarray(norms, dtype=np.float32), np.asarray(uvs, dtype=np.float32)
-
-
-_VERTS, _NORMALS, _UVS = _sphere()
-_FACES = np.arange(len(_VERTS), dtype=np.int32).reshape(-1, 3)
+_VERTS, _NORMALS, _UVS, _FACES = _load_table()
 
 
 def create_capsule(radius, half_height, up_axis, diffuse_map, specular_map) -> Model:
-    """Capsule of `radius` whose hemispheres sit +-half_height along up_axis."""
+    """Capsule of `radius` whose hemispheres sit +-half_height along up_axis:
+    the table's coordinates permuted so that its z axis becomes up_axis,
+    scaled by radius in float32, then half_height added to the vertices with
+    a positive up coordinate and subtracted from the others."""
     up = int(up_axis)
     shuffled = np.array(((1, 2, 0), (0, 1, 2), (2, 0, 1)))[up]
     verts = _VERTS[:, shuffled] * np.float32(radius)
-    verts[:, up] = verts[:, up] + np.where(verts[:, up] > 0, np.float32(half_height), -np.float32(half_height))
+    hh = np.float32(half_height)
+    verts[:, up] = verts[:, up] + np.where(verts[:, up] > 0, hh, -hh)
     return Model(
         verts=verts.astype(np.float32),
         norms=_NORMALS[:, shuffled].copy(),

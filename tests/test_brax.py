@@ -57,3 +57,55 @@ def test_reference_fixture_structure():
     assert bb.scenes.n_scenes == 2 and len(objects) == 18
     assert bb.scenes.n_faces.tolist() == [3276, 3276]
     assert (bb.camera.viewWidth, bb.camera.viewHeight) == (960, 540)
+
+
+GOLDEN = Path(__file__).resolve().parent / "golden"
+
+
+def test_npz_archive_round_trip(tmp_path):
+    objects, camera, target = synthetic.ant_like_batched(3)
+    path = tmp_path / "ant.npz"
+    brax.save_batched_npz(path, objects, camera, target)
+    got_objects, got_camera, got_target = brax.load_batched_npz(path)
+    for a, b in zip(objects, got_objects):
+        for field in ("local_scaling", "transform", "double_sided"):
+            np.testing.assert_array_equal(np.asarray(getattr(a, field)), np.asarray(getattr(b, field)))
+        for field in a.model._fields:
+            np.testing.assert_array_equal(np.asarray(getattr(a.model, field)), np.asarray(getattr(b.model, field)))
+    for field in camera._fields:
+        np.testing.assert_array_equal(np.asarray(getattr(camera, field)), np.asarray(getattr(got_camera, field)))
+    np.testing.assert_array_equal(target, got_target)
+
+
+def test_committed_fixture_archives():
+    """tests/golden/brax_ant_{2,30}.npz: the reference's inputs-{2,30}.zip
+    (SHA-256 recorded in each archive), 18 objects, 3,276 triangles per frame."""
+    for n, sha in ((2, "38d050833a0307409f28b5ed2633a7b8f3e14287cf607a4df9426872e8192db3"),
+                   (30, "0ef2738b6c4cee12b94b2569679ff71598b27df77dc53dd9762302f9d71fab7f")):
+        with np.load(GOLDEN / f"brax_ant_{n}.npz") as z:
+            assert str(z["source_sha256"]) == sha
+        objects, camera, target = brax.load_batched_npz(GOLDEN / f"brax_ant_{n}.npz")
+        bb = brax.scenes_from_batched(objects, camera, target)
+        assert bb.scenes.n_scenes == n and bb.scenes.n_faces.tolist() == [3276] * n
+        assert (bb.camera.viewWidth, bb.camera.viewHeight) == (960, 540)
+
+
+@pytest.mark.skipif(not (REFERENCE / "test_resources/pre-gen-brax/inputs-30.zip").exists(),
+                    reason="the reference's fixtures are not on this machine")
+@pytest.mark.parametrize("n", [2, 30])
+def test_fixture_archives_equal_the_reference_pickles(n):
+    import hashlib
+
+    src = REFERENCE / f"test_resources/pre-gen-brax/inputs-{n}.zip"
+    with np.load(GOLDEN / f"brax_ant_{n}.npz") as z:
+        assert str(z["source_sha256"]) == hashlib.sha256(src.read_bytes()).hexdigest()
+    ref = brax.load_batched_inputs(str(src))
+    got = brax.load_batched_npz(GOLDEN / f"brax_ant_{n}.npz")
+    for a, b in zip(ref[0], got[0]):
+        for field in ("local_scaling", "transform", "double_sided"):
+            np.testing.assert_array_equal(np.asarray(getattr(a, field)), np.asarray(getattr(b, field)))
+        for field in a.model._fields:
+            np.testing.assert_array_equal(np.asarray(getattr(a.model, field)), np.asarray(getattr(b.model, field)))
+    for field in ref[1]._fields:
+        np.testing.assert_array_equal(np.asarray(getattr(ref[1], field)), np.asarray(getattr(got[1], field)))
+    np.testing.assert_array_equal(ref[2], got[2])

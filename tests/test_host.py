@@ -95,3 +95,47 @@ def test_brax_like_scene_sizes():
     rng = np.random.Generator(np.random.PCG64(synthetic.BASE_SEED + 1))
     sizes = [synthetic.brax_like_scene(rng).n_faces for _ in range(20)]
     assert 2 + 8 * 12 <= min(sizes) and max(sizes) <= 2 + 32 * 512
+
+
+def test_create_capsule_reproduces_the_reference_fixture_capsules():
+    """The 17 capsules of the reference's Brax Ant inputs (tests/golden/
+    brax_ant_30.npz, made by the reference's create_capsule from its
+    tabulated sphere) come out of create_capsule bit for bit."""
+    from pathlib import Path
+
+    from jaxrenderer_gb300 import brax
+
+    objects, _, _ = brax.load_batched_npz(Path(__file__).resolve().parent / "golden" / "brax_ant_30.npz")
+    r8, h1, h2 = F32(0.08), F32(0.1414213627576828), F32(0.2828427255153656)
+    params = [(F32(0.25), F32(0))] + [(r8, h) for h in (h1, h1, h1, h1, h1, h2, 0, h1, h2, 0, h1, h2, 0, h1, h2, 0)]
+    for o, (radius, hh) in zip(objects[1:], params):
+        m = o.model
+        k = jr.create_capsule(radius, hh, jr.UpAxis.Z, np.asarray(m.diffuse_map)[0], np.asarray(m.specular_map)[0])
+        for field in ("verts", "norms", "uvs", "faces", "faces_norm", "faces_uv"):
+            np.testing.assert_array_equal(getattr(k, field), np.asarray(getattr(m, field))[0], err_msg=field)
+
+
+def test_batched_camera_setup_matches_the_per_scene_setup_bitwise():
+    """batch._cameras / _light_cameras (one camera per scene, vectorised)
+    give each scene the bits Renderer.create_camera_from_parameters and
+    Shadow.light_camera give it alone."""
+    from jaxrenderer_gb300 import batch as jb
+    from jaxrenderer_gb300.geometry import Camera, apply_vec_rows
+    from jaxrenderer_gb300.shadow import Shadow
+
+    rng = np.random.default_rng(5)
+    pos = (rng.normal(size=(24, 3)) * 6).astype(F32)
+    tgt = rng.normal(size=(24, 3)).astype(F32)
+    params = jr.CameraParameters(viewWidth=96, viewHeight=64, hfov=58.0, vfov=32.625)
+    w2c, w2e, view, vp = jb._cameras(pos, params, tgt)
+    d = np.array((0.57735, -0.57735, 0.57735), F32)
+    up = np.array((0, 0, 1), F32)
+    sw, se = jb._light_cameras(d, vp, tgt, up)
+    ldir = apply_vec_rows(d, view)
+    for k in range(24):
+        cam = jr.Renderer.create_camera_from_parameters(params._replace(position=pos[k], target=tgt[k]))
+        light = Shadow.light_camera(d, vp, tgt[k], up)
+        for got, want in ((w2c[k], cam.world_to_clip), (w2e[k], cam.world_to_eye_norm), (view[k], cam.view),
+                          (sw[k], light.world_to_clip), (se[k], light.world_to_eye_norm),
+                          (ldir[k], Camera.apply_vec(d, cam.view))):
+            np.testing.assert_array_equal(got.view(np.uint32), np.asarray(want, F32).view(np.uint32))
