@@ -67,9 +67,8 @@ def workload_key(jobs: np.ndarray, device: torch.device) -> str:
             + (f"|layers{layers}" if layers > 0 else "") + f"|{props.name}|sm{props.multi_processor_count}")
 
 
-def _time(runner, name, b, cfg, reps=3) -> float:
-    dev = runner.sb.device
-    lib = runner.lib
+def _time(dev, b, cfg, reps=3) -> float:
+    lib = _lib.load()
     nbytes = int(lib.rast_tiled_workspace_bytes(ctypes.byref(b), ctypes.byref(cfg)))
     ws = torch.empty(max(nbytes, 256), dtype=torch.uint8, device=dev)
     s = torch.cuda.current_stream(dev)
@@ -89,7 +88,15 @@ def _time(runner, name, b, cfg, reps=3) -> float:
 
 def tiled_config_for(runner, name: str, b, jobs: np.ndarray) -> "_lib.RastTiledConfig":
     """Tuned RastTiledConfig for one pass of a BatchRunner."""
-    key = workload_key(jobs, runner.sb.device)
+    return tiled_config_for_batch(runner.sb.device, b, jobs)
+
+
+def tiled_config_for_batch(device: torch.device, b, jobs: np.ndarray) -> "_lib.RastTiledConfig":
+    """Tuned RastTiledConfig for a RastBatch `b` whose job table is `jobs`
+    (structured array with the RastJob layout).  Tuning renders `b` several
+    times into its own output pools: pass a batch whose outputs may be
+    overwritten."""
+    key = workload_key(jobs, device)
     with _LOCK:
         cache = _load()
         hit = cache.get(key)
@@ -101,7 +108,7 @@ def tiled_config_for(runner, name: str, b, jobs: np.ndarray) -> "_lib.RastTiledC
     for tw, th in LAYERED_SHAPES if layered else SHAPES:
         for small in (0,) if layered else SMALL_AREAS:
             cfg = _lib.RastTiledConfig(tw, th, 0, small)
-            ms, entries = _time(runner, name, b, cfg)
+            ms, entries = _time(device, b, cfg)
             if best is None or ms < best[0]:
                 best = (ms, tw, th, entries, small)
     ms, tw, th, entries, small = best
@@ -113,4 +120,4 @@ def tiled_config_for(runner, name: str, b, jobs: np.ndarray) -> "_lib.RastTiledC
     return _lib.RastTiledConfig(tw, th, cap, small)
 
 
-__all__ = ["tiled_config_for", "workload_key", "cache_path", "SHAPES", "LAYERED_SHAPES", "SMALL_AREAS"]
+__all__ = ["tiled_config_for", "tiled_config_for_batch", "workload_key", "cache_path", "SHAPES", "LAYERED_SHAPES", "SMALL_AREAS"]

@@ -424,6 +424,7 @@ class BatchRunner:
                                           dtype=torch.float32, device=dev)
             self.shadow_prim = torch.empty_like(self.shadow_map, dtype=torch.int32) if want_prim_id else None
             self.shadow_batch = _rast_batch(sb.shadow_jobs, sb.pools, self.shadow_map, None, self.shadow_prim, None, self.keep)
+            self.shadow_jobs_dev = self.keep[-1][2]  # device copy of the depth pass's job table (uint8)
             pools = dict(sb.pools)
             pools["shadow_map"] = self.shadow_map
         else:
@@ -479,6 +480,32 @@ class BatchRunner:
                 st = self.lib.rast_render_tiled_profiled(ctypes.byref(b), self._cfg(name), buf.data_ptr(), nbytes,
                                                          stream_handle, ctypes.byref(profile))
         _lib.check(st, f"rast_render_{self.form}")
+
+    def set_job_tables(self, main_jobs: np.ndarray, shadow_jobs: Optional[np.ndarray] = None,
+                       stream: Optional[torch.cuda.Stream] = None) -> None:
+        """Replace the device job tables with new ones of the same jobs (new
+        matrices and light terms; sizes, offsets and shaders unchanged, so
+        the workspaces and tiled configs stay valid).  Stream-ordered."""
+        s = stream if stream is not None else torch.cuda.current_stream(self.sb.device)
+        staging = self.__dict__.setdefault("_job_staging", {})
+        for name, dev, tbl in (("main", self.main_jobs_dev, main_jobs),
+                               ("shadow", getattr(self, "shadow_jobs_dev", None), shadow_jobs)):
+            if dev is None or tbl is None:
+                continue
+            host = np.ascontiguousarray(tbl).view(np.uint8).reshape(-1)
+            if host.size != dev.numel():
+                raise ValueError("set_job_tables: the new table has another number of jobs")
+            buf, done = staging.get(name, (None, None))
+            if buf is None:
+                buf = torch.empty(host.size, dtype=torch.uint8, pin_memory=True)
+            elif done is not None:
+                done.synchronize()  # the previous copy out of this pinned buffer has finished
+            buf.numpy()[:] = host
+            with torch.cuda.stream(s):
+                dev.copy_(buf, non_blocking=True)
+                done = torch.cuda.Event()
+                done.record(s)
+            staging[name] = (buf, done)
 
     def job_floats(self) -> torch.Tensor:
         """The main pass's device job table viewed as (n_jobs, sizeof(RastJob)/4)
@@ -538,6 +565,11 @@ class BatchRunner:
         _lib.check(self.lib.rast_tiled_stats(ctypes.byref(b), self._cfg(name), buf.data_ptr(), s.cuda_stream,
                                              ctypes.byref(out)), "rast_tiled_stats")
         return out
+
+    def set_colour_default(self, colour) -> None:
+        """Canvas value of pixels no primitive writes (Renderer.create_buffers'
+        colour_default); run() resets the canvases to it."""
+        self._colour.copy_(torch.as_tensor(np.asarray(colour, F32).reshape(-1)[:3]))
 
     def _reset(self, zbuffer_default: float):
         self.zbuffer.fill_(zbuffer_default)

@@ -364,6 +364,22 @@ def render_tiled(packed: PackedBatch, tile=(8, 8), bin_capacity: int = 0,
     return stats
 
 
+def render_tiled_config(packed: PackedBatch, cfg: "_lib.RastTiledConfig",
+                        stream: Optional[torch.cuda.Stream] = None) -> None:
+    """Run the tiled form on a packed batch with `cfg` (stream-ordered; no sync)."""
+    lib = _lib.load()
+    b = packed.batch
+    nbytes = int(lib.rast_tiled_workspace_bytes(ctypes.byref(b), ctypes.byref(cfg)))
+    if nbytes == 0:
+        raise ValueError(f"tile shape {cfg.tile_w}x{cfg.tile_h} has no kernel")
+    dev = packed.zbuffer.device
+    ws = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+    packed.keep.append(ws)
+    s = stream if stream is not None else torch.cuda.current_stream(dev)
+    _lib.check(lib.rast_render_tiled(ctypes.byref(b), ctypes.byref(cfg), ws.data_ptr(), nbytes, s.cuda_stream),
+               "rast_render_tiled")
+
+
 def unpack(packed: PackedBatch, specs: Sequence[JobSpec]):
     """Per-job views of the output pools: (zbuffer, canvas or None, prim_id or None)."""
     out = []
@@ -376,4 +392,5 @@ def unpack(packed: PackedBatch, specs: Sequence[JobSpec]):
     return out
 
 
-__all__ = ["JobSpec", "job_from_extra", "pack", "render_plain", "render_tiled", "unpack", "PackedBatch"]
+__all__ = ["JobSpec", "job_from_extra", "pack", "render_plain", "render_tiled", "render_tiled_config", "unpack",
+           "PackedBatch"]

@@ -13,6 +13,7 @@ from __future__ import annotations
 import numpy as np
 import torch
 
+from . import dispatch as _dispatch
 from . import jobs as _jobs
 from .geometry import Camera
 from .hooks import apply_hooks
@@ -32,13 +33,21 @@ def _faces(face_indices):
     return np.ascontiguousarray(np.asarray(face_indices, dtype=np.int32).reshape(-1, 3))
 
 
-def render_job(spec: _jobs.JobSpec, zbuffer, canvas, device=None, count_ties: bool = False):
-    """Render one JobSpec; returns (zbuffer, canvas or None, prim_id, near_ties tensor or None)."""
+def render_job(spec: _jobs.JobSpec, zbuffer, canvas, device=None, count_ties: bool = False, form=None):
+    """Render one JobSpec with the form dispatch.choose picks (`form` pins
+    it); returns (zbuffer, canvas or None, prim_id, near_ties tensor or None)."""
+    zs, cs, ps, ties = render_jobs([spec], [zbuffer], [canvas], device, count_ties, form)
+    return zs[0], cs[0], ps[0], ties
+
+
+def render_jobs(specs, zbuffers, canvases, device=None, count_ties: bool = False, form=None):
+    """Render several jobs as one pass (one RastBatch); returns per-job lists
+    (zbuffers, canvases or None, prim_ids) and the pass's near-tie counter."""
     device = device if device is not None else default_device()
-    packed = _jobs.pack([spec], [zbuffer], [canvas], device, want_prim_id=True, count_ties=count_ties)
-    _jobs.render_plain(packed)
-    z, c, p = _jobs.unpack(packed, [spec])[0]
-    return z, c, p, packed.near_ties
+    packed = _jobs.pack(specs, zbuffers, canvases, device, want_prim_id=True, count_ties=count_ties)
+    _dispatch.run(packed, form)
+    out = _jobs.unpack(packed, specs)
+    return [o[0] for o in out], [o[1] for o in out], [o[2] for o in out], packed.near_ties
 
 
 def render_with_ids(camera: Camera, shader, buffers: Buffers, face_indices, extra,
@@ -62,10 +71,11 @@ def render(camera: Camera, shader, buffers: Buffers, face_indices, extra, loop_u
     default chooser / mix or the compiled hooks of `hooks` assigned to the
     shader's `primitive_chooser` / `mix`.
 
-    `loop_unroll` is accepted for API compatibility; the CUDA kernels have
-    no row loop to unroll.
+    The plain or the tiled form renders it, by size (dispatch.choose):
+    identical buffers either way.  `loop_unroll` is accepted for API
+    compatibility; the CUDA kernels have no row loop to unroll.
     """
     return render_with_ids(camera, shader, buffers, face_indices, extra, loop_unroll)[0]
 
 
-__all__ = ["render", "render_with_ids", "render_job", "default_device"]
+__all__ = ["render", "render_with_ids", "render_job", "render_jobs", "default_device"]

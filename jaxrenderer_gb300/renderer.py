@@ -14,7 +14,9 @@ import torch
 
 from .geometry import Camera, _arr, normalise
 from .model import MergedModel, ModelObject, merge_objects
-from .pipeline import default_device, render_with_ids
+from . import _lib
+from .jobs import JobSpec, job_from_extra
+from .pipeline import default_device, render_jobs
 from .shaders.phong_reflection import PhongReflectionTextureExtraInput, PhongReflectionTextureShader
 from .shaders.phong_reflection_shadow import (
     PhongReflectionShadowTextureExtraInput,
@@ -138,35 +140,148 @@ class Renderer:
         )
         return extra, face_indices
 
+    # ------------------------------------------------------------ batching
+    #
+    # Every argument may carry one extra leading axis of B scenes, as under
+    # jax.vmap of these calls (examples/batch_rendering.py:87-95 vmaps
+    # Renderer.render over batch_models(...) and batched buffers; the
+    # notebooks vmap get_camera_image over batched ModelObjects and
+    # CameraParameters).  _UNBATCHED_NDIM gives each field's rank without it.
+
+    _UNBATCHED_NDIM = {
+        "MergedModel": dict(verts=2, norms=2, uvs=2, faces=2, faces_norm=2, faces_uv=2, texture_shape=2,
+                            texture_index=1, double_sided=1, offset=0, diffuse_map=3, specular_map=2),
+        "Model": dict(verts=2, norms=2, uvs=2, faces=2, faces_norm=2, faces_uv=2, diffuse_map=3, specular_map=2),
+        "ModelObject": dict(local_scaling=1, transform=2, double_sided=0),
+        "Camera": dict(view=2, projection=2, viewport=2, world_to_clip=2, world_to_eye_norm=2,
+                       world_to_screen=2, view_inv=2, screen_to_world=2),
+        "CameraParameters": dict(viewWidth=0, viewHeight=0, viewDepth=0, near=0, far=0, hfov=0, vfov=0,
+                                 position=1, target=1, up=1),
+        "LightParameters": dict(direction=1, colour=1, ambient=1, diffuse=1, specular=1),
+        "ShadowParameters": dict(centre=1, up=1, strength=1, offset=0),
+    }
+
+    @classmethod
+    def _batch_size(cls, *trees):
+        """B when any argument carries a leading batch axis (all batched
+        arguments must agree), else None."""
+        sizes = set()
+        for t in trees:
+            if t is None:
+                continue
+            if isinstance(t, (list, tuple)) and not hasattr(t, "_fields"):
+                for x in t:
+                    b = cls._batch_size(x)
+                    if b is not None:
+                        sizes.add(b)
+                continue
+            ranks = cls._UNBATCHED_NDIM.get(type(t).__name__)
+            if ranks is None:
+                continue
+            for name in t._fields:
+                v = getattr(t, name)
+                if name == "model":
+                    b = cls._batch_size(v)
+                    if b is not None:
+                        sizes.add(b)
+                elif name in ranks and np.ndim(v) == ranks[name] + 1:
+                    sizes.add(int(np.shape(v)[0]))
+        if len(sizes) > 1:
+            raise ValueError(f"batched arguments disagree on the batch size: {sorted(sizes)}")
+        return sizes.pop() if sizes else None
+
+    @classmethod
+    def _take(cls, t, b: int):
+        """Scene b of a possibly batched argument (unbatched fields are shared)."""
+        if t is None:
+            return None
+        if isinstance(t, (list, tuple)) and not hasattr(t, "_fields"):
+            return [cls._take(x, b) for x in t]
+        ranks = cls._UNBATCHED_NDIM.get(type(t).__name__)
+        if ranks is None:
+            return t
+        out = {}
+        for name in t._fields:
+            v = getattr(t, name)
+            if name == "model":
+                out[name] = cls._take(v, b)
+            elif name in ranks and np.ndim(v) == ranks[name] + 1:
+                out[name] = v[b]
+            else:
+                out[name] = v
+        return type(t)(**out)
+
+    @classmethod
+    def _scene_specs(cls, model: MergedModel, light: LightParameters, camera: Camera, width: int, height: int,
+                     shadow_param: Optional[ShadowParameters]):
+        """(DepthShader JobSpec or None, Phong-reflection JobSpec) of one
+        scene, as Renderer.render issues them (renderer.py:254-385): with
+        shadows, the light-space depth pass over the merged vertices into a
+        map of the canvas size through the camera's viewport
+        (Shadow.render_shadow_map, shadow.py:49-125), then the shadowed
+        shader reading it (its shadow_map is set once the pass has run)."""
+        extra, face_indices = cls._extra(model, light, camera)
+        if shadow_param is None:
+            main = job_from_extra(_lib.SHADER_PHONG_REFLECTION, camera, extra, width, height)
+            main.faces = face_indices
+            return None, main
+        scam = Shadow.light_camera(_arr(light.direction, F32), camera.viewport, shadow_param.centre,
+                                   shadow_param.up)
+        depth = JobSpec(shader=_lib.SHADER_DEPTH, width=width, height=height, viewport=scam.viewport,
+                        world_to_clip=scam.world_to_clip, world_to_eye_norm=scam.world_to_eye_norm,
+                        position=_arr(model.verts, F32), faces=np.asarray(model.faces, np.int32).reshape(-1, 3),
+                        depth_offset=float(np.float32(shadow_param.offset)), apply_depth_offset=True)
+        shadow = Shadow(shadow_map=None, strength=_arr(shadow_param.strength, F32), camera=scam)
+        sextra = PhongReflectionShadowTextureExtraInput(**extra._asdict(), shadow=shadow, camera=camera)
+        main = job_from_extra(_lib.SHADER_PHONG_REFLECTION_SHADOW, camera, sextra, width, height)
+        main.faces = face_indices
+        return depth, main
+
+    @classmethod
+    def _render_scenes(cls, scenes, zbuffers, canvases, device):
+        """Render scenes [(model, light, camera, shadow_param)] into their
+        buffers: every scene's depth pass as one batch, then every scene's
+        main pass as one batch.  Returns per-scene (zbuffer, canvas, prim_id)."""
+        width, height = int(zbuffers[0].shape[0]), int(zbuffers[0].shape[1])
+        pairs = [cls._scene_specs(m, l, c, width, height, sp) for m, l, c, sp in scenes]
+        depth = [(k, d) for k, (d, _) in enumerate(pairs) if d is not None]
+        if depth:
+            fmax = float(DtypeInfo.create(np.float32).max)
+            init = [torch.full((width, height), fmax, dtype=torch.float32, device=device)] * len(depth)
+            maps, _, _, _ = render_jobs([d for _, d in depth], init, [None] * len(depth), device)
+            for (k, _), smap in zip(depth, maps):
+                pairs[k][1].shadow_map = smap
+        mains = [m for _, m in pairs]
+        return render_jobs(mains, zbuffers, canvases, device)[:3]
+
     @classmethod
     def render(cls, model: MergedModel, light: LightParameters, camera: Camera, buffers: Buffers,
                shadow_param: Optional[ShadowParameters] = None, loop_unroll: int = 1,
                with_ids: bool = False):
         """Render a merged model (renderer.py:254-385).  With `with_ids`
-        returns (buffers, winning-primitive buffer)."""
-        extra, face_indices = cls._extra(model, light, camera)
-        if shadow_param is None:
-            out, ids, _ = render_with_ids(camera, PhongReflectionTextureShader, buffers, face_indices, extra)
-            return (out, ids) if with_ids else out
+        returns (buffers, winning-primitive buffer).
+
+        Any argument may carry a leading batch axis (the model from
+        batch_models, buffers from create_buffers(batch=B), batched cameras,
+        lights or shadow parameters): all B scenes then render as one
+        batch per pass, and the buffers come back batched."""
         zb = buffers.zbuffer
-        fmax = float(DtypeInfo.create(np.float32).max)
-        shadow_map = torch.full(tuple(zb.shape), fmax, dtype=torch.float32,
-                                device=zb.device if isinstance(zb, torch.Tensor) else default_device())
-        shadow = Shadow.render_shadow_map(
-            shadow_map=shadow_map,
-            verts=_arr(model.verts, F32),
-            faces=np.asarray(model.faces, np.int32),
-            light_direction=_arr(light.direction, F32),
-            viewport_matrix=camera.viewport,
-            centre=shadow_param.centre,
-            up=shadow_param.up,
-            strength=shadow_param.strength,
-            offset=shadow_param.offset,
-            loop_unroll=loop_unroll,
-        )
-        _extra = PhongReflectionShadowTextureExtraInput(**extra._asdict(), shadow=shadow, camera=camera)
-        out, ids, _ = render_with_ids(camera, PhongReflectionShadowTextureShader, buffers, face_indices, _extra)
-        return (out, ids) if with_ids else out
+        canvas = buffers.targets[0] if len(buffers.targets) > 0 else None
+        B = cls._batch_size(model, light, camera, shadow_param)
+        if B is None and np.ndim(zb) == 3:
+            B = int(zb.shape[0])
+        device = zb.device if isinstance(zb, torch.Tensor) else default_device()
+        if B is None:
+            z, c, p = cls._render_scenes([(model, light, camera, shadow_param)], [zb], [canvas], device)
+            out = Buffers(zbuffer=z[0], targets=(c[0],) if c[0] is not None else ())
+            return (out, p[0]) if with_ids else out
+        scenes = [(cls._take(model, b), cls._take(light, b), cls._take(camera, b), cls._take(shadow_param, b))
+                  for b in range(B)]
+        zbs = [zb[b] if np.ndim(zb) == 3 else zb for b in range(B)]
+        cvs = [None if canvas is None else (canvas[b] if np.ndim(canvas) == 4 else canvas) for b in range(B)]
+        z, c, p = cls._render_scenes(scenes, zbs, cvs, device)
+        out = Buffers(zbuffer=torch.stack(z), targets=(torch.stack(c),) if c[0] is not None else ())
+        return (out, torch.stack(p)) if with_ids else out
 
     @classmethod
     def get_camera_image(cls, objects: Sequence[ModelObject], light: LightParameters,
@@ -175,7 +290,21 @@ class Renderer:
                          zbuffer_default=np.array(1, dtype=F32),
                          shadow_param: Optional[ShadowParameters] = None,
                          loop_unroll: int = 1) -> torch.Tensor:
-        """Render objects to a (width, height, 3) canvas (renderer.py:395-476)."""
+        """Render objects to a (width, height, 3) canvas (renderer.py:395-476).
+
+        Batched inputs (every ModelObject array, the camera, the light or the
+        shadow parameters with a leading axis of B frames, the form the
+        reference's notebooks pass to jax.vmap(get_camera_image)) give a
+        (B, width, height, 3) canvas, all frames rendered as one batch; when
+        the frames share their meshes (only transforms, cameras, lights and
+        shadow centres change), the batch is merged on the device and its
+        set-up is kept between calls (batched_api)."""
+        B = cls._batch_size(objects, light, camera, shadow_param)
+        if B is not None:
+            from . import batched_api
+
+            return batched_api.get_camera_image(objects, light, camera, width, height, colour_default,
+                                                zbuffer_default, shadow_param, B)
         _camera = cls.create_camera_from_parameters(camera) if isinstance(camera, CameraParameters) else camera
         buffers = cls.create_buffers(width=width, height=height, colour_default=colour_default,
                                      zbuffer_default=zbuffer_default)

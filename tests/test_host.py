@@ -139,3 +139,25 @@ def test_batched_camera_setup_matches_the_per_scene_setup_bitwise():
                           (sw[k], light.world_to_clip), (se[k], light.world_to_eye_norm),
                           (ldir[k], Camera.apply_vec(d, cam.view))):
             np.testing.assert_array_equal(got.view(np.uint32), np.asarray(want, F32).view(np.uint32))
+
+
+def test_batch_axis_detection_and_frame_selection():
+    """Renderer._batch_size / _take: a field with one more leading axis than
+    the reference's NamedTuple gives it is a batch (jax.vmap of the call)."""
+    from pathlib import Path
+
+    from jaxrenderer_gb300 import brax
+
+    objects, camera, target = brax.load_batched_npz(Path(__file__).resolve().parent / "golden" / "brax_ant_2.npz")
+    R = jr.Renderer
+    assert R._batch_size(objects) == 2 and R._batch_size(camera) == 2
+    assert R._batch_size(jr.LightParameters(), jr.ShadowParameters()) is None
+    assert R._batch_size(jr.ShadowParameters(centre=target)) == 2
+    one = R._take(list(objects), 1)
+    np.testing.assert_array_equal(one[3].transform, np.asarray(objects[3].transform)[1])
+    assert np.shape(one[3].model.verts) == (576, 3)
+    cam = R._take(camera, 1)
+    np.testing.assert_array_equal(cam.position, np.asarray(camera.position)[1])
+    assert int(cam.viewWidth) == 960
+    with pytest.raises(ValueError):
+        R._batch_size(camera, jr.ShadowParameters(centre=np.zeros((3, 3), F32)))
