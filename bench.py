@@ -102,6 +102,7 @@ class Workload:
     notebook: bool = False  # step = device merge + render + uint8 display epilogue, as the notebooks time it
     published: Optional[float] = None  # the reference's published frames/s for this configuration
     display: object = None  # uint8 display images of the notebook step
+    api_inputs: object = None  # (objects, camera, target, light) host arrays for the get_camera_image e2e
     pipeline: Optional[Callable[[], object]] = None  # builds a batch.InstancedPipeline (instanced workloads)
     data: str = "synthetic (seeded stand-ins with the stated shapes)"
 
@@ -110,12 +111,19 @@ def _pass_work(spec) -> float:
     return float(spec.width) * spec.height * spec.n_faces if spec is not None else 0.0
 
 
-def build_brax84(n, rank, dev):
-    from jaxrenderer_gb300 import batch as jb, synthetic
+def build_brax84(n, rank, dev, world=1):
+    """The 4096-scene brax-like batch; with N ranks, one batch of N x 4096
+    scenes split into N contiguous cost-balanced ranges (shard.partition),
+    rank r rendering range r."""
+    from jaxrenderer_gb300 import batch as jb, shard, synthetic
 
     W = H = 84
     shadow = (128, 128)
-    inst = synthetic.brax_like_instances(n, seed=synthetic.BASE_SEED + 1 + rank)
+    everything = synthetic.brax_like_instances(n * world, seed=synthetic.BASE_SEED + 1)
+    costs = shard.scene_costs(everything.n_faces, W, H, shadow[0] * shadow[1])
+    begin, end = shard.partition(costs, world)[rank]
+    inst = everything.subset(begin, end) if world > 1 else everything
+    n = end - begin
     n_faces = inst.n_faces
     work = n_faces.astype(np.float64) * (W * H + shadow[0] * shadow[1])
 
@@ -130,7 +138,8 @@ def build_brax84(n, rank, dev):
     return Workload("brax84", "brax-like 84x84 x 4096 scenes, phong_reflection_shadow + 128x128 depth pass", n,
                     chain, work, groups, merges=merges, instances=inst,
                     config={"scenes": n, "mean_faces_per_scene": float(n_faces.mean()),
-                            "objects": int(inst.n_instances), "resolution": [W, H], "shadow_map": list(shadow)},
+                            "objects": int(inst.n_instances), "resolution": [W, H], "shadow_map": list(shadow),
+                            "shard": [int(begin), int(end)] if world > 1 else None},
                     pipeline=lambda prepare=None: jb.InstancedPipeline(inst, W, H, shadow_size=shadow, device=dev,
                                                                        prepare=prepare))
 
@@ -138,13 +147,13 @@ def build_brax84(n, rank, dev):
 GLASS = {"layers": 4, "opacity": 0.6, "background": (0.55, 0.7, 0.9)}
 
 
-def build_glass84(n, rank, dev):
+def build_glass84(n, rank, dev, world=1):
     """The brax-like 84x84 batch through the compiled chooser / mix hooks:
     the 4 nearest candidates of every pixel blended front to back with
     opacity 0.6 over a sky colour (timed forward only)."""
     from jaxrenderer_gb300 import _lib, batch as jb
 
-    wl = build_brax84(n, rank, dev)
+    wl = build_brax84(n, rank, dev, world)
     hooks = dict(layers=GLASS["layers"], mixer=_lib.MIX_OVER, opacity=GLASS["opacity"],
                  background=GLASS["background"])
     for sb in wl.groups:
@@ -166,7 +175,7 @@ def build_glass84(n, rank, dev):
     return wl
 
 
-def build_cube640(n, rank, dev):
+def build_cube640(n, rank, dev, world=1):
     import jaxrenderer_gb300 as jr
     from jaxrenderer_gb300 import _lib, batch as jb
     from jaxrenderer_gb300.jobs import job_from_extra
@@ -186,7 +195,7 @@ def build_cube640(n, rank, dev):
                     config={"scenes": n, "faces": 12, "resolution": [W, H]})
 
 
-def build_overdraw960(n, rank, dev):
+def build_overdraw960(n, rank, dev, world=1):
     from jaxrenderer_gb300 import _lib, batch as jb, synthetic
     from jaxrenderer_gb300.jobs import JobSpec
 
@@ -201,7 +210,7 @@ def build_overdraw960(n, rank, dev):
                             "estimated_overdraw": round(overdraw, 2)})
 
 
-def build_phong128(n, rank, dev):
+def build_phong128(n, rank, dev, world=1):
     from jaxrenderer_gb300 import batch as jb, synthetic
 
     rng = np.random.Generator(np.random.PCG64(synthetic.BASE_SEED + 40 + rank))
@@ -220,7 +229,7 @@ def build_phong128(n, rank, dev):
                     phong=phong)
 
 
-def build_mixed1024(n, rank, dev):
+def build_mixed1024(n, rank, dev, world=1):
     from jaxrenderer_gb300 import batch as jb, synthetic
 
     flat = synthetic.cube_scene_batch(n, seed=synthetic.BASE_SEED + 5 + rank)
@@ -256,7 +265,7 @@ def build_mixed1024(n, rank, dev):
 ANT_FIXTURE = ROOT / "tests" / "golden" / "brax_ant_30.npz"
 
 
-def build_ant84(n, rank, dev):
+def build_ant84(n, rank, dev, world=1):
     """The notebooks' benchmark (84x84/A100.ipynb cells 4-7) on the
     reference's own Brax Ant frames (test_resources/pre-gen-brax/
     inputs-30.zip, held as the pickle-free archive tests/golden/
@@ -269,6 +278,12 @@ def build_ant84(n, rank, dev):
     W = H = 84
     objects, camera, target = brax.load_batched_npz(ANT_FIXTURE)
     frames = [(k + rank * n) % 30 for k in range(n)]
+    # the batch as the notebook's prepare_data makes it (frames cycled), for the get_camera_image e2e
+    idx = np.asarray(frames)
+    cyc = lambda a: np.ascontiguousarray(np.asarray(a)[idx])  # noqa: E731
+    api_objects = [o._replace(model=type(o.model)(*(cyc(x) for x in o.model)), local_scaling=cyc(o.local_scaling),
+                              transform=cyc(o.transform), double_sided=cyc(o.double_sided)) for o in objects]
+    api_camera = type(camera)(*(cyc(x) for x in camera))
     bb = brax.scenes_from_batched(objects, camera, target, frames=frames)
     inst = bb.scenes
     work = inst.n_faces.astype(np.float64) * (2 * W * H)
@@ -284,7 +299,7 @@ def build_ant84(n, rank, dev):
     if dev is not None:
         sb, merge = brax.scene_batch(bb, W, H, dev)
         groups, merges = [sb], [merge]
-    return Workload("ant84", f"Brax Ant 84x84 x {n} frames (the reference's inputs-30.zip frames cycled; 18 objects, "
+    wl = Workload("ant84", f"Brax Ant 84x84 x {n} frames (the reference's inputs-30.zip frames cycled; 18 objects, "
                     "3,276 tris; 960x540 camera), phong_reflection_shadow, device merge + render + uint8 display "
                     "per step", n, chain, work,
                     groups, merges=merges, instances=inst, notebook=True, published=888.6 if n == 200 else None,
@@ -293,6 +308,8 @@ def build_ant84(n, rank, dev):
                     config={"scenes": n, "faces_per_scene": 3276, "resolution": [W, H],
                             "camera_viewport": [960, 540], "shadow_map": [W, H],
                             "published": "888.6 frames/s, A100, batch 200 (notebooks/84x84/A100.ipynb:1308)"})
+    wl.api_inputs = (api_objects, api_camera, cyc(target), bb.light)
+    return wl
 
 
 BUILDERS = {"ant84": build_ant84, "brax84": build_brax84, "cube640": build_cube640, "overdraw960": build_overdraw960,
@@ -489,7 +506,7 @@ def run_ours(args, rank, world, local):
 
         dist.init_process_group("nccl")
     _lib.load()
-    wl = BUILDERS[args.workload](args.scenes, rank, dev)
+    wl = BUILDERS[args.workload](args.scenes, rank, dev, world)
     stream = torch.cuda.current_stream(dev)
     form, form_times = args.form, None
     if args.form == "auto":
@@ -509,7 +526,12 @@ def run_ours(args, rank, world, local):
         for _ in range(args.warmup):
             step()
         ms_per_step = timed(step, args.steps, 0)
-    value = world * wl.frames / (ms_per_step / 1e3)
+    total_frames = wl.frames
+    if world > 1:  # every rank's frames (equal under weak scaling, cost-balanced ranges for brax84)
+        t = torch.tensor([float(wl.frames)], device=dev)
+        torch.distributed.all_reduce(t)
+        total_frames = int(t.item())
+    value = total_frames / (ms_per_step / 1e3)
     prof = profile_kernels(mr, args.steps, stream)
     visible = count_visible(mr)
 
@@ -517,25 +539,37 @@ def run_ours(args, rank, world, local):
     if not args.no_plain:  # the plain form as the reference's method runs: eager, one pass per call
         plain = jb.MultiRunner(wl.groups, form="plain", want_prim_id=False)
         pms = timed(lambda: plain.run(stream), max(1, min(args.steps, 3)), 1)
-        comparison = {"plain_fwd": world * wl.frames / (pms / 1e3), "plain_ms_per_step": pms}
+        comparison = {"plain_fwd": total_frames / (pms / 1e3), "plain_ms_per_step": pms}
         if form == "tiled":
             comparison["tiled_over_plain"] = pms / ms_per_step
         else:  # small workload: the graph-replayed plain form was the faster
             comparison["tiled_graph_ms_per_step"] = form_times["tiled"]
-            comparison["tiled_fwd"] = world * wl.frames / (form_times["tiled"] / 1e3)
+            comparison["tiled_fwd"] = total_frames / (form_times["tiled"] / 1e3)
         del plain
         torch.cuda.empty_cache()
 
     fwd_bwd = {}
     if not args.no_bwd and wl.bwd is not None:
-        fwd_bwd = measure_fwd_bwd(wl, args, stream, timed, world)
+        fwd_bwd = measure_fwd_bwd(wl, args, stream, timed, total_frames)
 
     e2e = None
     if not args.no_e2e:
-        e2e = measure_e2e(wl, mr, step, args, dev, stream, world)
+        e2e = measure_e2e(wl, mr, step, args, dev, stream, total_frames)
+        if wl.notebook and world == 1:
+            # the same frames through the reference's call, Renderer.get_camera_image on batched inputs
+            api = measure_e2e_api(wl, args, dev, stream, total_frames)
+            e2e = dict(api, pipelined=e2e)
 
+    ties = count_near_ties(mr)
     kernels_per_step = prof["launches_per_step"]
     clocks = clk.summary()
+    roof, per_kernel = roofline(prof, visible, clocks)
+    detail = {"kernels": prof["summary"], "per_kernel": per_kernel,
+              "backward_kernels_ms": fwd_bwd.pop("backward_kernels_ms", None), "fwd_bwd_grads": fwd_bwd.pop("grads", None)}
+    detail_path = ROOT / "gpurun_out" / f"bench_{args.workload}_n{world}_detail.json"
+    if rank == 0:
+        detail_path.parent.mkdir(exist_ok=True)
+        detail_path.write_text(json.dumps(detail, indent=1))
     out = {
         "metric": METRIC,
         "value": value,
@@ -563,12 +597,16 @@ def run_ours(args, rank, world, local):
                    % (2 * L2_BYTES >> 20, in_bytes / 1e6)),
             "parallelism": f"scene-sharded x{world} (no collective)",
         }, **wl.config),
+        "fwd_tiled_over_plain": comparison.get("tiled_over_plain"),
+        "fwd_bwd_tiled_over_plain": fwd_bwd.get("tiled_over_plain"),
+        "fwd_bwd_value": fwd_bwd.get("tiled", {}).get("value"),
         "fwd_comparison": comparison,
         "fwd_bwd": fwd_bwd,
-        "roofline": roofline(prof, visible, clocks),
-        "kernels": prof["summary"],
+        "near_ties": ties,
+        "roofline": roof,
         "gpu_launches": kernels_per_step * args.steps,
         "clocks": clocks,
+        "detail_file": str(detail_path.relative_to(ROOT)),
     }
     if e2e is not None:
         out["e2e"] = e2e
@@ -578,6 +616,75 @@ def run_ours(args, rank, world, local):
         print(json.dumps(out), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def count_near_ties(mr):
+    """Pixels whose two best candidate depths lie within 1 ulp of each other
+    (counted by the kernels, resolved exactly by the lowest primitive id), per
+    pass, from one counting render of every scene in the timed form (the
+    tiled form counts with its small-face path off)."""
+    import torch
+
+    from jaxrenderer_gb300 import batch as jb
+
+    out = {"main": 0, "shadow": 0, "main_pixels": 0, "shadow_pixels": 0}
+    for r in mr.runners:
+        rr = jb.BatchRunner(r.sb, form=r.form, want_prim_id=False, count_ties=True)
+        rr.ties.zero_()
+        rr.shadow_ties.zero_()
+        rr.run()
+        torch.cuda.synchronize()
+        out["main"] += int(rr.ties.item())
+        out["main_pixels"] += int(rr.canvas.shape[0] * rr.canvas.shape[1] * rr.canvas.shape[2])
+        if rr.shadow_map is not None:
+            out["shadow"] += int(rr.shadow_ties.item())
+            out["shadow_pixels"] += int(rr.shadow_map.numel())
+        del rr
+    torch.cuda.empty_cache()
+    return out
+
+
+def measure_e2e_api(wl: Workload, args, dev, stream, total_frames):
+    """The notebooks' step through the reference's own call: host-resident
+    batched ModelObjects / CameraParameters / shadow centres ->
+    Renderer.get_camera_image (one batch, set-up cached between calls, the
+    transforms and job tables copied to the device every call) -> uint8
+    display epilogue -> pinned host memory, all inside the timed region."""
+    import torch
+
+    import jaxrenderer_gb300 as jr
+    from jaxrenderer_gb300.utils import display_u8
+
+    objects, camera, target, light = wl.api_inputs
+    W, H = wl.config["resolution"]
+    shadow = jr.ShadowParameters(centre=target)
+    n = int(np.asarray(target).shape[0])
+    out_host = torch.empty((n, H, W, 3), dtype=torch.uint8, pin_memory=True)
+
+    def api_step():
+        img = jr.Renderer.get_camera_image(objects, light, camera, W, H, shadow_param=shadow)
+        out_host.copy_(display_u8(img), non_blocking=True)
+
+    api_step()  # first call: builds and caches the instanced set-up
+    torch.cuda.synchronize(dev)
+    steps = max(1, min(args.steps, 10))
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t0 = time.perf_counter()
+    start.record(stream)
+    for _ in range(steps):
+        api_step()
+    stop.record(stream)
+    torch.cuda.synchronize(dev)
+    wall = (time.perf_counter() - t0) * 1e3 / steps
+    ms = max(start.elapsed_time(stop) / steps, wall)
+    n_obj = len(objects)
+    h2d = n * n_obj * (16 + 3) * 4 + 2 * n * int(np.dtype(wl.groups[0].main_jobs.dtype).itemsize)
+    return {"value": total_frames / (ms / 1e3), "unit": UNIT, "ms_per_step": ms, "steps": steps,
+            "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(out_host.numel()),
+            "inputs": "Renderer.get_camera_image(batched ModelObjects, LightParameters, batched CameraParameters, "
+                      "84, 84, shadow_param=ShadowParameters(centre=batched target)) on host arrays, the "
+                      "notebooks' vmapped call: transforms, local scalings and job tables copied every call",
+            "outputs": "uint8 display images (clamp, x255, transpose_for_display) to pinned host memory"}
 
 
 def choose_form(wl: Workload, dev):
@@ -659,7 +766,7 @@ def count_visible(mr):
     return out
 
 
-def measure_fwd_bwd(wl: Workload, args, stream, timed, world):
+def measure_fwd_bwd(wl: Workload, args, stream, timed, total_frames):
     """Forward + backward per step.  "mse": MSE against a fixed image per
     scene: render (prim-id buffer saved), dL/dcanvas, rast_backward into
     reused gradient arrays (per-vertex, per-texel, per-scene camera/light).
@@ -699,7 +806,7 @@ def measure_fwd_bwd(wl: Workload, args, stream, timed, world):
             runners = mr.runners
             mr = None
         ms = timed(step, steps, warm)
-        out[form] = {"value": world * wl.frames / (ms / 1e3), "ms_per_step": ms, "steps": steps}
+        out[form] = {"value": total_frames / (ms / 1e3), "ms_per_step": ms, "steps": steps}
         if form == "tiled":
             # backward alone, and its kernels (CUDA events inside the library)
             step()
@@ -844,6 +951,7 @@ def pass_info(runner, pass_name):
     if runner.form == "tiled":
         st = runner.stats(pass_name)
         info["E"], info["T"] = float(st.bin_entries), float(st.tiles)
+        info["pixel_tests"] = float(st.pixel_tests)
     return info
 
 
@@ -874,10 +982,30 @@ def kernel_bytes(kname, info, visible):
     return table.get(kname, 0.0)
 
 
+def library_digest() -> str:
+    """SHA-256 (16 hex digits) of the CUDA sources the library is built from."""
+    import hashlib
+
+    h = hashlib.sha256()
+    for p in sorted((ROOT / "jaxrenderer_gb300" / "csrc").glob("*.cu*")):
+        h.update(p.name.encode())
+        h.update(p.read_bytes())
+    return h.hexdigest()[:16]
+
+
+# library_digest() of the sources the NCU_* counts below were captured on:
+# when the kernels change, the counts no longer describe them and the bench
+# reports traffic and the issue figure as null until they are captured again.
+NCU_SOURCE_DIGEST = "none"
+
+
+def ncu_counts_current() -> bool:
+    return library_digest() == NCU_SOURCE_DIGEST
+
+
 # DRAM bytes per unit of work of the forward kernels measured by ncu
 # (dram__bytes_read.sum + dram__bytes_write.sum) on the 256-scene brax-like
-# case (profiles/ncu_forward_tiled_brax84x256.md: 1,470,504 faces per pass,
-# 1,806,336 main-pass pixels): setup_bin 136.6 MB per pass, scatter 12.4 MB,
+# case (ncu capture: 1,470,504 faces per pass, 1,806,336 main-pass pixels): setup_bin 136.6 MB per pass, scatter 12.4 MB,
 # face_varyings 44.1 MB, tiled_shade 108.4 MB.  Their traffic grows with the
 # faces (F) or pixels (P) processed, so a full launch's is this times its
 # units.  The raster kernel's depends on the tile shape the autotuner picks
@@ -905,7 +1033,7 @@ NCU_WARP_INSTR_PER_UNIT = {
 
 # The raster kernel's DRAM bytes and warp instructions per launch, measured by
 # ncu on the full 4096-scene brax-like batch (one-pass metrics, the launches of
-# its first render; profiles/ncu_raster_brax84x4096.md), keyed by (tile width,
+# its first render), keyed by (tile width,
 # tile height, pixels of the pass): its traffic depends on the tile shape and
 # the scenes, so it applies to that workload's launches only.
 NCU_RASTER_LAUNCH = {
@@ -982,7 +1110,12 @@ def roofline(prof, visible, clocks=None):
     r_dom, p_dom, k_dom = prof["where"][dom]
     cfg = r_dom.configs.get(p_dom)
     small = cfg is not None and int(cfg.small_area) > 0
-    measured = raster_launch_counts(cfg, info) if k_dom == "raster_kernel" and info["slots"] == 1 else None
+    current = ncu_counts_current()
+    if not current:
+        traffic_note = (f"null: the kernels changed since the ncu capture the per-unit counts come from "
+                        f"(sources {library_digest()}, capture {NCU_SOURCE_DIGEST})")
+        small = True  # no per-unit counts apply
+    measured = raster_launch_counts(cfg, info) if current and k_dom == "raster_kernel" and info["slots"] == 1 else None
     if measured is not None:
         traffic = float(measured[0])
         traffic_note = "ncu DRAM bytes of this launch on this workload at full size (one-pass metrics)"
@@ -994,6 +1127,7 @@ def roofline(prof, visible, clocks=None):
                         f"{'faces' if unit == 'F' else 'pixels'}")
     out = {
         "bound": "hbm",
+        "limiter": "hbm",
         "kernel": dom,
         "achieved": achieved,
         "peak": peak,
@@ -1002,9 +1136,9 @@ def roofline(prof, visible, clocks=None):
         "frac": achieved / peak,
         "traffic": traffic,
         "traffic_note": traffic_note,
+        "ncu_counts_digest": NCU_SOURCE_DIGEST,
         "algorithmic_bytes_per_launch": alg,
         "avg_launch_ms": ms,
-        "per_kernel": per_kernel,
     }
     if measured is not None:
         out["issue"] = issue_roofline(k_dom, info, ms, clocks, warp_instr=float(measured[1]),
@@ -1013,16 +1147,21 @@ def roofline(prof, visible, clocks=None):
         issue = issue_roofline(k_dom, info, ms, clocks)
         if issue is not None:
             out["issue"] = issue
+    issue = out.get("issue")
+    if issue is not None and issue["frac"] > out["frac"]:
+        out["limiter"] = "issue"  # instruction issue, not DRAM bandwidth, bounds this kernel (frac in "issue")
     kname = prof["where"][dom][2]
     if kname in ("scan_kernel", "raster_kernel"):
-        tests = info["tests"] if kname == "scan_kernel" else None
+        tests = info["tests"] if kname == "scan_kernel" else info.get("pixel_tests")
         out["coverage"] = {"pixel_triangle_tests_per_s": tests / (ms / 1e3) if tests else None,
+                           "pixel_triangle_tests_per_launch": tests or None,
                            "bin_entries": info["E"] or None,
-                           "note": "coverage is FP32-issue bound; issue-slot utilisation in profiles/"}
-    return out
+                           "counted": ("W x H x F of the pass" if kname == "scan_kernel" else
+                                       "in the kernel: staged bin entries x tile pixels, one add per warp")}
+    return out, per_kernel
 
 
-def measure_e2e(wl: Workload, mr, step, args, dev, stream, world):
+def measure_e2e(wl: Workload, mr, step, args, dev, stream, total_frames):
     """Public-API path with host inputs, all inside the timed region:
     instanced workloads copy the objects' transforms and scalings (pinned
     host -> device), rebuild the per-corner pools with rast_merge_objects and
@@ -1121,7 +1260,7 @@ def measure_e2e(wl: Workload, mr, step, args, dev, stream, world):
         stop.record(stream)
         torch.cuda.synchronize(dev)
     ms = start.elapsed_time(stop) / steps
-    out = {"value": world * wl.frames / (ms / 1e3), "unit": UNIT, "ms_per_step": ms,
+    out = {"value": total_frames / (ms / 1e3), "unit": UNIT, "ms_per_step": ms,
            "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h), "steps": steps,
            "inputs": ("object transforms + local scalings; per-corner pools rebuilt on the device "
                       "(rast_merge_objects)") if wl.merges else "per-corner input pools",
@@ -1190,9 +1329,28 @@ def run_reference(args, rank, world, local):
     print(json.dumps(out), flush=True)
 
 
+def launch_ranks(n: int) -> int:
+    """`--gpus N` outside a launcher: start one process per GPU as
+    `python -m torch.distributed.run --nnodes=1 --nproc-per-node N` would
+    (rendezvous on 127.0.0.1) and return their exit status."""
+    import socket
+
+    with socket.socket() as so:
+        so.bind(("127.0.0.1", 0))
+        port = so.getsockname()[1]
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={n}",
+           "--master-addr", "127.0.0.1", f"--master-port={port}", str(Path(__file__).resolve()), *sys.argv[1:]]
+    return subprocess.call(cmd)
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
+    if "WORLD_SIZE" not in os.environ and args.gpus > 1:
+        sys.exit(launch_ranks(args.gpus))
+    if world != args.gpus:
+        print(json.dumps({"error": f"--gpus {args.gpus} but {world} ranks were launched"}), flush=True)
+        sys.exit(2)
     if args.impl == "reference":
         run_reference(args, rank, world, local)
     else:

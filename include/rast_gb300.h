@@ -37,7 +37,8 @@
 extern "C" {
 #endif
 
-#define RAST_ABI_VERSION 2  /* 2: chooser / mix hook fields (RastJob.layers ..., RastPools.face_alpha, RastBatch.max_layers) */
+#define RAST_ABI_VERSION 3  /* 2: chooser / mix hook fields (RastJob.layers ..., RastPools.face_alpha, RastBatch.max_layers);
+                                 3: RastTiledStats.pixel_tests */
 
 /* Built-in shader classes (renderer/shaders/*.py), one kernel path each. */
 typedef enum RastShader {
@@ -287,6 +288,9 @@ typedef struct RastTiledStats {
   uint64_t tiles;         /* tile slots (jobs x tiles of the largest job) */
   uint32_t overflow;      /* 1: some tiles exceeded the capacity and were full-scanned */
   uint32_t reserved;
+  uint64_t pixel_tests;   /* pixel-triangle pairs the raster kernel tested: staged bin entries (those
+                             whose triangle can reach the tile) x the tile's pixels, counted per warp
+                             (faces of the small-face path are not included) */
 } RastTiledStats;
 
 int rast_tiled_stats(const RastBatch* batch, const RastTiledConfig* cfg, const void* workspace,

@@ -124,9 +124,8 @@ def scene_batch_tables(flat, width: int = 84, height: int = 84,
     Ts = int(getattr(flat, "spec_size", None) or T)
     params = camera_params or CameraParameters(viewWidth=width, viewHeight=height, near=0.01, far=1000.0,
                                                hfov=58.0, vfov=58.0, target=np.zeros(3, F32))
-    w2c, w2e, views, viewport = _cameras(flat.camera_position, params, getattr(flat, "camera_target", None))
+    viewport = Renderer.create_camera_from_parameters(params).viewport
     light_dir = normalise(np.asarray(light.direction, F32))
-    light_dir_eye = apply_vec_rows(light_dir, views)
 
     shadow = shadow_param is not None
     mask = np.ones(n, bool) if shadow_mask is None else np.asarray(shadow_mask, bool)
@@ -153,11 +152,8 @@ def scene_batch_tables(flat, width: int = 84, height: int = 84,
     main["spec_w"] = Ts * flat.n_objects
     main["spec_h"] = Ts
     main["viewport"] = np.broadcast_to(viewport.reshape(16), (n, 16))
-    main["world_to_clip"] = w2c.reshape(n, 16)
-    main["world_to_eye_norm"] = w2e.reshape(n, 16)
     main["light_direction"] = light_dir
     main["light_colour"] = np.asarray(light.colour, F32)
-    main["light_dir_eye"] = light_dir_eye
     main["ambient"] = np.asarray(light.ambient, F32)
     main["diffuse"] = np.asarray(light.diffuse, F32)
     main["specular"] = np.asarray(light.specular, F32)
@@ -168,14 +164,6 @@ def scene_batch_tables(flat, width: int = 84, height: int = 84,
         # size; "camera": Renderer.render, the scene camera's viewport
         svp = viewport if shadow_viewport == "camera" else \
             Camera.viewport_matrix(np.zeros(2, np.int32), np.array((sw, sh)), 1.0)
-        centre = np.asarray(shadow_param.centre, F32)
-        if centre.ndim == 2:  # one shadow centre per scene
-            s_w2c, s_w2e = _light_cameras(light.direction, svp, centre, shadow_param.up)
-            scam = Shadow.light_camera(np.asarray(light.direction, F32), svp, centre[0], shadow_param.up)
-        else:
-            scam = Shadow.light_camera(np.asarray(light.direction, F32), svp, centre, shadow_param.up)
-            s_w2c = np.broadcast_to(scam.world_to_clip, (n, 4, 4))
-            s_w2e = np.broadcast_to(scam.world_to_eye_norm, (n, 4, 4))
         sel = np.nonzero(mask)[0]
         shadow_jobs = job_table(len(sel))
         shadow_jobs["shader"] = _lib.SHADER_DEPTH
@@ -188,21 +176,51 @@ def scene_batch_tables(flat, width: int = 84, height: int = 84,
         shadow_jobs["vout_begin"] = np.concatenate([[0], np.cumsum(nvt)[:-1]])
         shadow_jobs["pixel_begin"] = np.arange(len(sel), dtype=np.int64) * sw * sh
         shadow_jobs["viewport"] = svp.reshape(16)
-        shadow_jobs["world_to_clip"] = s_w2c[sel].reshape(-1, 16)
-        shadow_jobs["world_to_eye_norm"] = s_w2e[sel].reshape(-1, 16)
         shadow_jobs["depth_offset"] = np.float32(shadow_param.offset)
         shadow_jobs["flags"] = _lib.JOB_APPLY_DEPTH_OFFSET
         main["shadow_begin"][sel] = shadow_jobs["pixel_begin"]
         main["shadow_w"][sel], main["shadow_h"][sel] = sw, sh
-        main["shadow_viewport"][sel] = scam.viewport.reshape(16)
-        main["shadow_world_to_clip"][sel] = s_w2c[sel].reshape(-1, 16)
+        main["shadow_viewport"][sel] = svp.reshape(16)
         main["shadow_strength"][sel] = np.asarray(shadow_param.strength, F32)
     if shadow_jobs is not None and len(shadow_jobs) == 0:
         shadow_jobs = None
     index = np.full(n, -1, np.int64)
     if shadow_jobs is not None:
         index[np.nonzero(mask)[0]] = np.arange(len(shadow_jobs))
-    return SceneTables(main, shadow_jobs, width, height, sw, sh, index)
+    t = SceneTables(main, shadow_jobs, width, height, sw, sh, index)
+    frame_matrices(t, flat.camera_position, getattr(flat, "camera_target", None), params, light, shadow_param)
+    return t
+
+
+def frame_matrices(t: SceneTables, positions, targets, params: CameraParameters, light: LightParameters,
+                   shadow_param: Optional[ShadowParameters]) -> SceneTables:
+    """Write the per-frame matrices into job tables from scene_batch_tables
+    (in place; same light, shadow set-up and scenes): the cameras at
+    `positions` / `targets` (world_to_clip, world_to_eye_norm and the eye-space
+    light direction of the main pass) and the light cameras at the shadow
+    centres (the depth pass's matrices and the main pass's
+    shadow_world_to_clip).  Each row gets the bits the per-scene set-up
+    (Renderer.create_camera_from_parameters, Shadow.light_camera) gives it."""
+    main = t.main_jobs
+    n = len(main)
+    w2c, w2e, views, _ = _cameras(positions, params, targets)
+    main["world_to_clip"] = w2c.reshape(n, 16)
+    main["world_to_eye_norm"] = w2e.reshape(n, 16)
+    main["light_dir_eye"] = apply_vec_rows(normalise(np.asarray(light.direction, F32)), views)
+    if t.shadow_jobs is not None:
+        svp = t.shadow_jobs["viewport"][0].reshape(4, 4)
+        centre = np.asarray(shadow_param.centre, F32)
+        if centre.ndim == 2:  # one shadow centre per scene
+            s_w2c, s_w2e = _light_cameras(light.direction, svp, centre, shadow_param.up)
+        else:
+            scam = Shadow.light_camera(np.asarray(light.direction, F32), svp, centre, shadow_param.up)
+            s_w2c = np.broadcast_to(scam.world_to_clip, (n, 4, 4))
+            s_w2e = np.broadcast_to(scam.world_to_eye_norm, (n, 4, 4))
+        sel = np.nonzero(t.shadow_index >= 0)[0]
+        t.shadow_jobs["world_to_clip"] = s_w2c[sel].reshape(-1, 16)
+        t.shadow_jobs["world_to_eye_norm"] = s_w2e[sel].reshape(-1, 16)
+        main["shadow_world_to_clip"][sel] = s_w2c[sel].reshape(-1, 16)
+    return t
 
 
 def flat_pools(flat, device) -> Dict[str, torch.Tensor]:
@@ -412,6 +430,7 @@ class BatchRunner:
         self.zbuffer = torch.empty((n, W, H), dtype=torch.float32, device=dev)
         self.prim_id = torch.empty((n, W, H), dtype=torch.int32, device=dev) if want_prim_id else None
         self.ties = torch.zeros(1, dtype=torch.int64, device=dev) if count_ties else None
+        self.shadow_ties = torch.zeros(1, dtype=torch.int64, device=dev) if count_ties else None
         self.shadow_map = None
         self.shadow_prim = None
         self.keep = []
@@ -423,7 +442,8 @@ class BatchRunner:
             self.shadow_map = torch.empty((len(sb.shadow_jobs), sb.shadow_width, sb.shadow_height),
                                           dtype=torch.float32, device=dev)
             self.shadow_prim = torch.empty_like(self.shadow_map, dtype=torch.int32) if want_prim_id else None
-            self.shadow_batch = _rast_batch(sb.shadow_jobs, sb.pools, self.shadow_map, None, self.shadow_prim, None, self.keep)
+            self.shadow_batch = _rast_batch(sb.shadow_jobs, sb.pools, self.shadow_map, None, self.shadow_prim,
+                                            self.shadow_ties, self.keep)
             self.shadow_jobs_dev = self.keep[-1][2]  # device copy of the depth pass's job table (uint8)
             pools = dict(sb.pools)
             pools["shadow_map"] = self.shadow_map

@@ -28,7 +28,7 @@ import numpy as np
 import torch
 
 from . import dispatch
-from .batch import BatchRunner, scene_batch_from_instances, scene_batch_tables
+from .batch import BatchRunner, frame_matrices, scene_batch_from_instances, scene_batch_tables
 from .instancing import InstancedScenes, MeshLibrary
 from .model import Model, merge_objects
 from .pipeline import default_device
@@ -56,7 +56,7 @@ def _first(a, rank: int) -> np.ndarray:
 
 def _same_every_frame(a, rank: int) -> bool:
     a = np.asarray(a)
-    return a.ndim == rank or all(np.array_equal(a[0], a[f]) for f in range(1, a.shape[0]))
+    return a.ndim == rank or bool(np.array_equal(a, np.broadcast_to(a[:1], a.shape)))
 
 
 class _Prepared:
@@ -74,6 +74,19 @@ class _Prepared:
                                                          device, params, shadow_viewport="camera")
         self.form = form
         self.runner = BatchRunner(self.sb, form=form, want_prim_id=False)
+        self.tables = None  # job tables of the last call, and the light / shadow set-up they hold
+        self.setup_key = None
+
+
+def _setup_key(light, shadow_param, params) -> bytes:
+    """Everything in the job tables besides the per-frame matrices."""
+    parts = [np.asarray(x, F32).tobytes() for x in light]
+    if shadow_param is not None:
+        parts += [np.asarray(shadow_param.up, F32).tobytes(), np.asarray(shadow_param.strength, F32).tobytes(),
+                  np.asarray(shadow_param.offset, F32).tobytes(), bytes([np.ndim(shadow_param.centre)])]
+    parts += [repr(tuple(getattr(params, f) for f in ("viewWidth", "viewHeight", "viewDepth", "near", "far", "hfov",
+                                                      "vfov"))).encode(), np.asarray(params.up, F32).tobytes()]
+    return b"|".join(parts)
 
 
 def _structure_key(objects, B, width, height, shadow, form, device):
@@ -197,8 +210,14 @@ def _render_instanced(objects, light, params, pos, tgt, width, height, colour_de
         prep.merge.merge(inst.transforms, inst.local_scaling)
     if shadow_param is not None and np.ndim(shadow_param.centre) == 1:
         shadow_param = shadow_param._replace(centre=np.broadcast_to(np.asarray(shadow_param.centre, F32), (B, 3)))
-    t = scene_batch_tables(inst.shell(), width, height, light, shadow_param, (width, height), params,
-                           shadow_viewport="camera")
+    skey = _setup_key(light, shadow_param, params)
+    if prep.tables is None or prep.setup_key != skey:
+        prep.tables = scene_batch_tables(inst.shell(), width, height, light, shadow_param, (width, height), params,
+                                         shadow_viewport="camera")
+        prep.setup_key = skey
+    else:  # same light and shadow set-up: only the frames' matrices change
+        frame_matrices(prep.tables, pos, tgt, params, light, shadow_param)
+    t = prep.tables
     r = prep.runner
     r.set_job_tables(t.main_jobs, t.shadow_jobs)
     r.set_colour_default(colour_default)

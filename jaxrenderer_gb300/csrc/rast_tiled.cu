@@ -644,6 +644,7 @@ raster_kernel(RastBatch B, Geometry G, const float4* __restrict__ setup,
   float4 (*rec)[3] = s_rec[warp];
   int* ids = s_id[warp];
   unsigned long long tie_count = 0;
+  unsigned long long tests = 0;  // pixel-triangle pairs this warp tested (staged entries x tile pixels)
   unsigned int chunk = 0;
   int taken = kTileChunk;  // tiles of the current chunk already processed
   while (true) {
@@ -735,6 +736,7 @@ raster_kernel(RastBatch B, Geometry G, const float4* __restrict__ setup,
       __syncwarp();
       // prefetch the next chunk while this one is tested
       if (base + kStage + lane < n) fetch(base + kStage + lane, n0, n1, n2, nid);
+      tests += static_cast<unsigned>(m) * static_cast<unsigned>(TW * TH);
       for (int e = 0; e < m; ++e) {
         const float4 a = rec[e][0], b = rec[e][1], cz = rec[e][2];
         const float y0 = y * a.w, y1 = y * b.x, y2 = y * b.y;
@@ -822,6 +824,8 @@ raster_kernel(RastBatch B, Geometry G, const float4* __restrict__ setup,
     for (int o = 16; o > 0; o >>= 1) tie_count += __shfl_xor_sync(0xffffffffu, tie_count, o);
     if (lane == 0 && tie_count) atomicAdd(B.near_ties, tie_count);
   }
+  // tests is warp-uniform: one add per warp (work + 4: the launch's 64-bit test counter)
+  if (lane == 0 && tests) atomicAdd(reinterpret_cast<unsigned long long*>(work + 4), tests);
 }
 
 // Vertex varyings of the three corners of every face some pixel needs
@@ -1081,7 +1085,8 @@ static int render(const RastBatch* batch, const RastTiledConfig* cfg, void* work
   uint32_t* bsums = reinterpret_cast<uint32_t*>(ws + L.bsums_off);
   int32_t* bins = reinterpret_cast<int32_t*>(ws + L.bins_off);
   int32_t* winner = reinterpret_cast<int32_t*>(ws + L.winner_off);
-  unsigned int* misc = reinterpret_cast<unsigned int*>(ws + L.misc_off);  // [0] work, [1] status
+  // [0] raster tile counter, [1] overflow status, [2..3] bin entries, [4..5] raster pixel tests
+  unsigned int* misc = reinterpret_cast<unsigned int*>(ws + L.misc_off);
   Profiler prof(profile, s);
 
   // counts and cursors are adjacent: one memset clears both, plus the counters
@@ -1188,13 +1193,14 @@ extern "C" int rast_tiled_stats(const RastBatch* batch, const RastTiledConfig* c
   if (shape_status != RAST_OK) return shape_status;
   const uint64_t cap = cfg && cfg->bin_capacity > 0 ? cfg->bin_capacity : tiled::default_bin_capacity(*batch);
   const tiled::Layout L = tiled::layout(*batch, ts, cap, tiled::small_area_of(cfg));
-  unsigned int misc[4] = {0, 0, 0, 0};
+  unsigned int misc[6] = {0, 0, 0, 0, 0, 0};
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   if (cudaMemcpyAsync(misc, static_cast<const char*>(workspace) + L.misc_off, sizeof(misc),
                       cudaMemcpyDeviceToHost, s) != cudaSuccess)
     return RAST_ERR_CUDA;
   if (cudaStreamSynchronize(s) != cudaSuccess) return RAST_ERR_CUDA;
   out->bin_entries = static_cast<uint64_t>(misc[2]) | (static_cast<uint64_t>(misc[3]) << 32);
+  out->pixel_tests = static_cast<uint64_t>(misc[4]) | (static_cast<uint64_t>(misc[5]) << 32);
   out->overflow = misc[1];
   out->tiles = static_cast<uint64_t>(L.n_tiles);
   out->bin_capacity = L.bin_capacity;

@@ -116,6 +116,15 @@ class InstancedScenes:
             if b > a and (sh[a:b, 0].max() != T or sh[a:b, 1].max() != T):
                 raise ValueError(f"scene {s}: its largest diffuse map is not {T}x{T}")
 
+    def subset(self, begin: int, end: int) -> "InstancedScenes":
+        """Scenes [begin, end) as their own batch (the mesh library shared)."""
+        i0, i1 = int(self.scene_begin[begin]), int(self.scene_begin[end])
+        cut = lambda a: None if a is None else a[begin:end]  # noqa: E731
+        return InstancedScenes(self.library, self.mesh[i0:i1], self.scene_begin[begin : end + 1] - i0,
+                               self.transforms[i0:i1], self.local_scaling[i0:i1], self.diffuse[i0:i1],
+                               self.specular[i0:i1], self.camera_position[begin:end], cut(self.camera_target),
+                               None if self.texture_shape is None else self.texture_shape[i0:i1])
+
     def _mesh_counts(self, field: str) -> np.ndarray:
         return self.library.table[field][self.mesh].astype(np.int64)
 

@@ -161,3 +161,23 @@ def test_batch_axis_detection_and_frame_selection():
     assert int(cam.viewWidth) == 960
     with pytest.raises(ValueError):
         R._batch_size(camera, jr.ShadowParameters(centre=np.zeros((3, 3), F32)))
+
+
+def test_frame_matrices_refresh_equals_a_full_table_build():
+    """batch.frame_matrices (the per-call update of the batched
+    get_camera_image path) writes what scene_batch_tables builds."""
+    from pathlib import Path
+
+    from jaxrenderer_gb300 import batch as jb, brax
+
+    objects, camera, target = brax.load_batched_npz(Path(__file__).resolve().parent / "golden" / "brax_ant_30.npz")
+    bb = brax.scenes_from_batched(objects, camera, target)
+    shell = bb.scenes.shell()
+    t = jb.scene_batch_tables(shell, 84, 84, bb.light, bb.shadow, (84, 84), bb.camera, shadow_viewport="camera")
+    order = np.arange(30)[::-1].copy()
+    shell.camera_position, shell.camera_target = shell.camera_position[order], shell.camera_target[order]
+    moved = bb.shadow._replace(centre=bb.shadow.centre[order])
+    want = jb.scene_batch_tables(shell, 84, 84, bb.light, moved, (84, 84), bb.camera, shadow_viewport="camera")
+    jb.frame_matrices(t, shell.camera_position, shell.camera_target, bb.camera, bb.light, moved)
+    assert t.main_jobs.tobytes() == want.main_jobs.tobytes()
+    assert t.shadow_jobs.tobytes() == want.shadow_jobs.tobytes()
