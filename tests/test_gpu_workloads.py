@@ -1,9 +1,13 @@
 """GPU parity on the benchmark workloads beyond the 84x84 batch: the
 389,120-triangle overdraw scene (tiled == plain bit-exact on the full frame,
-the oracle on a band of columns) and the mixed-resolution / mixed-shader
-batch rendered through one MultiRunner graph (tiled == plain, the oracle on
-a few scenes of every resolution class, backward of both forms)."""
+near ties counted alike; the oracle on bands of columns, near ties
+included) and the mixed-resolution / mixed-shader batch at its configured
+triangle counts (log-uniform 100 .. 100,000 per scene) rendered through one
+MultiRunner graph (tiled == plain, the oracle on the smallest and the
+largest scenes of every resolution class, the largest also with its bins
+forced to overflow; backward of both forms)."""
 import copy
+import os
 
 import numpy as np
 import pytest
@@ -17,6 +21,7 @@ from tests.test_gpu_plain import assert_parity
 pytestmark = pytest.mark.gpu
 F32 = np.float32
 CLASSES = [(32, 32), (84, 84), (480, 270)]
+THREADS = max(1, len(os.sched_getaffinity(0)))
 
 
 @pytest.fixture(scope="module")
@@ -68,18 +73,32 @@ def band(spec: JobSpec, i0: int, w: int) -> JobSpec:
     return b
 
 
-def test_overdraw_scene_band_matches_oracle(overdraw):
+@pytest.mark.parametrize("i0,w", [(468, 24), (150, 16)])
+def test_overdraw_scene_band_matches_oracle_near_ties_included(cuda_device, overdraw, i0, w):
+    """Bands of columns (the middle of the frame, where the spheres pile up
+    and duplicates tie exactly, and one off centre): the full frame's pixels
+    bit-exact, and the band rendered alone counts the oracle's near ties
+    (the tie rule: shader.py:207-251, argmin, first index)."""
     spec, z0, c0, out = overdraw
     z, c, p, _ = out["tiled"]
-    i0, w = 468, 24  # the middle of the frame, where the spheres pile up
-    ref = oracle.render(band(spec, i0, w), z0[i0 : i0 + w], c0[i0 : i0 + w])
+    bspec = band(spec, i0, w)
+    ref = oracle.render(bspec, z0[i0 : i0 + w], c0[i0 : i0 + w], n_threads=THREADS)
     assert_parity(z[i0 : i0 + w], c[i0 : i0 + w], p[i0 : i0 + w], ref, "overdraw band")
+    for form in ("plain", "tiled"):
+        packed = pack([bspec], [z0[i0 : i0 + w]], [c0[i0 : i0 + w]], cuda_device, count_ties=True)
+        if form == "plain":
+            render_plain(packed)
+        else:
+            render_tiled(packed, tile=(8, 8))
+        assert int(packed.near_ties.item()) == ref["near_ties"], form
+    if i0 == 468:
+        assert ref["near_ties"] > 0  # the band holds ties
 
 
 @pytest.fixture(scope="module")
 def mixed(cuda_device):
     n = 36
-    flat = synthetic.cube_scene_batch(n, seed=synthetic.BASE_SEED + 15, f_min=100, f_max=20_000)
+    flat = synthetic.cube_scene_batch(n, seed=synthetic.BASE_SEED + 17, f_min=100, f_max=100_000)
     rng = np.random.Generator(np.random.PCG64(synthetic.BASE_SEED + 16))
     res = np.arange(n) % 3
     rng.shuffle(res)
@@ -115,27 +134,56 @@ def test_mixed_batch_graph_tiled_equals_plain(mixed):
 
 def test_mixed_batch_matches_oracle(mixed):
     flat, res, shadow, groups = mixed
+    assert int(flat.n_faces.max()) >= 80_000 and int((flat.n_faces >= 50_000).sum()) >= 3
     for c, (idx, sb) in enumerate(groups):
         w, h = CLASSES[c]
         sub = synthetic.flat_subset(flat, idx)
         tables = jb.scene_batch_tables(sub, w, h, shadow_size=(w, h), shadow_mask=shadow[idx])
         out = jb.MultiRunner([sb], form="tiled").run()[0]
-        # the cheapest scene with and the cheapest without a shadow pass
+        # the cheapest scene with and the cheapest without a shadow pass, and the largest scene
         picks = []
         for want in (True, False):
             cand = [k for k in np.argsort(sub.n_faces) if bool(shadow[idx[k]]) == want]
             if cand:
                 picks.append(int(cand[0]))
+        picks.append(int(np.argmax(sub.n_faces)))
         for k in picks:
             dspec, mspec = jb.scene_job_specs(sub, tables, k)
             if dspec is not None:
-                dref = oracle.render(dspec, np.full((w, h), np.finfo(F32).max, F32))
+                dref = oracle.render(dspec, np.full((w, h), np.finfo(F32).max, F32), n_threads=THREADS)
                 srow = int(tables.shadow_index[k])
                 np.testing.assert_array_equal(out.shadow_map[srow].cpu().numpy().view(np.uint32),
                                               dref["zbuffer"].view(np.uint32))
                 mspec.shadow_map = dref["zbuffer"]
-            ref = oracle.render(mspec, np.ones((w, h), F32), np.ones((w, h, 3), F32))
-            assert_parity(out.zbuffer[k], out.canvas[k], out.prim_id[k], ref, f"class {w}x{h} scene {k}")
+            ref = oracle.render(mspec, np.ones((w, h), F32), np.ones((w, h, 3), F32), n_threads=THREADS)
+            assert_parity(out.zbuffer[k], out.canvas[k], out.prim_id[k], ref,
+                          f"class {w}x{h} scene {k} ({int(sub.n_faces[k])} faces)")
+
+
+def test_largest_mixed_scene_with_overflowing_bins_matches_oracle(cuda_device, mixed):
+    """The largest 480x270 scene of the batch (tens of thousands of
+    triangles) rendered with a bin capacity far below what it requests:
+    tiles whose bins overflow fall back to a scan of the whole job, with the
+    same results."""
+    flat, res, shadow, groups = mixed
+    c = 2
+    idx, _ = groups[c]
+    w, h = CLASSES[c]
+    sub = synthetic.flat_subset(flat, idx)
+    k = int(np.argmax(sub.n_faces))
+    tables = jb.scene_batch_tables(sub, w, h, shadow_size=(w, h), shadow_mask=np.zeros(len(idx), bool))
+    _, mspec = jb.scene_job_specs(sub, tables, k)
+    z0, c0 = np.ones((w, h), F32), np.ones((w, h, 3), F32)
+    packed = pack([mspec], [z0], [c0], cuda_device)
+    full = render_tiled(packed, tile=(16, 16), bin_capacity=64 * mspec.n_faces)
+    assert full.overflow == 0 and full.bin_entries > 10_000
+    small = pack([mspec], [z0], [c0], cuda_device)
+    st = render_tiled(small, tile=(16, 16), bin_capacity=int(full.bin_entries // 8))
+    assert st.overflow == 1
+    ref = oracle.render(mspec, z0, c0, n_threads=THREADS)
+    for pk, what in ((packed, "fitting bins"), (small, "overflowing bins")):
+        zz, cc, pp = unpack(pk, [mspec])[0]
+        assert_parity(zz, cc, pp, ref, f"{int(sub.n_faces[k])}-face scene, {what}")
 
 
 def test_mixed_batch_backward_tiled_matches_plain(mixed):
