@@ -1277,6 +1277,35 @@ def measure_e2e(wl: Workload, mr, step, args, dev, stream, total_frames):
         b.record(stream)
         torch.cuda.synchronize(dev)
         out["device_merge_ms"] = a.elapsed_time(b) / steps
+    out["link"] = copy_rates(dev, h2d, d2h)
+    return out
+
+
+def copy_rates(dev, h2d_bytes: int, d2h_bytes: int, reps: int = 3):
+    """Host <-> device copy rates of one step's bytes, pinned host memory,
+    one cudaMemcpyAsync each way on an idle stream (outside the timed
+    region): what the e2e step's copies cost on this machine's link."""
+    import torch
+
+    out = {}
+    s = torch.cuda.Stream(dev)
+    for name, nbytes in (("h2d", h2d_bytes), ("d2h", d2h_bytes)):
+        if nbytes <= 0:
+            continue
+        host = torch.empty(int(nbytes), dtype=torch.uint8, pin_memory=True)
+        devbuf = torch.empty(int(nbytes), dtype=torch.uint8, device=dev)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(s):
+            (devbuf.copy_(host, non_blocking=True) if name == "h2d" else host.copy_(devbuf, non_blocking=True))
+            a.record(s)
+            for _ in range(reps):
+                (devbuf.copy_(host, non_blocking=True) if name == "h2d" else host.copy_(devbuf, non_blocking=True))
+            b.record(s)
+        torch.cuda.synchronize(dev)
+        ms = a.elapsed_time(b) / reps
+        out[f"{name}_gbs"] = nbytes / (ms / 1e3) / 1e9
+        out[f"{name}_ms_per_step"] = ms
+        del host, devbuf
     return out
 
 

@@ -604,7 +604,9 @@ class BatchRunner:
         with torch.cuda.stream(s):
             self._reset(zbuffer_default)
             for name, _ in self.batches():
+                torch.cuda.nvtx.range_push(f"{name} pass")
                 self.launch(name, s.cuda_stream)
+                torch.cuda.nvtx.range_pop()
         return self.outputs()
 
     def outputs(self) -> BatchOutputs:

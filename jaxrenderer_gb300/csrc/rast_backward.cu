@@ -1192,7 +1192,7 @@ static int run(const RastBatch* batch, const float* grad_canvas, const float* gr
          L.vacc_stride,
          reinterpret_cast<const int2*>(ws + L.fmap_off), reinterpret_cast<const int2*>(ws + L.vmap_off),
          reinterpret_cast<unsigned*>(ws + L.start_off)};
-  Profiler prof(profile, s);
+  Profiler prof(profile, s, "rast_backward");
   if (cudaMemsetAsync(w.fvis, 0, static_cast<size_t>(b.total_setup), s) != cudaSuccess) return RAST_ERR_CUDA;
   if (cudaMemsetAsync(w.vvis, 0, static_cast<size_t>(b.total_vout), s) != cudaSuccess) return RAST_ERR_CUDA;
   const int mask = b.shader_mask;

@@ -35,6 +35,7 @@ display_kernel(const float* __restrict__ canvas, int width, int height, int chan
 extern "C" int rast_display_u8(const float* canvas, int64_t n_images, int32_t width, int32_t height,
                                int32_t channels, int32_t flip_vertical, uint8_t* out, void* stream) {
   using namespace rast;
+  NvtxRange range("rast_display_u8");
   if (n_images < 0 || width < 0 || height < 0 || channels <= 0) return RAST_ERR_INVALID_ARGUMENT;
   if (n_images == 0 || width == 0 || height == 0) return RAST_OK;
   if (!canvas || !out) return RAST_ERR_INVALID_ARGUMENT;

@@ -3,6 +3,8 @@
 // barycentrics, fragment, mixer) and buffer merge.
 #pragma once
 
+#include <nvtx3/nvToolsExt.h>
+
 #include <cstddef>
 #include <cstdint>
 
@@ -528,12 +530,25 @@ __device__ __forceinline__ void store_pixel(const RastJob& J, const RastPools& P
 }
 
 // Optional per-kernel event timing of an entry point (RastProfile).
+// NVTX range over one entry point's host-side launch sequence (header-only
+// NVTX3: without a profiler attached a push / pop is a check of a null hook).
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange&) = delete;
+  NvtxRange& operator=(const NvtxRange&) = delete;
+};
+
+// Per-kernel CUDA-event timing of an entry point (the *_profiled entry
+// points) and its NVTX annotation: a range named after the entry point and
+// one NVTX mark per kernel launched, named after the kernel.
 struct Profiler {
   RastProfile* prof;
   cudaStream_t stream;
   cudaEvent_t ev[17];
   int n = 0;
-  Profiler(RastProfile* p, cudaStream_t s) : prof(p), stream(s) {
+  NvtxRange range;
+  Profiler(RastProfile* p, cudaStream_t s, const char* entry) : prof(p), stream(s), range(entry) {
     if (prof) {
       prof->n = 0;
       cudaEventCreate(&ev[0]);
@@ -541,6 +556,7 @@ struct Profiler {
     }
   }
   void mark(const char* name) {
+    nvtxMarkA(name);
     if (!prof || n >= 16) return;
     cudaEventCreate(&ev[n + 1]);
     cudaEventRecord(ev[n + 1], stream);

@@ -367,5 +367,6 @@ extern "C" size_t rast_merge_workspace_bytes(const RastMergeBatch* batch) {
 
 extern "C" int rast_merge_objects(const RastMergeBatch* batch, void* workspace, size_t workspace_bytes,
                                   void* stream) {
+  rast::NvtxRange range("rast_merge_objects");
   return merge::run(batch, workspace, workspace_bytes, stream);
 }

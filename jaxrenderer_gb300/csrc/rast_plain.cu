@@ -215,7 +215,7 @@ static int render_plain(const RastBatch* batch, void* workspace, size_t workspac
   float* var = reinterpret_cast<float*>(ws + L.var_off);
   float4* setup = reinterpret_cast<float4*>(ws + L.setup_off);
   int32_t* winner = reinterpret_cast<int32_t*>(ws + L.winner_off);
-  Profiler prof(profile, s);
+  Profiler prof(profile, s, "rast_render_plain");
 
   if (b.total_vout > 0) {
     const dim3 grid(static_cast<unsigned>((b.max_verts + 255) / 256), static_cast<unsigned>(b.n_jobs));

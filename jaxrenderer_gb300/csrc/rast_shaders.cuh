@@ -38,9 +38,9 @@ __device__ __forceinline__ void load3(const float* p, int64_t row, float* out) {
 
 // Vertex shader of job J for vertex row `v` (0-based within the job).
 // Writes gl_Position (clip, 4) and the shader's varyings (var).
-// depth.py:47-61, gouraud.py:119-149, gouraud_texture.py:253-286,
-// phong.py:430-456, phong_darboux.py:120-170, phong_reflection.py:104-132,
-// phong_reflection_shadow.py:373-408.
+// depth.py:47-61, gouraud.py:58-88, gouraud_texture.py:68-101,
+// phong.py:78-104, phong_darboux.py:120-170, phong_reflection.py:104-132,
+// phong_reflection_shadow.py:115-150.
 // kClip = false skips gl_Position (the deferred shading re-run needs only
 // the varyings).
 template <bool kClip = true>
@@ -135,7 +135,7 @@ __device__ __forceinline__ bool fragment_shader(const RastJob& J, const RastPool
   switch (sh) {
     case RAST_SHADER_DEPTH:  // shader.py:333
       return true;
-    case RAST_SHADER_GOURAUD: {  // gouraud.py:155-185
+    case RAST_SHADER_GOURAUD: {  // gouraud.py:94-124
       bool ok = front;
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
@@ -144,7 +144,7 @@ __device__ __forceinline__ bool fragment_shader(const RastJob& J, const RastPool
       }
       return ok;
     }
-    case RAST_SHADER_GOURAUD_TEXTURE: {  // gouraud_texture.py:292-329
+    case RAST_SHADER_GOURAUD_TEXTURE: {  // gouraud_texture.py:107-144
       const float u = interp1(b, v0[kVUvG], v1[kVUvG], v2[kVUvG]);
       const float w = interp1(b, v0[kVUvG + 1], v1[kVUvG + 1], v2[kVUvG + 1]);
       const int ui = pymod(f2i(floorf(u)), J.tex_w);
@@ -161,7 +161,7 @@ __device__ __forceinline__ bool fragment_shader(const RastJob& J, const RastPool
       return ok;
     }
     case RAST_SHADER_PHONG:
-    case RAST_SHADER_PHONG_DARBOUX: {  // phong.py:462-516, phong_darboux.py:212-293
+    case RAST_SHADER_PHONG_DARBOUX: {  // phong.py:110-164, phong_darboux.py:212-293
       float nrm[3], n[3];
 #pragma unroll
       for (int c = 0; c < 3; ++c) nrm[c] = interp1(b, v0[kVNormal + c], v1[kVNormal + c], v2[kVNormal + c]);
@@ -216,7 +216,7 @@ __device__ __forceinline__ bool fragment_shader(const RastJob& J, const RastPool
     }
     case RAST_SHADER_PHONG_REFLECTION:
     case RAST_SHADER_PHONG_REFLECTION_SHADOW: {
-      // phong_reflection.py:158-235, phong_reflection_shadow.py:436-529
+      // phong_reflection.py:158-235, phong_reflection_shadow.py:178-271
       const bool shadowed = sh == RAST_SHADER_PHONG_REFLECTION_SHADOW;
       float shadow[3] = {1.0f, 1.0f, 1.0f};
       if (shadowed) {

@@ -1087,7 +1087,7 @@ static int render(const RastBatch* batch, const RastTiledConfig* cfg, void* work
   int32_t* winner = reinterpret_cast<int32_t*>(ws + L.winner_off);
   // [0] raster tile counter, [1] overflow status, [2..3] bin entries, [4..5] raster pixel tests
   unsigned int* misc = reinterpret_cast<unsigned int*>(ws + L.misc_off);
-  Profiler prof(profile, s);
+  Profiler prof(profile, s, "rast_render_tiled");
 
   // counts and cursors are adjacent: one memset clears both, plus the counters
   if (cudaMemsetAsync(counts, 0, L.offsets_off - L.counts_off, s) != cudaSuccess) return RAST_ERR_CUDA;

@@ -1,4 +1,4 @@
-"""GouraudShader (renderer/shaders/gouraud.py:82-185)."""
+"""GouraudShader (renderer/shaders/gouraud.py:49-124)."""
 from typing import Any, NamedTuple
 
 from .. import _lib

@@ -1,4 +1,4 @@
-"""GouraudTextureShader (renderer/shaders/gouraud_texture.py:207-352)."""
+"""GouraudTextureShader (renderer/shaders/gouraud_texture.py:55-167)."""
 from typing import Any, NamedTuple
 
 from .. import _lib

@@ -1,4 +1,4 @@
-"""PhongTextureShader (renderer/shaders/phong.py:374-539)."""
+"""PhongTextureShader (renderer/shaders/phong.py:65-187)."""
 from typing import Any, NamedTuple
 
 from .. import _lib

@@ -269,7 +269,7 @@ static void vertex_shader(const Scene* s, int v, VOut* o) {
   switch (s->shader) {
     case OR_SHADER_DEPTH: /* depth.py:47-61 */
       break;
-    case OR_SHADER_GOURAUD: { /* gouraud.py:119-149 */
+    case OR_SHADER_GOURAUD: { /* gouraud.py:58-88 */
       real n[3], l[3];
       normalise3(s->normal + 3 * v, n);
       normalise3(s->light_direction, l);
@@ -277,7 +277,7 @@ static void vertex_shader(const Scene* s, int v, VOut* o) {
       for (int c = 0; c < 3; ++c) o->var[V_COLOUR + c] = (s->colour[3 * v + c] * s->light_colour[c]) * intensity;
       break;
     }
-    case OR_SHADER_GOURAUD_TEXTURE: { /* gouraud_texture.py:253-286 */
+    case OR_SHADER_GOURAUD_TEXTURE: { /* gouraud_texture.py:68-101 */
       real n[3], l[3];
       normalise3(s->normal + 3 * v, n);
       normalise3(s->light_direction, l);
@@ -291,8 +291,8 @@ static void vertex_shader(const Scene* s, int v, VOut* o) {
     case OR_SHADER_PHONG_REFLECTION:
     case OR_SHADER_PHONG_REFLECTION_SHADOW:
     case OR_SHADER_PHONG_DARBOUX: {
-      /* phong.py:430-456, phong_reflection.py:104-132,
-       * phong_reflection_shadow.py:373-408, phong_darboux.py:120-170 */
+      /* phong.py:78-104, phong_reflection.py:104-132,
+       * phong_reflection_shadow.py:115-150, phong_darboux.py:120-170 */
       real n1[3];
       normalise3(s->normal + 3 * v, n1);
       apply_vec(s->world_to_eye_norm, n1, o->var + V_NORMAL);
@@ -407,7 +407,7 @@ static int fragment(const Scene* s, const VOut* v0, const VOut* v1, const VOut* 
   switch (s->shader) {
     case OR_SHADER_DEPTH: /* shader.py:333 default fragment */
       return 1;
-    case OR_SHADER_GOURAUD: { /* gouraud.py:155-185 */
+    case OR_SHADER_GOURAUD: { /* gouraud.py:94-124 */
       int ok = front;
       for (int c = 0; c < 3; ++c) {
         colour[c] = var[V_COLOUR + c];
@@ -416,7 +416,7 @@ static int fragment(const Scene* s, const VOut* v0, const VOut* v1, const VOut* 
       *branch = branch_sig(0, 0, ok);
       return ok;
     }
-    case OR_SHADER_GOURAUD_TEXTURE: { /* gouraud_texture.py:292-329 */
+    case OR_SHADER_GOURAUD_TEXTURE: { /* gouraud_texture.py:107-144 */
       int u = pymod(f2i(R_FLOOR(var[V_UVG + 0])), s->tex_w);
       int w = pymod(f2i(R_FLOOR(var[V_UVG + 1])), s->tex_h);
       real tc[3];
@@ -430,7 +430,7 @@ static int fragment(const Scene* s, const VOut* v0, const VOut* v1, const VOut* 
       *branch = branch_sig(u, w, ok);
       return ok;
     }
-    case OR_SHADER_PHONG: { /* phong.py:462-516 */
+    case OR_SHADER_PHONG: { /* phong.py:110-164 */
       int u = pymod(f2i(R_FLOOR(var[V_UV + 0])), s->tex_w);
       int w = pymod(f2i(R_FLOOR(var[V_UV + 1])), s->tex_h);
       real tc[3], n[3], l[3], lc[3];
@@ -496,7 +496,7 @@ static int fragment(const Scene* s, const VOut* v0, const VOut* v1, const VOut* 
     }
     case OR_SHADER_PHONG_REFLECTION:
     case OR_SHADER_PHONG_REFLECTION_SHADOW: {
-      /* phong_reflection.py:158-235, phong_reflection_shadow.py:436-529 */
+      /* phong_reflection.py:158-235, phong_reflection_shadow.py:178-271 */
       int shadowed = s->shader == OR_SHADER_PHONG_REFLECTION_SHADOW;
       int shadow_bit = 0;
       real shadow[3] = {(real)1, (real)1, (real)1};

@@ -104,7 +104,7 @@ def test_ties_go_to_the_lowest_primitive():
 def test_back_facing_first_primitive_fallback():
     # primitive 0 back-facing and alone: the default chooser falls back to
     # index 0; DepthShader (no front-facing test in its fragment) writes it,
-    # Gouraud discards it (shader.py:215-217, gouraud.py:171-183).
+    # Gouraud discards it (shader.py:215-217, gouraud.py:94-124).
     spec = _two_triangle_job(_lib.SHADER_DEPTH, second_offset=-50.0, flip_first=True)
     spec.faces = spec.faces[:1]
     z0, _ = scenes.initial_buffers(spec)
