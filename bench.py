@@ -589,7 +589,7 @@ def run_ours(args, rank, world, local):
                 "" if form_times is None else
                 ", the faster of the two forms on this workload (" +
                 ", ".join(f"{k} {v:.3f} ms" for k, v in form_times.items()) + " per step)"),
-            "tiled_config": {name: [c.tile_w, c.tile_h, int(c.bin_capacity), int(c.small_area)]
+            "tiled_config": {name: [c.tile_w, c.tile_h, int(c.bin_capacity), int(c.small_area), int(c.warps_per_tile)]
                              for name, r, p in prof["passes"]
                              for c in [r.configs.get(p)] if c is not None},
             "l2": ("inputs larger than L2 (input pools %.2f GB)" % (in_bytes / 1e9)) if not flush else
@@ -1045,7 +1045,7 @@ NCU_RASTER_LAUNCH = {
 def raster_launch_counts(cfg, info):
     """(DRAM bytes, warp instructions) of a raster launch measured on this
     very configuration, or None."""
-    if cfg is None:
+    if cfg is None or int(getattr(cfg, "warps_per_tile", 1)) > 1:
         return None
     return NCU_RASTER_LAUNCH.get((int(cfg.tile_w), int(cfg.tile_h), int(round(info["P"]))))
 

@@ -37,8 +37,8 @@
 extern "C" {
 #endif
 
-#define RAST_ABI_VERSION 3  /* 2: chooser / mix hook fields (RastJob.layers ..., RastPools.face_alpha, RastBatch.max_layers);
-                                 3: RastTiledStats.pixel_tests */
+#define RAST_ABI_VERSION 4  /* 2: chooser / mix hook fields (RastJob.layers ..., RastPools.face_alpha, RastBatch.max_layers);
+                                 3: RastTiledStats.pixel_tests; 4: RastTiledConfig.warps_per_tile, rast_autotune */
 
 /* Built-in shader classes (renderer/shaders/*.py), one kernel path each. */
 typedef enum RastShader {
@@ -217,8 +217,9 @@ typedef struct RastProfile {
 int rast_render_plain_profiled(const RastBatch* batch, void* workspace, size_t workspace_bytes,
                                void* stream, RastProfile* profile);
 
-/* Tiled form parameters (chosen by the autotuner).  Zero fields take the
- * defaults: 8x8 tiles, bin capacity of 4 entries per face. */
+/* Tiled form parameters (chosen by the autotuner, rast_autotune).  Zero
+ * fields take the defaults: 8x8 tiles, bin capacity of 4 entries per face,
+ * no small-face path, one warp per tile. */
 typedef struct RastTiledConfig {
   int32_t tile_w;          /* tile (w, h) pixels along x (buffer axis 0) and y (axis 1): */
   int32_t tile_h;          /* 8x8, 16x8, 16x16, 32x8, 8x32, 8x4 or 4x8 */
@@ -227,7 +228,8 @@ typedef struct RastTiledConfig {
                               many pixels are rasterised by the setup kernel (64-bit atomicMin of the
                               packed key per pixel) instead of being binned; ignored while near ties
                               are counted */
-  int32_t reserved;
+  int32_t warps_per_tile;  /* 0 or 1: one warp rasterises a tile; 2: two warps each take half of the
+                              tile's rows (bins stay per tile): tile shapes 8x8, 8x16 and 16x16 */
 } RastTiledConfig;
 
 /* Workspace bytes rast_render_tiled needs for `batch` under `cfg` (NULL = defaults);
@@ -279,6 +281,21 @@ int rast_render_tiled_profiled(const RastBatch* batch, const RastTiledConfig* cf
  * Outputs, statuses and results are those of rast_render_tiled. */
 #define RAST_STATIC_SCRATCH_BYTES (64u << 20)
 int rast_render_tiled_static(const RastBatch* batch, const RastTiledConfig* cfg, void* stream);
+
+/* Autotuner of the tiled form: renders `batch` with every configuration the
+ * tiled form has a kernel for (tile shape, small-face path off / on at 32
+ * pixels, one or two warps per tile; the layered shapes for batches with
+ * layered jobs), each with a bin capacity of 1.25x the entries its shape
+ * requests, times three renders of each with CUDA events on `stream` and
+ * writes the fastest to *out.  Results are cached in the library per
+ * workload class (canvas size, faces per job and jobs rounded to powers of
+ * two, shaders, layers, tie counting, device), guarded by a mutex; a cached
+ * class returns at once without rendering.  The renders write the batch's
+ * output pools: their contents afterwards are unspecified (render again).
+ * Allocates its own workspace (cudaMallocAsync / cudaFreeAsync on `stream`)
+ * and synchronises `stream`.  No counterpart call exists in the reference
+ * (JAX compiles one form). */
+int rast_autotune(const RastBatch* batch, void* stream, RastTiledConfig* out);
 
 /* Bin statistics of the last rast_render_tiled call that used `workspace`
  * (synchronises `stream`; for autotuning and diagnostics). */

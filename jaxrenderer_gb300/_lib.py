@@ -20,7 +20,7 @@ SHADER_PHONG_DARBOUX = 4
 SHADER_PHONG_REFLECTION = 5
 SHADER_PHONG_REFLECTION_SHADOW = 6
 
-ABI_VERSION = 3  # RAST_ABI_VERSION of the header these structures mirror
+ABI_VERSION = 4  # RAST_ABI_VERSION of the header these structures mirror
 
 JOB_APPLY_DEPTH_OFFSET = 1
 JOB_FACE_ALPHA = 2
@@ -146,7 +146,7 @@ class RastProfile(ctypes.Structure):
 
 class RastTiledConfig(ctypes.Structure):
     _fields_ = [("tile_w", c_int32), ("tile_h", c_int32), ("bin_capacity", c_uint64), ("small_area", c_int32),
-                ("reserved", c_int32)]
+                ("warps_per_tile", c_int32)]
 
 
 class RastTiledStats(ctypes.Structure):
@@ -205,6 +205,7 @@ PROTOTYPES = [
     ("rast_render_tiled_profiled", c_int,
      [POINTER(RastBatch), POINTER(RastTiledConfig), c_void_p, c_size_t, c_void_p, POINTER(RastProfile)]),
     ("rast_render_tiled_static", c_int, [POINTER(RastBatch), POINTER(RastTiledConfig), c_void_p]),
+    ("rast_autotune", c_int, [POINTER(RastBatch), c_void_p, POINTER(RastTiledConfig)]),
     ("rast_tiled_stats", c_int,
      [POINTER(RastBatch), POINTER(RastTiledConfig), c_void_p, c_void_p, POINTER(RastTiledStats)]),
     ("rast_backward_workspace_bytes", c_size_t, [POINTER(RastBatch)]),

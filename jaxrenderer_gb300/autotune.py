@@ -1,15 +1,16 @@
-"""Autotuner of the tiled form: tile shape, small-face path and bin
-capacity per workload.
+"""Autotuner of the tiled form: tile shape, small-face path, warps per
+tile and bin capacity per workload.
 
-For a pass (one RastBatch) the tile shapes 8x8, 16x8, 16x16, 32x8, 8x32,
-8x4 and 4x8 (pixels along x by y), each with the setup kernel's small-face
-rasterisation off and on, are timed on the batch itself; the fastest wins.
-Passes with layered-chooser jobs try the four shapes that have a layered
-raster variant, without the small-face path.
-The bin capacity is then set to 1.25x the bin entries that shape requested.
-Results are cached in a JSON file keyed by (width, height, faces-per-job
-bucket, shader mask, device name, SM count), so a workload class is tuned
-once per machine.
+The search itself is the library's rast_autotune (C ABI): every tile shape
+with a kernel (8x8, 16x8, 16x16, 32x8, 8x32, 8x4 and 4x8 with one warp per
+tile; 8x8, 8x16 and 16x16 with two warps each taking half of the rows; the
+layered shapes for passes with layered-chooser jobs), with the setup
+kernel's small-face rasterisation off and on, is timed on the batch itself
+with a bin capacity of 1.25x the entries its shape requests, and the
+fastest wins.  The library caches results per process; this module keeps
+them across processes in a JSON file keyed by (width, height, faces-per-job
+bucket, jobs bucket, shader mask, layers, device name, SM count), so a
+workload class is tuned once per machine.
 """
 from __future__ import annotations
 
@@ -25,8 +26,9 @@ import torch
 
 from . import _lib
 
-SHAPES = ((8, 8), (16, 8), (16, 16), (32, 8), (8, 32), (8, 4), (4, 8))
-LAYERED_SHAPES = ((8, 8), (16, 8), (8, 4), (4, 8))  # shapes with a layered-chooser raster variant
+SHAPES = ((8, 8), (16, 8), (16, 16), (32, 8), (8, 32), (8, 4), (4, 8))  # one warp per tile
+TWO_WARP_SHAPES = ((8, 8), (8, 16), (16, 16))  # two warps per tile, half of the rows each
+LAYERED_SHAPES = ((8, 8), (16, 8), (8, 4), (4, 8))  # one-warp shapes with a layered-chooser raster variant
 SMALL_AREAS = (0, 32)  # small-face rasterisation in the setup kernel: off, or rectangles up to 32 pixels
 _LOCK = threading.Lock()
 
@@ -63,27 +65,8 @@ def workload_key(jobs: np.ndarray, device: torch.device) -> str:
     bucket = 2 ** int(round(math.log2(max(f, 1.0))))
     mask = int(np.bitwise_or.reduce(1 << jobs["shader"].astype(np.int64)))
     layers = int(jobs["layers"].max())
-    return (f"v3|{w}x{h}|f~{bucket}|jobs~{2 ** int(round(math.log2(max(len(jobs), 1))))}|mask{mask}"
+    return (f"v4|{w}x{h}|f~{bucket}|jobs~{2 ** int(round(math.log2(max(len(jobs), 1))))}|mask{mask}"
             + (f"|layers{layers}" if layers > 0 else "") + f"|{props.name}|sm{props.multi_processor_count}")
-
-
-def _time(dev, b, cfg, reps=3) -> float:
-    lib = _lib.load()
-    nbytes = int(lib.rast_tiled_workspace_bytes(ctypes.byref(b), ctypes.byref(cfg)))
-    ws = torch.empty(max(nbytes, 256), dtype=torch.uint8, device=dev)
-    s = torch.cuda.current_stream(dev)
-    st = lib.rast_render_tiled(ctypes.byref(b), ctypes.byref(cfg), ws.data_ptr(), nbytes, s.cuda_stream)
-    _lib.check(st, "autotune warm-up")
-    stats = _lib.RastTiledStats()
-    _lib.check(lib.rast_tiled_stats(ctypes.byref(b), ctypes.byref(cfg), ws.data_ptr(), s.cuda_stream,
-                                    ctypes.byref(stats)), "autotune stats")
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(s)
-    for _ in range(reps):
-        lib.rast_render_tiled(ctypes.byref(b), ctypes.byref(cfg), ws.data_ptr(), nbytes, s.cuda_stream)
-    e1.record(s)
-    torch.cuda.synchronize(dev)
-    return e0.elapsed_time(e1) / reps, int(stats.bin_entries)
 
 
 def tiled_config_for(runner, name: str, b, jobs: np.ndarray) -> "_lib.RastTiledConfig":
@@ -102,22 +85,18 @@ def tiled_config_for_batch(device: torch.device, b, jobs: np.ndarray) -> "_lib.R
         hit = cache.get(key)
     if hit is not None:
         return _lib.RastTiledConfig(int(hit["tile_w"]), int(hit["tile_h"]), int(hit["bin_capacity"]),
-                                    int(hit.get("small_area", 0)))
-    best = None
-    layered = int(jobs["layers"].max()) > 0  # no small-face path and fewer shapes
-    for tw, th in LAYERED_SHAPES if layered else SHAPES:
-        for small in (0,) if layered else SMALL_AREAS:
-            cfg = _lib.RastTiledConfig(tw, th, 0, small)
-            ms, entries = _time(device, b, cfg)
-            if best is None or ms < best[0]:
-                best = (ms, tw, th, entries, small)
-    ms, tw, th, entries, small = best
-    cap = int(entries * 1.25) + 4096
+                                    int(hit.get("small_area", 0)), int(hit.get("warps_per_tile", 1)))
+    cfg = _lib.RastTiledConfig()
+    with torch.cuda.device(device):
+        s = torch.cuda.current_stream(device)
+        _lib.check(_lib.load().rast_autotune(ctypes.byref(b), s.cuda_stream, ctypes.byref(cfg)), "rast_autotune")
     with _LOCK:
         cache = _load()
-        cache[key] = {"tile_w": tw, "tile_h": th, "bin_capacity": cap, "small_area": small, "ms": ms}
+        cache[key] = {"tile_w": cfg.tile_w, "tile_h": cfg.tile_h, "bin_capacity": int(cfg.bin_capacity),
+                      "small_area": cfg.small_area, "warps_per_tile": cfg.warps_per_tile}
         _store(cache)
-    return _lib.RastTiledConfig(tw, th, cap, small)
+    return cfg
 
 
-__all__ = ["tiled_config_for", "tiled_config_for_batch", "workload_key", "cache_path", "SHAPES", "LAYERED_SHAPES", "SMALL_AREAS"]
+__all__ = ["tiled_config_for", "tiled_config_for_batch", "workload_key", "cache_path", "SHAPES", "TWO_WARP_SHAPES",
+           "LAYERED_SHAPES", "SMALL_AREAS"]

@@ -19,7 +19,12 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <map>
 #include <mutex>
+#include <string>
+#include <vector>
 
 #include "rast_internal.cuh"
 
@@ -630,12 +635,16 @@ __host__ __device__ constexpr int raster_min_blocks() {
   return (kL == 1 && TW * TH <= 128) ? 10 : (TW * TH <= 64 ? 8 : 0);
 }
 
-template <int TW, int TH, bool kKeys, bool kTies, int kL>
+// kWPT warps per bin tile: the bin tile is TW x (kWPT TH) pixels and a
+// work unit u is its rows [(u % kWPT) TH, (u % kWPT + 1) TH), so bins can be
+// coarser than the sub-tile each warp rasterises (every warp of a tile
+// reads the tile's whole bin and drops the entries that miss its rows).
+template <int TW, int TH, bool kKeys, bool kTies, int kL, int kWPT>
 __global__ void __launch_bounds__(32 * kRasterWarps, raster_min_blocks<TW, TH, kL>())
 raster_kernel(RastBatch B, Geometry G, const float4* __restrict__ setup,
               const uint32_t* __restrict__ counts, const uint32_t* __restrict__ offsets,
               const int32_t* __restrict__ bins, int32_t* __restrict__ winner,
-              unsigned int* __restrict__ work, int64_t n_tiles, unsigned char* __restrict__ visible,
+              unsigned int* __restrict__ work, int64_t n_units, unsigned char* __restrict__ visible,
               const unsigned long long* __restrict__ keys) {
   constexpr int PPL = TW * TH / 32;
   __shared__ float4 s_rec[kRasterWarps][kStage][3];
@@ -655,28 +664,30 @@ raster_kernel(RastBatch B, Geometry G, const float4* __restrict__ setup,
       chunk = __shfl_sync(0xffffffffu, chunk, 0);
       taken = 0;
     }
-    const unsigned int t = chunk + taken++;
-    if (t >= n_tiles) break;
+    const unsigned int unit = chunk + taken++;
+    if (unit >= n_units) break;
+    const unsigned int t = unit / kWPT;  // bin tile
     const int jid = static_cast<int>(t / G.tiles_per_job);
     const int local = static_cast<int>(t % G.tiles_per_job);
     const int tx = local % G.tiles_x, ty = local / G.tiles_x;
+    const int y0 = ty * (TH * kWPT) + static_cast<int>(unit % kWPT) * TH;  // first row of this warp's part
     const RastJob& J = B.jobs[jid];
     const int W = J.width, H = J.height;
-    if (tx * TW >= W || ty * TH >= H) continue;
+    if (tx * TW >= W || y0 >= H) continue;
     const float sx = J.viewport[0], ox = J.viewport[3], sy = J.viewport[5], oy = J.viewport[7];
     const float vp22 = J.viewport[10], vp23 = J.viewport[11];
     // lane -> one column j of the tile (TH divides 32) and PPL rows i:
     // every pixel of a lane shares y, so y * inv[1][k] is computed once per
     // entry (the same rounded product each pixel would compute).
     constexpr int LPC = 32 / TH;
-    const int pj = ty * TH + lane % TH;
+    const int pj = y0 + lane % TH;
     const float y = (static_cast<float>(pj) - oy) / sy;
     // NDC of the tile's first and last pixel (inside the job) for the
     // per-entry rejection test: the same quotients the pixels compute
     const float xa = (static_cast<float>(tx * TW) - ox) / sx;
     const float xb = (static_cast<float>(min(tx * TW + TW - 1, W - 1)) - ox) / sx;
-    const float ya = (static_cast<float>(ty * TH) - oy) / sy;
-    const float yb = (static_cast<float>(min(ty * TH + TH - 1, H - 1)) - oy) / sy;
+    const float ya = (static_cast<float>(y0) - oy) / sy;
+    const float yb = (static_cast<float>(min(y0 + TH - 1, H - 1)) - oy) / sy;
     const float XM = fmaxf(fabsf(xa), fabsf(xb)), YM = fmaxf(fabsf(ya), fabsf(yb));
     float x[PPL], best_z[PPL];
     unsigned long long best[PPL][kL];
@@ -1004,32 +1015,46 @@ static int small_area_of(const RastTiledConfig* cfg) {
   return std::min(cfg->small_area, kSmallArea);
 }
 
-static bool valid_shape(TileShape t) {
-  return (t.tw == 8 && t.th == 8) || (t.tw == 16 && t.th == 16) || (t.tw == 32 && t.th == 8) ||
-         (t.tw == 8 && t.th == 32) || (t.tw == 16 && t.th == 8) || (t.tw == 8 && t.th == 4) ||
-         (t.tw == 4 && t.th == 8);
+// Bin tile shapes with a raster kernel: one warp per tile for every shape
+// offered to the autotuner; two warps per tile (each rasterising half the
+// rows) for the bin tiles whose halves are 8x4, 8x8 or 16x8.
+static bool valid_shape(TileShape t, int wpt) {
+  if (wpt == 2)
+    return (t.tw == 8 && t.th == 8) || (t.tw == 8 && t.th == 16) || (t.tw == 16 && t.th == 16);
+  return wpt == 1 &&
+         ((t.tw == 8 && t.th == 8) || (t.tw == 16 && t.th == 16) || (t.tw == 32 && t.th == 8) ||
+          (t.tw == 8 && t.th == 32) || (t.tw == 16 && t.th == 8) || (t.tw == 8 && t.th == 4) ||
+          (t.tw == 4 && t.th == 8));
 }
 
 // Shapes with a layered raster variant: at most four pixels per lane, so
-// the RAST_MAX_LAYERS keys of every pixel stay in registers.
-static bool valid_layered_shape(TileShape t) {
+// the RAST_MAX_LAYERS keys of every pixel stay in registers (every
+// two-warp shape's halves qualify).
+static bool valid_layered_shape(TileShape t, int wpt) {
+  if (wpt == 2) return valid_shape(t, 2);
   return (t.tw == 8 && t.th == 8) || (t.tw == 16 && t.th == 8) || (t.tw == 8 && t.th == 4) ||
          (t.tw == 4 && t.th == 8);
+}
+
+// Warps per tile of a config (0 or absent: one).
+static int warps_per_tile_of(const RastTiledConfig* cfg) {
+  return cfg && cfg->warps_per_tile > 0 ? cfg->warps_per_tile : 1;
 }
 
 // RAST_OK, or the status rast_render_tiled returns for a tile shape it has
 // no kernel for.  Checked before any layout arithmetic (which divides by the
 // tile's sides).
-static int check_shape(const RastBatch& b, TileShape t) {
-  if (!valid_shape(t)) return RAST_ERR_INVALID_ARGUMENT;
-  if (b.max_layers > 0 && !valid_layered_shape(t)) return RAST_ERR_UNSUPPORTED;
+static int check_shape(const RastBatch& b, TileShape t, int wpt) {
+  if (!valid_shape(t, wpt)) return RAST_ERR_INVALID_ARGUMENT;
+  if (b.max_layers > 0 && !valid_layered_shape(t, wpt)) return RAST_ERR_UNSUPPORTED;
   return RAST_OK;
 }
 
 template <bool kKeys, bool kTies, int kL>
 // The raster kernel is persistent: one resident wave of blocks (SMs x the
-// blocks of this instance that fit on an SM) takes the tiles.
-static void launch_raster(TileShape ts, int sms, cudaStream_t s, const RastBatch& b, const Layout& L,
+// blocks of this instance that fit on an SM) takes the work units (bin
+// tiles x warps per tile).
+static void launch_raster(TileShape ts, int wpt, int sms, cudaStream_t s, const RastBatch& b, const Layout& L,
                           const float4* setup, const uint32_t* counts, const uint32_t* offsets, const int32_t* bins,
                           int32_t* winner, unsigned int* misc, unsigned char* vis,
                           const unsigned long long* keys) {
@@ -1040,23 +1065,32 @@ static void launch_raster(TileShape ts, int sms, cudaStream_t s, const RastBatch
         per_sm <= 0)
       per_sm = 8;
     const unsigned grid = static_cast<unsigned>(std::max(sms, 1) * per_sm);
-    kernel<<<grid, block, 0, s>>>(b, L.G, setup, counts, offsets, bins, winner, misc, L.n_tiles, vis, keys);
+    kernel<<<grid, block, 0, s>>>(b, L.G, setup, counts, offsets, bins, winner, misc, L.n_tiles * wpt, vis, keys);
   };
+  if (wpt == 2) {  // the warp's sub-tile is (tw, th / 2)
+    if (ts.tw == 8 && ts.th == 16)
+      go(raster_kernel<8, 8, kKeys, kTies, kL, 2>);
+    else if (ts.tw == 16 && ts.th == 16)
+      go(raster_kernel<16, 8, kKeys, kTies, kL, 2>);
+    else
+      go(raster_kernel<8, 4, kKeys, kTies, kL, 2>);
+    return;
+  }
   if (ts.tw == 8 && ts.th == 8)
-    go(raster_kernel<8, 8, kKeys, kTies, kL>);
+    go(raster_kernel<8, 8, kKeys, kTies, kL, 1>);
   else if (ts.tw == 8 && ts.th == 4)
-    go(raster_kernel<8, 4, kKeys, kTies, kL>);
+    go(raster_kernel<8, 4, kKeys, kTies, kL, 1>);
   else if (ts.tw == 4 && ts.th == 8)
-    go(raster_kernel<4, 8, kKeys, kTies, kL>);
+    go(raster_kernel<4, 8, kKeys, kTies, kL, 1>);
   else if (ts.tw == 16 && ts.th == 8)
-    go(raster_kernel<16, 8, kKeys, kTies, kL>);
+    go(raster_kernel<16, 8, kKeys, kTies, kL, 1>);
   else if constexpr (kL == 1) {  // eight pixels per lane: default chooser only
     if (ts.tw == 16 && ts.th == 16)
-      go(raster_kernel<16, 16, kKeys, kTies, kL>);
+      go(raster_kernel<16, 16, kKeys, kTies, kL, 1>);
     else if (ts.tw == 32 && ts.th == 8)
-      go(raster_kernel<32, 8, kKeys, kTies, kL>);
+      go(raster_kernel<32, 8, kKeys, kTies, kL, 1>);
     else
-      go(raster_kernel<8, 32, kKeys, kTies, kL>);
+      go(raster_kernel<8, 32, kKeys, kTies, kL, 1>);
   }
 }
 
@@ -1066,7 +1100,8 @@ static int render(const RastBatch* batch, const RastTiledConfig* cfg, void* work
   if (st != RAST_OK) return st;
   const RastBatch& b = *batch;
   TileShape ts{cfg ? cfg->tile_w : 8, cfg ? cfg->tile_h : 8};
-  st = check_shape(b, ts);
+  const int wpt = warps_per_tile_of(cfg);
+  st = check_shape(b, ts, wpt);
   if (st != RAST_OK) return st;
   const uint64_t cap = cfg && cfg->bin_capacity > 0 ? cfg->bin_capacity : default_bin_capacity(b);
   const int small_area = small_area_of(cfg);
@@ -1131,17 +1166,17 @@ static int render(const RastBatch* batch, const RastTiledConfig* cfg, void* work
       // the key path exists only when ties are not counted and no job is
       // layered
       if (keys)
-        launch_raster<true, false, 1>(ts, sms, s, b, L, setup, counts, offsets, bins, winner, misc, vis, keys);
+        launch_raster<true, false, 1>(ts, wpt, sms, s, b, L, setup, counts, offsets, bins, winner, misc, vis, keys);
       else if (b.max_layers > 0 && b.near_ties)
-        launch_raster<false, true, RAST_MAX_LAYERS>(ts, sms, s, b, L, setup, counts, offsets, bins, winner, misc,
+        launch_raster<false, true, RAST_MAX_LAYERS>(ts, wpt, sms, s, b, L, setup, counts, offsets, bins, winner, misc,
                                                     vis, nullptr);
       else if (b.max_layers > 0)
-        launch_raster<false, false, RAST_MAX_LAYERS>(ts, sms, s, b, L, setup, counts, offsets, bins, winner, misc,
+        launch_raster<false, false, RAST_MAX_LAYERS>(ts, wpt, sms, s, b, L, setup, counts, offsets, bins, winner, misc,
                                                      vis, nullptr);
       else if (b.near_ties)
-        launch_raster<false, true, 1>(ts, sms, s, b, L, setup, counts, offsets, bins, winner, misc, vis, nullptr);
+        launch_raster<false, true, 1>(ts, wpt, sms, s, b, L, setup, counts, offsets, bins, winner, misc, vis, nullptr);
       else
-        launch_raster<false, false, 1>(ts, sms, s, b, L, setup, counts, offsets, bins, winner, misc, vis, nullptr);
+        launch_raster<false, false, 1>(ts, wpt, sms, s, b, L, setup, counts, offsets, bins, winner, misc, vis, nullptr);
     } else {
       if (cudaMemsetAsync(winner, 0xff, static_cast<size_t>(b.total_pixels) * 4 * L.winner_layers, s) != cudaSuccess)
         return RAST_ERR_CUDA;
@@ -1180,7 +1215,7 @@ using namespace rast;
 extern "C" size_t rast_tiled_workspace_bytes(const RastBatch* batch, const RastTiledConfig* cfg) {
   if (!batch) return 0;
   tiled::TileShape ts{cfg ? cfg->tile_w : 8, cfg ? cfg->tile_h : 8};
-  if (tiled::check_shape(*batch, ts) != RAST_OK) return 0;
+  if (tiled::check_shape(*batch, ts, tiled::warps_per_tile_of(cfg)) != RAST_OK) return 0;
   const uint64_t cap = cfg && cfg->bin_capacity > 0 ? cfg->bin_capacity : tiled::default_bin_capacity(*batch);
   return tiled::layout(*batch, ts, cap, tiled::small_area_of(cfg)).total;
 }
@@ -1189,7 +1224,7 @@ extern "C" int rast_tiled_stats(const RastBatch* batch, const RastTiledConfig* c
                                 void* stream, RastTiledStats* out) {
   if (!batch || !workspace || !out) return RAST_ERR_INVALID_ARGUMENT;
   tiled::TileShape ts{cfg ? cfg->tile_w : 8, cfg ? cfg->tile_h : 8};
-  const int shape_status = tiled::check_shape(*batch, ts);
+  const int shape_status = tiled::check_shape(*batch, ts, tiled::warps_per_tile_of(cfg));
   if (shape_status != RAST_OK) return shape_status;
   const uint64_t cap = cfg && cfg->bin_capacity > 0 ? cfg->bin_capacity : tiled::default_bin_capacity(*batch);
   const tiled::Layout L = tiled::layout(*batch, ts, cap, tiled::small_area_of(cfg));
@@ -1216,6 +1251,133 @@ extern "C" int rast_render_tiled_profiled(const RastBatch* batch, const RastTile
                                           void* workspace, size_t workspace_bytes, void* stream,
                                           RastProfile* profile) {
   return tiled::render(batch, cfg, workspace, workspace_bytes, stream, profile);
+}
+
+// ------------------------------------------------------------ autotuning
+
+namespace {
+
+struct TuneCandidate {
+  int tw, th, wpt, small;
+};
+
+// Every configuration the tiled form has a kernel for.
+std::vector<TuneCandidate> tune_candidates(const RastBatch& b) {
+  const bool layered = b.max_layers > 0;
+  const bool small_ok = !layered && b.near_ties == nullptr;
+  std::vector<TuneCandidate> out;
+  const int shapes1[7][2] = {{8, 8}, {16, 8}, {16, 16}, {32, 8}, {8, 32}, {8, 4}, {4, 8}};
+  const int shapes2[3][2] = {{8, 8}, {8, 16}, {16, 16}};
+  for (int small : {0, 32}) {
+    if (small && !small_ok) continue;
+    for (const auto& sh : shapes1) {
+      const tiled::TileShape t{sh[0], sh[1]};
+      if (tiled::check_shape(b, t, 1) == RAST_OK) out.push_back({sh[0], sh[1], 1, small});
+    }
+    for (const auto& sh : shapes2) {
+      const tiled::TileShape t{sh[0], sh[1]};
+      if (tiled::check_shape(b, t, 2) == RAST_OK) out.push_back({sh[0], sh[1], 2, small});
+    }
+  }
+  return out;
+}
+
+// Workload class of a batch: canvas size, faces per job and jobs (powers of
+// two), shaders, chooser layers, tie counting, device.
+std::string tune_key(const RastBatch& b, int dev) {
+  auto bucket = [](double v) { return v < 1.0 ? 0 : static_cast<int>(std::lround(std::log2(v))); };
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  char key[256];
+  std::snprintf(key, sizeof(key), "%dx%d|f%d|j%d|m%d|l%d|t%d|d%d|s%d", b.max_width, b.max_height,
+                bucket(static_cast<double>(b.total_setup) / std::max(b.n_jobs, 1)), bucket(b.n_jobs), b.shader_mask,
+                b.max_layers, b.near_ties != nullptr, dev, sms);
+  return key;
+}
+
+std::mutex g_tune_mutex;
+std::map<std::string, RastTiledConfig> g_tune_cache;
+
+}  // namespace
+
+extern "C" int rast_autotune(const RastBatch* batch, void* stream, RastTiledConfig* out) {
+  int st = check_batch(batch);
+  if (st != RAST_OK) return st;
+  if (!out) return RAST_ERR_INVALID_ARGUMENT;
+  const RastBatch& b = *batch;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return RAST_ERR_CUDA;
+  const std::string key = tune_key(b, dev);
+  {
+    std::lock_guard<std::mutex> lock(g_tune_mutex);
+    auto it = g_tune_cache.find(key);
+    if (it != g_tune_cache.end()) {
+      *out = it->second;
+      return RAST_OK;
+    }
+  }
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) return RAST_ERR_CUDA;
+  void* ws = nullptr;
+  size_t ws_bytes = 0;
+  float best_ms = 0.0f;
+  RastTiledConfig best{};
+  bool found = false;
+  st = RAST_OK;
+  for (const TuneCandidate& c : tune_candidates(b)) {
+    RastTiledConfig cfg{c.tw, c.th, 0, c.small, c.wpt};
+    // capacity for the timed renders: 1.25 x the entries this shape requests
+    for (int round = 0; round < 2 && st == RAST_OK; ++round) {
+      const size_t need = rast_tiled_workspace_bytes(&b, &cfg);
+      if (need > ws_bytes) {
+        if (ws) cudaFreeAsync(ws, s);
+        ws = nullptr;
+        if (cudaMallocAsync(&ws, need, s) != cudaSuccess) {
+          st = RAST_ERR_CUDA;
+          break;
+        }
+        ws_bytes = need;
+      }
+      if (round == 0) {
+        st = rast_render_tiled(&b, &cfg, ws, ws_bytes, s);
+        RastTiledStats stats{};
+        if (st == RAST_OK) st = rast_tiled_stats(&b, &cfg, ws, s, &stats);
+        cfg.bin_capacity = stats.bin_entries + stats.bin_entries / 4 + 4096;
+      }
+    }
+    if (st != RAST_OK) break;
+    constexpr int kReps = 3;
+    if (cudaEventRecord(e0, s) != cudaSuccess) {
+      st = RAST_ERR_CUDA;
+      break;
+    }
+    for (int r = 0; r < kReps && st == RAST_OK; ++r) st = rast_render_tiled(&b, &cfg, ws, ws_bytes, s);
+    if (st != RAST_OK) break;
+    float ms = 0.0f;
+    if (cudaEventRecord(e1, s) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+        cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) {
+      st = RAST_ERR_CUDA;
+      break;
+    }
+    if (!found || ms < best_ms) {
+      best_ms = ms;
+      best = cfg;
+      found = true;
+    }
+  }
+  if (ws) cudaFreeAsync(ws, s);
+  cudaStreamSynchronize(s);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (st != RAST_OK) return st;
+  if (!found) return RAST_ERR_UNSUPPORTED;
+  {
+    std::lock_guard<std::mutex> lock(g_tune_mutex);
+    g_tune_cache[key] = best;
+  }
+  *out = best;
+  return RAST_OK;
 }
 
 // ------------------------------------------------ allocation-free variant
@@ -1297,7 +1459,8 @@ int static_scratch(void** out) {
 extern "C" int rast_render_tiled_static(const RastBatch* batch, const RastTiledConfig* cfg, void* stream) {
   int st = check_batch(batch);
   if (st != RAST_OK) return st;
-  st = tiled::check_shape(*batch, tiled::TileShape{cfg ? cfg->tile_w : 8, cfg ? cfg->tile_h : 8});
+  st = tiled::check_shape(*batch, tiled::TileShape{cfg ? cfg->tile_w : 8, cfg ? cfg->tile_h : 8},
+                          tiled::warps_per_tile_of(cfg));
   if (st != RAST_OK) return st;
   const size_t need = rast_tiled_workspace_bytes(batch, cfg);
   if (need > RAST_STATIC_SCRATCH_BYTES) return RAST_ERR_STATIC_SCRATCH_TOO_SMALL;

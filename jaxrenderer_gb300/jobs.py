@@ -345,12 +345,13 @@ def render_plain(packed: PackedBatch, stream: Optional[torch.cuda.Stream] = None
 
 
 def render_tiled(packed: PackedBatch, tile=(8, 8), bin_capacity: int = 0,
-                 stream: Optional[torch.cuda.Stream] = None, small_area: int = 0) -> "_lib.RastTiledStats":
+                 stream: Optional[torch.cuda.Stream] = None, small_area: int = 0,
+                 warps_per_tile: int = 1) -> "_lib.RastTiledStats":
     """Run the tiled form on a packed batch; returns its bin statistics
     (reading them synchronises the stream)."""
     lib = _lib.load()
     b = packed.batch
-    cfg = _lib.RastTiledConfig(int(tile[0]), int(tile[1]), int(bin_capacity), int(small_area))
+    cfg = _lib.RastTiledConfig(int(tile[0]), int(tile[1]), int(bin_capacity), int(small_area), int(warps_per_tile))
     nbytes = lib.rast_tiled_workspace_bytes(ctypes.byref(b), ctypes.byref(cfg))
     dev = packed.zbuffer.device
     ws = torch.empty(max(int(nbytes), 256), dtype=torch.uint8, device=dev)

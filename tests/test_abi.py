@@ -38,7 +38,7 @@ def test_every_declared_symbol_is_exported(lib):
 
 
 def test_host_only_entry_points(lib):
-    assert lib.rast_abi_version() == _lib.ABI_VERSION == 3
+    assert lib.rast_abi_version() == _lib.ABI_VERSION == 4
     assert lib.rast_error_string(0) == b"ok"
     assert lib.rast_error_string(6) == b"tile bin capacity exceeded"
     job = _lib.RastJob()
@@ -91,7 +91,14 @@ def test_tile_shapes_without_a_kernel_are_refused_before_any_size_arithmetic(lib
         assert lib.rast_tiled_stats(ctypes.byref(b), ctypes.byref(cfg), fake_ws, None, ctypes.byref(stats)) == 1
         assert lib.rast_render_tiled(ctypes.byref(b), ctypes.byref(cfg), fake_ws, 1 << 20, None) == 1
         assert lib.rast_render_tiled_static(ctypes.byref(b), ctypes.byref(cfg), None) == 1
-    b.max_layers = 2  # layered batches have kernels for 8x8, 16x8, 8x4 and 4x8 only
+    for tw, th in ((16, 8), (32, 8), (8, 4)):  # two warps per tile: 8x8, 8x16 and 16x16 tiles only
+        cfg = _lib.RastTiledConfig(tw, th, 0, 0, 2)
+        assert lib.rast_tiled_workspace_bytes(ctypes.byref(b), ctypes.byref(cfg)) == 0
+        assert lib.rast_render_tiled(ctypes.byref(b), ctypes.byref(cfg), fake_ws, 1 << 20, None) == 1
+    assert lib.rast_tiled_workspace_bytes(ctypes.byref(b), ctypes.byref(_lib.RastTiledConfig(8, 16, 0, 0, 1))) == 0
+    assert lib.rast_autotune(None, None, ctypes.byref(_lib.RastTiledConfig())) == 1  # no batch: refused on the host
+    b.max_layers = 2  # layered batches have kernels for 8x8, 16x8, 8x4 and 4x8 only (and the two-warp tiles)
     cfg = _lib.RastTiledConfig(16, 16, 0)
     assert lib.rast_tiled_workspace_bytes(ctypes.byref(b), ctypes.byref(cfg)) == 0
     assert lib.rast_render_tiled_static(ctypes.byref(b), ctypes.byref(cfg), None) == 4
+    assert lib.rast_tiled_workspace_bytes(ctypes.byref(b), ctypes.byref(_lib.RastTiledConfig(16, 16, 0, 0, 2))) > 0

@@ -19,7 +19,7 @@ from tests.test_gpu_plain import assert_parity
 pytestmark = pytest.mark.gpu
 F32 = np.float32
 LAYERED_SHADERS = [s for s in scenes.ALL_SHADERS if s != _lib.SHADER_DEPTH]
-LAYERED_TILES = [(8, 8), (16, 8), (8, 4), (4, 8)]
+LAYERED_TILES = [(8, 8), (16, 8), (8, 4), (4, 8), (16, 16, 2), (8, 16, 2), (8, 8, 2)]  # (w, h[, warps per tile])
 
 
 def layered_job(shader, seed, layers, mixer, opacity=0.5, F=90):
@@ -40,7 +40,7 @@ def _render(specs, device, form, tile=(8, 8), count_ties=True):
     if form == "plain":
         render_plain(packed)
     else:
-        assert render_tiled(packed, tile=tile).overflow == 0
+        assert render_tiled(packed, tile=tile[:2], warps_per_tile=tile[2] if len(tile) > 2 else 1).overflow == 0
     outs = [tuple(t.clone() for t in o) for o in unpack(packed, specs)]
     ties = None if packed.near_ties is None else int(packed.near_ties.item())
     return outs, bufs, ties

@@ -15,11 +15,14 @@ from tests.test_gpu_plain import assert_parity
 pytestmark = pytest.mark.gpu
 F32 = np.float32
 SHAPES = [(8, 8), (16, 8), (16, 16), (32, 8), (8, 32), (8, 4), (4, 8)]
+# tiles rasterised by two warps, each taking half of the rows
+TWO_WARP_SHAPES = [(8, 8, 2), (8, 16, 2), (16, 16, 2)]
 
 
 def _tiled_job(spec, z0, c0, device, tile=(8, 8), cap=0, ties=False, small=0):
     packed = pack([spec], [z0], [c0], device, count_ties=ties)
-    stats = render_tiled(packed, tile=tile, bin_capacity=cap, small_area=small)
+    wpt = tile[2] if len(tile) > 2 else 1
+    stats = render_tiled(packed, tile=tile[:2], bin_capacity=cap, small_area=small, warps_per_tile=wpt)
     z, c, p = unpack(packed, [spec])[0]
     return z, c, p, packed.near_ties, stats
 
@@ -28,11 +31,12 @@ def _tiled_job(spec, z0, c0, device, tile=(8, 8), cap=0, ties=False, small=0):
 def test_tiled_random_scene_parity(cuda_device, shader):
     spec = scenes.random_job(shader, seed=700 + shader, W=57, H=45, F=150, spread=2.0)
     z0, c0 = scenes.initial_buffers(spec)
-    z, c, p, ties, stats = _tiled_job(spec, z0, c0, cuda_device, ties=True)
     ref = oracle.render(spec, z0, c0)
-    assert_parity(z, c, p, ref, f"tiled shader {shader}")
-    assert int(ties.item()) == ref["near_ties"]
-    assert stats.overflow == 0
+    for tile in ((8, 8), (16, 16, 2)):
+        z, c, p, ties, stats = _tiled_job(spec, z0, c0, cuda_device, tile=tile, ties=True)
+        assert_parity(z, c, p, ref, f"tiled shader {shader} tile {tile}")
+        assert int(ties.item()) == ref["near_ties"]
+        assert stats.overflow == 0
 
 
 @pytest.mark.parametrize("shader", scenes.ALL_SHADERS)
@@ -46,7 +50,7 @@ def test_small_face_path_parity(cuda_device, shader):
         assert_parity(z, c, p, oracle.render(spec, z0, c0), f"small path shader {shader} tile {tile}")
 
 
-@pytest.mark.parametrize("tile", SHAPES)
+@pytest.mark.parametrize("tile", SHAPES + TWO_WARP_SHAPES)
 def test_tile_shapes_and_unbounded_regions(cuda_device, tile):
     # eye inside the soup: many primitives straddle w = 0, so their coverage
     # regions are unbounded and must be clipped to the screen, not dropped
@@ -86,11 +90,12 @@ def _copy(out):
 
 
 @pytest.mark.parametrize("tile,small", [((8, 8), 0), ((16, 16), 0), ((32, 8), 0), ((8, 4), 0), ((4, 8), 0),
-                                        ((8, 8), 32), ((16, 8), 32), ((8, 4), 32)])
+                                        ((8, 8), 32), ((16, 8), 32), ((8, 4), 32),
+                                        ((8, 16, 2), 0), ((16, 16, 2), 32), ((8, 8, 2), 0)])
 def test_tiled_batch_equals_plain_batch(cuda_device, brax_batch, tile, small):
     flat, sb = brax_batch
     plain = _copy(jb.BatchRunner(sb, form="plain").run())
-    cfg = _lib.RastTiledConfig(tile[0], tile[1], 0, small)
+    cfg = _lib.RastTiledConfig(tile[0], tile[1], 0, small, tile[2] if len(tile) > 2 else 1)
     runner = jb.BatchRunner(sb, form="tiled", tiled_config=cfg)
     tiled = _copy(runner.run())
     torch.cuda.synchronize()
@@ -196,7 +201,7 @@ def test_adversarial_faces_tiled_equals_plain_and_oracle(cuda_device, shader):
     render_plain(packed)
     zp, cp, pp = (None if t is None else t.clone() for t in unpack(packed, [spec])[0])
     assert_parity(zp, cp, pp, ref, f"plain adversarial shader {shader}")
-    for tile in SHAPES:
+    for tile in SHAPES + TWO_WARP_SHAPES:
         for small in (0, 32):
             z, c, p, _, stats = _tiled_job(spec, z0, c0, cuda_device, tile=tile, small=small)
             assert stats.overflow == 0
@@ -230,11 +235,38 @@ def test_ragged_edge_case_batch(cuda_device):
     bufs = [scenes.initial_buffers(s) for s in specs]
     refs = [oracle.render(s, *b) for s, b in zip(specs, bufs)]
     assert (refs[0]["prim_id"] == -1).all() and (refs[5]["prim_id"] >= 0).any()
-    for form, tile in (("plain", None), ("tiled", (8, 8)), ("tiled", (4, 8)), ("tiled", (16, 8))):
+    for form, tile in (("plain", None), ("tiled", (8, 8)), ("tiled", (4, 8)), ("tiled", (16, 8)),
+                       ("tiled", (16, 16, 2)), ("tiled", (8, 16, 2))):
         packed = pack(specs, [b[0] for b in bufs], [b[1] for b in bufs], cuda_device)
         if form == "plain":
             render_plain(packed)
         else:
-            assert render_tiled(packed, tile=tile).overflow == 0
+            assert render_tiled(packed, tile=tile[:2], warps_per_tile=tile[2] if len(tile) > 2 else 1).overflow == 0
         for k, (s, out) in enumerate(zip(specs, unpack(packed, specs))):
             assert_parity(*out, refs[k], f"{form} {tile} job {k}")
+
+
+def test_autotune_through_the_c_abi(cuda_device, brax_batch):
+    """rast_autotune picks a configuration the tiled form has a kernel for,
+    caches it per workload class (the second call renders nothing), and the
+    picked configuration renders what the plain form renders."""
+    import ctypes
+
+    flat, sb = brax_batch
+    runner = jb.BatchRunner(sb, form="plain")
+    plain = _copy(runner.run())
+    lib = _lib.load()
+    stream = torch.cuda.current_stream(cuda_device).cuda_stream
+    cfg = _lib.RastTiledConfig()
+    assert lib.rast_autotune(ctypes.byref(runner.main_batch), stream, ctypes.byref(cfg)) == 0
+    shape = (cfg.tile_w, cfg.tile_h, cfg.warps_per_tile)
+    assert shape[2] in (1, 2) and shape[:2] in [s[:2] for s in SHAPES + TWO_WARP_SHAPES]
+    assert cfg.bin_capacity > 0 and cfg.small_area in (0, 32)
+    again = _lib.RastTiledConfig()
+    assert lib.rast_autotune(ctypes.byref(runner.main_batch), stream, ctypes.byref(again)) == 0
+    assert bytes(again) == bytes(cfg)
+    tiled = jb.BatchRunner(sb, form="tiled", tiled_config=cfg)
+    got = _copy(tiled.run())
+    torch.cuda.synchronize()
+    assert torch.equal(got["prim_id"], plain["prim_id"])
+    assert torch.equal(got["canvas"].view(torch.int32), plain["canvas"].view(torch.int32))
