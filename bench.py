@@ -70,6 +70,9 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-plain", action="store_true")
     p.add_argument("--no-bwd", action="store_true")
+    p.add_argument("--tile-config", default=None,
+                   help="pin the tiled form's config per pass instead of the autotuner's, e.g. "
+                        "shadow=16x8,main=8x8x1 (width x height [x warps per tile]; bin capacity sized from a first render)")
     a = p.parse_args()
     if a.scenes is None:
         a.scenes = DEFAULT_SCENES[a.workload]
@@ -103,6 +106,7 @@ class Workload:
     published: Optional[float] = None  # the reference's published frames/s for this configuration
     display: object = None  # uint8 display images of the notebook step
     api_inputs: object = None  # (objects, camera, target, light) host arrays for the get_camera_image e2e
+    pinned: Optional[dict] = None  # {pass: RastTiledConfig} from --tile-config
     pipeline: Optional[Callable[[], object]] = None  # builds a batch.InstancedPipeline (instanced workloads)
     data: str = "synthetic (seeded stand-ins with the stated shapes)"
 
@@ -509,13 +513,16 @@ def run_ours(args, rank, world, local):
     wl = BUILDERS[args.workload](args.scenes, rank, dev, world)
     stream = torch.cuda.current_stream(dev)
     form, form_times = args.form, None
-    if args.form == "auto":
+    if args.form == "auto" and not args.tile_config:
         form, form_times = choose_form(wl, dev)
+    elif args.form == "auto":
+        form = "tiled"
     in_bytes = input_bytes(wl.groups)
     flush = in_bytes < 2 * L2_BYTES
     timed = Timer(dev, stream, world, flush)
 
-    mr = jb.MultiRunner(wl.groups, form=form, want_prim_id=False)
+    pinned = wl.pinned = pinned_configs(args.tile_config, wl.groups)
+    mr = jb.MultiRunner(wl.groups, form=form, want_prim_id=False, tiled_config=pinned)
     if wl.notebook:
         step, wl.display = notebook_step(wl, mr, dev, capture=True)
     else:
@@ -566,7 +573,7 @@ def run_ours(args, rank, world, local):
     roof, per_kernel = roofline(prof, visible, clocks)
     detail = {"kernels": prof["summary"], "per_kernel": per_kernel,
               "backward_kernels_ms": fwd_bwd.pop("backward_kernels_ms", None), "fwd_bwd_grads": fwd_bwd.pop("grads", None)}
-    detail_path = ROOT / "gpurun_out" / f"bench_{args.workload}_n{world}_detail.json"
+    detail_path = ROOT / "gpurun_out" / f"bench_{args.workload}_s{args.scenes}_n{world}_detail.json"
     if rank == 0:
         detail_path.parent.mkdir(exist_ok=True)
         detail_path.write_text(json.dumps(detail, indent=1))
@@ -629,7 +636,7 @@ def count_near_ties(mr):
 
     out = {"main": 0, "shadow": 0, "main_pixels": 0, "shadow_pixels": 0}
     for r in mr.runners:
-        rr = jb.BatchRunner(r.sb, form=r.form, want_prim_id=False, count_ties=True)
+        rr = jb.BatchRunner(r.sb, form=r.form, want_prim_id=False, count_ties=True, tiled_config=dict(r.configs) or None)
         rr.ties.zero_()
         rr.shadow_ties.zero_()
         rr.run()
@@ -685,6 +692,41 @@ def measure_e2e_api(wl: Workload, args, dev, stream, total_frames):
                       "84, 84, shadow_param=ShadowParameters(centre=batched target)) on host arrays, the "
                       "notebooks' vmapped call: transforms, local scalings and job tables copied every call",
             "outputs": "uint8 display images (clamp, x255, transpose_for_display) to pinned host memory"}
+
+
+def pinned_configs(spec: Optional[str], groups):
+    """{pass: RastTiledConfig} from --tile-config ("shadow=16x8,main=8x8x1"),
+    each with a bin capacity of 1.25x the entries a first render of the
+    largest group requests; None without the option."""
+    if not spec:
+        return None
+    import ctypes
+
+    import torch
+
+    from jaxrenderer_gb300 import _lib, batch as jb
+
+    out = {}
+    for item in spec.split(","):
+        name, shape = item.split("=")
+        dims = [int(v) for v in shape.lower().split("x")]
+        out[name.strip()] = _lib.RastTiledConfig(dims[0], dims[1], 0, 0, dims[2] if len(dims) > 2 else 1)
+    probe = jb.BatchRunner(max(groups, key=lambda sb: sb.n_scenes), form="tiled", want_prim_id=False,
+                           tiled_config={k: _lib.RastTiledConfig.from_buffer_copy(v) for k, v in out.items()})
+    for name, cfg in out.items():
+        if name not in probe.configs:
+            continue
+        c = probe.configs[name]
+        c.bin_capacity = 64 * int(probe.sb.total_faces)  # ample for the probe render
+        nbytes = int(probe._ws_bytes(name, probe.shadow_batch if name == "shadow" else probe.main_batch))
+        probe.ws[name] = (torch.empty(max(nbytes, 256), dtype=torch.uint8, device=probe.sb.device), nbytes)
+    probe.run()
+    for name, cfg in out.items():
+        if name in probe.configs:
+            cfg.bin_capacity = int(probe.stats(name).bin_entries * 1.25) + 4096
+    del probe
+    torch.cuda.empty_cache()
+    return out
 
 
 def choose_form(wl: Workload, dev):
@@ -756,7 +798,7 @@ def count_visible(mr):
 
     out = []
     for r in mr.runners:
-        rr = jb.BatchRunner(r.sb, form=r.form, want_prim_id=True, tiled_config=r.configs.get("main"))
+        rr = jb.BatchRunner(r.sb, form=r.form, want_prim_id=True, tiled_config=dict(r.configs) or None)
         rr.run()
         pid = rr.prim_id.reshape(r.sb.n_scenes, -1).to(torch.int64)
         key = torch.arange(r.sb.n_scenes, device=pid.device)[:, None] * (1 << 32) + pid
@@ -788,7 +830,8 @@ def measure_fwd_bwd(wl: Workload, args, stream, timed, total_frames):
             step, r, extra = phong_step(wl, form)
             runners = [r]
         else:
-            mr = jb.MultiRunner(wl.groups, form=form, want_prim_id=True)
+            mr = jb.MultiRunner(wl.groups, form=form, want_prim_id=True,
+                                tiled_config=wl.pinned if form == "tiled" else None)
             grads = mr.grad_buffers()
             gen = torch.Generator().manual_seed(0)
             targets = [torch.rand(r.canvas.shape, generator=gen).to(r.canvas.device) for r in mr.runners]
@@ -982,12 +1025,20 @@ def kernel_bytes(kname, info, visible):
     return table.get(kname, 0.0)
 
 
-def library_digest() -> str:
-    """SHA-256 (16 hex digits) of the CUDA sources the library is built from."""
+# The sources the tiled forward kernels are built from: the ncu counts below
+# describe these kernels only while these files are unchanged.
+FORWARD_SOURCES = ("jaxrenderer_gb300/csrc/rast_tiled.cu", "jaxrenderer_gb300/csrc/rast_internal.cuh",
+                   "jaxrenderer_gb300/csrc/rast_math.cuh", "jaxrenderer_gb300/csrc/rast_shaders.cuh",
+                   "include/rast_gb300.h")
+
+
+def library_digest(files=FORWARD_SOURCES) -> str:
+    """SHA-256 (16 hex digits) of the given CUDA sources (names and bytes)."""
     import hashlib
 
     h = hashlib.sha256()
-    for p in sorted((ROOT / "jaxrenderer_gb300" / "csrc").glob("*.cu*")):
+    for name in files:
+        p = ROOT / name
         h.update(p.name.encode())
         h.update(p.read_bytes())
     return h.hexdigest()[:16]
@@ -996,77 +1047,55 @@ def library_digest() -> str:
 # library_digest() of the sources the NCU_* counts below were captured on:
 # when the kernels change, the counts no longer describe them and the bench
 # reports traffic and the issue figure as null until they are captured again.
-NCU_SOURCE_DIGEST = "none"
+NCU_SOURCE_DIGEST = "55d0e3f282d38792"
 
 
 def ncu_counts_current() -> bool:
     return library_digest() == NCU_SOURCE_DIGEST
 
 
-# DRAM bytes per unit of work of the forward kernels measured by ncu
-# (dram__bytes_read.sum + dram__bytes_write.sum) on the 256-scene brax-like
-# case (ncu capture: 1,470,504 faces per pass, 1,806,336 main-pass pixels): setup_bin 136.6 MB per pass, scatter 12.4 MB,
-# face_varyings 44.1 MB, tiled_shade 108.4 MB.  Their traffic grows with the
-# faces (F) or pixels (P) processed, so a full launch's is this times its
-# units.  The raster kernel's depends on the tile shape the autotuner picks
-# for a batch size and is not scaled.
-NCU_BYTES_PER_UNIT = {
-    "setup_bin_kernel": ("F", 92.9),
-    "scatter_kernel": ("F", 8.4),
-    "face_varyings_kernel": ("F", 30.0),
-    "tiled_shade_kernel": ("P", 60.0),
-}
-
-# Warp instructions executed per unit of work (ncu smsp__inst_executed.sum,
-# same capture, per launch): setup_bin 34.4 / 39.0 M (shadow / main pass),
-# scatter 6.3 / 12.2 M, face_varyings 6.8 M, tiled_shade 56.4 M.  These
-# kernels are bound by instruction issue and latency, not DRAM: achieved warp
-# instructions per second over the SMs' issue rate (4 schedulers per SM, one
-# warp instruction per clock each) is the ceiling they approach.
-NCU_WARP_INSTR_PER_UNIT = {
-    "setup_bin_kernel": ("F", 25.0),
-    "scatter_kernel": ("F", 6.3),
-    "face_varyings_kernel": ("F", 4.6),
-    "tiled_shade_kernel": ("P", 31.2),
+# Per-unit counts of the forward kernels measured by ncu on the 256-scene
+# brax-like batch with the full run's tile configs pinned (shadow 16x8, main
+# 8x8, one warp per tile): DRAM bytes (dram__bytes_read.sum +
+# dram__bytes_write.sum) and warp instructions (smsp__inst_executed.sum) per
+# face (F, 1,470,504 per pass) or per pixel of the pass (P: 1,806,336 main,
+# 4,194,304 shadow).  Both grow with the faces or pixels a launch processes,
+# so a full launch's are these times its units.  Keyed by (pass, kernel);
+# the raster kernel's also by its tile shape and warps per tile.
+NCU_PER_UNIT = {
+    ("shadow", "setup_bin_kernel"): ("F", 93.71, 25.16),
+    ("main", "setup_bin_kernel"): ("F", 96.31, 27.92),
+    ("shadow", "scatter_kernel"): ("F", 8.28, 3.89),
+    ("main", "scatter_kernel"): ("F", 8.27, 7.24),
+    ("shadow", "raster_kernel", 16, 8, 1): ("P", 3.02, 13.45),
+    ("main", "raster_kernel", 8, 8, 1): ("P", 26.50, 36.38),
+    ("main", "face_varyings_kernel"): ("F", 29.93, 4.60),
+    ("main", "tiled_shade_kernel"): ("P", 59.94, 31.21),
 }
 
 
-# The raster kernel's DRAM bytes and warp instructions per launch, measured by
-# ncu on the full 4096-scene brax-like batch (one-pass metrics, the launches of
-# its first render), keyed by (tile width,
-# tile height, pixels of the pass): its traffic depends on the tile shape and
-# the scenes, so it applies to that workload's launches only.
-NCU_RASTER_LAUNCH = {
-    (16, 8, 67108864): (193032704 + 230909440, 887395880),  # shadow pass, 4096 x 128x128
-    (8, 8, 28901376): (767270400 + 121109504, 1036404822),  # main pass, 4096 x 84x84
-}
+def ncu_per_unit(pass_name, kname, cfg):
+    """(unit, DRAM bytes per unit, warp instructions per unit) measured for
+    this kernel on this pass (and tile config), or None."""
+    if kname == "raster_kernel":
+        if cfg is None:
+            return None
+        return NCU_PER_UNIT.get((pass_name, kname, int(cfg.tile_w), int(cfg.tile_h),
+                                 max(int(getattr(cfg, "warps_per_tile", 1)), 1)))
+    return NCU_PER_UNIT.get((pass_name, kname))
 
 
-def raster_launch_counts(cfg, info):
-    """(DRAM bytes, warp instructions) of a raster launch measured on this
-    very configuration, or None."""
-    if cfg is None or int(getattr(cfg, "warps_per_tile", 1)) > 1:
-        return None
-    return NCU_RASTER_LAUNCH.get((int(cfg.tile_w), int(cfg.tile_h), int(round(info["P"]))))
-
-
-def issue_roofline(kname, info, ms, clocks, warp_instr=None, source=None):
-    """Issue-slot ceiling of a launch of `kname`: ncu's warp instructions per
-    unit times the launch's units (or `warp_instr` measured for this very
-    launch), per second of the live launch time, over SMs x 4 schedulers x the
-    median SM clock sampled during the run."""
+def issue_roofline(ms, clocks, warp_instr, source):
+    """Issue-slot ceiling of a launch: `warp_instr` warp instructions per
+    second of the live launch time, over SMs x 4 schedulers x the median SM
+    clock sampled during the run."""
     import torch
 
-    if (warp_instr is None and kname not in NCU_WARP_INSTR_PER_UNIT) or ms <= 0:
+    if ms <= 0 or warp_instr is None:
         return None
     mhz = (clocks or {}).get("sm_mhz") or (clocks or {}).get("sm_max_mhz")
     if not mhz:
         return None
-    if warp_instr is None:
-        unit, per = NCU_WARP_INSTR_PER_UNIT[kname]
-        warp_instr = per * info[unit]
-        source = (f"ncu warp instructions per {'face' if unit == 'F' else 'pixel'} on the 256-scene "
-                  f"brax-like case x this launch's units")
     sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
     peak = sms * 4 * float(mhz) * 1e6
     achieved = warp_instr / (ms / 1e3)
@@ -1101,30 +1130,39 @@ def roofline(prof, visible, clocks=None):
     alg, info = bytes_of(dom)
     achieved = alg / (ms / 1e3) / 1e9 if ms > 0 else 0.0
     per_kernel = {}
+    current = ncu_counts_current()
     for name in cands:
-        b, _ = bytes_of(name)
+        b, inf = bytes_of(name)
         v = summ[name]
         gbs = b / (v["avg_ms"] / 1e3) / 1e9 if v["avg_ms"] > 0 else None
         per_kernel[name] = {"bytes": b, "GB/s": gbs, "frac": gbs / peak if gbs is not None else None}
-    traffic, traffic_note = None, None
+        r_k, p_k, k_k = prof["where"][name]
+        c_k = r_k.configs.get(p_k)
+        per_k = ncu_per_unit(p_k, k_k, c_k) if current and inf["slots"] == 1 and not (
+            c_k is not None and int(c_k.small_area) > 0) else None
+        if per_k is not None:
+            per_kernel[name]["traffic"] = per_k[1] * inf[per_k[0]]
+            iss = issue_roofline(v["avg_ms"], clocks, per_k[2] * inf[per_k[0]], "ncu per-unit count")
+            per_kernel[name]["issue_frac"] = iss["frac"] if iss else None
+    traffic, traffic_note, issue = None, None, None
     r_dom, p_dom, k_dom = prof["where"][dom]
     cfg = r_dom.configs.get(p_dom)
     small = cfg is not None and int(cfg.small_area) > 0
-    current = ncu_counts_current()
-    if not current:
+    per = ncu_per_unit(p_dom, k_dom, cfg)
+    if not ncu_counts_current():
         traffic_note = (f"null: the kernels changed since the ncu capture the per-unit counts come from "
                         f"(sources {library_digest()}, capture {NCU_SOURCE_DIGEST})")
-        small = True  # no per-unit counts apply
-    measured = raster_launch_counts(cfg, info) if current and k_dom == "raster_kernel" and info["slots"] == 1 else None
-    if measured is not None:
-        traffic = float(measured[0])
-        traffic_note = "ncu DRAM bytes of this launch on this workload at full size (one-pass metrics)"
-    elif k_dom in NCU_BYTES_PER_UNIT and not small and info["slots"] == 1:
-        unit, per = NCU_BYTES_PER_UNIT[k_dom]
-        traffic = per * info[unit]
-        traffic_note = (f"ncu DRAM bytes per {'face' if unit == 'F' else 'pixel'} of this kernel on the 256-scene "
-                        f"brax-like case, times this launch's {int(info[unit])} "
-                        f"{'faces' if unit == 'F' else 'pixels'}")
+    elif per is None or small or info["slots"] != 1:
+        traffic_note = "null: no ncu count for this kernel, pass and configuration"
+    else:
+        unit, bytes_per, instr_per = per
+        units = info[unit]
+        what = "face" if unit == "F" else "pixel"
+        traffic = bytes_per * units
+        traffic_note = (f"ncu DRAM bytes per {what} of this kernel and pass on the 256-scene brax-like case "
+                        f"(same tile config) x this launch's {int(units)} {what}s")
+        issue = issue_roofline(ms, clocks, instr_per * units,
+                               f"ncu warp instructions per {what} on the 256-scene case x this launch's {what}s")
     out = {
         "bound": "hbm",
         "limiter": "hbm",
@@ -1140,13 +1178,8 @@ def roofline(prof, visible, clocks=None):
         "algorithmic_bytes_per_launch": alg,
         "avg_launch_ms": ms,
     }
-    if measured is not None:
-        out["issue"] = issue_roofline(k_dom, info, ms, clocks, warp_instr=float(measured[1]),
-                                      source="ncu warp instructions of this launch on this workload at full size")
-    elif not small and info["slots"] == 1:
-        issue = issue_roofline(k_dom, info, ms, clocks)
-        if issue is not None:
-            out["issue"] = issue
+    if issue is not None:
+        out["issue"] = issue
     issue = out.get("issue")
     if issue is not None and issue["frac"] > out["frac"]:
         out["limiter"] = "issue"  # instruction issue, not DRAM bandwidth, bounds this kernel (frac in "issue")

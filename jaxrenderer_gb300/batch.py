@@ -415,7 +415,8 @@ class BatchRunner:
 
     form="plain": per-pixel scan over every primitive (rast_render_plain);
     form="tiled": binned tiles (rast_render_tiled) with `tiled_config`
-    (tile shape, bin capacity) from the autotuner when not given.
+    (one RastTiledConfig for both passes, or a {"shadow" / "main": config}
+    dict) from the autotuner where not given.
     `capture()` records one full render (buffer reset, depth pass, main pass)
     into a CUDA graph that `replay()` re-issues with a single launch.
     """
@@ -463,8 +464,11 @@ class BatchRunner:
             from .autotune import tiled_config_for
 
             for name, b, tbl in (("shadow", self.shadow_batch, sb.shadow_jobs), ("main", self.main_batch, sb.main_jobs)):
-                if b is not None:
-                    self.configs[name] = tiled_config if tiled_config is not None else tiled_config_for(self, name, b, tbl)
+                if b is None:
+                    continue
+                # one config for both passes, a {pass name: config} dict, or None (the autotuner's)
+                cfg = tiled_config.get(name) if isinstance(tiled_config, dict) else tiled_config
+                self.configs[name] = cfg if cfg is not None else tiled_config_for(self, name, b, tbl)
         self.ws = {}
         for name, b in (("shadow", self.shadow_batch), ("main", self.main_batch)):
             if b is None:

@@ -117,18 +117,36 @@ __device__ __forceinline__ int wrap_clamp(int i, int n) {
 }
 
 // Sequential (index-order) sum of squares of the `count` floats at v, by one
-// warp: lanes stage 32 values at a time in `stage`, lane 0 adds them in
-// order.  Every lane gets the total.
+// warp: every lane squares 4 values of a 128-value round into `stage`
+// (128 floats), lane 0 adds the round's squares in index order from
+// registers, and the next round's values are loaded while it adds.  The
+// running sum starts at +0 and the padding past `count` adds +0: a sum of
+// squares is never -0, so neither changes a bit of the index-order sum.
+// Every lane gets the total.
 __device__ __forceinline__ float warp_sum_sq_sequential(const float* v, int64_t count, float* stage) {
+  constexpr int kRound = 128;
   const int lane = threadIdx.x & 31;
+  auto load = [&](int64_t base, float* x) {
+#pragma unroll
+    for (int j = 0; j < kRound / 32; ++j) {
+      const int64_t k = base + 32 * j + lane;
+      x[j] = k < count ? v[k] : 0.0f;
+    }
+  };
   float acc = 0.0f;
-  for (int64_t base = 0; base < count; base += 32) {
-    const int64_t k = base + lane;
-    stage[lane] = k < count ? v[k] : 0.0f;
+  float x[kRound / 32];
+  load(0, x);
+  for (int64_t base = 0; base < count; base += kRound) {
+#pragma unroll
+    for (int j = 0; j < kRound / 32; ++j) stage[32 * j + lane] = x[j] * x[j];
     __syncwarp();
+    if (base + kRound < count) load(base + kRound, x);  // in flight while lane 0 adds
     if (lane == 0) {
-      const int m = static_cast<int>(min(static_cast<int64_t>(32), count - base));
-      for (int q = 0; q < m; ++q) acc = (base + q == 0) ? stage[q] * stage[q] : acc + stage[q] * stage[q];
+      float sq[kRound];
+#pragma unroll
+      for (int q = 0; q < kRound; ++q) sq[q] = stage[q];
+#pragma unroll
+      for (int q = 0; q < kRound; ++q) acc = acc + sq[q];
     }
     __syncwarp();
   }
@@ -138,7 +156,7 @@ __device__ __forceinline__ float warp_sum_sq_sequential(const float* v, int64_t 
 // One warp per mesh: the global norm of its normals (normalise() divides a
 // whole array by one norm).  Grid: ceil(n_meshes * 32 / kThreads).
 __global__ void __launch_bounds__(kThreads) mesh_norm_kernel(RastMergeBatch B, float* __restrict__ mesh_norm) {
-  __shared__ float stage[kThreads / 32][32];
+  __shared__ float stage[kThreads / 32][128];
   const int m = static_cast<int>((static_cast<int64_t>(blockIdx.x) * kThreads + threadIdx.x) >> 5);
   if (m >= B.n_meshes) return;
   const RastMesh M = B.meshes[m];
@@ -173,7 +191,7 @@ __device__ __forceinline__ void world_position(const float* p, const float* s, c
 __global__ void __launch_bounds__(kThreads)
 instance_kernel(RastMergeBatch B, const float* __restrict__ mesh_norm, float* __restrict__ mpos,
                 int* __restrict__ mobj, float* __restrict__ mnrm, float* __restrict__ muv) {
-  __shared__ float stage[kThreads / 32][32];
+  __shared__ float stage[kThreads / 32][128];
   const int o = static_cast<int>((static_cast<int64_t>(blockIdx.x) * kThreads + threadIdx.x) >> 5);
   const int lane = threadIdx.x & 31;
   if (o >= B.n_instances) return;  // whole warps

@@ -1,5 +1,6 @@
-"""bench.py's roofline arithmetic on the CPU: algorithmic bytes, the measured
-raster launch counts (applied only to the launch they were measured on) and
+"""bench.py's roofline arithmetic on the CPU: algorithmic bytes, the ncu
+per-unit counts (applied only to the pass and tile configuration they were
+measured on, and only while the kernels' sources are the ones measured) and
 the issue-slot ceiling.  No GPU: the device's SM count is faked."""
 import types
 
@@ -25,22 +26,27 @@ def test_kernel_bytes_raster_and_shade():
     assert bench.kernel_bytes("no_such_kernel", info, 0) == 0.0
 
 
-def test_raster_counts_only_for_the_measured_launch():
-    main = types.SimpleNamespace(tile_w=8, tile_h=8)
-    assert bench.raster_launch_counts(main, {"P": 4096 * 84 * 84.0}) == bench.NCU_RASTER_LAUNCH[(8, 8, 28901376)]
-    assert bench.raster_launch_counts(main, {"P": 256 * 84 * 84.0}) is None  # another batch size
-    assert bench.raster_launch_counts(types.SimpleNamespace(tile_w=16, tile_h=8), {"P": 4096 * 84 * 84.0}) is None
-    assert bench.raster_launch_counts(None, {"P": 1.0}) is None
+def test_ncu_counts_only_for_the_measured_pass_and_config():
+    cfg = lambda w, h, wpt=1: types.SimpleNamespace(tile_w=w, tile_h=h, warps_per_tile=wpt)  # noqa: E731
+    assert bench.ncu_per_unit("main", "raster_kernel", cfg(8, 8)) == bench.NCU_PER_UNIT[("main", "raster_kernel", 8, 8, 1)]
+    assert bench.ncu_per_unit("main", "raster_kernel", cfg(16, 8)) is None  # another tile shape
+    assert bench.ncu_per_unit("main", "raster_kernel", cfg(8, 8, 2)) is None  # two warps per tile
+    assert bench.ncu_per_unit("shadow", "raster_kernel", cfg(16, 8))[0] == "P"
+    assert bench.ncu_per_unit("main", "tiled_shade_kernel", None)[0] == "P"
+    assert bench.ncu_per_unit("main", "raster_kernel", None) is None
+
+
+def test_counts_are_stamped_with_the_forward_sources():
+    assert len(bench.NCU_SOURCE_DIGEST) == 16
+    assert bench.library_digest() == bench.library_digest(bench.FORWARD_SOURCES)
+    assert bench.library_digest(bench.FORWARD_SOURCES[:1]) != bench.library_digest()
 
 
 def test_issue_roofline(fake_device):
     clocks = {"sm_mhz": 2000.0, "sm_max_mhz": 2070.0}
     peak = 152 * 4 * 2000e6
-    got = bench.issue_roofline("raster_kernel", {"P": 1.0}, 2.0, clocks, warp_instr=peak * 1e-3, source="test")
+    got = bench.issue_roofline(2.0, clocks, peak * 1e-3, "test")
     assert got["peak"] == peak
     assert got["frac"] == pytest.approx(0.5)
-    per = bench.NCU_WARP_INSTR_PER_UNIT["tiled_shade_kernel"][1]
-    got = bench.issue_roofline("tiled_shade_kernel", {"P": 1e6}, 1.0, clocks)
-    assert got["achieved"] == pytest.approx(per * 1e6 / 1e-3)
-    assert bench.issue_roofline("raster_kernel", {"P": 1.0}, 1.0, clocks) is None  # no per-unit count
-    assert bench.issue_roofline("tiled_shade_kernel", {"P": 1.0}, 1.0, {"sm_mhz": None}) is None
+    assert bench.issue_roofline(1.0, clocks, None, "test") is None
+    assert bench.issue_roofline(1.0, {"sm_mhz": None}, 1.0, "test") is None
