@@ -248,6 +248,22 @@ size_t rast_tiled_workspace_bytes(const RastBatch* batch, const RastTiledConfig*
 int rast_render_tiled(const RastBatch* batch, const RastTiledConfig* cfg, void* workspace,
                       size_t workspace_bytes, void* stream);
 
+/* The two phases of rast_render_tiled, for callers that overlap passes.
+ * RAST_PHASE_COVERAGE: set-up, binning, rasterisation (depth-only jobs are
+ * complete after it) and the varyings of the faces that won a pixel, left
+ * in `workspace`; RAST_PHASE_SHADE: the deferred shading of those winners.
+ * A shade call must follow the coverage call of the same batch, config and
+ * workspace (stream-ordered); between the two the workspace must not be
+ * reused, and the inputs the shading reads (the shadow maps of
+ * PHONG_REFLECTION_SHADOW jobs, textures) may still be written, which is
+ * what lets a light-space depth pass run beside the main pass's coverage.
+ * Both bits = rast_render_tiled.  No counterpart in the reference (it
+ * traces one sequential program). */
+#define RAST_PHASE_COVERAGE 1
+#define RAST_PHASE_SHADE 2
+int rast_render_tiled_phase(const RastBatch* batch, const RastTiledConfig* cfg, void* workspace,
+                            size_t workspace_bytes, void* stream, int phase);
+
 /* rast_render_tiled with per-kernel timing (synchronises `stream`). */
 int rast_render_tiled_profiled(const RastBatch* batch, const RastTiledConfig* cfg, void* workspace,
                                size_t workspace_bytes, void* stream, RastProfile* profile);

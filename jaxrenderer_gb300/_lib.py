@@ -41,6 +41,8 @@ STATUS_NAMES = {
     8: "RAST_ERR_STATIC_SCRATCH_TOO_SMALL",
 }
 STATIC_SCRATCH_BYTES = 64 << 20
+PHASE_COVERAGE = 1
+PHASE_SHADE = 2
 
 F16 = c_float * 16
 F3 = c_float * 3
@@ -206,6 +208,8 @@ PROTOTYPES = [
      [POINTER(RastBatch), POINTER(RastTiledConfig), c_void_p, c_size_t, c_void_p, POINTER(RastProfile)]),
     ("rast_render_tiled_static", c_int, [POINTER(RastBatch), POINTER(RastTiledConfig), c_void_p]),
     ("rast_autotune", c_int, [POINTER(RastBatch), c_void_p, POINTER(RastTiledConfig)]),
+    ("rast_render_tiled_phase", c_int, [POINTER(RastBatch), POINTER(RastTiledConfig), c_void_p, c_size_t, c_void_p,
+                                        c_int]),
     ("rast_tiled_stats", c_int,
      [POINTER(RastBatch), POINTER(RastTiledConfig), c_void_p, c_void_p, POINTER(RastTiledStats)]),
     ("rast_backward_workspace_bytes", c_size_t, [POINTER(RastBatch)]),

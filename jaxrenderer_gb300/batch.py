@@ -422,9 +422,10 @@ class BatchRunner:
     """
 
     def __init__(self, sb: SceneBatch, form: str = "plain", want_prim_id: bool = True, count_ties: bool = False,
-                 tiled_config=None):
+                 tiled_config=None, overlap_passes: bool = True):
         self.sb = sb
         self.form = form
+        self.overlap_passes = overlap_passes
         dev = sb.device
         n, W, H = sb.n_scenes, sb.width, sb.height
         self.canvas = torch.empty((n, W, H, 3), dtype=torch.float32, device=dev)
@@ -488,9 +489,16 @@ class BatchRunner:
             return self.lib.rast_plain_workspace_bytes(ctypes.byref(b))
         return self.lib.rast_tiled_workspace_bytes(ctypes.byref(b), self._cfg(name))
 
-    def launch(self, name, stream_handle, profile=None) -> None:
+    def launch(self, name, stream_handle, profile=None, phase: int = 3) -> None:
+        """Render pass `name` on the stream; `phase` (tiled form) selects
+        rast_render_tiled_phase's coverage (1) or shade (2) half, 3 both."""
         b = self.shadow_batch if name == "shadow" else self.main_batch
         buf, nbytes = self.ws[name]
+        if self.form == "tiled" and phase != 3 and profile is None:
+            st = self.lib.rast_render_tiled_phase(ctypes.byref(b), self._cfg(name), buf.data_ptr(), nbytes,
+                                                  stream_handle, int(phase))
+            _lib.check(st, "rast_render_tiled_phase")
+            return
         if self.form == "plain":
             if profile is None:
                 st = self.lib.rast_render_plain(ctypes.byref(b), buf.data_ptr(), nbytes, stream_handle)
@@ -602,16 +610,38 @@ class BatchRunner:
             self.shadow_map.fill_(float(np.finfo(np.float32).max))
 
     def run(self, stream: Optional[torch.cuda.Stream] = None, zbuffer_default: float = 1.0) -> BatchOutputs:
-        """Reset the buffers to their defaults and render every scene
-        (depth pass, then main pass) on `stream`."""
+        """Reset the buffers to their defaults and render every scene on
+        `stream`: the depth pass, then the main pass.  In the tiled form with
+        `overlap_passes`, the depth pass runs on a side stream beside the main
+        pass's coverage phase (which reads no shadow map), and the main
+        pass's shading waits for both: a fork and a join, which a CUDA graph
+        capture records as two branches."""
         s = stream if stream is not None else torch.cuda.current_stream(self.sb.device)
         with torch.cuda.stream(s):
             self._reset(zbuffer_default)
-            for name, _ in self.batches():
-                torch.cuda.nvtx.range_push(f"{name} pass")
-                self.launch(name, s.cuda_stream)
+            if self.form == "tiled" and self.shadow_batch is not None and self.overlap_passes:
+                side = self._side_stream()
+                side.wait_stream(s)
+                with torch.cuda.stream(side):
+                    torch.cuda.nvtx.range_push("shadow pass")
+                    self.launch("shadow", side.cuda_stream)
+                    torch.cuda.nvtx.range_pop()
+                torch.cuda.nvtx.range_push("main pass")
+                self.launch("main", s.cuda_stream, phase=_lib.PHASE_COVERAGE)
+                s.wait_stream(side)
+                self.launch("main", s.cuda_stream, phase=_lib.PHASE_SHADE)
                 torch.cuda.nvtx.range_pop()
+            else:
+                for name, _ in self.batches():
+                    torch.cuda.nvtx.range_push(f"{name} pass")
+                    self.launch(name, s.cuda_stream)
+                    torch.cuda.nvtx.range_pop()
         return self.outputs()
+
+    def _side_stream(self) -> torch.cuda.Stream:
+        if getattr(self, "_side", None) is None:
+            self._side = torch.cuda.Stream(self.sb.device)
+        return self._side
 
     def outputs(self) -> BatchOutputs:
         return BatchOutputs(self.canvas, self.zbuffer, self.prim_id, self.shadow_map, self.shadow_prim, self.ties)

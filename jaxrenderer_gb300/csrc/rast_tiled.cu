@@ -1095,9 +1095,11 @@ static void launch_raster(TileShape ts, int wpt, int sms, cudaStream_t s, const 
 }
 
 static int render(const RastBatch* batch, const RastTiledConfig* cfg, void* workspace,
-                  size_t workspace_bytes, void* stream, RastProfile* profile) {
+                  size_t workspace_bytes, void* stream, RastProfile* profile,
+                  int phase = RAST_PHASE_COVERAGE | RAST_PHASE_SHADE) {
   int st = check_batch(batch);
   if (st != RAST_OK) return st;
+  if (phase < 1 || phase > (RAST_PHASE_COVERAGE | RAST_PHASE_SHADE)) return RAST_ERR_INVALID_ARGUMENT;
   const RastBatch& b = *batch;
   TileShape ts{cfg ? cfg->tile_w : 8, cfg ? cfg->tile_h : 8};
   const int wpt = warps_per_tile_of(cfg);
@@ -1124,68 +1126,72 @@ static int render(const RastBatch* batch, const RastTiledConfig* cfg, void* work
   unsigned int* misc = reinterpret_cast<unsigned int*>(ws + L.misc_off);
   Profiler prof(profile, s, "rast_render_tiled");
 
-  // counts and cursors are adjacent: one memset clears both, plus the counters
-  if (cudaMemsetAsync(counts, 0, L.offsets_off - L.counts_off, s) != cudaSuccess) return RAST_ERR_CUDA;
-  if (cudaMemsetAsync(misc, 0, 256, s) != cudaSuccess) return RAST_ERR_CUDA;
-  unsigned long long* keys = nullptr;
-  if (L.small_path && b.total_pixels > 0 && b.total_setup > 0) {
-    keys = reinterpret_cast<unsigned long long*>(ws + L.keys_off);
-    if (cudaMemsetAsync(keys, 0xff, static_cast<size_t>(b.total_pixels) * sizeof(unsigned long long), s) !=
-        cudaSuccess)  // every key starts as kEmptyKey
-      return RAST_ERR_CUDA;
-  }
+  const bool cover = (phase & RAST_PHASE_COVERAGE) != 0, shade = (phase & RAST_PHASE_SHADE) != 0;
   unsigned char* vis = L.vstride > 0 ? reinterpret_cast<unsigned char*>(ws + L.vis_off) : nullptr;
   float* fvar = L.vstride > 0 ? reinterpret_cast<float*>(ws + L.fvar_off) : nullptr;
-  if (vis && b.total_setup > 0 && cudaMemsetAsync(vis, 0, static_cast<size_t>(b.total_setup), s) != cudaSuccess)
-    return RAST_ERR_CUDA;
-  prof.mark("memset");
-  int2* fmap = reinterpret_cast<int2*>(ws + L.fmap_off);
-  if (b.total_setup > 0) {
-    if (build_block_map(b, kMapFaces, kSetupThreads, fmap, reinterpret_cast<unsigned*>(ws + L.fstart_off), s) !=
-        cudaSuccess)
-      return RAST_ERR_CUDA;
-    prof.mark("block_map_kernel");
-    const unsigned grid = L.fmap_blocks;
-    if (keys)
-      setup_bin_kernel<true><<<grid, kSetupThreads, 0, s>>>(b, L.G, fmap, setup, bbox, counts, keys, small_area);
-    else
-      setup_bin_kernel<false><<<grid, kSetupThreads, 0, s>>>(b, L.G, fmap, setup, bbox, counts, nullptr, 0);
-    prof.mark("setup_bin_kernel");
-    scan_local_kernel<<<static_cast<unsigned>(L.n_scan_blocks), 256, 0, s>>>(counts, offsets, bsums, L.n_tiles);
-    scan_apply_kernel<<<static_cast<unsigned>(L.n_scan_blocks), 256, 0, s>>>(counts, offsets, bsums, L.n_tiles,
-                                                                              L.bin_capacity, misc + 1);
-    prof.mark("scan_kernels");
-    scatter_kernel<<<grid, kSetupThreads, 0, s>>>(b, L.G, fmap, bbox, offsets, cursors, bins);
-    prof.mark("scatter_kernel");
-  }
-  if (b.total_pixels > 0) {
-    int sms = 0, dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (b.total_setup > 0) {
-      // the key path exists only when ties are not counted and no job is
-      // layered
-      if (keys)
-        launch_raster<true, false, 1>(ts, wpt, sms, s, b, L, setup, counts, offsets, bins, winner, misc, vis, keys);
-      else if (b.max_layers > 0 && b.near_ties)
-        launch_raster<false, true, RAST_MAX_LAYERS>(ts, wpt, sms, s, b, L, setup, counts, offsets, bins, winner, misc,
-                                                    vis, nullptr);
-      else if (b.max_layers > 0)
-        launch_raster<false, false, RAST_MAX_LAYERS>(ts, wpt, sms, s, b, L, setup, counts, offsets, bins, winner, misc,
-                                                     vis, nullptr);
-      else if (b.near_ties)
-        launch_raster<false, true, 1>(ts, wpt, sms, s, b, L, setup, counts, offsets, bins, winner, misc, vis, nullptr);
-      else
-        launch_raster<false, false, 1>(ts, wpt, sms, s, b, L, setup, counts, offsets, bins, winner, misc, vis, nullptr);
-    } else {
-      if (cudaMemsetAsync(winner, 0xff, static_cast<size_t>(b.total_pixels) * 4 * L.winner_layers, s) != cudaSuccess)
+  // shaded jobs resolve in the deferred shade (from the per-face varyings when there are faces)
+  const bool shading = b.total_pixels > 0 && (b.shader_mask != (1 << RAST_SHADER_DEPTH) || b.total_setup == 0);
+  const bool pre = shading && fvar != nullptr && b.total_setup > 0;
+  if (cover) {
+    // counts and cursors are adjacent: one memset clears both, plus the counters
+    if (cudaMemsetAsync(counts, 0, L.offsets_off - L.counts_off, s) != cudaSuccess) return RAST_ERR_CUDA;
+    if (cudaMemsetAsync(misc, 0, 256, s) != cudaSuccess) return RAST_ERR_CUDA;
+    unsigned long long* keys = nullptr;
+    if (L.small_path && b.total_pixels > 0 && b.total_setup > 0) {
+      keys = reinterpret_cast<unsigned long long*>(ws + L.keys_off);
+      if (cudaMemsetAsync(keys, 0xff, static_cast<size_t>(b.total_pixels) * sizeof(unsigned long long), s) !=
+          cudaSuccess)  // every key starts as kEmptyKey
         return RAST_ERR_CUDA;
     }
-    prof.mark("raster_kernel");
-    const int64_t max_px = static_cast<int64_t>(b.max_width) * b.max_height;
-    const dim3 sgrid(static_cast<unsigned>((max_px + 255) / 256), static_cast<unsigned>(b.n_jobs));
-    if (b.shader_mask != (1 << RAST_SHADER_DEPTH) || b.total_setup == 0) {
-      const bool pre = fvar != nullptr && b.total_setup > 0;
+    if (vis && b.total_setup > 0 && cudaMemsetAsync(vis, 0, static_cast<size_t>(b.total_setup), s) != cudaSuccess)
+      return RAST_ERR_CUDA;
+    prof.mark("memset");
+    int2* fmap = reinterpret_cast<int2*>(ws + L.fmap_off);
+    if (b.total_setup > 0) {
+      if (build_block_map(b, kMapFaces, kSetupThreads, fmap, reinterpret_cast<unsigned*>(ws + L.fstart_off), s) !=
+          cudaSuccess)
+        return RAST_ERR_CUDA;
+      prof.mark("block_map_kernel");
+      const unsigned grid = L.fmap_blocks;
+      if (keys)
+        setup_bin_kernel<true><<<grid, kSetupThreads, 0, s>>>(b, L.G, fmap, setup, bbox, counts, keys, small_area);
+      else
+        setup_bin_kernel<false><<<grid, kSetupThreads, 0, s>>>(b, L.G, fmap, setup, bbox, counts, nullptr, 0);
+      prof.mark("setup_bin_kernel");
+      scan_local_kernel<<<static_cast<unsigned>(L.n_scan_blocks), 256, 0, s>>>(counts, offsets, bsums, L.n_tiles);
+      scan_apply_kernel<<<static_cast<unsigned>(L.n_scan_blocks), 256, 0, s>>>(counts, offsets, bsums, L.n_tiles,
+                                                                                L.bin_capacity, misc + 1);
+      prof.mark("scan_kernels");
+      scatter_kernel<<<grid, kSetupThreads, 0, s>>>(b, L.G, fmap, bbox, offsets, cursors, bins);
+      prof.mark("scatter_kernel");
+    }
+    if (b.total_pixels > 0) {
+      int sms = 0, dev = 0;
+      cudaGetDevice(&dev);
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+      if (b.total_setup > 0) {
+        // the key path exists only when ties are not counted and no job is
+        // layered
+        if (keys)
+          launch_raster<true, false, 1>(ts, wpt, sms, s, b, L, setup, counts, offsets, bins, winner, misc, vis, keys);
+        else if (b.max_layers > 0 && b.near_ties)
+          launch_raster<false, true, RAST_MAX_LAYERS>(ts, wpt, sms, s, b, L, setup, counts, offsets, bins, winner,
+                                                      misc, vis, nullptr);
+        else if (b.max_layers > 0)
+          launch_raster<false, false, RAST_MAX_LAYERS>(ts, wpt, sms, s, b, L, setup, counts, offsets, bins, winner,
+                                                       misc, vis, nullptr);
+        else if (b.near_ties)
+          launch_raster<false, true, 1>(ts, wpt, sms, s, b, L, setup, counts, offsets, bins, winner, misc, vis,
+                                        nullptr);
+        else
+          launch_raster<false, false, 1>(ts, wpt, sms, s, b, L, setup, counts, offsets, bins, winner, misc, vis,
+                                         nullptr);
+      } else {
+        if (cudaMemsetAsync(winner, 0xff, static_cast<size_t>(b.total_pixels) * 4 * L.winner_layers, s) !=
+            cudaSuccess)
+          return RAST_ERR_CUDA;
+      }
+      prof.mark("raster_kernel");
       if (pre) {
         int2* vmap = reinterpret_cast<int2*>(ws + L.vmap_off);
         if (build_block_map(b, kMapFaces, kVaryRows, vmap, reinterpret_cast<unsigned*>(ws + L.vstart_off), s) !=
@@ -1194,13 +1200,17 @@ static int render(const RastBatch* batch, const RastTiledConfig* cfg, void* work
         face_varyings_kernel<<<L.vmap_blocks, kFaceThreads, 0, s>>>(b, vmap, vis, fvar, L.vstride);
         prof.mark("face_varyings_kernel");
       }
-      const float* fv = pre ? fvar : nullptr;
-      if (b.max_layers > 0)
-        tiled_shade_kernel<true><<<sgrid, 256, 0, s>>>(b, setup, winner, b.total_setup > 0, fv, L.vstride);
-      else
-        tiled_shade_kernel<false><<<sgrid, 256, 0, s>>>(b, setup, winner, b.total_setup > 0, fv, L.vstride);
-      prof.mark("tiled_shade_kernel");
     }
+  }
+  if (shade && shading) {
+    const int64_t max_px = static_cast<int64_t>(b.max_width) * b.max_height;
+    const dim3 sgrid(static_cast<unsigned>((max_px + 255) / 256), static_cast<unsigned>(b.n_jobs));
+    const float* fv = pre ? fvar : nullptr;
+    if (b.max_layers > 0)
+      tiled_shade_kernel<true><<<sgrid, 256, 0, s>>>(b, setup, winner, b.total_setup > 0, fv, L.vstride);
+    else
+      tiled_shade_kernel<false><<<sgrid, 256, 0, s>>>(b, setup, winner, b.total_setup > 0, fv, L.vstride);
+    prof.mark("tiled_shade_kernel");
   }
   const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return RAST_ERR_CUDA;
@@ -1245,6 +1255,11 @@ extern "C" int rast_tiled_stats(const RastBatch* batch, const RastTiledConfig* c
 extern "C" int rast_render_tiled(const RastBatch* batch, const RastTiledConfig* cfg, void* workspace,
                                  size_t workspace_bytes, void* stream) {
   return tiled::render(batch, cfg, workspace, workspace_bytes, stream, nullptr);
+}
+
+extern "C" int rast_render_tiled_phase(const RastBatch* batch, const RastTiledConfig* cfg, void* workspace,
+                                       size_t workspace_bytes, void* stream, int phase) {
+  return tiled::render(batch, cfg, workspace, workspace_bytes, stream, nullptr, phase);
 }
 
 extern "C" int rast_render_tiled_profiled(const RastBatch* batch, const RastTiledConfig* cfg,
