@@ -61,10 +61,7 @@ def _cameras(positions: np.ndarray, params: CameraParameters, targets=None):
     Renderer.create_camera_from_parameters gives for that camera, plus the
     shared viewport."""
     positions = np.asarray(positions, F32).reshape(-1, 3)
-    first = params._replace(position=positions[0])
-    if targets is not None:
-        first = first._replace(target=np.asarray(targets, F32).reshape(-1, 3)[0])
-    cam = Renderer.create_camera_from_parameters(first)  # projection and viewport are shared
+    cam = _lens(params)  # projection and viewport are shared
     centre = np.asarray(targets if targets is not None else params.target, F32)
     up = np.asarray(params.up, F32)
     view = view_matrices(positions, centre, up)
@@ -74,9 +71,28 @@ def _cameras(positions: np.ndarray, params: CameraParameters, targets=None):
     return w2c, w2e, view, cam.viewport
 
 
-def _light_cameras(light_direction, viewport, centres: np.ndarray, up):
+_LENSES: dict = {}
+
+
+def _lens(params: CameraParameters) -> Camera:
+    """A camera of `params` (its projection and viewport, which do not depend
+    on the position or target), built once per set of shared parameters."""
+    key = repr(tuple(np.asarray(getattr(params, f)).tolist() for f in
+                     ("viewWidth", "viewHeight", "viewDepth", "near", "far", "hfov", "vfov", "up")))
+    cam = _LENSES.get(key)
+    if cam is None:
+        with np.errstate(all="ignore"):  # the stand-in position may be parallel to `up`: its view is unused
+            cam = Renderer.create_camera_from_parameters(params._replace(position=np.array((1.0, 0.0, 0.0), F32),
+                                                                         target=np.zeros(3, F32)))
+        _LENSES[key] = cam
+    return cam
+
+
+def _light_cameras(light_direction, viewport, centres: np.ndarray, up, eye_norm: bool = True):
     """Shadow.light_camera for one centre per row: (world_to_clip,
-    world_to_eye_norm), bit for bit the single-centre results."""
+    world_to_eye_norm), bit for bit the single-centre results.  With
+    `eye_norm` False the second is None (the DepthShader the light cameras
+    serve reads no normal transform)."""
     from .geometry import _arr, lu_inverse
 
     d = _arr(light_direction, F32)
@@ -85,7 +101,7 @@ def _light_cameras(light_direction, viewport, centres: np.ndarray, up):
     view = view_matrices(eye, c, _arr(up, F32))
     ortho = Camera.orthographic_projection_matrix(-1.0, 1.0, -1.0, 1.0, -1.0, 1.0)
     w2c = bmatmul(ortho, view)
-    w2e = np.ascontiguousarray(np.swapaxes(lu_inverse(view), -1, -2))
+    w2e = np.ascontiguousarray(np.swapaxes(lu_inverse(view), -1, -2)) if eye_norm else None
     return w2c, w2e
 
 
@@ -211,14 +227,14 @@ def frame_matrices(t: SceneTables, positions, targets, params: CameraParameters,
         svp = t.shadow_jobs["viewport"][0].reshape(4, 4)
         centre = np.asarray(shadow_param.centre, F32)
         if centre.ndim == 2:  # one shadow centre per scene
-            s_w2c, s_w2e = _light_cameras(light.direction, svp, centre, shadow_param.up)
+            s_w2c, _ = _light_cameras(light.direction, svp, centre, shadow_param.up, eye_norm=False)
         else:
             scam = Shadow.light_camera(np.asarray(light.direction, F32), svp, centre, shadow_param.up)
             s_w2c = np.broadcast_to(scam.world_to_clip, (n, 4, 4))
-            s_w2e = np.broadcast_to(scam.world_to_eye_norm, (n, 4, 4))
         sel = np.nonzero(t.shadow_index >= 0)[0]
         t.shadow_jobs["world_to_clip"] = s_w2c[sel].reshape(-1, 16)
-        t.shadow_jobs["world_to_eye_norm"] = s_w2e[sel].reshape(-1, 16)
+        # the DepthShader transforms no normals: its world_to_eye_norm stays the identity
+        t.shadow_jobs["world_to_eye_norm"] = np.identity(4, dtype=F32).reshape(16)
         main["shadow_world_to_clip"][sel] = s_w2c[sel].reshape(-1, 16)
     return t
 
