@@ -1190,7 +1190,7 @@ def roofline(prof, visible, clocks=None):
                            "pixel_triangle_tests_per_launch": tests or None,
                            "bin_entries": info["E"] or None,
                            "counted": ("W x H x F of the pass" if kname == "scan_kernel" else
-                                       "in the kernel: staged bin entries x tile pixels, one add per warp")}
+                                       "in the kernel: dense entries x the warp's pixels + pair-path pairs, one add per warp")}
     return out, per_kernel
 
 

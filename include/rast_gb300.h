@@ -237,14 +237,18 @@ typedef struct RastTiledConfig {
 size_t rast_tiled_workspace_bytes(const RastBatch* batch, const RastTiledConfig* cfg);
 
 /* Tiled form for many scenes per call.  Per face: clip positions, set-up and
- * a conservative tile range of its coverage (a superset of the pixels whose
- * FP32 edge functions can pass); bin counts, exclusive prefix sum, scatter of
- * primitive ids into per-tile bins; persistent warps rasterise one tile at a
- * time with bin entries staged in shared memory (packed depth|id minimum per
- * pixel); deferred shading of the winners.  Identical results to
- * rast_render_plain.  Tiles whose bins exceed bin_capacity are rasterised by a
- * scan over all primitives of their job (same results, slower).  Launches only
- * kernels and memsets on `stream`: capturable in a CUDA graph. */
+ * a conservative pixel rectangle of its coverage (a superset of the pixels
+ * whose FP32 edge functions can pass); bin counts, exclusive prefix sum,
+ * scatter of primitive ids into the bins of the tiles the rectangle touches;
+ * persistent warps rasterise one tile at a time with bin entries staged in
+ * shared memory (packed depth|id minimum per pixel; an entry whose rectangle
+ * covers few pixels of the tile is tested at those pixels only); deferred
+ * shading of the winners.  Identical results to rast_render_plain.  Tiles
+ * whose bins exceed bin_capacity are rasterised by a scan over all primitives
+ * of their job (same results, slower).  Jobs wider or taller than 65535
+ * pixels: RAST_ERR_UNSUPPORTED (the rectangles are 16-bit; the plain form
+ * has no such limit).  Launches only kernels and memsets on `stream`:
+ * capturable in a CUDA graph. */
 int rast_render_tiled(const RastBatch* batch, const RastTiledConfig* cfg, void* workspace,
                       size_t workspace_bytes, void* stream);
 
@@ -321,9 +325,11 @@ typedef struct RastTiledStats {
   uint64_t tiles;         /* tile slots (jobs x tiles of the largest job) */
   uint32_t overflow;      /* 1: some tiles exceeded the capacity and were full-scanned */
   uint32_t reserved;
-  uint64_t pixel_tests;   /* pixel-triangle pairs the raster kernel tested: staged bin entries (those
-                             whose triangle can reach the tile) x the tile's pixels, counted per warp
-                             (faces of the small-face path are not included) */
+  uint64_t pixel_tests;   /* pixel-triangle pairs the raster kernel tested, counted per warp: entries
+                             tested against every pixel of the warp's part of the tile x its pixels,
+                             plus the (entry, pixel) pairs of the pair path (the pixels of an
+                             entry's coverage rectangle inside the tile); faces of the small-face
+                             path are not included */
 } RastTiledStats;
 
 int rast_tiled_stats(const RastBatch* batch, const RastTiledConfig* cfg, const void* workspace,

@@ -134,8 +134,9 @@ __device__ __forceinline__ void clip_push0(ClipStage& s, ClipStage& s1, ClipStag
 // box by one pixel.  When those three half-planes bound a triangle whose
 // corners are known to a quarter pixel, the clipping is skipped: the
 // corners' box, clamped to the screen, contains the clipped box (equals it
-// for a triangle inside the rectangle).  Returns false when no pixel can be
-// covered.
+// for a triangle inside the rectangle), and half a pixel of margin covers
+// the corners' error and the rounding of the pixel <-> NDC maps.  Returns
+// false when no pixel can be covered.
 // The job's screen rectangle one pixel wider on every side, in NDC (pixels
 // -1 and W), computed once per block.
 struct ScreenRect {
@@ -231,6 +232,7 @@ __device__ __forceinline__ bool coverage_bbox(const float* inv, const RastJob& J
   float mnx, mxx, mny, mxy;
   float tx[3], ty[3];
   const float psx = fabsf(sx), psy = fabsf(sy);
+  bool tight = false;  // the box is the widened triangle's (corners known to a quarter pixel)
   if (widened_triangle(a0, b0, c0, a1, b1, c1, a2, b2, c2, psx, psy, tx, ty)) {
     // the region lies in the triangle tx, ty: its corners' box (clamped to
     // the screen below) contains the clipped box, and equals it when the
@@ -239,6 +241,7 @@ __device__ __forceinline__ bool coverage_bbox(const float* inv, const RastJob& J
     mxx = fmaxf(tx[0], fmaxf(tx[1], tx[2]));
     mny = fminf(ty[0], fminf(ty[1], ty[2]));
     mxy = fmaxf(ty[0], fmaxf(ty[1], ty[2]));
+    tight = true;
   } else {
     ClipStage s0{a0, b0, c0, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, false};
     ClipStage s1{a1, b1, c1, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, false};
@@ -256,8 +259,25 @@ __device__ __forceinline__ bool coverage_bbox(const float* inv, const RastJob& J
   // NDC -> pixel index: i = x * sx + ox (monotone in x with the sign of sx)
   const float pa = mnx * sx + ox, pb = mxx * sx + ox;
   const float qa = mny * sy + oy, qb = mxy * sy + oy;
-  const float ilo = floorf(fminf(pa, pb)) - 1.0f, ihi = ceilf(fmaxf(pa, pb)) + 1.0f;
-  const float jlo = floorf(fminf(qa, qb)) - 1.0f, jhi = ceilf(fmaxf(qa, qb)) + 1.0f;
+  float ilo, ihi, jlo, jhi;
+  if (tight) {
+    // Corners within a quarter pixel: a pixel i whose rounded NDC x lies in
+    // the region has i >= min(pa, pb) - 1/4 - e, e the rounding of pa
+    // (2u |pa|) and of the pixel's quotient (2u |i - ox| pixels), both below
+    // 1/8 pixel for |pa| < 2^20 (beyond that the clamp below decides), so
+    // i >= ceil(min - 1/2); likewise i <= floor(max + 1/2).
+    ilo = ceilf(fminf(pa, pb) - 0.5f);
+    ihi = floorf(fmaxf(pa, pb) + 0.5f);
+    jlo = ceilf(fminf(qa, qb) - 0.5f);
+    jhi = floorf(fmaxf(qa, qb) + 0.5f);
+  } else {
+    // the clipped polygon's corners come from fast quotients: one pixel of
+    // margin on each side
+    ilo = floorf(fminf(pa, pb)) - 1.0f;
+    ihi = ceilf(fmaxf(pa, pb)) + 1.0f;
+    jlo = floorf(fminf(qa, qb)) - 1.0f;
+    jhi = ceilf(fmaxf(qa, qb)) + 1.0f;
+  }
   if (!(ihi >= 0.0f) || !(ilo <= static_cast<float>(W - 1)) || !(jhi >= 0.0f) ||
       !(jlo <= static_cast<float>(H - 1)))
     return false;
@@ -271,11 +291,17 @@ __device__ __forceinline__ bool coverage_bbox(const float* inv, const RastJob& J
 // ------------------------------------------------------------------ kernels
 
 struct Geometry {
-  int tw, th;       // tile shape
+  int tw, th;       // bin tile shape (powers of two)
+  int tws, ths;     // log2 of tw, th: pixel index -> tile index by shifting
   int tiles_x;      // tiles along x of the largest job (stride)
   int tiles_y;
   int tiles_per_job;
 };
+
+// Per-face coverage rectangle in pixels, [x, z] x [y, w] (ushort4: i0, j0,
+// i1, j1); empty (x > z) for faces that are not binned.
+constexpr unsigned short kNoRect = 0xffff;
+__device__ __forceinline__ ushort4 empty_rect() { return make_ushort4(kNoRect, kNoRect, 0, 0); }
 
 // Vertex positions of face f of job J -> clip space (same operations as the
 // vertex shader's gl_Position).
@@ -410,7 +436,7 @@ setup_bin_kernel(RastBatch B, Geometry G, const int2* __restrict__ fmap, float4*
     setup[row * 4 + 3] = make_float4(det, __int_as_float(flags), 0.0f, 0.0f);
     cand = (flags & kCandidate) == kCandidate;
     queued = cand || f == 0;
-    if (!cand) bbox[row] = make_ushort4(1, 1, 0, 0);  // empty: lo > hi
+    if (!cand) bbox[row] = empty_rect();
   }
   const unsigned qm = __ballot_sync(0xffffffffu, queued);
   int base = 0;
@@ -442,16 +468,16 @@ setup_bin_kernel(RastBatch B, Geometry G, const int2* __restrict__ fmap, float4*
       out[1] = make_float4(iv[4], iv[5], iv[6], iv[7]);
       out[2] = make_float4(iv[8], s_m[9][q], s_m[10][q], s_m[11][q]);
       if (!(entry & kRecordOnly)) {
-        ushort4 bb = make_ushort4(1, 1, 0, 0);
+        ushort4 bb = empty_rect();
         if (coverage_bbox(iv, J, s_rect, &i0, &i1, &j0, &j1)) {
           if (kSmall && (i1 - i0 + 1) * (j1 - j0 + 1) <= small_area) {
             small = true;  // rasterised in phase 3, not binned
           } else {
-            tx0 = i0 / G.tw;
-            tx1 = i1 / G.tw;
-            ty0 = j0 / G.th;
-            ty1 = j1 / G.th;
-            bb = make_ushort4(tx0, ty0, tx1, ty1);
+            tx0 = i0 >> G.tws;
+            tx1 = i1 >> G.tws;
+            ty0 = j0 >> G.ths;
+            ty1 = j1 >> G.ths;
+            bb = make_ushort4(i0, j0, i1, j1);  // the raster kernel tests only these pixels of each tile
           }
         }
         bbox[J.setup_begin + fq] = bb;
@@ -586,11 +612,18 @@ scatter_kernel(RastBatch B, Geometry G, const int2* __restrict__ fmap, const ush
   const int nf = __ldg(&B.jobs[jid].n_faces);
   const int f = blk.y + static_cast<int>(threadIdx.x);
   if (f - static_cast<int>(threadIdx.x & 31) >= nf) return;  // the whole warp is past the faces
-  ushort4 bb = make_ushort4(1, 1, 0, 0);
+  ushort4 bb = empty_rect();
   if (f < nf) bb = bbox[__ldg(&B.jobs[jid].setup_begin) + f];
+  int tx0 = 1, ty0 = 1, tx1 = 0, ty1 = 0;  // the pixel rectangle's tiles
+  if (bb.x <= bb.z && bb.y <= bb.w) {
+    tx0 = bb.x >> G.tws;
+    tx1 = bb.z >> G.tws;
+    ty0 = bb.y >> G.ths;
+    ty1 = bb.w >> G.ths;
+  }
   const int64_t tb = static_cast<int64_t>(jid) * G.tiles_per_job;
   const int lane = threadIdx.x & 31;
-  warp_tiles(bb.x, bb.y, bb.z, bb.w, G.tiles_x, [&](int owner, int tile, bool valid) {
+  warp_tiles(tx0, ty0, tx1, ty1, G.tiles_x, [&](int owner, int tile, bool valid) {
     const uint32_t o = valid ? offsets[tb + tile] : kOverflow;
     const bool write = !(o & kOverflow);
     const unsigned peers = __match_any_sync(0xffffffffu, write ? tile : -1);
@@ -619,20 +652,46 @@ __device__ __forceinline__ bool edge_misses_tile(float ea, float eb, float ec, f
 
 // Persistent warps: each takes one tile (of any job) at a time.  Lane l owns
 // PPL pixels of the tile.  Bin entries are staged 32 at a time in the warp's
-// slice of shared memory (one record per lane), then every lane tests its
-// pixels against the 32 staged setups.  Tiles whose bin overflowed scan
-// every primitive of the job instead.  Each pixel keeps its kL smallest
-// keys (kL = 1: the default chooser; kL = RAST_MAX_LAYERS for batches with
-// layered jobs), slot s written to winner[s * total_pixels + pixel].
+// slice of shared memory (one record per lane), then tested against the
+// tile's pixels.  Tiles whose bin overflowed scan every primitive of the job
+// instead.  Each pixel keeps its kL smallest keys (kL = 1: the default
+// chooser; kL = RAST_MAX_LAYERS for batches with layered jobs), slot s
+// written to winner[s * total_pixels + pixel].
+//
+// Pair path (kL = 1 without near-tie counting): an entry's coverage
+// rectangle (from the set-up) cut to the warp's pixels is usually a few
+// pixels; entries of at most kPairMax such pixels are not tested against
+// every pixel of the tile but as (entry, pixel) pairs spread over the lanes,
+// 32 per round (a lane finds its entry by binary search over the warp's
+// prefix sums), each folding its key into the pixel's minimum in shared
+// memory with a 64-bit atomicMin.  Larger entries take the dense loop (each
+// lane its own pixels, keys in registers).  The minimum of packed keys does
+// not depend on the order, and both paths evaluate the same operations, so
+// the results are those of the dense loop alone.
 // Ten blocks per SM (48 registers) for the shapes of at most 128 pixels
 // with the default chooser: more resident warps beat the few spills
 // (16x8: 1.02 -> 0.88 ms, 8x8: 1.03 -> 1.01 ms on the 4096-scene
 // brax-like batch; 12 and 16 blocks measured slower).  The layered
 // variants of at most 64 pixels take eight (64 registers: 1.32 -> 1.18 ms
 // with 4 layers).  The others keep the compiler's choice (0: no minimum).
-template <int TW, int TH, int kL>
+template <int TW, int TH, int kL, bool kPairs>
 __host__ __device__ constexpr int raster_min_blocks() {
-  return (kL == 1 && TW * TH <= 128) ? 10 : (TW * TH <= 64 ? 8 : 0);
+  return kPairs ? (TW * TH <= 128 ? 8 : 0) : (kL == 1 && TW * TH <= 128) ? 10 : (TW * TH <= 64 ? 8 : 0);
+}
+
+// Largest (entry, pixel) pair count of an entry on the pair path: about
+// where its pairs cost what the dense loop's pass over the warp's pixels does.
+template <int TW, int TH>
+__host__ __device__ constexpr int pair_max() {
+  return TW * TH / 4 + 4;
+}
+
+// Inverse of depth_order where it is one to one: false for the keys of NaN
+// and of +-0 (whose sign the order drops).
+__device__ __forceinline__ bool depth_of_order(uint32_t o, float* z) {
+  if (o == 0u || o == 0x80000000u) return false;
+  *z = __uint_as_float((o & 0x80000000u) ? (o & 0x7fffffffu) : ~o);
+  return true;
 }
 
 // kWPT warps per bin tile: the bin tile is TW x (kWPT TH) pixels and a
@@ -640,80 +699,69 @@ __host__ __device__ constexpr int raster_min_blocks() {
 // coarser than the sub-tile each warp rasterises (every warp of a tile
 // reads the tile's whole bin and drops the entries that miss its rows).
 template <int TW, int TH, bool kKeys, bool kTies, int kL, int kWPT>
-__global__ void __launch_bounds__(32 * kRasterWarps, raster_min_blocks<TW, TH, kL>())
-raster_kernel(RastBatch B, Geometry G, const float4* __restrict__ setup,
+__global__ void __launch_bounds__(32 * kRasterWarps, raster_min_blocks<TW, TH, kL, kL == 1 && !kTies>())
+raster_kernel(RastBatch B, Geometry G, const float4* __restrict__ setup, const ushort4* __restrict__ rects,
               const uint32_t* __restrict__ counts, const uint32_t* __restrict__ offsets,
               const int32_t* __restrict__ bins, int32_t* __restrict__ winner,
               unsigned int* __restrict__ work, int64_t n_units, unsigned char* __restrict__ visible,
               const unsigned long long* __restrict__ keys) {
   constexpr int PPL = TW * TH / 32;
+  constexpr bool kPairs = kL == 1 && !kTies;
+  constexpr int kPW = kPairs ? kRasterWarps : 1;  // pair-path arrays only where used
   __shared__ float4 s_rec[kRasterWarps][kStage][3];
   __shared__ int s_id[kRasterWarps][kStage];
+  __shared__ unsigned long long s_best[kPW][kPairs ? TW * TH : 1];  // pixel (li, lj) at li * TH + lj
+  __shared__ float s_x[kPW][kPairs ? TW : 1], s_y[kPW][kPairs ? TH : 1];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   float4 (*rec)[3] = s_rec[warp];
   int* ids = s_id[warp];
+  unsigned long long* sbest = s_best[kPairs ? warp : 0];
+  float* tx_ndc = s_x[kPairs ? warp : 0];
+  float* ty_ndc = s_y[kPairs ? warp : 0];
   unsigned long long tie_count = 0;
-  unsigned long long tests = 0;  // pixel-triangle pairs this warp tested (staged entries x tile pixels)
-  unsigned int chunk = 0;
-  int taken = kTileChunk;  // tiles of the current chunk already processed
-  while (true) {
-    // tiles are taken kTileChunk at a time: one atomic on the shared
-    // counter per chunk instead of per tile
-    if (taken == kTileChunk) {
-      if (lane == 0) chunk = atomicAdd(work, static_cast<unsigned>(kTileChunk));
-      chunk = __shfl_sync(0xffffffffu, chunk, 0);
-      taken = 0;
+  unsigned long long tests = 0;  // pixel-triangle pairs this warp tested
+  // Tiles are grabbed one ahead and their bin offset and count loaded one
+  // ahead, so the counter atomic and those loads overlap a tile's work.
+  unsigned int next = 0;
+  if (lane == 0) next = atomicAdd(work, 1u);
+  unsigned int unit = 0;
+  uint32_t m_off = 0, m_cnt = 0;  // of `unit`
+  auto advance = [&]() {
+    unit = __shfl_sync(0xffffffffu, next, 0);
+    if (unit < n_units) {
+      m_off = offsets[unit / kWPT];
+      m_cnt = counts[unit / kWPT];
+      if (lane == 0) next = atomicAdd(work, 1u);
     }
-    const unsigned int unit = chunk + taken++;
-    if (unit >= n_units) break;
-    const unsigned int t = unit / kWPT;  // bin tile
+  };
+  advance();
+  while (unit < n_units) {
+    const unsigned int cur = unit;
+    const uint32_t off = m_off, t_count = m_cnt;
+    const unsigned int t = cur / kWPT;  // bin tile
     const int jid = static_cast<int>(t / G.tiles_per_job);
     const int local = static_cast<int>(t % G.tiles_per_job);
     const int tx = local % G.tiles_x, ty = local / G.tiles_x;
-    const int y0 = ty * (TH * kWPT) + static_cast<int>(unit % kWPT) * TH;  // first row of this warp's part
+    const int y0 = ty * (TH * kWPT) + static_cast<int>(cur % kWPT) * TH;  // first row of this warp's part
+    const int x0 = tx * TW;
     const RastJob& J = B.jobs[jid];
     const int W = J.width, H = J.height;
-    if (tx * TW >= W || y0 >= H) continue;
-    const float sx = J.viewport[0], ox = J.viewport[3], sy = J.viewport[5], oy = J.viewport[7];
-    const float vp22 = J.viewport[10], vp23 = J.viewport[11];
-    // lane -> one column j of the tile (TH divides 32) and PPL rows i:
-    // every pixel of a lane shares y, so y * inv[1][k] is computed once per
-    // entry (the same rounded product each pixel would compute).
-    constexpr int LPC = 32 / TH;
-    const int pj = y0 + lane % TH;
-    const float y = (static_cast<float>(pj) - oy) / sy;
-    // NDC of the tile's first and last pixel (inside the job) for the
-    // per-entry rejection test: the same quotients the pixels compute
-    const float xa = (static_cast<float>(tx * TW) - ox) / sx;
-    const float xb = (static_cast<float>(min(tx * TW + TW - 1, W - 1)) - ox) / sx;
-    const float ya = (static_cast<float>(y0) - oy) / sy;
-    const float yb = (static_cast<float>(min(y0 + TH - 1, H - 1)) - oy) / sy;
-    const float XM = fmaxf(fabsf(xa), fabsf(xb)), YM = fmaxf(fabsf(ya), fabsf(yb));
-    float x[PPL], best_z[PPL];
-    unsigned long long best[PPL][kL];
-    uint32_t second[PPL];
-    unsigned z_known = 0;  // bit q: best_z[q] holds the depth of best[q] (set by this kernel's tests)
-#pragma unroll
-    for (int q = 0; q < PPL; ++q) {
-      const int pi = tx * TW + q * LPC + lane / TH;
-      x[q] = (static_cast<float>(pi) - ox) / sx;
-      // the minimum over the faces the setup kernel rasterised itself
-      best[q][0] = (kKeys && pi < W && pj < H) ? keys[J.pixel_begin + static_cast<int64_t>(pi) * H + pj] : kEmptyKey;
-#pragma unroll
-      for (int l = 1; l < kL; ++l) best[q][l] = kEmptyKey;
-      best_z[q] = 0.0f;
-      second[q] = 0xffffffffu;
+    if (x0 >= W || y0 >= H) {
+      advance();
+      continue;
     }
     const float4* jrec = setup + J.setup_begin * 4;
-    const uint32_t off = offsets[t];
+    const ushort4* jrect = rects + J.setup_begin;
     const bool overflow = (off & kOverflow) != 0;
-    const int n = overflow ? J.n_faces : static_cast<int>(counts[t]);
-    // entry `e` of the tile's list -> (record, id); ids of non-candidates
-    // (only met on the full-scan path) are -1 and their records unused
-    auto fetch = [&](int e, float4& r0, float4& r1, float4& r2, int& id) {
+    const int n = overflow ? J.n_faces : static_cast<int>(t_count);
+    // entry `e` of the tile's list -> (record, id, rectangle); ids of
+    // non-candidates (only met on the full-scan path) are -1 and their
+    // records unused
+    auto fetch = [&](int e, float4& r0, float4& r1, float4& r2, int& id, ushort4& rc) {
       const int fid = overflow ? e : __ldg(bins + static_cast<int64_t>(off) + e);
       const float4* r = jrec + static_cast<int64_t>(fid) * 4;
       id = fid;
+      if (kPairs) rc = __ldg(jrect + fid);
       if (overflow && (__float_as_int(__ldg(r + 3).y) & kCandidate) != kCandidate) {
         id = -1;
         r0 = r1 = r2 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
@@ -725,37 +773,130 @@ raster_kernel(RastBatch B, Geometry G, const float4* __restrict__ setup,
     };
     float4 n0, n1, n2;
     int nid = -1;
-    if (lane < n) fetch(lane, n0, n1, n2, nid);
+    ushort4 nrc = empty_rect();
+    if (lane < n) fetch(lane, n0, n1, n2, nid, nrc);  // first: its loads overlap the tile's set-up
+    const float sx = J.viewport[0], ox = J.viewport[3], sy = J.viewport[5], oy = J.viewport[7];
+    const float vp22 = J.viewport[10], vp23 = J.viewport[11];
+    // lane -> one column j of the tile (TH divides 32) and PPL rows i:
+    // every pixel of a lane shares y, so y * inv[1][k] is computed once per
+    // entry (the same rounded product each pixel would compute).
+    constexpr int LPC = 32 / TH;
+    const int pj = y0 + lane % TH;
+    float y;
+    float x[PPL], best_z[PPL];
+    if (kPairs) {
+      // the pixels' NDC quotients, once per tile: tx_ndc[li] for pixel
+      // x0 + li, ty_ndc[lj] for y0 + lj
+      for (int k = lane; k < TW + TH; k += 32) {
+        if (k < TW)
+          tx_ndc[k] = (static_cast<float>(x0 + k) - ox) / sx;
+        else
+          ty_ndc[k - TW] = (static_cast<float>(y0 + k - TW) - oy) / sy;
+      }
+#pragma unroll
+      for (int q = 0; q < PPL; ++q) sbest[q * 32 + lane] = kEmptyKey;
+      __syncwarp();
+      y = ty_ndc[lane % TH];
+#pragma unroll
+      for (int q = 0; q < PPL; ++q) x[q] = tx_ndc[q * LPC + lane / TH];
+    } else {
+      y = (static_cast<float>(pj) - oy) / sy;
+#pragma unroll
+      for (int q = 0; q < PPL; ++q) x[q] = (static_cast<float>(x0 + q * LPC + lane / TH) - ox) / sx;
+    }
+    // NDC of the tile's first and last pixel (inside the job) for the
+    // per-entry rejection test: the same quotients the pixels compute
+    const int lxe = min(TW - 1, W - 1 - x0), lye = min(TH - 1, H - 1 - y0);  // last pixel inside the job
+    float xa, xb, ya, yb;
+    if (kPairs) {
+      xa = tx_ndc[0], xb = tx_ndc[lxe], ya = ty_ndc[0], yb = ty_ndc[lye];
+    } else {
+      xa = (static_cast<float>(x0) - ox) / sx;
+      xb = (static_cast<float>(x0 + lxe) - ox) / sx;
+      ya = (static_cast<float>(y0) - oy) / sy;
+      yb = (static_cast<float>(y0 + lye) - oy) / sy;
+    }
+    const float XM = fmaxf(fabsf(xa), fabsf(xb)), YM = fmaxf(fabsf(ya), fabsf(yb));
+    unsigned long long best[PPL][kL];
+    uint32_t second[PPL];
+    unsigned z_known = 0;  // bit q: best_z[q] holds the depth of best[q] (set by this kernel's tests)
+#pragma unroll
+    for (int q = 0; q < PPL; ++q) {
+      const int pi = x0 + q * LPC + lane / TH;
+      // the minimum over the faces the setup kernel rasterised itself
+      best[q][0] = (kKeys && pi < W && pj < H) ? keys[J.pixel_begin + static_cast<int64_t>(pi) * H + pj] : kEmptyKey;
+#pragma unroll
+      for (int l = 1; l < kL; ++l) best[q][l] = kEmptyKey;
+      best_z[q] = 0.0f;
+      second[q] = 0xffffffffu;
+    }
     for (int base = 0; base < n; base += kStage) {
       // entries whose triangle misses every pixel of the tile (one edge
       // negative over the whole tile) are dropped; the rest are staged
       // compacted
       bool take = lane < min(kStage, n - base) && nid >= 0;
-      if (take)
+      int cnt = 0, pinfo = 0;
+      float prcp = 0.0f;
+      if (kPairs) {
+        // the entry's rectangle cut to the warp's pixels (tile-local); on
+        // the full-scan path faces without one (small faces of the set-up's
+        // own rasterisation, non-candidates) drop out here
+        const int lx0 = max(static_cast<int>(nrc.x) - x0, 0), lx1 = min(static_cast<int>(nrc.z) - x0, lxe);
+        const int ly0 = max(static_cast<int>(nrc.y) - y0, 0), ly1 = min(static_cast<int>(nrc.w) - y0, lye);
+        take = take && lx0 <= lx1 && ly0 <= ly1;
+        if (take) {
+          const float ra = tx_ndc[lx0], rb = tx_ndc[lx1], sa = ty_ndc[ly0], sb = ty_ndc[ly1];
+          const float RX = fmaxf(fabsf(ra), fabsf(rb)), RY = fmaxf(fabsf(sa), fabsf(sb));
+          take = !(edge_misses_tile(n0.x, n0.w, n1.z, ra, rb, sa, sb, RX, RY) ||
+                   edge_misses_tile(n0.y, n1.x, n1.w, ra, rb, sa, sb, RX, RY) ||
+                   edge_misses_tile(n0.z, n1.y, n2.x, ra, rb, sa, sb, RX, RY));
+          const int w = lx1 - lx0 + 1;
+          cnt = w * (ly1 - ly0 + 1);
+          pinfo = lx0 | (ly0 << 8) | (w << 16);
+          prcp = __frcp_rn(static_cast<float>(w));
+        }
+      } else if (take) {
         take = !(edge_misses_tile(n0.x, n0.w, n1.z, xa, xb, ya, yb, XM, YM) ||
                  edge_misses_tile(n0.y, n1.x, n1.w, xa, xb, ya, yb, XM, YM) ||
                  edge_misses_tile(n0.z, n1.y, n2.x, xa, xb, ya, yb, XM, YM));
-      const unsigned keep = __ballot_sync(0xffffffffu, take);
+      }
+      const bool pair = kPairs && take && cnt <= pair_max<TW, TH>();
+      const bool dense = take && !pair;
+      const unsigned keep = __ballot_sync(0xffffffffu, dense);
       const int m = __popc(keep);
-      if (take) {
-        const int slot = __popc(keep & lanemask_lt());
+      const unsigned pmask = kPairs ? __ballot_sync(0xffffffffu, pair) : 0u;
+      if (dense || pair) {
+        // dense entries in slots [0, m), pair entries after them, each in
+        // lane order
+        const int slot = dense ? __popc(keep & lanemask_lt()) : m + __popc(pmask & lanemask_lt());
         rec[slot][0] = n0;
         rec[slot][1] = n1;
         rec[slot][2] = n2;
         ids[slot] = nid;
       }
+      // pair path: inclusive prefix sum of the pair counts in lane order
+      int pincl = pair ? cnt : 0, ptotal = 0;
+      if (kPairs) {
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+          const int v = __shfl_up_sync(0xffffffffu, pincl, d);
+          if (lane >= d) pincl += v;
+        }
+        ptotal = __shfl_sync(0xffffffffu, pincl, 31);
+      }
+      const int pexcl = pincl - (pair ? cnt : 0);
       __syncwarp();
       // prefetch the next chunk while this one is tested
-      if (base + kStage + lane < n) fetch(base + kStage + lane, n0, n1, n2, nid);
-      tests += static_cast<unsigned>(m) * static_cast<unsigned>(TW * TH);
+      if (base + kStage + lane < n) fetch(base + kStage + lane, n0, n1, n2, nid, nrc);
+      tests += static_cast<unsigned>(m) * static_cast<unsigned>(TW * TH) + static_cast<unsigned>(ptotal);
       for (int e = 0; e < m; ++e) {
         const float4 a = rec[e][0], b = rec[e][1], cz = rec[e][2];
-        const float y0 = y * a.w, y1 = y * b.x, y2 = y * b.y;
+        const float y0p = y * a.w, y1p = y * b.x, y2p = y * b.y;
 #pragma unroll
         for (int q = 0; q < PPL; ++q) {
-          const float c0 = (x[q] * a.x + y0) + b.z;
-          const float c1 = (x[q] * a.y + y1) + b.w;
-          const float c2 = (x[q] * a.z + y2) + cz.x;
+          const float c0 = (x[q] * a.x + y0p) + b.z;
+          const float c1 = (x[q] * a.y + y1p) + b.w;
+          const float c2 = (x[q] * a.z + y2p) + cz.x;
           if (all_nonneg(c0, c1, c2)) {  // staged entries are candidates (id >= 0)
             const float z = ((c0 * cz.y + c1 * cz.z) + c2 * cz.w) * vp22 + vp23;
             const unsigned long long key = pack_key(z, ids[e]);
@@ -770,13 +911,61 @@ raster_kernel(RastBatch B, Geometry G, const float4* __restrict__ setup,
           }
         }
       }
+      if (kPairs) {
+        for (int pb = 0; pb < ptotal; pb += 32) {
+          const int pk = pb + lane;
+          int owner = 0;  // lanes whose pairs all precede pair pk
+#pragma unroll
+          for (int step = 16; step > 0; step >>= 1) {
+            const int v = __shfl_sync(0xffffffffu, pincl, owner + step - 1);
+            if (v <= pk) owner += step;
+          }
+          const int o_excl = __shfl_sync(0xffffffffu, pexcl, owner);
+          const int o_info = __shfl_sync(0xffffffffu, pinfo, owner);
+          const float o_rcp = __shfl_sync(0xffffffffu, prcp, owner);
+          if (pk < ptotal) {
+            // pair -> pixel of the owner's rectangle, row-major over its
+            // width w (w <= 32 and pk - o_excl < TW * TH: the rounded
+            // quotient (k + 1/2) / w stays more than 1/64 from an integer)
+            const int k = pk - o_excl;
+            const int w = o_info >> 16;
+            const int r = __float2int_rz((static_cast<float>(k) + 0.5f) * o_rcp);
+            const int li = min((o_info & 0xff) + (k - r * w), TW - 1);
+            const int lj = min(((o_info >> 8) & 0xff) + r, TH - 1);
+            const int slot = m + __popc(pmask & ((1u << owner) - 1u));
+            const float px = tx_ndc[li], py = ty_ndc[lj];
+            const float4 a = rec[slot][0], b = rec[slot][1], cz = rec[slot][2];
+            const float c0 = (px * a.x + py * a.w) + b.z;
+            const float c1 = (px * a.y + py * b.x) + b.w;
+            const float c2 = (px * a.z + py * b.y) + cz.x;
+            if (all_nonneg(c0, c1, c2)) {
+              const float z = ((c0 * cz.y + c1 * cz.z) + c2 * cz.w) * vp22 + vp23;
+              atomicMin(sbest + li * TH + lj, pack_key(z, ids[slot]));
+            }
+          }
+        }
+      }
       __syncwarp();
+    }
+    advance();  // the next tile's loads overlap this one's epilogue
+    if (kPairs) {
+      // the pair path's minima join the lane's own (same pixel layout:
+      // pixel q of lane l is li * TH + lj = 32 q + l)
+#pragma unroll
+      for (int q = 0; q < PPL; ++q) {
+        const unsigned long long k = sbest[q * 32 + lane];
+        if (k < best[q][0]) {
+          best[q][0] = k;
+          z_known &= ~(1u << q);
+        }
+      }
+      __syncwarp();  // every lane has read its minima before the next tile's reset
     }
     const bool depth_only = J.shader == RAST_SHADER_DEPTH;
     const int layers = kL > 1 ? job_layers(J, B.max_layers) : 0;
 #pragma unroll
     for (int q = 0; q < PPL; ++q) {
-      const int pi = tx * TW + q * LPC + lane / TH;
+      const int pi = x0 + q * LPC + lane / TH;
       if (pi < W && pj < H) {
         const uint32_t o1 = static_cast<uint32_t>(best[q][0] >> 32);
         const bool found = !(best[q][0] == kEmptyKey || o1 == kInfOrder);
@@ -804,9 +993,9 @@ raster_kernel(RastBatch B, Geometry G, const float4* __restrict__ setup,
         bool keep = found;
         float z = best_z[q];
         int prim = found ? static_cast<int>(best[q][0] & 0xffffffffu) : 0;
-        if (kKeys && found && !(z_known & (1u << q))) {
-          // the winner came from the setup kernel's own rasterisation: its
-          // depth again, with the same operations
+        if ((kKeys || kPairs) && found && !(z_known & (1u << q)) && !depth_of_order(o1, &z)) {
+          // the winner came from a key alone and its depth is NaN or +-0:
+          // its depth again, with the same operations
           const float4* r = jrec + static_cast<int64_t>(prim) * 4;
           const float4 a = __ldg(r), b = __ldg(r + 1), cz = __ldg(r + 2);
           const float c0 = (x[q] * a.x + y * a.w) + b.z;
@@ -968,6 +1157,8 @@ static Layout layout(const RastBatch& b, TileShape ts, uint64_t bin_capacity, in
   Layout L{};
   L.G.tw = ts.tw;
   L.G.th = ts.th;
+  L.G.tws = __builtin_ctz(static_cast<unsigned>(ts.tw));
+  L.G.ths = __builtin_ctz(static_cast<unsigned>(ts.th));
   L.G.tiles_x = ceil_div(std::max(b.max_width, 1), ts.tw);
   L.G.tiles_y = ceil_div(std::max(b.max_height, 1), ts.th);
   L.G.tiles_per_job = L.G.tiles_x * L.G.tiles_y;
@@ -1055,7 +1246,7 @@ template <bool kKeys, bool kTies, int kL>
 // blocks of this instance that fit on an SM) takes the work units (bin
 // tiles x warps per tile).
 static void launch_raster(TileShape ts, int wpt, int sms, cudaStream_t s, const RastBatch& b, const Layout& L,
-                          const float4* setup, const uint32_t* counts, const uint32_t* offsets, const int32_t* bins,
+                          const float4* setup, const ushort4* rects, const uint32_t* counts, const uint32_t* offsets, const int32_t* bins,
                           int32_t* winner, unsigned int* misc, unsigned char* vis,
                           const unsigned long long* keys) {
   const unsigned block = 32 * kRasterWarps;
@@ -1065,7 +1256,8 @@ static void launch_raster(TileShape ts, int wpt, int sms, cudaStream_t s, const 
         per_sm <= 0)
       per_sm = 8;
     const unsigned grid = static_cast<unsigned>(std::max(sms, 1) * per_sm);
-    kernel<<<grid, block, 0, s>>>(b, L.G, setup, counts, offsets, bins, winner, misc, L.n_tiles * wpt, vis, keys);
+    kernel<<<grid, block, 0, s>>>(b, L.G, setup, rects, counts, offsets, bins, winner, misc, L.n_tiles * wpt, vis,
+                                  keys);
   };
   if (wpt == 2) {  // the warp's sub-tile is (tw, th / 2)
     if (ts.tw == 8 && ts.th == 16)
@@ -1111,7 +1303,7 @@ static int render(const RastBatch* batch, const RastTiledConfig* cfg, void* work
   if (workspace_bytes < L.total) return RAST_ERR_WORKSPACE_TOO_SMALL;
   if (L.total > 0 && (workspace == nullptr || (reinterpret_cast<uintptr_t>(workspace) & 255)))
     return RAST_ERR_INVALID_ARGUMENT;
-  if (b.max_width > 65535 * ts.tw || b.max_height > 65535 * ts.th) return RAST_ERR_UNSUPPORTED;
+  if (b.max_width > 65535 || b.max_height > 65535) return RAST_ERR_UNSUPPORTED;  // pixel rectangles are 16-bit
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   char* ws = static_cast<char*>(workspace);
   float4* setup = reinterpret_cast<float4*>(ws + L.setup_off);
@@ -1173,18 +1365,18 @@ static int render(const RastBatch* batch, const RastTiledConfig* cfg, void* work
         // the key path exists only when ties are not counted and no job is
         // layered
         if (keys)
-          launch_raster<true, false, 1>(ts, wpt, sms, s, b, L, setup, counts, offsets, bins, winner, misc, vis, keys);
+          launch_raster<true, false, 1>(ts, wpt, sms, s, b, L, setup, bbox, counts, offsets, bins, winner, misc, vis, keys);
         else if (b.max_layers > 0 && b.near_ties)
-          launch_raster<false, true, RAST_MAX_LAYERS>(ts, wpt, sms, s, b, L, setup, counts, offsets, bins, winner,
+          launch_raster<false, true, RAST_MAX_LAYERS>(ts, wpt, sms, s, b, L, setup, bbox, counts, offsets, bins, winner,
                                                       misc, vis, nullptr);
         else if (b.max_layers > 0)
-          launch_raster<false, false, RAST_MAX_LAYERS>(ts, wpt, sms, s, b, L, setup, counts, offsets, bins, winner,
+          launch_raster<false, false, RAST_MAX_LAYERS>(ts, wpt, sms, s, b, L, setup, bbox, counts, offsets, bins, winner,
                                                        misc, vis, nullptr);
         else if (b.near_ties)
-          launch_raster<false, true, 1>(ts, wpt, sms, s, b, L, setup, counts, offsets, bins, winner, misc, vis,
+          launch_raster<false, true, 1>(ts, wpt, sms, s, b, L, setup, bbox, counts, offsets, bins, winner, misc, vis,
                                         nullptr);
         else
-          launch_raster<false, false, 1>(ts, wpt, sms, s, b, L, setup, counts, offsets, bins, winner, misc, vis,
+          launch_raster<false, false, 1>(ts, wpt, sms, s, b, L, setup, bbox, counts, offsets, bins, winner, misc, vis,
                                          nullptr);
       } else {
         if (cudaMemsetAsync(winner, 0xff, static_cast<size_t>(b.total_pixels) * 4 * L.winner_layers, s) !=

@@ -25,6 +25,8 @@ FORMS = ("auto", "plain", "tiled")
 # ~1e8 pixel-triangle pairs: about where the plain scan's time (at ~1.3e12
 # pairs/s on a GB300) passes the tiled form's fixed launch cost
 TILED_MIN_PAIRS = 1 << 27
+# the tiled form's per-face pixel rectangles are 16-bit
+TILED_MAX_SIDE = 65535
 _state = threading.local()
 
 
@@ -47,6 +49,8 @@ def pass_pairs(packed: _jobs.PackedBatch) -> int:
 def choose(packed: _jobs.PackedBatch, form: Optional[str] = None) -> str:
     f = form or render_form()
     if f == "auto":
+        if any(int(j.width) > TILED_MAX_SIDE or int(j.height) > TILED_MAX_SIDE for j in packed.jobs):
+            return "plain"
         return "tiled" if pass_pairs(packed) >= TILED_MIN_PAIRS else "plain"
     if f not in ("plain", "tiled"):
         raise ValueError(f"form must be one of {FORMS}")
