@@ -75,10 +75,14 @@ __device__ __forceinline__ void add_texel_grad(float* g, int64_t base, int ch, c
   }
 }
 
-// ---- warp-aggregated atomics: lanes hold (key, value); lanes whose keys
-// are equal and adjacent form a segment; the segment's last lane adds the
-// segment's sum.  Every lane of the warp must call these.
 constexpr unsigned kFull = 0xffffffffu;
+
+// Fire-and-forget global float add.  The accumulation targets are read back
+// from shared memory as generic pointers, for which atomicAdd would be a
+// generic atomic that returns the old value; this is the global reduction.
+__device__ __forceinline__ void red_add(float* p, float v) {
+  asm volatile("red.global.add.f32 [%0], %1;" ::"l"(__cvta_generic_to_global(p)), "f"(v) : "memory");
+}
 
 // Template values of the shader-specialised kernels: a shader id, kAnyShader
 // (any mix, dispatch on each job's shader) or kReflectionShaders (jobs of
@@ -92,45 +96,51 @@ __host__ __device__ constexpr bool may(int x) {
          (SH == kReflectionShaders && (x == RAST_SHADER_PHONG_REFLECTION || x == RAST_SHADER_PHONG_REFLECTION_SHADOW));
 }
 
-struct Seg {
-  int rel;      // this lane's offset from the first lane of its segment
-  bool tail;    // last lane of its segment (and active)
-  int levels;   // shuffle levels that cover the longest segment of the warp
-};
-
-__device__ __forceinline__ Seg segment(long long key, bool active) {
+// Lanes whose key differs from the next lane's (or lane 31): the last lane
+// of each run of equal keys.  Inactive lanes get keys of their own, so each
+// stands alone.  Every lane of the warp must call it.
+__device__ __forceinline__ unsigned run_tails(long long key, bool active) {
   const int lane = threadIdx.x & 31;
-  const long long k = active ? key : -2 - lane;  // inactive lanes stand alone
-  const long long prev = __shfl_up_sync(kFull, k, 1);
+  const long long k = active ? key : -2 - lane;
   const long long next = __shfl_down_sync(kFull, k, 1);
-  const bool head = lane == 0 || prev != k;
-  const bool tail = lane == 31 || next != k;
-  const unsigned heads = __ballot_sync(kFull, head);
-  const unsigned upto = heads & (0xffffffffu >> (31 - lane));
-  Seg s;
-  s.rel = lane - (31 - __clz(upto));
-  s.tail = tail && active;
-  const unsigned len = tail ? static_cast<unsigned>(s.rel + 1) : 0u;
-  const unsigned longest = __reduce_max_sync(kFull, len);
-  s.levels = longest <= 1u ? 0 : 32 - __clz(longest - 1u);  // ceil(log2(longest))
-  return s;
+  return __ballot_sync(kFull, lane == 31 || next != k);
 }
 
-// Inclusive segmented sums of N values up to this lane (the tail lane holds
-// the totals), in place.  Levels outside, values inside: the level test and
-// the lane's predicate are paid once per level, not once per value.
-template <int N>
-__device__ __forceinline__ void seg_sums(float* v, const Seg& s) {
-#pragma unroll
-  for (int l = 0; l < 5; ++l) {
-    if (l >= s.levels) break;  // uniform over the warp
-    const int d = 1 << l;
-    const bool take = s.rel >= d;
-#pragma unroll
-    for (int k = 0; k < N; ++k) {
-      const float o = __shfl_up_sync(kFull, v[k], d);
-      if (take) v[k] += o;
-    }
+// Per-pixel contributions of the pixel kernel, summed per run of equal keys
+// along the warp's 32 pixels (pixels run along a column, so neighbours
+// usually share the face and the texel) with one atomic per run and value.
+// Each lane writes its pixel's values as one row of the warp's table
+// (columns below) and the target addresses of its pixel; then lane c walks
+// column c down the 32 rows, adding, and at the end of each run adds the
+// run's sum to its target: 32 shared loads per value instead of a shuffle
+// tree per value.  Columns: dL/dm (9) and dL/dz_clip (3) per face; dL/d
+// carried varying (3 per corner vertex); dL/dtexel (3); dL/d specular
+// exponent (1); with phong_darboux, dL/d Darboux triangle (9, vertex 0's
+// row) and dL/d normal-map texel (3).
+enum AccTarget { kTgtFace, kTgtVert0, kTgtVert1, kTgtVert2, kTgtTexel, kTgtExponent, kTgtNormalMap, kTgtCount };
+template <bool kDarboux>
+struct AccLayout {
+  static constexpr int kCols = kDarboux ? 37 : 25;
+  static constexpr int kRow = kDarboux ? 44 : 28;  // an odd number of float4: conflict-free row stores
+  static constexpr int kTargets = kDarboux ? kTgtCount : kTgtNormalMap;
+};
+
+// Target (address slot, offset) and key kind of column c.  Key kinds: 0
+// face, 1 texel, 2 specular exponent, 3 normal-map texel.
+template <bool kDarboux>
+__device__ __forceinline__ void acc_column(int c, int tex_channels, int* target, int* offset, int* kind) {
+  if (c < 12) {
+    *target = kTgtFace, *offset = c, *kind = 0;
+  } else if (c < 21) {
+    *target = kTgtVert0 + (c - 12) / 3, *offset = (c - 12) % 3, *kind = 0;
+  } else if (c < 24) {
+    *target = kTgtTexel, *offset = tex_channels == 1 ? 0 : c - 21, *kind = 1;
+  } else if (c == 24) {
+    *target = kTgtExponent, *offset = 0, *kind = 2;
+  } else if (kDarboux && c < 34) {
+    *target = kTgtVert0, *offset = 3 + (c - 25), *kind = 0;
+  } else {
+    *target = kTgtNormalMap, *offset = c - 34, *kind = 3;
   }
 }
 
@@ -178,30 +188,40 @@ struct NoPost {
 // [kLo, kLo + kSpan) of BITS, up to 32 parameters, is summed by a transpose
 // through shared memory (each lane stores its values, lane n adds parameter
 // kLo + n's 32 values) instead of one shuffle tree per parameter.  Rows of
-// 36 floats: the 128-bit row reads of 8 lanes hit distinct banks.
+// 36 floats: the 128-bit row reads of 8 lanes hit distinct banks.  The
+// transpose uses the caller's shared scratch `cols` of
+// transpose_floats<BITS>() floats (16-byte aligned).
+template <unsigned long long BITS>
+__host__ __device__ constexpr int param_span() {
+  return BITS ? 64 - __builtin_clzll(BITS) - (BITS ? __builtin_ctzll(BITS) : 0) : 0;
+}
+template <unsigned long long BITS>
+__host__ __device__ constexpr int transpose_floats() {
+  return (kThreads / 32) * param_span<BITS>() * 36;
+}
 template <unsigned long long BITS, bool kTransposed = false, class Post = NoPost>
 __device__ __forceinline__ void reduce_params(const ParamGrad& pg, float* job_params, bool active, int job,
-                                              const Post& post = Post()) {
+                                              const Post& post = Post(), float* cols = nullptr) {
   constexpr int kLo = BITS ? __builtin_ctzll(BITS) : 0;
-  constexpr int kSpan = BITS ? 64 - __builtin_clzll(BITS) - kLo : 0;
+  constexpr int kSpan = param_span<BITS>();
   constexpr bool kTranspose = kTransposed && kSpan > 0 && kSpan <= 32;
   __shared__ float s_red[kThreads / 32][RAST_NPARAM];
-  __shared__ float4 s_col[kTranspose ? kThreads / 32 : 1][kTranspose ? kSpan : 1][9];
   __shared__ float s_tot[Post::kActive ? RAST_NPARAM : 1];
   if (BITS == 0ull || !job_params) return;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const bool warp_active = __any_sync(0xffffffffu, active);
   if (kTranspose) {
     if (warp_active) {
-      float* col = reinterpret_cast<float*>(s_col[warp]);
+      float* col = cols + warp * kSpan * 36;  // this warp's rows: parameter n at col[n * 36 ...]
 #pragma unroll
       for (int n = 0; n < kSpan; ++n) col[n * 36 + lane] = ((BITS >> (kLo + n)) & 1ull) ? pg.v[kLo + n] : 0.0f;
       __syncwarp();
       if (lane < kSpan) {
         float a = 0.0f, b = 0.0f, c = 0.0f, d = 0.0f;
+        const float4* row = reinterpret_cast<const float4*>(col + lane * 36);
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
-          const float4 t = s_col[warp][lane][q];
+          const float4 t = row[q];
           a += t.x;
           b += t.y;
           c += t.z;
@@ -697,6 +717,7 @@ pixel_kernel(RastBatch B, Work w, const float* __restrict__ grad_canvas, const f
              RastGradPools G) {
   __shared__ RastJob sJ;
   __shared__ LightUnit sL;
+  constexpr bool kDarboux = may<SH>(RAST_SHADER_PHONG_DARBOUX);
   load_job_to_shared(B.jobs + blockIdx.y, &sJ);
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -735,11 +756,24 @@ pixel_kernel(RastBatch B, Work w, const float* __restrict__ grad_canvas, const f
   if (kLayers) load_grads();
   float transmit = 1.0f;  // the over mixer's T
   bool shown = false;     // a slot of this pixel was kept
-  constexpr bool kDarboux = may<SH>(RAST_SHADER_PHONG_DARBOUX);
+  // the warp's table of per-pixel contributions (AccLayout) and their
+  // targets; after the passes the same shared memory holds the per-scene
+  // parameters' transpose
+  using Acc = AccLayout<kDarboux>;
+  // the background has a gradient only in layered batches
+  constexpr unsigned long long kBits = pixel_bits(SH) & (kLayers ? ~0ull : ~range_bits(RAST_GRAD_BACKGROUND, 3));
+  constexpr int kTabFloats = (kThreads / 32) * 32 * Acc::kRow;
+  static_assert(transpose_floats<kBits>() <= kTabFloats, "the parameter transpose reuses the table");
+  __shared__ __align__(16) float s_tab[kTabFloats];
+  __shared__ float* s_tgt[kThreads / 32][32][Acc::kTargets];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  float* acc_tab = s_tab + warp * 32 * Acc::kRow;
+  float** acc_tgt = &s_tgt[warp][0][0];
+  const int tex_c = J.tex_c;
   for (int pass = 0; pass < passes; ++pass) {
     int p = -1;
     if (in_job) p = over ? P.layer_prim[pass * B.total_pixels + pix] : P.prim_id[pix];
-    // per-pixel contributions, added with warp-aggregated atomics below
+    // per-pixel contributions, summed per run and added with atomics below
     int64_t frow = -1;
     float fval[12];
     float vval[9];
@@ -775,27 +809,18 @@ pixel_kernel(RastBatch B, Work w, const float* __restrict__ grad_canvas, const f
       const float wr = (c[0] + c[1]) + c[2];
       const float b[3] = {c[0] / wr, c[1] / wr, c[2] / wr};
       if (!kLayers) load_grads();
-      float r0[kMaxVarying], r1[kMaxVarying], r2[kMaxVarying];
-      const int nv = sh != RAST_SHADER_DEPTH ? varying_count(sh) : 0;
-      bool loaded = false;
-      auto load_rows = [&]() {
-#pragma unroll
-        for (int k = 0; k < kMaxVarying; ++k) {
-          if (k < nv) {
-            r0[k] = w.vvar[vrows[0] * w.vstride + k];
-            r1[k] = w.vvar[vrows[1] * w.vstride + k];
-            r2[k] = w.vvar[vrows[2] * w.vstride + k];
-          }
-        }
-        loaded = true;
-      };
+      // the corners' varying rows, read where they are used (neighbouring
+      // pixels share them, so the reads hit L1) rather than held in registers
+      // across the fragment's reverse mode
+      const float* r0 = w.vvar + vrows[0] * w.vstride;
+      const float* r1 = w.vvar + vrows[1] * w.vstride;
+      const float* r2 = w.vvar + vrows[2] * w.vstride;
       float wgt = 1.0f, gz = gz_px;
       bool keep = true;
       if (over) {
         // the slot counts only when its fragment shader keeps it (the
         // Gouraud shaders drop negative interpolated colours)
         if (sh == RAST_SHADER_GOURAUD || sh == RAST_SHADER_GOURAUD_TEXTURE) {
-          load_rows();
 #pragma unroll
           for (int q = 0; q < 3; ++q) keep = keep && interp1(b, r0[kVColour + q], r1[kVColour + q], r2[kVColour + q]) >= 0.0f;
         }
@@ -820,7 +845,6 @@ pixel_kernel(RastBatch B, Work w, const float* __restrict__ grad_canvas, const f
         }
         const float gcv[3] = {wgt * gcv_px[0], wgt * gcv_px[1], wgt * gcv_px[2]};
         if (sh != RAST_SHADER_DEPTH && (gcv[0] != 0.0f || gcv[1] != 0.0f || gcv[2] != 0.0f)) {
-          if (!loaded) load_rows();
           float gi[3];
           fragment_bwd<SH>(J, P, G, r0, r1, r2, b, gcv, gi, pg, tg, tval, sL);
           if (gi[0] != 0.0f || gi[1] != 0.0f || gi[2] != 0.0f) {
@@ -854,48 +878,56 @@ pixel_kernel(RastBatch B, Work w, const float* __restrict__ grad_canvas, const f
         for (int k = 0; k < 3; ++k) fval[9 + k] = gzc[k];
       }
     }
-    // ---- warp-aggregated accumulation (pixels of a warp run along a column,
-    // so neighbours usually share the face and the texel)
+    // ---- per-run sums and atomics (AccLayout): this pixel's row of values
+    // and its targets, then lane c sums column c down the warp's rows
     {
-      const Seg sf = segment(frow, frow >= 0);
-      float* facc = w.facc + (frow >= 0 ? frow : 0) * 12;
-      const int nf = grad_zbuffer ? 12 : 9;  // dL/dz_clip only with a depth gradient
-      if (grad_zbuffer)
-        seg_sums<12>(fval, sf);
-      else
-        seg_sums<9>(fval, sf);
-      seg_sums<9>(vval, sf);
-      if (sf.tail) {
-#pragma unroll
-        for (int k = 0; k < 12; ++k)
-          if (k < nf && fval[k] != 0.0f) atomicAdd(facc + k, fval[k]);
-#pragma unroll
-        for (int k = 0; k < 9; ++k)
-          if (vval[k] != 0.0f) atomicAdd(w.vacc + vrows[k / 3] * w.vacc_stride + (k % 3), vval[k]);
+      float4* row = reinterpret_cast<float4*>(acc_tab + lane * Acc::kRow);
+      row[0] = make_float4(fval[0], fval[1], fval[2], fval[3]);
+      row[1] = make_float4(fval[4], fval[5], fval[6], fval[7]);
+      row[2] = make_float4(fval[8], fval[9], fval[10], fval[11]);
+      row[3] = make_float4(vval[0], vval[1], vval[2], vval[3]);
+      row[4] = make_float4(vval[4], vval[5], vval[6], vval[7]);
+      row[5] = make_float4(vval[8], tg.gt[0], tg.gt[1], tg.gt[2]);
+      if (kDarboux) {
+        row[6] = make_float4(tg.gs, tval[0], tval[1], tval[2]);
+        row[7] = make_float4(tval[3], tval[4], tval[5], tval[6]);
+        row[8] = make_float4(tval[7], tval[8], tg.gn[0], tg.gn[1]);
+        row[9] = make_float4(tg.gn[2], 0.0f, 0.0f, 0.0f);
+      } else {
+        row[6] = make_float4(tg.gs, 0.0f, 0.0f, 0.0f);
       }
-      if (kDarboux && w.vacc_stride > 3) {
-        seg_sums<9>(tval, sf);
-        if (sf.tail) {
+      float** tgt = acc_tgt + lane * Acc::kTargets;
+      const bool face = frow >= 0;
+      tgt[kTgtFace] = face ? w.facc + frow * 12 : nullptr;
 #pragma unroll
-          for (int k = 0; k < 9; ++k)
-            if (tval[k] != 0.0f) atomicAdd(w.vacc + vrows[0] * w.vacc_stride + 3 + k, tval[k]);
+      for (int k = 0; k < 3; ++k) tgt[kTgtVert0 + k] = face ? w.vacc + vrows[k] * w.vacc_stride : nullptr;
+      tgt[kTgtTexel] = (G.texture && tg.tb >= 0) ? G.texture + tg.tb : nullptr;
+      tgt[kTgtExponent] = (G.specular_map && tg.sidx >= 0) ? G.specular_map + tg.sidx : nullptr;
+      if (kDarboux) tgt[kTgtNormalMap] = (G.normal_map && tg.nb >= 0) ? G.normal_map + tg.nb : nullptr;
+      // last pixel of each run, per key kind (face, texel, exponent, normal-map texel)
+      const unsigned tails_face = run_tails(frow, face);
+      const unsigned tails_texel = run_tails(tg.tb, tg.tb >= 0);
+      const unsigned tails_exp = run_tails(tg.sidx, tg.sidx >= 0);
+      const unsigned tails_nm = kDarboux ? run_tails(tg.nb, tg.nb >= 0) : 0u;
+      __syncwarp();
+      for (int c = lane; c < Acc::kCols; c += 32) {  // a second column per lane with phong_darboux
+        int target, offset, kind;
+        acc_column<kDarboux>(c, tex_c, &target, &offset, &kind);
+        const unsigned tails = kind == 0 ? tails_face : kind == 1 ? tails_texel : kind == 2 ? tails_exp : tails_nm;
+        float sum = 0.0f;
+#pragma unroll
+        for (int q = 0; q < 32; ++q) {
+          sum += acc_tab[q * Acc::kRow + c];
+          if ((tails >> q) & 1u) {
+            if (sum != 0.0f) {
+              float* base = acc_tgt[q * Acc::kTargets + target];
+              if (base) red_add(base + offset, sum);
+            }
+            sum = 0.0f;
+          }
         }
       }
-    }
-    if (kDarboux && G.normal_map) {
-      const Seg sn = segment(tg.nb, tg.nb >= 0);
-      seg_sums<3>(tg.gn, sn);
-      if (sn.tail) add_texel_grad(G.normal_map, tg.nb, 3, tg.gn);
-    }
-    if (G.texture) {
-      const Seg st = segment(tg.tb, tg.tb >= 0);
-      seg_sums<3>(tg.gt, st);
-      if (st.tail) add_texel_grad(G.texture, tg.tb, tg.ch, tg.gt);
-    }
-    if (G.specular_map) {
-      const Seg ss = segment(tg.sidx, tg.sidx >= 0);
-      seg_sums<1>(&tg.gs, ss);
-      if (ss.tail && tg.gs != 0.0f) atomicAdd(G.specular_map + tg.sidx, tg.gs);
+      __syncwarp();  // the table is rewritten by the next pass
     }
   }
   // over: the background is seen through what the kept slots let pass
@@ -903,10 +935,9 @@ pixel_kernel(RastBatch B, Work w, const float* __restrict__ grad_canvas, const f
 #pragma unroll
     for (int q = 0; q < 3; ++q) pg.v[RAST_GRAD_BACKGROUND + q] += gcv_px[q] * transmit;
   }
-  // the background has a gradient only in layered batches
-  constexpr unsigned long long kBits = pixel_bits(SH) & (kLayers ? ~0ull : ~range_bits(RAST_GRAD_BACKGROUND, 3));
+  __syncthreads();  // every warp is done with its table before the transpose reuses the memory
   reduce_params<kBits, true>(pg, G.job_params, in_job && (over ? shown : P.prim_id[pix] >= 0), blockIdx.y,
-                             LightPost{&sL, sh});
+                             LightPost{&sL, sh}, s_tab);
 }
 
 // dL/dM = -m^T (dL/dm) m^T for the [x, y, w] rows of the clip positions,
