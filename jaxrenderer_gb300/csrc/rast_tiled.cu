@@ -10,7 +10,8 @@
 //                      conservative tile range of its coverage region, bin counts
 //   scan_local_kernel  \  exclusive prefix sum of bin counts -> bin offsets;
 //   scan_apply_kernel  /  tiles whose bins exceed the capacity are marked
-//   scatter_kernel     one warp per 32 faces: face id into every bin it overlaps
+//   scatter_kernel     over the binned faces the set-up listed, one warp per 32:
+//                      face id into every bin its rectangle overlaps
 //   raster_kernel      persistent warps, one tile each: bin entries staged in
 //                      shared memory, per-pixel packed (depth | id) minimum
 //   tiled_shade_kernel one thread per pixel: deferred shading of the winner,
@@ -296,7 +297,18 @@ struct Geometry {
   int tiles_x;      // tiles along x of the largest job (stride)
   int tiles_y;
   int tiles_per_job;
+  // ceil(2^64 / d) for d = tiles_per_job and tiles_x (0 for d = 1): the
+  // raster kernel's per-tile quotients as one high multiply (fast_div)
+  unsigned long long tpj_inv, tx_inv;
 };
+
+// n / d for n < 2^32 from inv = ceil(2^64 / d): floor(n inv / 2^64) = n / d
+// + n e / 2^64 with 0 <= e < 1 floors to floor(n / d), since the fraction of
+// n / d is at most 1 - 1/d and n e / 2^64 < 2^-32 <= 1/d.  inv = 0 marks d = 1.
+__host__ __device__ inline unsigned long long div_inverse(unsigned d) { return d <= 1u ? 0ull : ~0ull / d + 1ull; }
+__device__ __forceinline__ unsigned fast_div(unsigned n, unsigned long long inv) {
+  return inv == 0ull ? n : static_cast<unsigned>(__umul64hi(static_cast<unsigned long long>(n), inv));
+}
 
 // Per-face coverage rectangle in pixels, [x, z] x [y, w] (ushort4: i0, j0,
 // i1, j1); empty (x > z) for faces that are not binned.
@@ -388,7 +400,7 @@ template <bool kSmall>
 __global__ void __launch_bounds__(kSetupThreads, setup_min_blocks(kSmall))
 setup_bin_kernel(RastBatch B, Geometry G, const int2* __restrict__ fmap, float4* __restrict__ setup,
                  ushort4* __restrict__ bbox, uint32_t* __restrict__ counts, unsigned long long* __restrict__ keys,
-                 int small_area) {
+                 int small_area, int4* __restrict__ binned, unsigned int* __restrict__ n_binned) {
   __shared__ RastJob sJ;
   __shared__ float s_m[12][kSetupThreads];
   __shared__ int s_face[kSetupThreads];
@@ -497,6 +509,13 @@ setup_bin_kernel(RastBatch B, Geometry G, const int2* __restrict__ fmap, float4*
       s_srect[e][0] = i0 | (i1 << 16);
       s_srect[e][1] = j0 | (j1 << 16);
     }
+    // binned faces (those with tiles) join the scatter's list: one atomic per warp
+    const bool bin = tx0 <= tx1 && ty0 <= ty1;
+    const unsigned bm = __ballot_sync(0xffffffffu, bin);
+    unsigned bbase = 0;
+    if ((threadIdx.x & 31) == 0 && bm) bbase = atomicAdd(n_binned, static_cast<unsigned>(__popc(bm)));
+    bbase = __shfl_sync(0xffffffffu, bbase, 0);
+    if (bin) binned[bbase + __popc(bm & lanemask_lt())] = make_int4(jid, fq, i0 | (j0 << 16), i1 | (j1 << 16));
     uint32_t* cnt = counts + static_cast<int64_t>(jid) * G.tiles_per_job;
     warp_tiles(tx0, ty0, tx1, ty1, G.tiles_x, [&](int, int tile, bool valid) {
       const unsigned peers = __match_any_sync(0xffffffffu, valid ? tile : -1);
@@ -598,42 +617,43 @@ scan_apply_kernel(const uint32_t* __restrict__ counts, uint32_t* __restrict__ of
   }
 }
 
-// Face ids into the bins of the tiles their rectangles cover, one warp per
-// 32 faces with the (face, tile) pairs spread over its lanes; lanes writing
-// to the same tile take their slots with one atomic (__match_any_sync).
-// Grid: one block per kSetupThreads faces of a job (face block map).
+// Face ids into the bins of the tiles their rectangles cover, over the list
+// of binned faces the set-up kernel appended (job, face, pixel rectangle):
+// faces without tiles cost nothing here.  One warp per 32 listed faces with
+// the (face, tile) pairs spread over its lanes; lanes writing to the same
+// tile take their slots with one atomic (__match_any_sync).  Grid: any
+// number of blocks of kSetupThreads threads, striding over the list.
 __global__ void __launch_bounds__(kSetupThreads)
-scatter_kernel(RastBatch B, Geometry G, const int2* __restrict__ fmap, const ushort4* __restrict__ bbox,
-               const uint32_t* __restrict__ offsets, uint32_t* __restrict__ cursors,
-               int32_t* __restrict__ bins) {
-  const int2 blk = fmap[blockIdx.x];
-  if (blk.x < 0) return;
-  const int jid = blk.x;
-  const int nf = __ldg(&B.jobs[jid].n_faces);
-  const int f = blk.y + static_cast<int>(threadIdx.x);
-  if (f - static_cast<int>(threadIdx.x & 31) >= nf) return;  // the whole warp is past the faces
-  ushort4 bb = empty_rect();
-  if (f < nf) bb = bbox[__ldg(&B.jobs[jid].setup_begin) + f];
-  int tx0 = 1, ty0 = 1, tx1 = 0, ty1 = 0;  // the pixel rectangle's tiles
-  if (bb.x <= bb.z && bb.y <= bb.w) {
-    tx0 = bb.x >> G.tws;
-    tx1 = bb.z >> G.tws;
-    ty0 = bb.y >> G.ths;
-    ty1 = bb.w >> G.ths;
-  }
-  const int64_t tb = static_cast<int64_t>(jid) * G.tiles_per_job;
+scatter_kernel(Geometry G, const int4* __restrict__ binned, const unsigned int* __restrict__ n_binned,
+               const uint32_t* __restrict__ offsets, uint32_t* __restrict__ cursors, int32_t* __restrict__ bins) {
+  const unsigned n = *n_binned;
   const int lane = threadIdx.x & 31;
-  warp_tiles(tx0, ty0, tx1, ty1, G.tiles_x, [&](int owner, int tile, bool valid) {
-    const uint32_t o = valid ? offsets[tb + tile] : kOverflow;
-    const bool write = !(o & kOverflow);
-    const unsigned peers = __match_any_sync(0xffffffffu, write ? tile : -1);
-    const int leader = __ffs(peers) - 1;
-    uint32_t slot = 0;
-    if (write && lane == leader) slot = atomicAdd(cursors + tb + tile, static_cast<unsigned>(__popc(peers)));
-    slot = __shfl_sync(0xffffffffu, slot, leader) + __popc(peers & lanemask_lt());
-    const int fid = __shfl_sync(0xffffffffu, f, owner);
-    if (write) bins[static_cast<int64_t>(o) + slot] = fid;
-  });
+  for (unsigned base = blockIdx.x * kSetupThreads; base < n; base += gridDim.x * kSetupThreads) {
+    const unsigned e = base + threadIdx.x;
+    if (base + (threadIdx.x & ~31u) >= n) break;  // the whole warp is past the list
+    int jid = 0, fq = 0, tx0 = 1, ty0 = 1, tx1 = 0, ty1 = 0;
+    if (e < n) {
+      const int4 b = binned[e];
+      jid = b.x;
+      fq = b.y;
+      tx0 = (b.z & 0xffff) >> G.tws;
+      ty0 = (b.z >> 16) >> G.ths;
+      tx1 = (b.w & 0xffff) >> G.tws;
+      ty1 = (b.w >> 16) >> G.ths;
+    }
+    warp_tiles(tx0, ty0, tx1, ty1, G.tiles_x, [&](int owner, int tile, bool valid) {
+      const int64_t gt = static_cast<int64_t>(__shfl_sync(0xffffffffu, jid, owner)) * G.tiles_per_job + tile;
+      const uint32_t o = valid ? offsets[gt] : kOverflow;
+      const bool write = !(o & kOverflow);
+      const unsigned peers = __match_any_sync(0xffffffffu, write ? gt : -1ll);
+      const int leader = __ffs(peers) - 1;
+      uint32_t slot = 0;
+      if (write && lane == leader) slot = atomicAdd(cursors + gt, static_cast<unsigned>(__popc(peers)));
+      slot = __shfl_sync(0xffffffffu, slot, leader) + __popc(peers & lanemask_lt());
+      const int fid = __shfl_sync(0xffffffffu, fq, owner);
+      if (write) bins[static_cast<int64_t>(o) + slot] = fid;
+    });
+  }
 }
 
 // True when edge function (x ea + y eb) + ec is negative at every pixel of
@@ -739,9 +759,11 @@ raster_kernel(RastBatch B, Geometry G, const float4* __restrict__ setup, const u
     const unsigned int cur = unit;
     const uint32_t off = m_off, t_count = m_cnt;
     const unsigned int t = cur / kWPT;  // bin tile
-    const int jid = static_cast<int>(t / G.tiles_per_job);
-    const int local = static_cast<int>(t % G.tiles_per_job);
-    const int tx = local % G.tiles_x, ty = local / G.tiles_x;
+    const unsigned jq = fast_div(t, G.tpj_inv);
+    const int jid = static_cast<int>(jq);
+    const int local = static_cast<int>(t - jq * static_cast<unsigned>(G.tiles_per_job));
+    const int ty = static_cast<int>(fast_div(static_cast<unsigned>(local), G.tx_inv));
+    const int tx = local - ty * G.tiles_x;
     const int y0 = ty * (TH * kWPT) + static_cast<int>(cur % kWPT) * TH;  // first row of this warp's part
     const int x0 = tx * TW;
     const RastJob& J = B.jobs[jid];
@@ -1142,7 +1164,7 @@ inline uint64_t default_bin_capacity(const RastBatch& b) {
 }
 
 struct Layout {
-  size_t setup_off, bbox_off, counts_off, offsets_off, cursors_off, bsums_off, bins_off, winner_off,
+  size_t setup_off, bbox_off, binned_off, counts_off, offsets_off, cursors_off, bsums_off, bins_off, winner_off,
       vis_off, fvar_off, fmap_off, fstart_off, vmap_off, vstart_off, keys_off, misc_off, total;
   unsigned fmap_blocks, vmap_blocks;  // face block maps: setup/scatter, face varyings
   bool small_path;  // setup kernel rasterises small faces (not when near ties are counted)
@@ -1162,6 +1184,8 @@ static Layout layout(const RastBatch& b, TileShape ts, uint64_t bin_capacity, in
   L.G.tiles_x = ceil_div(std::max(b.max_width, 1), ts.tw);
   L.G.tiles_y = ceil_div(std::max(b.max_height, 1), ts.th);
   L.G.tiles_per_job = L.G.tiles_x * L.G.tiles_y;
+  L.G.tpj_inv = div_inverse(static_cast<unsigned>(L.G.tiles_per_job));
+  L.G.tx_inv = div_inverse(static_cast<unsigned>(L.G.tiles_x));
   L.n_tiles = static_cast<int64_t>(b.n_jobs) * L.G.tiles_per_job;
   L.n_scan_blocks = (L.n_tiles + kScanBlock - 1) / kScanBlock;
   L.bin_capacity = bin_capacity;
@@ -1173,6 +1197,7 @@ static Layout layout(const RastBatch& b, TileShape ts, uint64_t bin_capacity, in
   };
   L.setup_off = take(static_cast<size_t>(b.total_setup) * 64);
   L.bbox_off = take(static_cast<size_t>(b.total_setup) * sizeof(ushort4));
+  L.binned_off = take(static_cast<size_t>(b.total_setup) * sizeof(int4));
   L.counts_off = take(static_cast<size_t>(L.n_tiles) * 4);
   L.cursors_off = take(static_cast<size_t>(L.n_tiles) * 4);
   L.offsets_off = take(static_cast<size_t>(L.n_tiles) * 4);
@@ -1314,8 +1339,10 @@ static int render(const RastBatch* batch, const RastTiledConfig* cfg, void* work
   uint32_t* bsums = reinterpret_cast<uint32_t*>(ws + L.bsums_off);
   int32_t* bins = reinterpret_cast<int32_t*>(ws + L.bins_off);
   int32_t* winner = reinterpret_cast<int32_t*>(ws + L.winner_off);
-  // [0] raster tile counter, [1] overflow status, [2..3] bin entries, [4..5] raster pixel tests
+  // [0] raster tile counter, [1] overflow status, [2..3] bin entries, [4..5] raster pixel tests,
+  // [6] binned faces
   unsigned int* misc = reinterpret_cast<unsigned int*>(ws + L.misc_off);
+  int4* binned = reinterpret_cast<int4*>(ws + L.binned_off);
   Profiler prof(profile, s, "rast_render_tiled");
 
   const bool cover = (phase & RAST_PHASE_COVERAGE) != 0, shade = (phase & RAST_PHASE_SHADE) != 0;
@@ -1346,15 +1373,24 @@ static int render(const RastBatch* batch, const RastTiledConfig* cfg, void* work
       prof.mark("block_map_kernel");
       const unsigned grid = L.fmap_blocks;
       if (keys)
-        setup_bin_kernel<true><<<grid, kSetupThreads, 0, s>>>(b, L.G, fmap, setup, bbox, counts, keys, small_area);
+        setup_bin_kernel<true><<<grid, kSetupThreads, 0, s>>>(b, L.G, fmap, setup, bbox, counts, keys, small_area,
+                                                             binned, misc + 6);
       else
-        setup_bin_kernel<false><<<grid, kSetupThreads, 0, s>>>(b, L.G, fmap, setup, bbox, counts, nullptr, 0);
+        setup_bin_kernel<false><<<grid, kSetupThreads, 0, s>>>(b, L.G, fmap, setup, bbox, counts, nullptr, 0,
+                                                              binned, misc + 6);
       prof.mark("setup_bin_kernel");
       scan_local_kernel<<<static_cast<unsigned>(L.n_scan_blocks), 256, 0, s>>>(counts, offsets, bsums, L.n_tiles);
       scan_apply_kernel<<<static_cast<unsigned>(L.n_scan_blocks), 256, 0, s>>>(counts, offsets, bsums, L.n_tiles,
                                                                                 L.bin_capacity, misc + 1);
       prof.mark("scan_kernels");
-      scatter_kernel<<<grid, kSetupThreads, 0, s>>>(b, L.G, fmap, bbox, offsets, cursors, bins);
+      {
+        int sms = 0, dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        // the list's length is on the device: a full wave of blocks strides over it
+        const unsigned sgrid = static_cast<unsigned>(std::max(sms, 1) * (2048 / kSetupThreads));
+        scatter_kernel<<<std::min(sgrid, grid), kSetupThreads, 0, s>>>(L.G, binned, misc + 6, offsets, cursors, bins);
+      }
       prof.mark("scatter_kernel");
     }
     if (b.total_pixels > 0) {

@@ -199,5 +199,11 @@ def test_mixed_batch_backward_tiled_matches_plain(mixed):
     torch.cuda.synchronize()
     for gt, gp in zip(grads["tiled"], grads["plain"]):
         for k in gt:
-            torch.testing.assert_close(gt[k], gp[k], rtol=1e-4, atol=1e-5, msg=k)
+            # Both forms hand the backward the same winners, so only the order
+            # of the FP32 atomic sums differs.  Per-scene terms add ~1e5 pixel
+            # contributions of either sign: run to run (same form) they move
+            # by up to 4e-7 of the tensor's largest entry (1.2e-4 at 352 on
+            # the 480x270 class), hence atol 1e-6 of that entry.
+            atol = max(1e-5, 1e-6 * float(gp[k].abs().max()))
+            torch.testing.assert_close(gt[k], gp[k], rtol=1e-4, atol=atol, msg=k)
         assert gt["position"].abs().sum() > 0
