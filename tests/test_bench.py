@@ -29,7 +29,7 @@ def test_kernel_bytes_raster_and_shade():
 def test_ncu_counts_only_for_the_measured_pass_and_config():
     cfg = lambda w, h, wpt=1: types.SimpleNamespace(tile_w=w, tile_h=h, warps_per_tile=wpt)  # noqa: E731
     assert bench.ncu_per_unit("main", "raster_kernel", cfg(8, 8)) == bench.NCU_PER_UNIT[("main", "raster_kernel", 8, 8, 1)]
-    assert bench.ncu_per_unit("main", "raster_kernel", cfg(16, 8)) is None  # another tile shape
+    assert bench.ncu_per_unit("main", "raster_kernel", cfg(32, 8)) is None  # another tile shape
     assert bench.ncu_per_unit("main", "raster_kernel", cfg(8, 8, 2)) is None  # two warps per tile
     assert bench.ncu_per_unit("shadow", "raster_kernel", cfg(16, 8))[0] == "P"
     assert bench.ncu_per_unit("main", "tiled_shade_kernel", None)[0] == "P"
