@@ -990,10 +990,11 @@ def pass_info(runner, pass_name):
         "slots": 4 if int(jobs["layers"].max()) > 0 else 1,  # chooser slots written per pixel
         "E": 0.0,
         "T": 0.0,
+        "B": 0.0,
     }
     if runner.form == "tiled":
         st = runner.stats(pass_name)
-        info["E"], info["T"] = float(st.bin_entries), float(st.tiles)
+        info["E"], info["T"], info["B"] = float(st.bin_entries), float(st.tiles), float(st.binned_faces)
         info["pixel_tests"] = float(st.pixel_tests)
     return info
 
@@ -1001,7 +1002,8 @@ def pass_info(runner, pass_name):
 def kernel_bytes(kname, info, visible):
     """Algorithmic bytes one launch of `kname` must move: inputs read once,
     outputs written once; re-reads served by caches are not counted.
-    F faces, P pixels, E bin entries, T tiles, V faces visible in the main
+    F faces, P pixels, E bin entries, T tiles, B binned faces (those with a
+    tile, listed for the scatter), V faces visible in the main
     pass (the front-most kept face of a pixel: with layered choosers a lower
     bound), vs varyings per corner, S chooser slots written per pixel."""
     F, P, E, T, vs = info["F"], info["P"], info["E"], info["T"], info["vs"]
@@ -1015,9 +1017,9 @@ def kernel_bytes(kname, info, visible):
         "scan_kernel": F * 48 + P * 4 * S,
         "shade_kernel": P * (4 * S + out_px) + info["Ptex"] + V * (64 + 3 * (16 + 4 * vs)),
         # tiled form
-        "setup_bin_kernel": F * (12 + 36 + 64 + 8) + E * 4,
+        "setup_bin_kernel": F * (12 + 36 + 64 + 8) + info.get("B", 0.0) * 16 + E * 4,
         "scan_kernels": T * 12,
-        "scatter_kernel": F * 8 + E * 12,
+        "scatter_kernel": info.get("B", 0.0) * 16 + E * 12,
         "raster_kernel": F * 48 + E * 4 + P * 4 * S,
         "face_varyings_kernel": F + V * (12 + 3 * (info["cin"] / max(info["corners"], 1)) + 3 * 4 * vs),
         "tiled_shade_kernel": P * (4 * S + out_px) + info["Ptex"] + V * (64 + 3 * 4 * vs),

@@ -37,8 +37,9 @@
 extern "C" {
 #endif
 
-#define RAST_ABI_VERSION 4  /* 2: chooser / mix hook fields (RastJob.layers ..., RastPools.face_alpha, RastBatch.max_layers);
-                                 3: RastTiledStats.pixel_tests; 4: RastTiledConfig.warps_per_tile, rast_autotune */
+#define RAST_ABI_VERSION 5  /* 2: chooser / mix hook fields (RastJob.layers ..., RastPools.face_alpha, RastBatch.max_layers);
+                                 3: RastTiledStats.pixel_tests; 4: RastTiledConfig.warps_per_tile, rast_autotune;
+                                 5: RastTiledStats.binned_faces (was reserved) */
 
 /* Built-in shader classes (renderer/shaders/*.py), one kernel path each. */
 typedef enum RastShader {
@@ -324,7 +325,7 @@ typedef struct RastTiledStats {
   uint64_t bin_capacity;  /* entries reserved */
   uint64_t tiles;         /* tile slots (jobs x tiles of the largest job) */
   uint32_t overflow;      /* 1: some tiles exceeded the capacity and were full-scanned */
-  uint32_t reserved;
+  uint32_t binned_faces;  /* faces with at least one tile (the scatter's list) */
   uint64_t pixel_tests;   /* pixel-triangle pairs the raster kernel tested, counted per warp: entries
                              tested against every pixel of the warp's part of the tile x its pixels,
                              plus the (entry, pixel) pairs of the pair path (the pixels of an

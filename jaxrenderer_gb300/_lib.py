@@ -20,7 +20,7 @@ SHADER_PHONG_DARBOUX = 4
 SHADER_PHONG_REFLECTION = 5
 SHADER_PHONG_REFLECTION_SHADOW = 6
 
-ABI_VERSION = 4  # RAST_ABI_VERSION of the header these structures mirror
+ABI_VERSION = 5  # RAST_ABI_VERSION of the header these structures mirror
 
 JOB_APPLY_DEPTH_OFFSET = 1
 JOB_FACE_ALPHA = 2
@@ -153,7 +153,7 @@ class RastTiledConfig(ctypes.Structure):
 
 class RastTiledStats(ctypes.Structure):
     _fields_ = [("bin_entries", c_uint64), ("bin_capacity", c_uint64), ("tiles", c_uint64),
-                ("overflow", ctypes.c_uint32), ("reserved", ctypes.c_uint32), ("pixel_tests", c_uint64)]
+                ("overflow", ctypes.c_uint32), ("binned_faces", ctypes.c_uint32), ("pixel_tests", c_uint64)]
 
 
 GRAD_WORLD_TO_CLIP = 0

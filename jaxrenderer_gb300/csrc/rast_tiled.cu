@@ -515,7 +515,10 @@ setup_bin_kernel(RastBatch B, Geometry G, const int2* __restrict__ fmap, float4*
     unsigned bbase = 0;
     if ((threadIdx.x & 31) == 0 && bm) bbase = atomicAdd(n_binned, static_cast<unsigned>(__popc(bm)));
     bbase = __shfl_sync(0xffffffffu, bbase, 0);
-    if (bin) binned[bbase + __popc(bm & lanemask_lt())] = make_int4(jid, fq, i0 | (j0 << 16), i1 | (j1 << 16));
+    if (bin)
+      binned[bbase + __popc(bm & lanemask_lt())] =
+          make_int4(jid, fq, static_cast<int>(static_cast<unsigned>(i0) | (static_cast<unsigned>(j0) << 16)),
+                    static_cast<int>(static_cast<unsigned>(i1) | (static_cast<unsigned>(j1) << 16)));
     uint32_t* cnt = counts + static_cast<int64_t>(jid) * G.tiles_per_job;
     warp_tiles(tx0, ty0, tx1, ty1, G.tiles_x, [&](int, int tile, bool valid) {
       const unsigned peers = __match_any_sync(0xffffffffu, valid ? tile : -1);
@@ -619,27 +622,33 @@ scan_apply_kernel(const uint32_t* __restrict__ counts, uint32_t* __restrict__ of
 
 // Face ids into the bins of the tiles their rectangles cover, over the list
 // of binned faces the set-up kernel appended (job, face, pixel rectangle):
-// faces without tiles cost nothing here.  One warp per 32 listed faces with
-// the (face, tile) pairs spread over its lanes; lanes writing to the same
-// tile take their slots with one atomic (__match_any_sync).  Grid: any
-// number of blocks of kSetupThreads threads, striding over the list.
+// faces without tiles cost nothing here.  Each warp takes up to 32 listed
+// faces, fewer when the list is short (so that every warp of the grid has
+// some: a warp's (face, tile) pairs are a chain of dependent loads and
+// atomics, and a short list on few warps leaves the GPU waiting on them),
+// with the pairs spread over its lanes; lanes writing to the same tile take
+// their slots with one atomic (__match_any_sync).  Grid: any number of
+// blocks of kSetupThreads threads, striding over the list.
 __global__ void __launch_bounds__(kSetupThreads)
 scatter_kernel(Geometry G, const int4* __restrict__ binned, const unsigned int* __restrict__ n_binned,
                const uint32_t* __restrict__ offsets, uint32_t* __restrict__ cursors, int32_t* __restrict__ bins) {
   const unsigned n = *n_binned;
   const int lane = threadIdx.x & 31;
-  for (unsigned base = blockIdx.x * kSetupThreads; base < n; base += gridDim.x * kSetupThreads) {
-    const unsigned e = base + threadIdx.x;
-    if (base + (threadIdx.x & ~31u) >= n) break;  // the whole warp is past the list
+  constexpr unsigned kWarps = kSetupThreads / 32;
+  const unsigned warps = gridDim.x * kWarps, wid = blockIdx.x * kWarps + (threadIdx.x >> 5);
+  const unsigned per_warp = max(1u, min(32u, (n + warps - 1) / warps));  // listed faces per warp
+  for (unsigned base = wid * per_warp; base < n; base += warps * per_warp) {
+    const unsigned e = base + lane;
     int jid = 0, fq = 0, tx0 = 1, ty0 = 1, tx1 = 0, ty1 = 0;
-    if (e < n) {
+    if (lane < static_cast<int>(per_warp) && e < n) {
       const int4 b = binned[e];
+      const unsigned lo = static_cast<unsigned>(b.z), hi = static_cast<unsigned>(b.w);
       jid = b.x;
       fq = b.y;
-      tx0 = (b.z & 0xffff) >> G.tws;
-      ty0 = (b.z >> 16) >> G.ths;
-      tx1 = (b.w & 0xffff) >> G.tws;
-      ty1 = (b.w >> 16) >> G.ths;
+      tx0 = static_cast<int>((lo & 0xffffu) >> G.tws);
+      ty0 = static_cast<int>((lo >> 16) >> G.ths);
+      tx1 = static_cast<int>((hi & 0xffffu) >> G.tws);
+      ty1 = static_cast<int>((hi >> 16) >> G.ths);
     }
     warp_tiles(tx0, ty0, tx1, ty1, G.tiles_x, [&](int owner, int tile, bool valid) {
       const int64_t gt = static_cast<int64_t>(__shfl_sync(0xffffffffu, jid, owner)) * G.tiles_per_job + tile;
@@ -1466,7 +1475,7 @@ extern "C" int rast_tiled_stats(const RastBatch* batch, const RastTiledConfig* c
   if (shape_status != RAST_OK) return shape_status;
   const uint64_t cap = cfg && cfg->bin_capacity > 0 ? cfg->bin_capacity : tiled::default_bin_capacity(*batch);
   const tiled::Layout L = tiled::layout(*batch, ts, cap, tiled::small_area_of(cfg));
-  unsigned int misc[6] = {0, 0, 0, 0, 0, 0};
+  unsigned int misc[7] = {0, 0, 0, 0, 0, 0, 0};
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   if (cudaMemcpyAsync(misc, static_cast<const char*>(workspace) + L.misc_off, sizeof(misc),
                       cudaMemcpyDeviceToHost, s) != cudaSuccess)
@@ -1475,6 +1484,7 @@ extern "C" int rast_tiled_stats(const RastBatch* batch, const RastTiledConfig* c
   out->bin_entries = static_cast<uint64_t>(misc[2]) | (static_cast<uint64_t>(misc[3]) << 32);
   out->pixel_tests = static_cast<uint64_t>(misc[4]) | (static_cast<uint64_t>(misc[5]) << 32);
   out->overflow = misc[1];
+  out->binned_faces = misc[6];
   out->tiles = static_cast<uint64_t>(L.n_tiles);
   out->bin_capacity = L.bin_capacity;
   return RAST_OK;

@@ -38,7 +38,7 @@ def test_every_declared_symbol_is_exported(lib):
 
 
 def test_host_only_entry_points(lib):
-    assert lib.rast_abi_version() == _lib.ABI_VERSION == 4
+    assert lib.rast_abi_version() == _lib.ABI_VERSION == 5
     assert lib.rast_error_string(0) == b"ok"
     assert lib.rast_error_string(6) == b"tile bin capacity exceeded"
     job = _lib.RastJob()

@@ -270,3 +270,31 @@ def test_autotune_through_the_c_abi(cuda_device, brax_batch):
     torch.cuda.synchronize()
     assert torch.equal(got["prim_id"], plain["prim_id"])
     assert torch.equal(got["canvas"].view(torch.int32), plain["canvas"].view(torch.int32))
+
+
+@pytest.mark.parametrize("flip", [(-1, 1), (1, -1), (-1, -1)])
+def test_mirrored_viewports_tiled_equals_plain_and_oracle(cuda_device, flip):
+    """Viewports with a negative x and/or y scale: the pixel <-> NDC maps
+    run backwards, so the per-face pixel rectangles, the per-tile NDC tables
+    and the pair path's entry rectangles all see decreasing coordinates."""
+    specs = []
+    for k, sh in enumerate((_lib.SHADER_GOURAUD, _lib.SHADER_DEPTH, _lib.SHADER_PHONG_REFLECTION)):
+        s = scenes.random_job(sh, seed=980 + k, W=53, H=38, F=300, spread=1.4)
+        vp = np.asarray(s.viewport, F32).reshape(4, 4).copy()
+        vp[0, 0] *= flip[0]
+        vp[1, 1] *= flip[1]
+        s.viewport = vp
+        specs.append(s)
+    bufs = [scenes.initial_buffers(s) for s in specs]
+    refs = [oracle.render(s, *b) for s, b in zip(specs, bufs)]
+    assert all((r["prim_id"] >= 0).sum() > 200 for r in refs)
+    for form, tile, small in (("plain", None, 0), ("tiled", (8, 8), 0), ("tiled", (16, 8), 0),
+                              ("tiled", (16, 16, 2), 0), ("tiled", (4, 8), 32)):
+        packed = pack(specs, [b[0] for b in bufs], [b[1] for b in bufs], cuda_device)
+        if form == "plain":
+            render_plain(packed)
+        else:
+            st = render_tiled(packed, tile=tile[:2], small_area=small, warps_per_tile=tile[2] if len(tile) > 2 else 1)
+            assert st.overflow == 0
+        for k, (s, out) in enumerate(zip(specs, unpack(packed, specs))):
+            assert_parity(*out, refs[k], f"{form} {tile} flip {flip} job {k}")

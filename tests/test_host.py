@@ -181,3 +181,16 @@ def test_frame_matrices_refresh_equals_a_full_table_build():
     jb.frame_matrices(t, shell.camera_position, shell.camera_target, bb.camera, bb.light, moved)
     assert t.main_jobs.tobytes() == want.main_jobs.tobytes()
     assert t.shadow_jobs.tobytes() == want.shadow_jobs.tobytes()
+
+
+def test_dispatch_sends_canvases_wider_than_the_tiled_rectangles_to_the_plain_form():
+    from types import SimpleNamespace
+
+    from jaxrenderer_gb300 import dispatch
+
+    def batch(w, h, f):
+        return SimpleNamespace(jobs=[SimpleNamespace(width=w, height=h, n_faces=f)])
+
+    assert dispatch.choose(batch(2048, 2048, 100_000), "auto") == "tiled"
+    assert dispatch.choose(batch(70_000, 4, 1_000_000), "auto") == "plain"  # 16-bit pixel rectangles
+    assert dispatch.choose(batch(84, 84, 10), "auto") == "plain"  # small pass: fewer launches

@@ -55,10 +55,14 @@ def test_static_scratch_entry_point_matches_workspace_entry_point(cuda_device):
     assert lib.rast_render_tiled(ctypes.byref(b), ctypes.byref(cfg), ws.data_ptr(), need, stream) == 0
     expected = _snapshot(packed)
 
-    for _ in range(2):  # the array keeps the previous call's contents
+    for k in range(2):  # the array keeps the previous call's contents
         _restore(packed, init)
+        torch.cuda.synchronize(cuda_device)
+        free_before = torch.cuda.mem_get_info(cuda_device)[0]
         assert lib.rast_render_tiled_static(ctypes.byref(b), ctypes.byref(cfg), stream) == 0
         torch.cuda.synchronize(cuda_device)
+        if k == 1:  # after the first call's one-time set-up: the device's free memory does not move
+            assert torch.cuda.mem_get_info(cuda_device)[0] == free_before
         _assert_same(_snapshot(packed), expected)
     assert (expected[2] >= 0).any()
 
