@@ -749,18 +749,28 @@ raster_kernel(RastBatch B, Geometry G, const float4* __restrict__ setup, const u
   float* ty_ndc = s_y[kPairs ? warp : 0];
   unsigned long long tie_count = 0;
   unsigned long long tests = 0;  // pixel-triangle pairs this warp tested
-  // Tiles are grabbed one ahead and their bin offset and count loaded one
-  // ahead, so the counter atomic and those loads overlap a tile's work.
+  // The next tile is grabbed (one atomic on the shared counter) when this
+  // tile's last chunk of bin entries is staged, so the atomic's latency
+  // overlaps the end of this tile's tests while a warp never sits on an
+  // unstarted tile for long (tiles stay balanced over the warps when each
+  // warp gets only a few heavy ones); its bin offset and count are loaded
+  // before this tile's epilogue.
   unsigned int next = 0;
   if (lane == 0) next = atomicAdd(work, 1u);
+  bool grabbed = true;  // `next` holds a grabbed unit not yet started
   unsigned int unit = 0;
   uint32_t m_off = 0, m_cnt = 0;  // of `unit`
+  auto grab = [&]() {
+    if (!grabbed && lane == 0) next = atomicAdd(work, 1u);
+    grabbed = true;
+  };
   auto advance = [&]() {
+    grab();
     unit = __shfl_sync(0xffffffffu, next, 0);
+    grabbed = false;
     if (unit < n_units) {
       m_off = offsets[unit / kWPT];
       m_cnt = counts[unit / kWPT];
-      if (lane == 0) next = atomicAdd(work, 1u);
     }
   };
   advance();
@@ -917,6 +927,7 @@ raster_kernel(RastBatch B, Geometry G, const float4* __restrict__ setup, const u
       }
       const int pexcl = pincl - (pair ? cnt : 0);
       __syncwarp();
+      if (base + kStage >= n) grab();  // the last chunk: the next tile's atomic overlaps its tests
       // prefetch the next chunk while this one is tested
       if (base + kStage + lane < n) fetch(base + kStage + lane, n0, n1, n2, nid, nrc);
       tests += static_cast<unsigned>(m) * static_cast<unsigned>(TW * TH) + static_cast<unsigned>(ptotal);
@@ -978,7 +989,7 @@ raster_kernel(RastBatch B, Geometry G, const float4* __restrict__ setup, const u
       }
       __syncwarp();
     }
-    advance();  // the next tile's loads overlap this one's epilogue
+    advance();  // the next tile's offset and count loads overlap this one's epilogue
     if (kPairs) {
       // the pair path's minima join the lane's own (same pixel layout:
       // pixel q of lane l is li * TH + lj = 32 q + l)
