@@ -306,25 +306,44 @@ struct Work {
 
 // --------------------------------------------------------------- kernels
 
-// Grid: (pixel blocks of the largest job, n_jobs) for pixel kernels,
-// (face blocks, n_jobs) and (vertex blocks, n_jobs) for the others.
+// Grids: (pixel blocks of the largest job, n_jobs) for the pixel kernel and
+// the mark kernel (whose blocks cover kMarkPixels * kThreads pixels); block
+// maps of kRows faces or vertices of one job for the others.
+
+// Pixels per thread of the mark kernel: their winners are loaded together,
+// so one block's load latency covers kMarkPixels * kThreads pixels.
+constexpr int kMarkPixels = 8;
 
 __global__ void __launch_bounds__(kThreads) mark_kernel(RastBatch B, Work w) {
   const RastJob& J = B.jobs[blockIdx.y];
   const int64_t npx = static_cast<int64_t>(J.width) * J.height;
-  const int64_t local = static_cast<int64_t>(blockIdx.x) * kThreads + threadIdx.x;
-  if (local >= npx || J.n_faces <= 0) return;
-  const int64_t pix = J.pixel_begin + local;
+  const int64_t first = static_cast<int64_t>(blockIdx.x) * kThreads * kMarkPixels;
+  if (first >= npx || J.n_faces <= 0) return;  // uniform over the block
   const int layers = job_layers(J, B.max_layers);
   if (layers > 0 && J.mixer == RAST_MIX_OVER && B.pools.layer_prim) {  // every slot the over mixer may blend
-    for (int s = 0; s < layers; ++s) {
-      const int p = B.pools.layer_prim[s * B.total_pixels + pix];
-      if (p >= 0) w.fvis[J.setup_begin + p] = 1;
+    for (int r = 0; r < kMarkPixels; ++r) {
+      const int64_t local = first + r * kThreads + threadIdx.x;
+      if (local >= npx) break;
+      for (int s = 0; s < layers; ++s) {
+        const int p = B.pools.layer_prim[s * B.total_pixels + J.pixel_begin + local];
+        if (p >= 0) w.fvis[J.setup_begin + p] = 1;
+      }
     }
     return;
   }
-  const int p = B.pools.prim_id[pix];
-  if (p >= 0) w.fvis[J.setup_begin + p] = 1;
+  int p[kMarkPixels];
+#pragma unroll
+  for (int r = 0; r < kMarkPixels; ++r) {
+    const int64_t local = first + r * kThreads + threadIdx.x;
+    p[r] = local < npx ? __ldg(B.pools.prim_id + J.pixel_begin + local) : -1;
+  }
+  // neighbouring pixels of a warp (along a column) mostly show the same
+  // face: one flag store per run of equal winners
+#pragma unroll
+  for (int r = 0; r < kMarkPixels; ++r) {
+    const int prev = __shfl_up_sync(kFull, p[r], 1);
+    if (p[r] >= 0 && ((threadIdx.x & 31) == 0 || prev != p[r])) w.fvis[J.setup_begin + p[r]] = 1;
+  }
 }
 
 // Per visible face: clip rows of its corners, their 3x3 inverse (the forward
@@ -351,9 +370,9 @@ __device__ __forceinline__ void face_prep(const RastBatch& B, const Work& w, con
   r[0] = make_float4(m[0], m[1], m[2], m[3]);
   r[1] = make_float4(m[4], m[5], m[6], m[7]);
   r[2] = make_float4(m[8], zc[0], zc[1], zc[2]);
-  float* a = w.facc + row * 12;
+  float4* a = reinterpret_cast<float4*>(w.facc + row * 12);  // 48-byte rows of a 256-byte aligned array
 #pragma unroll
-  for (int k = 0; k < 12; ++k) a[k] = 0.0f;
+  for (int k = 0; k < 3; ++k) a[k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
 }
 
 // Per flagged vertex: the vertex shader's varyings, accumulators zeroed.
@@ -1184,7 +1203,9 @@ static void launch_all(const RastBatch& b, const Work& w, const Layout& L, const
   const unsigned fgrid = L.fblocks, vgrid = L.vblocks;
   build_block_map(b, kMapFaces, kRows, const_cast<int2*>(w.fmap), w.starts, s);
   build_block_map(b, kMapVertices, kRows, const_cast<int2*>(w.vmap), w.starts + b.n_jobs + 1, s);
-  mark_kernel<<<pgrid, kThreads, 0, s>>>(b, w);
+  const int64_t mark_px = static_cast<int64_t>(kThreads) * kMarkPixels;
+  mark_kernel<<<dim3(static_cast<unsigned>((max_px + mark_px - 1) / mark_px), static_cast<unsigned>(b.n_jobs)),
+                kThreads, 0, s>>>(b, w);
   prof.mark("backward_mark_kernels");
   face_prep_kernel<<<fgrid, kThreads, 0, s>>>(b, w);
   prof.mark("backward_face_prep_kernel");
