@@ -1049,7 +1049,7 @@ def library_digest(files=FORWARD_SOURCES) -> str:
 # library_digest() of the sources the NCU_* counts below were captured on:
 # when the kernels change, the counts no longer describe them and the bench
 # reports traffic and the issue figure as null until they are captured again.
-NCU_SOURCE_DIGEST = "f3fda1e3ffb65505"
+NCU_SOURCE_DIGEST = "183f3e47c15fbd81"
 
 
 def ncu_counts_current() -> bool:
@@ -1057,8 +1057,9 @@ def ncu_counts_current() -> bool:
 
 
 # Per-unit counts of the forward kernels measured by ncu on the 256-scene
-# brax-like batch with tile configs pinned (shadow 16x8; main 16x8, and 8x8
-# for the main raster's second entry; one warp per tile): DRAM bytes
+# brax-like batch with tile configs pinned (shadow 16x16 with two warps per
+# tile, main 16x8: the autotuner's choice for the 4096-scene batch; and
+# shadow 16x8 / main 8x8 for the raster's other entries): DRAM bytes
 # (dram__bytes_read.sum + dram__bytes_write.sum) and warp instructions
 # (smsp__inst_executed.sum) per face (F, 1,470,504 per pass) or per pixel of
 # the pass (P: 1,806,336 main, 4,194,304 shadow).  Both grow with the faces or
@@ -1066,15 +1067,16 @@ def ncu_counts_current() -> bool:
 # Keyed by (pass, kernel); the raster kernel's also by its tile shape and
 # warps per tile.
 NCU_PER_UNIT = {
-    ("shadow", "setup_bin_kernel"): ("F", 97.07, 25.19),
-    ("main", "setup_bin_kernel"): ("F", 103.52, 26.49),
-    ("shadow", "scatter_kernel"): ("F", 1.77, 1.17),
-    ("main", "scatter_kernel"): ("F", 6.74, 3.64),
-    ("shadow", "raster_kernel", 16, 8, 1): ("P", 3.40, 11.53),
-    ("main", "raster_kernel", 16, 8, 1): ("P", 29.31, 16.46),
-    ("main", "raster_kernel", 8, 8, 1): ("P", 29.14, 19.27),
-    ("main", "face_varyings_kernel"): ("F", 29.95, 4.60),
-    ("main", "tiled_shade_kernel"): ("P", 59.90, 31.21),
+    ("shadow", "setup_bin_kernel"): ("F", 97.04, 25.07),
+    ("main", "setup_bin_kernel"): ("F", 103.53, 26.49),
+    ("shadow", "scatter_kernel"): ("F", 1.69, 1.56),
+    ("main", "scatter_kernel"): ("F", 6.74, 3.97),
+    ("shadow", "raster_kernel", 16, 16, 2): ("P", 3.15, 11.62),
+    ("shadow", "raster_kernel", 16, 8, 1): ("P", 3.40, 11.68),
+    ("main", "raster_kernel", 16, 8, 1): ("P", 29.32, 16.66),
+    ("main", "raster_kernel", 8, 8, 1): ("P", 29.22, 19.56),
+    ("main", "face_varyings_kernel"): ("F", 29.90, 4.60),
+    ("main", "tiled_shade_kernel"): ("P", 59.80, 31.21),
 }
 
 
