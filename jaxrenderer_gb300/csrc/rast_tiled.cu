@@ -35,7 +35,6 @@ namespace tiled {
 constexpr int kSetupThreads = 128;    // faces per setup/scatter block (256: 1 % slower, 64: 7 %)
 constexpr int kScanBlock = 1024;       // elements per scan block (256 threads x 4)
 constexpr int kRasterWarps = 4;        // warps per CTA of the raster kernel
-constexpr int kTileChunk = 1;          // tiles a raster warp takes per atomic
 constexpr int kStage = 32;             // bin entries staged per warp round
 constexpr uint32_t kOverflow = 0x80000000u;
 
