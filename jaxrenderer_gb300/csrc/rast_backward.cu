@@ -42,10 +42,26 @@ constexpr int kThreads = 256;
 constexpr int kRowsPerThread = 32;
 constexpr int kRows = kThreads * kRowsPerThread;
 
-// y = v / |v|;  dv = (dy - y (y . dy)) / |v|  (one division, three products)
+// Gradient-only arithmetic.  Values that feed gradients alone (checked to a
+// relative tolerance) and no branch of the forward's (the texel index, the
+// shadow lookup and the barycentrics keep the forward's IEEE operations) use
+// the hardware's approximate reciprocal and reciprocal square root, a few
+// ulp, instead of IEEE division and square root.
+__device__ __forceinline__ float grad_rcp(float x) { return __fdividef(1.0f, x); }
+
+// out = v / |v| with the approximate reciprocal square root; returns |v|.
+__device__ __forceinline__ float unit3_grad(const float* v, float* out) {
+  const float ss = (v[0] * v[0] + v[1] * v[1]) + v[2] * v[2];
+  const float r = rsqrtf(ss);
+#pragma unroll
+  for (int k = 0; k < 3; ++k) out[k] = v[k] * r;
+  return ss * r;
+}
+
+// y = v / |v|;  dv = (dy - y (y . dy)) / |v|  (one reciprocal, three products)
 __device__ __forceinline__ void normalise3_bwd(const float* y, float norm, const float* dy, float* dv) {
   const float s = (y[0] * dy[0] + y[1] * dy[1]) + y[2] * dy[2];
-  const float r = 1.0f / norm;
+  const float r = grad_rcp(norm);
 #pragma unroll
   for (int k = 0; k < 3; ++k) dv[k] = (dy[k] - y[k] * s) * r;
 }
@@ -475,8 +491,7 @@ __device__ __forceinline__ void fragment_bwd(const RastJob& J, const RastPools& 
   float nrm[3], n[3];
 #pragma unroll
   for (int q = 0; q < 3; ++q) nrm[q] = interp1(b, r0[kVNormal + q], r1[kVNormal + q], r2[kVNormal + q]);
-  const float nrmn = norm3(nrm);
-  normalise3(nrm, n);
+  const float nrmn = unit3_grad(nrm, n);
   float gn[3] = {0.0f, 0.0f, 0.0f};
   if (may<SH>(RAST_SHADER_PHONG_DARBOUX) && sh == RAST_SHADER_PHONG_DARBOUX) {
     // phong_darboux.py:212-293: a Darboux frame from vertex 0's NDC and uv
@@ -503,9 +518,7 @@ __device__ __forceinline__ void fragment_bwd(const RastJob& J, const RastPools& 
       vi[r] = dot3(AI + 3 * r, bi);
       vj[r] = dot3(AI + 3 * r, bj);
     }
-    const float vin = norm3(vi), vjn = norm3(vj);
-    normalise3(vi, ni);
-    normalise3(vj, nj);
+    const float vin = unit3_grad(vi, ni), vjn = unit3_grad(vj, nj);
     float nm[3], bn[3], n2[3], tc[3], l[3], lc[3];
     texel3(P.normal_map + J.normal_map_begin, J.nm_w, J.nm_h, 3, ui, wi, nm);
 #pragma unroll
@@ -513,8 +526,7 @@ __device__ __forceinline__ void fragment_bwd(const RastJob& J, const RastPools& 
       const float row[3] = {ni[r], nj[r], n[r]};
       bn[r] = dot3(row, nm);
     }
-    const float bnn = norm3(bn);
-    normalise3(bn, n2);
+    const float bnn = unit3_grad(bn, n2);
     texel3(P.texture + J.texture_begin, J.tex_w, J.tex_h, J.tex_c, ui, wi, tc);
     l[0] = lu.dir[0], l[1] = lu.dir[1], l[2] = lu.dir[2];
     const float d = dot3(n2, l);
@@ -662,8 +674,7 @@ __device__ __forceinline__ void fragment_bwd(const RastJob& J, const RastPools& 
     float r[3], rn[3];
 #pragma unroll
     for (int q = 0; q < 3; ++q) r[q] = ((2.0f * d) * n[q]) - l[q];
-    const float rnorm = norm3(r);
-    normalise3(r, rn);
+    const float rnorm = unit3_grad(r, rn);
     const int su = gather_clamp(ui, J.spec_w), sv = gather_clamp(wi, J.spec_h);
     const int64_t sidx = J.specular_begin + static_cast<int64_t>(su) * J.spec_h + sv;
     const float sexp = __ldg(P.specular_map + sidx);
@@ -691,7 +702,7 @@ __device__ __forceinline__ void fragment_bwd(const RastJob& J, const RastPools& 
       tg.gs = gspec * spec * logf(rz);
     }
     // s x^(s-1) = s x^s / x for x > 0 (no second pow); at x = 0 the pow form
-    const float dspec_drz = (sexp == 0.0f) ? 0.0f : (rz > 0.0f ? sexp * (spec / rz) : sexp * powf(rz, sexp - 1.0f));
+    const float dspec_drz = (sexp == 0.0f) ? 0.0f : (rz > 0.0f ? sexp * (spec * grad_rcp(rz)) : sexp * powf(rz, sexp - 1.0f));
     // through max(rn_z, 0): zero below the kink, without forming 0 * inf
     // (pow's slope at 0 is infinite for exponents below 1)
     const float dmz = dmax0(rn[2]);
@@ -881,7 +892,7 @@ pixel_kernel(RastBatch B, Work w, const float* __restrict__ grad_canvas, const f
             }
             // b = c / sum(c)
             const float s = (gb[0] * b[0] + gb[1] * b[1]) + gb[2] * b[2];
-            const float rw = __frcp_rn(wr);
+            const float rw = grad_rcp(wr);
 #pragma unroll
             for (int k = 0; k < 3; ++k) gc[k] += (gb[k] - s) * rw;
           }
