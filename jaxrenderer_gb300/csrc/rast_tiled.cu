@@ -688,7 +688,7 @@ __device__ __forceinline__ bool edge_misses_tile(float ea, float eb, float ec, f
 //
 // Pair path (kL = 1 without near-tie counting): an entry's coverage
 // rectangle (from the set-up) cut to the warp's pixels is usually a few
-// pixels; entries of at most kPairMax such pixels are not tested against
+// pixels; entries of at most pair_max() such pixels are not tested against
 // every pixel of the tile but as (entry, pixel) pairs spread over the lanes,
 // 32 per round (a lane finds its entry by binary search over the warp's
 // prefix sums), each folding its key into the pixel's minimum in shared
@@ -696,12 +696,14 @@ __device__ __forceinline__ bool edge_misses_tile(float ea, float eb, float ec, f
 // lane its own pixels, keys in registers).  The minimum of packed keys does
 // not depend on the order, and both paths evaluate the same operations, so
 // the results are those of the dense loop alone.
-// Ten blocks per SM (48 registers) for the shapes of at most 128 pixels
-// with the default chooser: more resident warps beat the few spills
-// (16x8: 1.02 -> 0.88 ms, 8x8: 1.03 -> 1.01 ms on the 4096-scene
-// brax-like batch; 12 and 16 blocks measured slower).  The layered
-// variants of at most 64 pixels take eight (64 registers: 1.32 -> 1.18 ms
-// with 4 layers).  The others keep the compiler's choice (0: no minimum).
+// Blocks per SM: the pair-path variants of at most 128 pixels take eight
+// (64 registers; ten at 48 registers spilled in the pair loop: main 16x8
+// 0.58 -> 0.64 ms on the 4096-scene brax-like batch).  The near-tie
+// counting one-slot variants take ten (48 registers): more resident warps
+// beat their few spills (16x8: 1.02 -> 0.88 ms, 8x8: 1.03 -> 1.01 ms before
+// the pair path; 12 and 16 blocks measured slower).  The layered variants
+// of at most 64 pixels take eight (64 registers: 1.32 -> 1.18 ms with 4
+// layers).  The others keep the compiler's choice (0: no minimum).
 template <int TW, int TH, int kL, bool kPairs>
 __host__ __device__ constexpr int raster_min_blocks() {
   return kPairs ? (TW * TH <= 128 ? 8 : 0) : (kL == 1 && TW * TH <= 128) ? 10 : (TW * TH <= 64 ? 8 : 0);
