@@ -810,8 +810,10 @@ def count_visible(mr):
 
 def measure_fwd_bwd(wl: Workload, args, stream, timed, total_frames):
     """Forward + backward per step.  "mse": MSE against a fixed image per
-    scene: render (prim-id buffer saved), dL/dcanvas, rast_backward into
-    reused gradient arrays (per-vertex, per-texel, per-scene camera/light).
+    scene: render (prim-id buffer saved), then rast_backward_mse into reused
+    gradient arrays (per-vertex, per-texel, per-scene camera/light), zeroed
+    first; it forms dL/dcanvas = (canvas - target) * 2/n per pixel inside the
+    backward (no gradient image is written or read).
     "phong": the differentiable phong batch through DifferentiableBatch and
     torch autograd: camera matrices from eye positions, render, MSE against
     the unperturbed meshes' images, backward to positions, texture, light
@@ -843,8 +845,8 @@ def measure_fwd_bwd(wl: Workload, args, stream, timed, total_frames):
                 fwd = lambda mr=mr: mr.run(stream)  # noqa: E731
 
             def step(mr=mr, fwd=fwd, grads=grads):
-                outs = fwd()
-                mr.backward([(o.canvas - t) * s for o, t, s in zip(outs, targets, scales)], out=grads)
+                fwd()
+                mr.backward_mse(targets, scales, out=grads)
 
             runners = mr.runners
             mr = None

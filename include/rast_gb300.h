@@ -37,9 +37,9 @@
 extern "C" {
 #endif
 
-#define RAST_ABI_VERSION 5  /* 2: chooser / mix hook fields (RastJob.layers ..., RastPools.face_alpha, RastBatch.max_layers);
+#define RAST_ABI_VERSION 6  /* 2: chooser / mix hook fields (RastJob.layers ..., RastPools.face_alpha, RastBatch.max_layers);
                                  3: RastTiledStats.pixel_tests; 4: RastTiledConfig.warps_per_tile, rast_autotune;
-                                 5: RastTiledStats.binned_faces (was reserved) */
+                                 5: RastTiledStats.binned_faces (was reserved); 6: rast_backward_mse */
 
 /* Built-in shader classes (renderer/shaders/*.py), one kernel path each. */
 typedef enum RastShader {
@@ -383,6 +383,21 @@ int rast_backward(const RastBatch* batch, const float* grad_canvas, const float*
 int rast_backward_profiled(const RastBatch* batch, const float* grad_canvas, const float* grad_zbuffer,
                            const RastGradPools* grads, void* workspace, size_t workspace_bytes, void* stream,
                            RastProfile* profile);
+
+/* rast_backward for the mean-squared-error image loss
+ *   L = (scale / 2) * sum over every canvas value of (canvas - target)^2
+ * (scale = 2 / n for the mean over n values): dL/dcanvas =
+ * (canvas - target) * scale is formed per pixel inside the backward, from
+ * batch->pools.canvas as the last render left it, instead of being read from
+ * a gradient image; that spares the caller an elementwise pass over three
+ * canvas-sized arrays.  The difference and the product are rounded as an
+ * FP32 elementwise pass would round them, so the result is rast_backward's
+ * with grad_canvas = (canvas - target) * scale.  target (pixels, 3) like the
+ * canvas; grad_zbuffer may be NULL.  NULL target or canvas:
+ * RAST_ERR_INVALID_ARGUMENT.  No counterpart in the reference, where the
+ * loss is the caller's traced code (tests/smoke_test_grad.py:92-128). */
+int rast_backward_mse(const RastBatch* batch, const float* target, float scale, const float* grad_zbuffer,
+                      const RastGradPools* grads, void* workspace, size_t workspace_bytes, void* stream);
 
 /* ---------------------------------------------------------------------
  * Device-side merge_objects + per-corner flattening (instanced scenes).

@@ -20,7 +20,7 @@ SHADER_PHONG_DARBOUX = 4
 SHADER_PHONG_REFLECTION = 5
 SHADER_PHONG_REFLECTION_SHADOW = 6
 
-ABI_VERSION = 5  # RAST_ABI_VERSION of the header these structures mirror
+ABI_VERSION = 6  # RAST_ABI_VERSION of the header these structures mirror
 
 JOB_APPLY_DEPTH_OFFSET = 1
 JOB_FACE_ALPHA = 2
@@ -218,6 +218,8 @@ PROTOTYPES = [
     ("rast_backward_profiled", c_int,
      [POINTER(RastBatch), c_void_p, c_void_p, POINTER(RastGradPools), c_void_p, c_size_t, c_void_p,
       POINTER(RastProfile)]),
+    ("rast_backward_mse", c_int,
+     [POINTER(RastBatch), c_void_p, ctypes.c_float, c_void_p, POINTER(RastGradPools), c_void_p, c_size_t, c_void_p]),
     ("rast_merge_workspace_bytes", c_size_t, [POINTER(RastMergeBatch)]),
     ("rast_merge_objects", c_int, [POINTER(RastMergeBatch), c_void_p, c_size_t, c_void_p]),
     ("rast_display_u8", c_int, [c_void_p, c_int64, c_int32, c_int32, c_int32, c_int32, c_void_p, c_void_p]),

@@ -571,11 +571,48 @@ class BatchRunner:
 
     def backward(self, grad_canvas: Optional[torch.Tensor], grad_zbuffer: Optional[torch.Tensor] = None,
                  stream: Optional[torch.cuda.Stream] = None,
-                 out: Optional[Dict[str, torch.Tensor]] = None, profile=None) -> Dict[str, torch.Tensor]:
+                 out: Optional[Dict[str, torch.Tensor]] = None, profile=None,
+                 accumulate: bool = False) -> Dict[str, torch.Tensor]:
         """Gradients of the last run() of the main pass (rast_backward):
         per-vertex position/normal, per-texel texture/specular exponent and
         per-scene camera/light terms (RAST_GRAD_* layout, (N, 56)).  With
-        `out` (from grad_buffers()) the arrays are zeroed and reused."""
+        `out` (from grad_buffers()) the arrays are zeroed and reused; with
+        `accumulate` as well the gradients are added to what `out` holds
+        (gradient accumulation over several renders)."""
+        gc = grad_canvas.contiguous() if grad_canvas is not None else None
+        gz = grad_zbuffer.contiguous() if grad_zbuffer is not None else None
+
+        def call(args):
+            if profile is None:
+                return self.lib.rast_backward(args[0], gc.data_ptr() if gc is not None else None, *args[1:])
+            return self.lib.rast_backward_profiled(args[0], gc.data_ptr() if gc is not None else None, *args[1:],
+                                                   ctypes.byref(profile))
+
+        return self._backward(call, gz, stream, out, accumulate, "rast_backward")
+
+    def backward_mse(self, target: torch.Tensor, scale: Optional[float] = None,
+                     grad_zbuffer: Optional[torch.Tensor] = None, stream: Optional[torch.cuda.Stream] = None,
+                     out: Optional[Dict[str, torch.Tensor]] = None,
+                     accumulate: bool = False) -> Dict[str, torch.Tensor]:
+        """Gradients of the mean-squared-error loss (scale / 2) * sum((canvas
+        - target)^2) of the last run() (rast_backward_mse): dL/dcanvas =
+        (canvas - target) * scale is formed inside the backward from the
+        rendered canvas, with no gradient image.  `scale` defaults to 2 /
+        canvas.numel(), the gradient of the mean.  The result equals
+        backward((canvas - target) * scale) up to the order of the atomic
+        sums; `out` and `accumulate` as in backward()."""
+        if target.shape != self.canvas.shape:
+            raise ValueError(f"target shape {tuple(target.shape)} != canvas shape {tuple(self.canvas.shape)}")
+        tg = target.to(dtype=torch.float32).contiguous()
+        sc = float(2.0 / self.canvas.numel() if scale is None else scale)
+        gz = grad_zbuffer.contiguous() if grad_zbuffer is not None else None
+
+        def call(args):
+            return self.lib.rast_backward_mse(args[0], tg.data_ptr(), sc, *args[1:])
+
+        return self._backward(call, gz, stream, out, accumulate, "rast_backward_mse")
+
+    def _backward(self, call, gz, stream, out, accumulate, name) -> Dict[str, torch.Tensor]:
         if self.prim_id is None:
             raise RuntimeError("backward needs the winning-primitive buffer: build the runner with want_prim_id=True")
         dev = self.sb.device
@@ -583,25 +620,19 @@ class BatchRunner:
             g = self.grad_buffers()
         else:
             g = out
-            for t in g.values():
-                t.zero_()
+            if not accumulate:
+                for t in g.values():
+                    t.zero_()
         gp = _lib.RastGradPools()
         for k, t in g.items():
             setattr(gp, k, t.data_ptr())
-        gc = grad_canvas.contiguous() if grad_canvas is not None else None
-        gz = grad_zbuffer.contiguous() if grad_zbuffer is not None else None
         s = stream if stream is not None else torch.cuda.current_stream(dev)
         nbytes = int(self.lib.rast_backward_workspace_bytes(ctypes.byref(self.main_batch)))
         if getattr(self, "_bwd_ws", None) is None or self._bwd_ws.numel() < nbytes:
             self._bwd_ws = torch.empty(max(nbytes, 256), dtype=torch.uint8, device=dev)
-        args = (ctypes.byref(self.main_batch), gc.data_ptr() if gc is not None else None,
-                gz.data_ptr() if gz is not None else None, ctypes.byref(gp), self._bwd_ws.data_ptr(), nbytes,
-                s.cuda_stream)
-        if profile is None:
-            st = self.lib.rast_backward(*args)
-        else:
-            st = self.lib.rast_backward_profiled(*args, ctypes.byref(profile))
-        _lib.check(st, "rast_backward")
+        args = (ctypes.byref(self.main_batch), gz.data_ptr() if gz is not None else None, ctypes.byref(gp),
+                self._bwd_ws.data_ptr(), nbytes, s.cuda_stream)
+        _lib.check(call(args), name)
         return g
 
     def stats(self, name="main"):
@@ -724,9 +755,20 @@ class MultiRunner:
         return [r.grad_buffers() for r in self.runners]
 
     def backward(self, grad_canvases: Sequence[torch.Tensor], out=None,
-                 stream: Optional[torch.cuda.Stream] = None) -> List[Dict[str, torch.Tensor]]:
+                 stream: Optional[torch.cuda.Stream] = None, accumulate: bool = False) -> List[Dict[str, torch.Tensor]]:
         outs = out if out is not None else [None] * len(self.runners)
-        return [r.backward(g, stream=stream, out=o) for r, g, o in zip(self.runners, grad_canvases, outs)]
+        return [r.backward(g, stream=stream, out=o, accumulate=accumulate)
+                for r, g, o in zip(self.runners, grad_canvases, outs)]
+
+    def backward_mse(self, targets: Sequence[torch.Tensor], scales: Optional[Sequence[float]] = None, out=None,
+                     stream: Optional[torch.cuda.Stream] = None,
+                     accumulate: bool = False) -> List[Dict[str, torch.Tensor]]:
+        """BatchRunner.backward_mse per group (the loss's scale per group:
+        2 / that group's canvas size by default)."""
+        outs = out if out is not None else [None] * len(self.runners)
+        scs = scales if scales is not None else [None] * len(self.runners)
+        return [r.backward_mse(t, c, stream=stream, out=o, accumulate=accumulate)
+                for r, t, c, o in zip(self.runners, targets, scs, outs)]
 
 
 class InstancedPipeline:

@@ -739,12 +739,27 @@ __host__ __device__ constexpr int pixel_min_blocks() {
           SH == RAST_SHADER_DEPTH) ? 4 : 3;
 }
 
+// dL/dcanvas: read from a gradient image, or formed from the rendered canvas
+// and a target for the mean-squared-error loss, (canvas - target) * scale:
+// the difference and the product a caller's own elementwise pass would
+// round, so both routes hand the kernel the same values.
+struct CanvasGrad {
+  const float* grad;    // (pixels, 3) or null
+  const float* canvas;  // the forward's canvas (with target)
+  const float* target;  // (pixels, 3): the MSE route when not null
+  float scale;
+};
+
+__device__ __forceinline__ float canvas_grad(const CanvasGrad& cg, int64_t k) {
+  if (cg.target) return (__ldg(cg.canvas + k) - __ldg(cg.target + k)) * cg.scale;
+  return cg.grad ? __ldg(cg.grad + k) : 0.0f;
+}
+
 // kLayers: the batch has layered jobs (their over-mixed pixels take one pass
 // per slot); without, the pass loop is compiled away.
 template <int SH, bool kLayers>
 __global__ void __launch_bounds__(kThreads, pixel_min_blocks<SH>())
-pixel_kernel(RastBatch B, Work w, const float* __restrict__ grad_canvas, const float* __restrict__ grad_zbuffer,
-             RastGradPools G) {
+pixel_kernel(RastBatch B, Work w, CanvasGrad cg, const float* __restrict__ grad_zbuffer, RastGradPools G) {
   __shared__ RastJob sJ;
   __shared__ LightUnit sL;
   constexpr bool kDarboux = may<SH>(RAST_SHADER_PHONG_DARBOUX);
@@ -781,7 +796,7 @@ pixel_kernel(RastBatch B, Work w, const float* __restrict__ grad_canvas, const f
   auto load_grads = [&]() {
     gz_px = (in_job && grad_zbuffer) ? grad_zbuffer[pix] : 0.0f;
 #pragma unroll
-    for (int q = 0; q < 3; ++q) gcv_px[q] = (in_job && grad_canvas) ? grad_canvas[pix * 3 + q] : 0.0f;
+    for (int q = 0; q < 3; ++q) gcv_px[q] = in_job ? canvas_grad(cg, pix * 3 + q) : 0.0f;
   };
   if (kLayers) load_grads();
   float transmit = 1.0f;  // the over mixer's T
@@ -1207,7 +1222,7 @@ static Layout layout(const RastBatch& b) {
 }
 
 template <int SH>
-static void launch_all(const RastBatch& b, const Work& w, const Layout& L, const float* gc, const float* gz,
+static void launch_all(const RastBatch& b, const Work& w, const Layout& L, const CanvasGrad& gc, const float* gz,
                        const RastGradPools& G, cudaStream_t s, Profiler& prof) {
   const int64_t max_px = static_cast<int64_t>(b.max_width) * b.max_height;
   const dim3 pgrid(static_cast<unsigned>((max_px + kThreads - 1) / kThreads), static_cast<unsigned>(b.n_jobs));
@@ -1233,12 +1248,13 @@ static void launch_all(const RastBatch& b, const Work& w, const Layout& L, const
   prof.mark("backward_vertex_post_kernel");
 }
 
-static int run(const RastBatch* batch, const float* grad_canvas, const float* grad_zbuffer,
+static int run(const RastBatch* batch, const CanvasGrad& grad_canvas, const float* grad_zbuffer,
                const RastGradPools* grads, void* workspace, size_t workspace_bytes, void* stream,
                RastProfile* profile) {
   int st = check_batch(batch);
   if (st != RAST_OK) return st;
   if (!grads || !batch->pools.prim_id) return RAST_ERR_INVALID_ARGUMENT;
+  if (grad_canvas.target && !grad_canvas.canvas) return RAST_ERR_INVALID_ARGUMENT;
   // the over mixer's gradient needs the slots the forward saved
   if (batch->max_layers > 0 && !batch->pools.layer_prim) return RAST_ERR_INVALID_ARGUMENT;
   const RastBatch& b = *batch;
@@ -1291,11 +1307,20 @@ extern "C" size_t rast_backward_workspace_bytes(const RastBatch* batch) {
 
 extern "C" int rast_backward(const RastBatch* batch, const float* grad_canvas, const float* grad_zbuffer,
                              const RastGradPools* grads, void* workspace, size_t workspace_bytes, void* stream) {
-  return bwd::run(batch, grad_canvas, grad_zbuffer, grads, workspace, workspace_bytes, stream, nullptr);
+  return bwd::run(batch, bwd::CanvasGrad{grad_canvas, nullptr, nullptr, 0.0f}, grad_zbuffer, grads, workspace,
+                  workspace_bytes, stream, nullptr);
 }
 
 extern "C" int rast_backward_profiled(const RastBatch* batch, const float* grad_canvas, const float* grad_zbuffer,
                                       const RastGradPools* grads, void* workspace, size_t workspace_bytes,
                                       void* stream, RastProfile* profile) {
-  return bwd::run(batch, grad_canvas, grad_zbuffer, grads, workspace, workspace_bytes, stream, profile);
+  return bwd::run(batch, bwd::CanvasGrad{grad_canvas, nullptr, nullptr, 0.0f}, grad_zbuffer, grads, workspace,
+                  workspace_bytes, stream, profile);
+}
+
+extern "C" int rast_backward_mse(const RastBatch* batch, const float* target, float scale, const float* grad_zbuffer,
+                                 const RastGradPools* grads, void* workspace, size_t workspace_bytes, void* stream) {
+  if (!batch || !target) return RAST_ERR_INVALID_ARGUMENT;
+  return bwd::run(batch, bwd::CanvasGrad{nullptr, batch->pools.canvas, target, scale}, grad_zbuffer, grads,
+                  workspace, workspace_bytes, stream, nullptr);
 }

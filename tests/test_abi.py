@@ -38,7 +38,7 @@ def test_every_declared_symbol_is_exported(lib):
 
 
 def test_host_only_entry_points(lib):
-    assert lib.rast_abi_version() == _lib.ABI_VERSION == 5
+    assert lib.rast_abi_version() == _lib.ABI_VERSION == 6
     assert lib.rast_error_string(0) == b"ok"
     assert lib.rast_error_string(6) == b"tile bin capacity exceeded"
     job = _lib.RastJob()
@@ -50,6 +50,7 @@ def test_host_only_entry_points(lib):
     job.shader = 5  # phong_reflection without textures
     assert lib.rast_validate_job(ctypes.byref(job)) == 1
     assert lib.rast_render_plain(None, None, 0, None) == 1
+    assert lib.rast_backward_mse(None, None, 1.0, None, None, None, 0, None) == 1
 
 
 def _c_layout(tmp_path, struct, fields):
