@@ -1051,7 +1051,7 @@ def library_digest(files=FORWARD_SOURCES) -> str:
 # library_digest() of the sources the NCU_* counts below were captured on:
 # when the kernels change, the counts no longer describe them and the bench
 # reports traffic and the issue figure as null until they are captured again.
-NCU_SOURCE_DIGEST = "3b9251edff105c11"
+NCU_SOURCE_DIGEST = "d4e29622dd43f128"
 
 
 def ncu_counts_current() -> bool:

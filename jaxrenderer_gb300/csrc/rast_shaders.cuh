@@ -42,15 +42,16 @@ __device__ __forceinline__ void load3(const float* p, int64_t row, float* out) {
 // phong.py:78-104, phong_darboux.py:120-170, phong_reflection.py:104-132,
 // phong_reflection_shadow.py:115-150.
 // kClip = false skips gl_Position (the deferred shading re-run needs only
-// the varyings).
-template <bool kClip = true>
+// the varyings).  SH >= 0: the job's shader, known at compile time (J.shader
+// must equal it); otherwise read from the job.
+template <bool kClip = true, int SH = -1>
 __device__ __forceinline__ void vertex_shader(const RastJob& J, const RastPools& P, int v,
                                               float* clip, float* var) {
   const int64_t row = J.vert_begin + v;
   float pos[3];
   load3(P.position, row, pos);
   if (kClip) to_clip(J.world_to_clip, pos[0], pos[1], pos[2], clip);
-  const int sh = J.shader;
+  const int sh = SH >= 0 ? SH : J.shader;
   if (sh == RAST_SHADER_GOURAUD || sh == RAST_SHADER_GOURAUD_TEXTURE) {
     float nin[3], n[3], l[3];
     load3(P.normal, row, nin);
