@@ -278,8 +278,9 @@ __device__ __forceinline__ void reduce_params(const ParamGrad& pg, float* job_pa
   if (mine && v != 0.0f) atomicAdd(job_params + static_cast<int64_t>(job) * RAST_NPARAM + threadIdx.x, v);
 }
 
-// The scene's light directions normalised once per block (the same
-// operations as the fragment shaders'), with their norms.
+// The scene's light directions normalised (the same operations as the
+// fragment shaders'), with their norms: once per job by light_kernel, read by
+// every pixel block of the job.
 struct LightUnit {
   float dir[3], dir_n;  // light_direction (phong, phong_darboux)
   float eye[3], eye_n;  // light_dir_eye (phong_reflection[_shadow])
@@ -318,6 +319,7 @@ struct Work {
   const int2* fmap;     // face block map (kRows faces per block)
   const int2* vmap;     // vertex block map
   unsigned* starts;     // per-job block starts of both maps (2 x (n_jobs + 1))
+  LightUnit* light;     // per job: normalised light directions
 };
 
 // --------------------------------------------------------------- kernels
@@ -360,6 +362,20 @@ __global__ void __launch_bounds__(kThreads) mark_kernel(RastBatch B, Work w) {
     const int prev = __shfl_up_sync(kFull, p[r], 1);
     if (p[r] >= 0 && ((threadIdx.x & 31) == 0 || prev != p[r])) w.fvis[J.setup_begin + p[r]] = 1;
   }
+}
+
+// One thread per job: its LightUnit, so that the pixel kernel's blocks load
+// it with the job instead of computing it on one thread between two barriers.
+__global__ void __launch_bounds__(kThreads) light_kernel(RastBatch B, Work w) {
+  const int j = static_cast<int>(blockIdx.x * blockDim.x + threadIdx.x);
+  if (j >= B.n_jobs) return;
+  const RastJob& J = B.jobs[j];
+  LightUnit u;
+  u.dir_n = norm3(J.light_direction);
+  normalise3(J.light_direction, u.dir);
+  u.eye_n = norm3(J.light_dir_eye);
+  normalise3(J.light_dir_eye, u.eye);
+  w.light[j] = u;
 }
 
 // Per visible face: clip rows of its corners, their 3x3 inverse (the forward
@@ -771,13 +787,9 @@ pixel_kernel(RastBatch B, Work w, CanvasGrad cg, const float* __restrict__ grad_
   __shared__ LightUnit sL;
   constexpr bool kDarboux = may<SH>(RAST_SHADER_PHONG_DARBOUX);
   load_job_to_shared(B.jobs + blockIdx.y, &sJ);
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    sL.dir_n = norm3(sJ.light_direction);
-    normalise3(sJ.light_direction, sL.dir);
-    sL.eye_n = norm3(sJ.light_dir_eye);
-    normalise3(sJ.light_dir_eye, sL.eye);
-  }
+  static_assert(sizeof(LightUnit) == 8 * sizeof(float), "eight floats");
+  if (threadIdx.x < 8)
+    reinterpret_cast<float*>(&sL)[threadIdx.x] = __ldg(reinterpret_cast<const float*>(w.light + blockIdx.y) + threadIdx.x);
   __syncthreads();
   const RastJob& J = sJ;
   const RastPools& P = B.pools;
@@ -1193,7 +1205,7 @@ __global__ void __launch_bounds__(kThreads, 5) vertex_post_kernel(RastBatch B, W
 // ------------------------------------------------------------------ layout
 
 struct Layout {
-  size_t fvis_off, frec_off, facc_off, vvis_off, vvar_off, vacc_off, fmap_off, vmap_off, start_off, total;
+  size_t fvis_off, frec_off, facc_off, vvis_off, vvar_off, vacc_off, fmap_off, vmap_off, start_off, light_off, total;
   int vacc_stride;
   int vstride;
   unsigned fblocks, vblocks;
@@ -1224,6 +1236,7 @@ static Layout layout(const RastBatch& b) {
   L.fmap_off = take(static_cast<size_t>(L.fblocks) * sizeof(int2));
   L.vmap_off = take(static_cast<size_t>(L.vblocks) * sizeof(int2));
   L.start_off = take(2 * block_start_bytes(b.n_jobs));
+  L.light_off = take(static_cast<size_t>(b.n_jobs) * sizeof(LightUnit));
   L.total = off;
   return L;
 }
@@ -1239,6 +1252,7 @@ static void launch_all(const RastBatch& b, const Work& w, const Layout& L, const
   const int64_t mark_px = static_cast<int64_t>(kThreads) * kMarkPixels;
   mark_kernel<<<dim3(static_cast<unsigned>((max_px + mark_px - 1) / mark_px), static_cast<unsigned>(b.n_jobs)),
                 kThreads, 0, s>>>(b, w);
+  light_kernel<<<static_cast<unsigned>((b.n_jobs + kThreads - 1) / kThreads), kThreads, 0, s>>>(b, w);
   prof.mark("backward_mark_kernels");
   face_prep_kernel<<<fgrid, kThreads, 0, s>>>(b, w);
   prof.mark("backward_face_prep_kernel");
@@ -1277,7 +1291,7 @@ static int run(const RastBatch* batch, const CanvasGrad& grad_canvas, const floa
          reinterpret_cast<float*>(ws + L.vvar_off), reinterpret_cast<float*>(ws + L.vacc_off), L.vstride,
          L.vacc_stride,
          reinterpret_cast<const int2*>(ws + L.fmap_off), reinterpret_cast<const int2*>(ws + L.vmap_off),
-         reinterpret_cast<unsigned*>(ws + L.start_off)};
+         reinterpret_cast<unsigned*>(ws + L.start_off), reinterpret_cast<LightUnit*>(ws + L.light_off)};
   Profiler prof(profile, s, "rast_backward");
   if (cudaMemsetAsync(w.fvis, 0, static_cast<size_t>(b.total_setup), s) != cudaSuccess) return RAST_ERR_CUDA;
   if (cudaMemsetAsync(w.vvis, 0, static_cast<size_t>(b.total_vout), s) != cudaSuccess) return RAST_ERR_CUDA;
