@@ -7,8 +7,9 @@ allocator, or a plugin whose host owns all device memory.  For them the
 library offers one entry point that runs the tiled form out of a static
 64 MiB device array instead of a caller-provided workspace.  This checks,
 through the C ABI, that two calls in a row give exactly what the
-workspace entry point gives, and that a batch too large for the array is
-refused before anything runs.  It sits in a file of its own that pytest
+workspace entry point gives without moving the device's free memory, that
+the call captured into a CUDA graph replays to the same buffers, and that a
+batch too large for the array is refused before anything runs.  It sits in a file of its own that pytest
 collects last.
 """
 import ctypes
@@ -63,6 +64,42 @@ def test_static_scratch_entry_point_matches_workspace_entry_point(cuda_device):
         torch.cuda.synchronize(cuda_device)
         if k == 1:  # after the first call's one-time set-up: the device's free memory does not move
             assert torch.cuda.mem_get_info(cuda_device)[0] == free_before
+        _assert_same(_snapshot(packed), expected)
+    assert (expected[2] >= 0).any()
+
+
+def test_static_scratch_entry_point_replays_from_a_cuda_graph(cuda_device):
+    """The entry point's purpose: a render captured into a CUDA graph with no
+    memory pool to draw on.  After one call outside the capture (the one-time
+    symbol lookup), the call is captured on a side stream and replayed twice;
+    each replay gives what an eager call gives."""
+    lib = _lib.load()
+    specs = [scenes.random_job(sh, seed=960 + sh, W=36 + 5 * sh, H=40, F=90) for sh in scenes.ALL_SHADERS]
+    bufs = [scenes.initial_buffers(s) for s in specs]
+    packed = pack(specs, [b[0] for b in bufs], [b[1] for b in bufs], cuda_device)
+    b = packed.batch
+    cfg = _lib.RastTiledConfig(16, 8, 0)
+    assert lib.rast_tiled_workspace_bytes(ctypes.byref(b), ctypes.byref(cfg)) <= _lib.STATIC_SCRATCH_BYTES
+    init = _snapshot(packed)
+    stream = torch.cuda.current_stream(cuda_device)
+    assert lib.rast_render_tiled_static(ctypes.byref(b), ctypes.byref(cfg), stream.cuda_stream) == 0
+    torch.cuda.synchronize(cuda_device)
+    expected = _snapshot(packed)
+    _restore(packed, init)
+    torch.cuda.synchronize(cuda_device)
+    graph = torch.cuda.CUDAGraph()
+    side = torch.cuda.Stream(cuda_device)
+    side.wait_stream(stream)
+    with torch.cuda.stream(side):
+        with torch.cuda.graph(graph, stream=side):
+            st = lib.rast_render_tiled_static(ctypes.byref(b), ctypes.byref(cfg), side.cuda_stream)
+    assert st == 0
+    torch.cuda.synchronize(cuda_device)
+    for _ in range(2):
+        _restore(packed, init)
+        torch.cuda.synchronize(cuda_device)
+        graph.replay()
+        torch.cuda.synchronize(cuda_device)
         _assert_same(_snapshot(packed), expected)
     assert (expected[2] >= 0).any()
 
