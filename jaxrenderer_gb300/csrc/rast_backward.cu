@@ -15,10 +15,12 @@
 //                        perspective-correct interpolation; accumulates
 //                        dL/dm and dL/dz_clip per face, dL/d(varying) per
 //                        vertex, texel gradients; per-scene light terms
-//   face_post_kernel     per visible face: dL/dM = -m^T (dL/dm) m^T, clip
-//                        rows -> dL/d world_to_clip and dL/d positions
-//   vertex_post_kernel   per flagged vertex: reverse mode of the vertex
-//                        shader (normal transform, Gouraud lighting)
+//   post_kernel          one launch of two block roles:
+//                        face_post, per visible face: dL/dM = -m^T (dL/dm)
+//                        m^T, clip rows -> dL/d world_to_clip and dL/d
+//                        positions; vertex_post, per flagged vertex: reverse
+//                        mode of the vertex shader (normal transform,
+//                        Gouraud lighting)
 //
 // Texel lookups are nearest, so uv gets no gradient (floor); the sampled
 // texel and specular exponent do (scatter-add).  The shadow-map comparison is
@@ -1049,19 +1051,18 @@ __device__ __forceinline__ void face_post(const RastBatch& B, const Work& w, con
   }
 }
 
-__global__ void __launch_bounds__(kThreads, 4) face_post_kernel(RastBatch B, Work w, RastGradPools G) {
-  __shared__ RastJob sJ;
-  __shared__ int s_q[kRows];
-  __shared__ int s_n;
-  const int2 blk = w.fmap[blockIdx.x];
-  if (blk.x < 0) return;
+// One block of face_post work (kRows faces of one job, from the face block
+// map); the block's shared job copy and queue are the caller's.
+__device__ __forceinline__ void face_post_block(const RastBatch& B, const Work& w, const RastGradPools& G, int2 blk,
+                                                RastJob& sJ, int* s_q, int* s_n) {
+  if (blk.x < 0) return;  // uniform over the block
   const int nf = __ldg(&B.jobs[blk.x].n_faces);
   load_job_to_shared(B.jobs + blk.x, &sJ);
-  if (threadIdx.x == 0) s_n = 0;
+  if (threadIdx.x == 0) *s_n = 0;
   __syncthreads();
   const RastJob& J = sJ;
   const int n = block_queue_rows<kRowsPerThread, kThreads>(
-      [&](int r) { return blk.y + r < nf && w.fvis[J.setup_begin + blk.y + r]; }, s_q, &s_n);
+      [&](int r) { return blk.y + r < nf && w.fvis[J.setup_begin + blk.y + r]; }, s_q, s_n);
   ParamGrad pg;
 #pragma unroll
   for (int k = 0; k < 16; ++k) pg.v[RAST_GRAD_WORLD_TO_CLIP + k] = 0.0f;
@@ -1180,26 +1181,48 @@ __device__ __forceinline__ void vertex_post(const RastBatch& B, const Work& w, c
   }
 }
 
+// One block of vertex_post work (kRows vertices of one job, from the
+// vertex block map), like face_post_block.
 template <int SH>
-__global__ void __launch_bounds__(kThreads, 5) vertex_post_kernel(RastBatch B, Work w, RastGradPools G) {
-  __shared__ RastJob sJ;
-  __shared__ int s_q[kRows];
-  __shared__ int s_n;
-  const int2 blk = w.vmap[blockIdx.x];
-  if (blk.x < 0) return;
+__device__ __forceinline__ void vertex_post_block(const RastBatch& B, const Work& w, const RastGradPools& G, int2 blk,
+                                                  RastJob& sJ, int* s_q, int* s_n) {
+  if (blk.x < 0) return;  // uniform over the block
   const int nvt = __ldg(&B.jobs[blk.x].n_verts);
   load_job_to_shared(B.jobs + blk.x, &sJ);
-  if (threadIdx.x == 0) s_n = 0;
+  if (threadIdx.x == 0) *s_n = 0;
   __syncthreads();
   const RastJob& J = sJ;
   const int sh = SH >= 0 ? SH : J.shader;
   const int n = sh == RAST_SHADER_DEPTH ? 0 : block_queue_rows<kRowsPerThread, kThreads>(
-      [&](int r) { return blk.y + r < nvt && w.vvis[J.vout_begin + blk.y + r]; }, s_q, &s_n);
+      [&](int r) { return blk.y + r < nvt && w.vvis[J.vout_begin + blk.y + r]; }, s_q, s_n);
   ParamGrad pg;
 #pragma unroll
   for (int k = 0; k < RAST_NPARAM; ++k) pg.v[k] = 0.0f;
   for (int t = threadIdx.x; t < n; t += kThreads) vertex_post<SH>(B, w, J, G, blk.y + s_q[t], pg);
   reduce_params<vertex_bits(SH)>(pg, G.job_params, static_cast<int>(threadIdx.x) < n, blk.x);
+}
+
+// face_post and vertex_post read only what the pixel kernel accumulated and
+// add into the gradients with atomics, so one launch runs both, each a
+// latency-bound gather over sparse rows: block b takes the face role when
+// floor((b + 1) nfb / (nfb + nvb)) > floor(b nfb / (nfb + nvb)) (face block
+// floor(b nfb / (nfb + nvb))), the vertex role otherwise (vertex block b
+// minus the face blocks before it), so the two kinds are spread evenly over
+// the grid and resident together.
+template <int SH>
+__global__ void __launch_bounds__(kThreads, 4) post_kernel(RastBatch B, Work w, RastGradPools G, unsigned nfb,
+                                                            unsigned nvb) {
+  __shared__ RastJob sJ;
+  __shared__ int s_q[kRows];
+  __shared__ int s_n;
+  const unsigned long long total = static_cast<unsigned long long>(nfb) + nvb;
+  const unsigned long long b = blockIdx.x;
+  const unsigned f0 = static_cast<unsigned>(b * nfb / total);
+  const unsigned f1 = static_cast<unsigned>((b + 1) * nfb / total);
+  if (f1 > f0)
+    face_post_block(B, w, G, w.fmap[f0], sJ, s_q, &s_n);
+  else
+    vertex_post_block<SH>(B, w, G, w.vmap[b - f0], sJ, s_q, &s_n);
 }
 
 // ------------------------------------------------------------------ layout
@@ -1263,10 +1286,8 @@ static void launch_all(const RastBatch& b, const Work& w, const Layout& L, const
   else
     pixel_kernel<SH, false><<<pgrid, kThreads, 0, s>>>(b, w, gc, gz, G);
   prof.mark("backward_pixel_kernel");
-  face_post_kernel<<<fgrid, kThreads, 0, s>>>(b, w, G);
-  prof.mark("backward_face_post_kernel");
-  vertex_post_kernel<SH><<<vgrid, kThreads, 0, s>>>(b, w, G);
-  prof.mark("backward_vertex_post_kernel");
+  if (fgrid + vgrid > 0) post_kernel<SH><<<fgrid + vgrid, kThreads, 0, s>>>(b, w, G, fgrid, vgrid);
+  prof.mark("backward_post_kernel");
 }
 
 static int run(const RastBatch* batch, const CanvasGrad& grad_canvas, const float* grad_zbuffer,
